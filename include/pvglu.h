@@ -1,0 +1,179 @@
+/*
+ * pvglu — GB300-native sparse LU hot path of the PV-plant power-flow Newton
+ * iteration: Jacobian value scatter -> GLU numeric refactorization ->
+ * forward/backward (and transposed) triangular solves, plus the symbolic
+ * analysis that feeds them.
+ *
+ * C ABI: plain pointers and sizes, int status codes, no C++ or CUDA types.
+ * Streams are passed as `void*` holding a cudaStream_t (NULL = legacy default
+ * stream).  Device pointers are caller-owned; handles own their structure.
+ * All device calls are asynchronous on the given stream unless they say
+ * otherwise.  A handle is not thread-safe.
+ *
+ * Each entry point names the reference interface it replaces
+ * (AlbertoJimenezRuiz/PhdThesis_AlbertoJimenezRuiz, PVPP_Plant_Simulator/).
+ */
+#ifndef PVGLU_H
+#define PVGLU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  The reference aborts on every one of these (gpu_util.h:39-47,
+ * util.cpp:11-17, GLU_CSC_CPU_levels_strings.cpp:15-30); here they return. */
+enum {
+  PVGLU_OK = 0,
+  PVGLU_ERR_BAD_ARG = 1,
+  PVGLU_ERR_STRUCTURAL = 2,      /* no row exchange for a zero diagonal (004b:82) */
+  PVGLU_ERR_ZERO_PIVOT = 3,      /* |U(j,j)| < pivot_tol or not finite (GLU_CSC_CPU_levels_strings.cpp:26-30) */
+  PVGLU_ERR_NONFINITE = 4,
+  PVGLU_ERR_CUDA = 5,
+  PVGLU_ERR_BARRIER_TIMEOUT = 6, /* persistent kernel grid barrier gave up */
+  PVGLU_ERR_NOT_CONVERGED = 7,
+  PVGLU_ERR_NO_MEMORY = 8,
+  PVGLU_ERR_TOO_LARGE = 9
+};
+
+enum { PVGLU_FP64 = 0, PVGLU_FP32 = 1 };
+
+/* Solve flags. */
+enum {
+  PVGLU_SOLVE_TRANSPOSE = 1,  /* solve J^T x = b (adjoint) instead of J x = b     */
+  PVGLU_SOLVE_ORIGINAL = 2    /* b and x in the caller's unknown order (the solve
+                                 applies the row/column permutations); without it
+                                 b and x are in the permuted order, as
+                                 triangular_substitution_LU_CUDA expects */
+};
+
+/* Refactor/solve schedules. */
+enum {
+  PVGLU_SCHED_LEVELS = 0,     /* one launch per level (the reference's shape)   */
+  PVGLU_SCHED_PERSISTENT = 1  /* one cooperative launch, bounded grid barriers  */
+};
+
+typedef struct pvglu_symbolic pvglu_symbolic;
+typedef struct pvglu_numeric pvglu_numeric;
+typedef struct pvglu_plant pvglu_plant;
+
+/* Message of the last failing call on this thread ("" if none). */
+const char* pvglu_last_error(void);
+/* Library version string. */
+const char* pvglu_version(void);
+
+/* ---------------- symbolic analysis (host) ------------------------------- */
+
+/* Replaces prepare_matrices (000_PVPP_simulator.cpp:10-93): ordering,
+ * zero-diagonal row exchanges (004b), fill-in (005), GLU/L/U dependencies and
+ * chained levels (006-009), CSR/CSC with cross maps (010).
+ * rowptr/colidx: pattern of the Jacobian in the caller's unknown order (CSR,
+ * n+1 / rowptr[n] entries, no duplicates).  perm: the ordering P in the
+ * reference's semantics (interchanges_position_row_columns, 004a:40-42:
+ * perm[k] = unknown placed at pivot k), e.g. the reference's AMD output; NULL
+ * selects the built-in minimum-degree ordering. */
+int pvglu_symbolic_create(int n, const int* rowptr, const int* colidx,
+                          const int* perm, pvglu_symbolic** out);
+int pvglu_symbolic_destroy(pvglu_symbolic* s);
+
+typedef struct {
+  int n;
+  int64_t nnz_a, nnz_lu, update_count;
+  int lu_levels, l_levels, u_levels, lt_levels;
+  int lu_chains, l_chains, u_chains, lt_chains;
+  int row_swaps;
+  int perm_rows_is_involution;
+  int64_t right_looking_hazards;
+  double flops_refactor;
+} pvglu_symbolic_info;
+int pvglu_symbolic_get_info(const pvglu_symbolic* s, pvglu_symbolic_info* info);
+
+/* Read-only views of the symbolic arrays (valid while the handle lives), by
+ * name.  Reference names in brackets (struct_CPU_CUDA_arrays,
+ * factorize_electrical_system.h:3-61):
+ *   perm_amd [interchanges_position_row_columns], perm_rows
+ *   [interchanges_position_row_columns_only_rows], row_orig, col_orig,
+ *   fill_rowptr/fill_col [nonzero_values], csr_rowptr [mat_A_CSR_start_rows],
+ *   csr_col, csc_colptr, csc_row, csr_to_csc
+ *   [mat_A_CSR_corresponding_value_in_CSC], csc_to_csr, csr_diag_start
+ *   [mat_A_CSR_start_from_diagonal], csc_diag_start, lu_sl/lu_sc/lu_cols
+ *   [start_levels_unified_LU / start_chains_columns_unified_LU /
+ *   chains_columns_unified_LU], l_*, u_*, lt_* (transposed-L levels),
+ *   max_elements_per_column, slot_src, diag_slot. */
+int pvglu_symbolic_get_array(const pvglu_symbolic* s, const char* name,
+                             const int** data, int64_t* len);
+
+/* ---------------- numeric state (device) --------------------------------- */
+
+/* Device structure + LU value storage for n_scenarios independent Jacobians
+ * sharing the symbolic analysis.  Values are stored slot-major with the
+ * scenario index fastest: value(slot, s) at [slot * ld + s], ld =
+ * pvglu_numeric_ld() (n_scenarios rounded up for aligned vector access).
+ * Replaces struct_CPU_CUDA_arrays::create_CUDA (factorize_electrical_system.h:63-98). */
+int pvglu_numeric_create(const pvglu_symbolic* s, int n_scenarios, int precision,
+                         pvglu_numeric** out);
+int pvglu_numeric_destroy(pvglu_numeric* h);
+int pvglu_numeric_ld(const pvglu_numeric* h);
+/* Device pointer to the LU values (double* for FP64, float* for FP32). */
+void* pvglu_numeric_values(pvglu_numeric* h);
+/* Refactor/solve schedule (PVGLU_SCHED_*) and the pivot threshold of the
+ * zero-pivot check (default 1e-8, the reference's). */
+int pvglu_numeric_set_schedule(pvglu_numeric* h, int schedule);
+int pvglu_numeric_set_pivot_tol(pvglu_numeric* h, double tol);
+
+/* (a) Scatter: LU(slot, s) = A(slot_src[slot], s), 0 at fill slots.
+ * a_values: device, FP64, [nnz_a * ld], A's entries in the caller's CSR order.
+ * Replaces the Newton-loop permutation + fill_values_CSC_only
+ * (000_PVPP_simulator.cpp:193-210, 010_create_CSR_CSC.cpp:142-155). */
+int pvglu_scatter(pvglu_numeric* h, const double* a_values, void* stream);
+
+/* (b) GLU numeric refactorization in place, every scenario.
+ * Replaces factorize_electrical_system_CUDA (factorize_electrical_system_CUDA.cu:61-152). */
+int pvglu_refactor(pvglu_numeric* h, void* stream);
+
+/* (c) Triangular solves with the stored factors, every scenario.
+ * x: device, [n * ld], same precision as the factors; holds b on entry.
+ * Replaces triangular_substitution_LU_CUDA (triangular_substitution.cu:232-271);
+ * with PVGLU_SOLVE_TRANSPOSE it solves the adjoint system. */
+int pvglu_solve(pvglu_numeric* h, void* x, int flags, void* stream);
+
+/* Error state of the last refactor (synchronizes the stream): status code,
+ * first failing column and scenario (-1 if none).  Clears the state. */
+int pvglu_numeric_check(pvglu_numeric* h, void* stream, int* code, int* column,
+                        int* scenario);
+
+/* Host-buffer drop-in used by the reference's C++ driver: copies the CSC
+ * values (FP64, [nnz_lu], single scenario) in, refactors, copies the combined
+ * LU back (factorize_electrical_system_CUDA semantics: host in, host out).
+ * Synchronous. */
+int pvglu_refactor_host(pvglu_numeric* h, double* csc_values);
+/* Host-buffer solve (triangular_substitution_LU_CUDA semantics, permuted
+ * space): b (FP64, [n]) in, x out.  Synchronous. */
+int pvglu_solve_host(pvglu_numeric* h, double* b);
+
+/* One full Newton linear step from host buffers: H2D of A's values
+ * ([nnz_a * ld], FP64) and b ([n * ld], FP64, original order), scatter,
+ * refactor, solve, D2H of x ([n * ld], FP64, original order).  FP64 handles
+ * only.  Asynchronous on `stream` (pinned host buffers give async copies). */
+int pvglu_scatter_refactor_solve_host(pvglu_numeric* h, const double* a_values_host,
+                                      const double* b_host, double* x_host,
+                                      void* stream);
+
+/* ---------------- FP32 factors + FP64 iterative refinement --------------- */
+
+/* Solves J x = b (original order) for every scenario with the FP32 factors of
+ * h (pvglu_scatter + pvglu_refactor done on an FP32 handle), refining in FP64:
+ * r = b - J x with J from a_values (FP64, [nnz_a * ld]), correction solved in
+ * FP32, accumulated in FP64.  Stops per scenario when
+ * max|dx| <= tol * max|x|, after at most max_sweeps sweeps.  b, x: FP64
+ * device [n * ld].  sweeps_out (device int[ld], may be NULL) receives the
+ * sweeps per scenario; -1 marks a scenario that did not converge. */
+int pvglu_solve_refined(pvglu_numeric* h, const double* a_values, const double* b,
+                        double* x, double tol, int max_sweeps, int* sweeps_out,
+                        void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PVGLU_H */

@@ -1,0 +1,187 @@
+"""ORACLE — test infrastructure only.
+
+ctypes loader for the CPU restatement (oracle/liboracle.so, built from
+oracle_glu.cpp) and, where the reference checkout was available at build
+time, for the reference's own code (oracle/_ref/libpvref.so, built by
+oracle/Makefile.ref).  Only tests, the smoke check and bench.py's CPU legs use
+this module; the product never imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent
+PORT_LIB = HERE / "liboracle.so"
+REF_LIB = HERE / "_ref" / "libpvref.so"
+REF_SRC = Path("/root/reference/PVPP_Plant_Simulator")
+
+ARRAYS = ("perm_amd", "perm_rows", "fill_rowptr", "fill_col", "lu_sl", "lu_sc", "lu_cols",
+          "l_sl", "l_sc", "l_cols", "u_sl", "u_sc", "u_cols", "max_elements_per_column",
+          "csr_rowptr", "csr_col", "csc_colptr", "csc_row", "csr_to_csc", "csc_to_csr",
+          "csr_diag_start", "csc_diag_start")
+
+
+def build_port() -> Path:
+    subprocess.run(["make", "-s", "-f", str(HERE / "Makefile"), "oracle/liboracle.so"],
+                   cwd=ROOT, check=True)
+    return PORT_LIB
+
+
+def build_ref() -> Path | None:
+    """Builds oracle/_ref/libpvref.so when the reference sources are present."""
+    if not REF_SRC.is_dir():
+        return None
+    subprocess.run(["make", "-s", "-j8", "-f", str(HERE / "Makefile.ref"), f"REF={REF_SRC}"],
+                   cwd=ROOT, check=True)
+    return REF_LIB
+
+
+def _p(a):
+    return C.c_void_p(0) if a is None else C.c_void_p(a.ctypes.data)
+
+
+class _Base:
+    prefix = ""
+
+    def __init__(self, lib: C.CDLL, handle):
+        self.lib = lib
+        self.h = handle
+
+    def get(self, name: str) -> np.ndarray:
+        ptr = C.POINTER(C.c_int)()
+        ln = C.c_longlong()
+        rc = getattr(self.lib, self.prefix + "get")(self.h, name.encode(), C.byref(ptr), C.byref(ln))
+        if rc:
+            raise KeyError(name)
+        if ln.value == 0:
+            return np.zeros(0, np.int32)
+        return np.ctypeslib.as_array(ptr, shape=(ln.value,)).copy()
+
+    def arrays(self, names=ARRAYS) -> dict[str, np.ndarray]:
+        return {k: self.get(k) for k in names}
+
+    def scatter(self, a_vals: np.ndarray) -> np.ndarray:
+        a = np.ascontiguousarray(a_vals, dtype=np.float64)
+        out = np.empty(len(self.get("csc_row")))
+        getattr(self.lib, self.prefix + "scatter")(self.h, _p(a), _p(out))
+        return out
+
+    def solve(self, lu: np.ndarray, b: np.ndarray) -> np.ndarray:
+        x = np.array(b, dtype=np.float64, copy=True)
+        getattr(self.lib, self.prefix + "solve")(self.h, _p(np.ascontiguousarray(lu)), _p(x))
+        return x
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            getattr(self.lib, self.prefix + "free")(self.h)
+            self.h = None
+
+
+class Port(_Base):
+    """The CPU restatement in oracle_glu.cpp (P must be supplied)."""
+
+    prefix = "oracle_"
+    _lib = None
+
+    @classmethod
+    def lib_(cls):
+        if cls._lib is None:
+            if not PORT_LIB.exists():
+                build_port()
+            lib = C.CDLL(str(PORT_LIB))
+            lib.oracle_symbolic.restype = C.c_void_p
+            lib.oracle_symbolic.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                            C.c_char_p, C.c_int]
+            for f in ("oracle_get",):
+                getattr(lib, f).argtypes = [C.c_void_p, C.c_char_p, C.c_void_p, C.c_void_p]
+            for f in ("oracle_scatter", "oracle_solve", "oracle_solve_transposed"):
+                getattr(lib, f).argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+            for f in ("oracle_refactor_levels", "oracle_refactor_sequential"):
+                getattr(lib, f).argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+            lib.oracle_scatter_refactor_solve.argtypes = [C.c_void_p] * 4
+            lib.oracle_free.argtypes = [C.c_void_p]
+            cls._lib = lib
+        return cls._lib
+
+    def __init__(self, rowptr, colidx, perm):
+        lib = self.lib_()
+        self._keep = [np.ascontiguousarray(rowptr, dtype=np.int32),
+                      np.ascontiguousarray(colidx, dtype=np.int32),
+                      np.ascontiguousarray(perm, dtype=np.int32)]
+        err = C.create_string_buffer(256)
+        h = lib.oracle_symbolic(len(rowptr) - 1, _p(self._keep[0]), _p(self._keep[1]),
+                                _p(self._keep[2]), err, 256)
+        if not h:
+            raise RuntimeError("oracle symbolic failed: " + err.value.decode())
+        super().__init__(lib, h)
+
+    def refactor(self, csc_vals: np.ndarray, sequential: bool = False) -> tuple[np.ndarray, int]:
+        v = np.array(csc_vals, dtype=np.float64, copy=True)
+        bad = C.c_int(-1)
+        f = self.lib.oracle_refactor_sequential if sequential else self.lib.oracle_refactor_levels
+        rc = f(self.h, _p(v), C.byref(bad))
+        if rc:
+            raise ZeroDivisionError(f"oracle pivot failure at column {bad.value}")
+        return v
+
+    def solve_transposed(self, lu: np.ndarray, b: np.ndarray) -> np.ndarray:
+        x = np.array(b, dtype=np.float64, copy=True)
+        self.lib.oracle_solve_transposed(self.h, _p(np.ascontiguousarray(lu)), _p(x))
+        return x
+
+    def scatter_refactor_solve(self, a_vals: np.ndarray, b: np.ndarray):
+        lu = np.empty(len(self.get("csc_row")))
+        x = np.array(b, dtype=np.float64, copy=True)
+        rc = self.lib.oracle_scatter_refactor_solve(self.h, _p(np.ascontiguousarray(a_vals)),
+                                                    _p(lu), _p(x))
+        if rc:
+            raise ZeroDivisionError("oracle pivot failure")
+        return lu, x
+
+
+class Ref(_Base):
+    """The reference's own code (needs oracle/_ref/libpvref.so)."""
+
+    prefix = "ref_"
+    _lib = None
+
+    @classmethod
+    def available(cls) -> bool:
+        return REF_LIB.exists()
+
+    @classmethod
+    def lib_(cls):
+        if cls._lib is None:
+            lib = C.CDLL(str(REF_LIB))
+            lib.ref_symbolic.restype = C.c_void_p
+            lib.ref_symbolic.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+            lib.ref_get.argtypes = [C.c_void_p, C.c_char_p, C.c_void_p, C.c_void_p]
+            for f in ("ref_scatter", "ref_solve"):
+                getattr(lib, f).argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+            for f in ("ref_refactor_levels", "ref_refactor_sequential"):
+                getattr(lib, f).argtypes = [C.c_void_p, C.c_void_p]
+            lib.ref_free.argtypes = [C.c_void_p]
+            cls._lib = lib
+        return cls._lib
+
+    def __init__(self, rowptr, colidx, perm=None):
+        lib = self.lib_()
+        self._keep = [np.ascontiguousarray(rowptr, dtype=np.int32),
+                      np.ascontiguousarray(colidx, dtype=np.int32)]
+        p = None
+        if perm is not None:
+            p = np.ascontiguousarray(perm, dtype=np.int32)
+            self._keep.append(p)
+        h = lib.ref_symbolic(len(rowptr) - 1, _p(self._keep[0]), _p(self._keep[1]), _p(p))
+        super().__init__(lib, h)
+
+    def refactor(self, csc_vals: np.ndarray, sequential: bool = False) -> np.ndarray:
+        v = np.array(csc_vals, dtype=np.float64, copy=True)
+        f = self.lib.ref_refactor_sequential if sequential else self.lib.ref_refactor_levels
+        f(self.h, _p(v))
+        return v

@@ -1,0 +1,16 @@
+"""GB300-native sparse LU hot path of the PV-plant power-flow Newton iteration.
+
+The product is the native library libpvglu.so (C ABI in include/pvglu.h):
+host symbolic analysis plus sm_103a kernels for the Jacobian value scatter,
+the GLU refactorization and the triangular solves.  This package is its
+Python view; importing it loads the library and fails if it is missing.
+"""
+from . import _native
+from ._native import FP32, FP64, SCHED_LEVELS, SCHED_PERSISTENT, PvgluError
+from .glu import Numeric, Symbolic
+from .plant import Plant
+
+_native.lib()  # fail loudly at import when the native library is absent
+
+__all__ = ["FP32", "FP64", "SCHED_LEVELS", "SCHED_PERSISTENT", "Numeric", "PvgluError",
+           "Plant", "Symbolic"]

@@ -1,0 +1,494 @@
+// C ABI of the hot path (include/pvglu.h): handles, device structure upload,
+// scatter / refactor / solve launch sequences.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/pvglu.h"
+#include "kernels.cuh"
+#include "persistent.cuh"
+#include "symbolic.hpp"
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+#define PVGLU_CUDA(call)                                                       \
+  do {                                                                         \
+    cudaError_t e_ = (call);                                                   \
+    if (e_ != cudaSuccess)                                                     \
+      return fail(PVGLU_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+template <typename T>
+int upload(const std::vector<T>& h, T** d) {
+  *d = nullptr;
+  const size_t bytes = std::max<size_t>(h.size(), 1) * sizeof(T);
+  PVGLU_CUDA(cudaMalloc((void**)d, bytes));
+  if (!h.empty()) PVGLU_CUDA(cudaMemcpy(*d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+  return PVGLU_OK;
+}
+
+}  // namespace
+
+struct pvglu_symbolic {
+  pvglu::Symbolic s;
+};
+
+struct pvglu_numeric {
+  const pvglu_symbolic* sym = nullptr;
+  int n = 0, nnz = 0, nnz_a = 0;
+  int S = 0, ld = 0, precision = PVGLU_FP64;
+  int schedule = PVGLU_SCHED_LEVELS;
+  double pivot_tol = 1e-8;
+  pvglu::DevStruct d{};
+  std::vector<void*> allocs;
+  void* values = nullptr;       // [nnz * ld] T
+  void* work = nullptr;         // [n * ld] T
+  double* work64 = nullptr;     // [nnz_a * ld] staging / [n * ld] vectors
+  double* b64 = nullptr;        // [n * ld]
+  int* row_pos = nullptr;       // inverse of row_orig
+  pvglu::DevStatus* status = nullptr;
+  int* ir_done = nullptr;
+  unsigned long long* ir_max_dx = nullptr;
+  unsigned long long* ir_max_x = nullptr;
+  // Host copies of the level starts (launch ranges).
+  std::vector<int> lu_sl, l_sl, u_sl, lt_sl;
+  // Persistent schedule.
+  pvglu::PersistentPlan plan{};
+  int persistent_grid = 0;
+  unsigned int* barrier = nullptr;  // [2]: count, generation
+  ~pvglu_numeric() {
+    for (void* p : allocs) cudaFree(p);
+  }
+  template <typename T>
+  int put(const std::vector<T>& h, const T** out) {
+    T* d = nullptr;
+    int st = upload(h, &d);
+    if (st) return st;
+    allocs.push_back(d);
+    *out = d;
+    return PVGLU_OK;
+  }
+  template <typename T>
+  int alloc(size_t count, T** out) {
+    PVGLU_CUDA(cudaMalloc((void**)out, std::max<size_t>(count, 1) * sizeof(T)));
+    allocs.push_back(*out);
+    return PVGLU_OK;
+  }
+};
+
+namespace {
+
+cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+int launch_blocks(int64_t threads, int block) {
+  int64_t b = (threads + block - 1) / block;
+  return (int)std::max<int64_t>(1, std::min<int64_t>(b, 1 << 30));
+}
+
+template <typename T>
+int refactor_levels(pvglu_numeric* h, cudaStream_t st) {
+  T* v = static_cast<T*>(h->values);
+  for (size_t lv = 0; lv + 1 < h->lu_sl.size(); lv++) {
+    const int cb = h->lu_sl[lv], ce = h->lu_sl[lv + 1];
+    const int64_t threads = (int64_t)(ce - cb) * h->ld;
+    pvglu::k_refactor_level<T><<<launch_blocks(threads, 128), 128, 0, st>>>(
+        h->d, v, h->ld, h->S, cb, ce, h->pivot_tol, h->status);
+  }
+  PVGLU_CUDA(cudaGetLastError());
+  return PVGLU_OK;
+}
+
+template <typename T, int KIND>
+void solve_phase(pvglu_numeric* h, const std::vector<int>& sl, T* x, cudaStream_t st) {
+  const T* v = static_cast<const T*>(h->values);
+  for (size_t lv = 0; lv + 1 < sl.size(); lv++) {
+    const int cb = sl[lv], ce = sl[lv + 1];
+    const int64_t threads = (int64_t)(ce - cb) * h->ld;
+    pvglu::k_solve_level<T, KIND><<<launch_blocks(threads, 128), 128, 0, st>>>(
+        h->d, v, x, h->ld, h->S, cb, ce);
+  }
+}
+
+template <typename T>
+int solve_permuted(pvglu_numeric* h, T* x, bool transpose, cudaStream_t st) {
+  if (h->schedule == PVGLU_SCHED_PERSISTENT) {
+    const int st_code = pvglu::launch_persistent<T>(
+        h->plan, h->d, static_cast<T*>(h->values), x, h->ld, h->S, h->pivot_tol,
+        h->status, h->barrier, h->persistent_grid,
+        transpose ? pvglu::PHASE_SOLVE_T : pvglu::PHASE_SOLVE, st);
+    if (st_code) return fail(PVGLU_ERR_CUDA, "persistent solve launch failed");
+    return PVGLU_OK;
+  }
+  if (!transpose) {
+    solve_phase<T, 0>(h, h->l_sl, x, st);
+    solve_phase<T, 1>(h, h->u_sl, x, st);
+  } else {
+    solve_phase<T, 2>(h, h->lu_sl, x, st);
+    solve_phase<T, 3>(h, h->lt_sl, x, st);
+  }
+  PVGLU_CUDA(cudaGetLastError());
+  return PVGLU_OK;
+}
+
+template <typename TI, typename TO>
+void permute(pvglu_numeric* h, const int* perm, const TI* x, TO* y, bool gather,
+             cudaStream_t st) {
+  const int64_t total = (int64_t)h->n * h->ld;
+  pvglu::k_permute<TI, TO><<<launch_blocks(total, 256), 256, 0, st>>>(
+      perm, h->n, h->ld, h->S, x, y, gather ? 1 : 0);
+}
+
+template <typename T>
+int solve_any(pvglu_numeric* h, T* x, int flags, cudaStream_t st) {
+  const bool tr = (flags & PVGLU_SOLVE_TRANSPOSE) != 0;
+  if (!(flags & PVGLU_SOLVE_ORIGINAL)) return solve_permuted<T>(h, x, tr, st);
+  T* w = static_cast<T*>(h->work);
+  // J x = b:   w = b[row_orig], solve M y = w, x[col_orig] = y
+  // J^T x = b: w = b[col_orig], solve M^T z = w, x[row_orig] = z
+  const int* in_perm = tr ? h->d.col_orig : h->d.row_orig;
+  const int* out_perm = tr ? h->d.row_orig : h->d.col_orig;
+  permute<T, T>(h, in_perm, x, w, true, st);
+  int rc = solve_permuted<T>(h, w, tr, st);
+  if (rc) return rc;
+  permute<T, T>(h, out_perm, w, x, false, st);
+  PVGLU_CUDA(cudaGetLastError());
+  return PVGLU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* pvglu_last_error(void) { return g_err.c_str(); }
+const char* pvglu_version(void) { return "pvglu 0.1 (sm_103a)"; }
+
+int pvglu_symbolic_create(int n, const int* rowptr, const int* colidx, const int* perm,
+                          pvglu_symbolic** out) {
+  if (!out) return fail(PVGLU_ERR_BAD_ARG, "out is NULL");
+  *out = nullptr;
+  auto* h = new pvglu_symbolic();
+  std::string err;
+  pvglu::SymbolicOptions opt;
+  const int st = pvglu::build_symbolic(n, rowptr, colidx, perm, opt, h->s, err);
+  if (st) {
+    delete h;
+    return fail(st, err);
+  }
+  *out = h;
+  return PVGLU_OK;
+}
+
+int pvglu_symbolic_destroy(pvglu_symbolic* s) {
+  delete s;
+  return PVGLU_OK;
+}
+
+int pvglu_symbolic_get_info(const pvglu_symbolic* h, pvglu_symbolic_info* info) {
+  if (!h || !info) return fail(PVGLU_ERR_BAD_ARG, "NULL argument");
+  const auto& s = h->s;
+  info->n = s.n;
+  info->nnz_a = s.nnz_a;
+  info->nnz_lu = s.nnz_lu;
+  info->update_count = s.update_count;
+  info->lu_levels = s.lu.num_levels();
+  info->l_levels = s.l.num_levels();
+  info->u_levels = s.u.num_levels();
+  info->lt_levels = s.lt.num_levels();
+  info->lu_chains = s.lu.num_chains();
+  info->l_chains = s.l.num_chains();
+  info->u_chains = s.u.num_chains();
+  info->lt_chains = s.lt.num_chains();
+  info->row_swaps = s.row_swaps;
+  info->perm_rows_is_involution = s.perm_rows_is_involution;
+  info->right_looking_hazards = s.right_looking_hazards;
+  info->flops_refactor = s.flops_refactor;
+  return PVGLU_OK;
+}
+
+int pvglu_symbolic_get_array(const pvglu_symbolic* h, const char* name, const int** data,
+                             int64_t* len) {
+  if (!h || !name || !data || !len) return fail(PVGLU_ERR_BAD_ARG, "NULL argument");
+  const auto& s = h->s;
+  const std::string k(name);
+  const std::vector<int>* v = nullptr;
+#define PVG(key, member) if (k == key) v = &s.member;
+  PVG("perm_amd", perm_amd) PVG("perm_rows", perm_rows) PVG("row_orig", row_orig)
+  PVG("col_orig", col_orig) PVG("fill_rowptr", fill_rowptr) PVG("fill_col", fill_col)
+  PVG("csr_rowptr", csr_rowptr) PVG("csr_col", csr_col) PVG("csc_colptr", csc_colptr)
+  PVG("csc_row", csc_row) PVG("csr_to_csc", csr_to_csc) PVG("csc_to_csr", csc_to_csr)
+  PVG("csr_diag_start", csr_diag_start) PVG("csc_diag_start", csc_diag_start)
+  PVG("lu_sl", lu.start_levels) PVG("lu_sc", lu.start_chains) PVG("lu_cols", lu.columns)
+  PVG("l_sl", l.start_levels) PVG("l_sc", l.start_chains) PVG("l_cols", l.columns)
+  PVG("u_sl", u.start_levels) PVG("u_sc", u.start_chains) PVG("u_cols", u.columns)
+  PVG("lt_sl", lt.start_levels) PVG("lt_sc", lt.start_chains) PVG("lt_cols", lt.columns)
+  PVG("max_elements_per_column", max_elements_per_column) PVG("slot_src", slot_src)
+  PVG("diag_slot", diag_slot) PVG("a_rowptr", a_rowptr) PVG("a_colidx", a_colidx)
+#undef PVG
+  if (!v) return fail(PVGLU_ERR_BAD_ARG, std::string("unknown array ") + name);
+  *data = v->data();
+  *len = (int64_t)v->size();
+  return PVGLU_OK;
+}
+
+int pvglu_numeric_create(const pvglu_symbolic* sym, int n_scenarios, int precision,
+                         pvglu_numeric** out) {
+  if (!sym || !out || n_scenarios <= 0 ||
+      (precision != PVGLU_FP64 && precision != PVGLU_FP32))
+    return fail(PVGLU_ERR_BAD_ARG, "bad numeric_create arguments");
+  *out = nullptr;
+  const auto& s = sym->s;
+  if (s.update_count > 0x7fffffffLL) return fail(PVGLU_ERR_TOO_LARGE, "update list > 2^31");
+  auto* h = new pvglu_numeric();
+  h->sym = sym;
+  h->n = s.n;
+  h->nnz = (int)s.nnz_lu;
+  h->nnz_a = (int)s.nnz_a;
+  h->S = n_scenarios;
+  h->ld = n_scenarios == 1 ? 1 : ((n_scenarios + 31) / 32) * 32;
+  h->precision = precision;
+  h->lu_sl = s.lu.start_levels;
+  h->l_sl = s.l.start_levels;
+  h->u_sl = s.u.start_levels;
+  h->lt_sl = s.lt.start_levels;
+  auto& d = h->d;
+  d.n = s.n;
+  d.nnz = (int)s.nnz_lu;
+  std::vector<int> upd_ptr32(s.upd_ptr.begin(), s.upd_ptr.end());
+  std::vector<int> row_pos(s.n);
+  for (int r = 0; r < s.n; r++) row_pos[s.row_orig[r]] = r;
+  int rc = 0;
+  rc |= h->put(s.csc_colptr, &d.colptr);
+  rc |= h->put(s.csc_row, &d.csc_row);
+  rc |= h->put(s.diag_slot, &d.diag);
+  rc |= h->put(s.slot_src, &d.slot_src);
+  rc |= h->put(upd_ptr32, &d.upd_ptr);
+  rc |= h->put(s.upd_tgt, &d.upd_tgt);
+  rc |= h->put(s.lrow_ptr, &d.lrow_ptr);
+  rc |= h->put(s.lrow_slot, &d.lrow_slot);
+  rc |= h->put(s.lrow_col, &d.lrow_col);
+  rc |= h->put(s.urow_ptr, &d.urow_ptr);
+  rc |= h->put(s.urow_slot, &d.urow_slot);
+  rc |= h->put(s.urow_col, &d.urow_col);
+  rc |= h->put(s.row_orig, &d.row_orig);
+  rc |= h->put(s.col_orig, &d.col_orig);
+  rc |= h->put(s.a_rowptr, &d.a_rowptr);
+  rc |= h->put(s.a_colidx, &d.a_colidx);
+  rc |= h->put(s.lu.start_chains, &d.lu_sc);
+  rc |= h->put(s.lu.columns, &d.lu_cols);
+  rc |= h->put(s.l.start_chains, &d.l_sc);
+  rc |= h->put(s.l.columns, &d.l_cols);
+  rc |= h->put(s.u.start_chains, &d.u_sc);
+  rc |= h->put(s.u.columns, &d.u_cols);
+  rc |= h->put(s.lt.start_chains, &d.lt_sc);
+  rc |= h->put(s.lt.columns, &d.lt_cols);
+  {
+    const int* rp = nullptr;
+    rc |= h->put(row_pos, &rp);
+    h->row_pos = const_cast<int*>(rp);
+  }
+  const size_t es = precision == PVGLU_FP64 ? sizeof(double) : sizeof(float);
+  rc |= h->alloc((size_t)h->nnz * h->ld * es, (char**)&h->values);
+  rc |= h->alloc((size_t)h->n * h->ld * es, (char**)&h->work);
+  rc |= h->alloc((size_t)std::max(h->nnz_a, h->n) * h->ld, &h->work64);
+  rc |= h->alloc((size_t)h->n * h->ld, &h->b64);
+  rc |= h->alloc(1, &h->status);
+  rc |= h->alloc((size_t)h->ld, &h->ir_done);
+  rc |= h->alloc((size_t)h->ld, &h->ir_max_dx);
+  rc |= h->alloc((size_t)h->ld, &h->ir_max_x);
+  rc |= h->alloc(4, &h->barrier);
+  if (rc) {
+    const std::string e = g_err;
+    delete h;
+    return fail(PVGLU_ERR_NO_MEMORY, "device allocation failed: " + e);
+  }
+  if (cudaMemset(h->status, 0, sizeof(pvglu::DevStatus)) != cudaSuccess ||
+      cudaMemset(h->barrier, 0, 4 * sizeof(unsigned int)) != cudaSuccess ||
+      cudaMemset(h->values, 0, (size_t)h->nnz * h->ld * es) != cudaSuccess) {
+    delete h;
+    return fail(PVGLU_ERR_CUDA, "cudaMemset failed");
+  }
+  // Persistent schedule plan (level ranges in one table).
+  h->plan = pvglu::make_plan(s, h->allocs, &rc);
+  if (rc) {
+    delete h;
+    return fail(PVGLU_ERR_NO_MEMORY, "persistent plan upload failed");
+  }
+  h->persistent_grid = precision == PVGLU_FP64 ? pvglu::persistent_grid<double>()
+                                               : pvglu::persistent_grid<float>();
+  *out = h;
+  return PVGLU_OK;
+}
+
+int pvglu_numeric_destroy(pvglu_numeric* h) {
+  delete h;
+  return PVGLU_OK;
+}
+
+int pvglu_numeric_ld(const pvglu_numeric* h) { return h ? h->ld : 0; }
+void* pvglu_numeric_values(pvglu_numeric* h) { return h ? h->values : nullptr; }
+
+int pvglu_numeric_set_schedule(pvglu_numeric* h, int schedule) {
+  if (!h || (schedule != PVGLU_SCHED_LEVELS && schedule != PVGLU_SCHED_PERSISTENT))
+    return fail(PVGLU_ERR_BAD_ARG, "bad schedule");
+  if (schedule == PVGLU_SCHED_PERSISTENT && h->persistent_grid <= 0)
+    return fail(PVGLU_ERR_CUDA, "cooperative launch unavailable on this device");
+  h->schedule = schedule;
+  return PVGLU_OK;
+}
+
+int pvglu_numeric_set_pivot_tol(pvglu_numeric* h, double tol) {
+  if (!h || !(tol >= 0.0)) return fail(PVGLU_ERR_BAD_ARG, "bad pivot tolerance");
+  h->pivot_tol = tol;
+  return PVGLU_OK;
+}
+
+int pvglu_scatter(pvglu_numeric* h, const double* a_values, void* stream) {
+  if (!h || !a_values) return fail(PVGLU_ERR_BAD_ARG, "NULL argument");
+  cudaStream_t st = as_stream(stream);
+  const int64_t total = (int64_t)h->nnz * h->ld;
+  const int blocks = launch_blocks(total, 256);
+  if (h->precision == PVGLU_FP64)
+    pvglu::k_scatter<double><<<blocks, 256, 0, st>>>(h->d.slot_src, h->nnz, h->ld, h->S,
+                                                     a_values, (double*)h->values);
+  else
+    pvglu::k_scatter<float><<<blocks, 256, 0, st>>>(h->d.slot_src, h->nnz, h->ld, h->S,
+                                                    a_values, (float*)h->values);
+  PVGLU_CUDA(cudaGetLastError());
+  return PVGLU_OK;
+}
+
+int pvglu_refactor(pvglu_numeric* h, void* stream) {
+  if (!h) return fail(PVGLU_ERR_BAD_ARG, "NULL handle");
+  cudaStream_t st = as_stream(stream);
+  if (h->schedule == PVGLU_SCHED_PERSISTENT) {
+    int rc = h->precision == PVGLU_FP64
+                 ? pvglu::launch_persistent<double>(h->plan, h->d, (double*)h->values,
+                                                    nullptr, h->ld, h->S, h->pivot_tol,
+                                                    h->status, h->barrier,
+                                                    h->persistent_grid,
+                                                    pvglu::PHASE_REFACTOR, st)
+                 : pvglu::launch_persistent<float>(h->plan, h->d, (float*)h->values,
+                                                   nullptr, h->ld, h->S, h->pivot_tol,
+                                                   h->status, h->barrier,
+                                                   h->persistent_grid,
+                                                   pvglu::PHASE_REFACTOR, st);
+    if (rc) return fail(PVGLU_ERR_CUDA, "persistent refactor launch failed");
+    return PVGLU_OK;
+  }
+  return h->precision == PVGLU_FP64 ? refactor_levels<double>(h, st)
+                                    : refactor_levels<float>(h, st);
+}
+
+int pvglu_solve(pvglu_numeric* h, void* x, int flags, void* stream) {
+  if (!h || !x) return fail(PVGLU_ERR_BAD_ARG, "NULL argument");
+  cudaStream_t st = as_stream(stream);
+  return h->precision == PVGLU_FP64 ? solve_any<double>(h, (double*)x, flags, st)
+                                    : solve_any<float>(h, (float*)x, flags, st);
+}
+
+int pvglu_numeric_check(pvglu_numeric* h, void* stream, int* code, int* column,
+                        int* scenario) {
+  if (!h) return fail(PVGLU_ERR_BAD_ARG, "NULL handle");
+  pvglu::DevStatus hs{};
+  PVGLU_CUDA(cudaMemcpyAsync(&hs, h->status, sizeof(hs), cudaMemcpyDeviceToHost,
+                             as_stream(stream)));
+  PVGLU_CUDA(cudaStreamSynchronize(as_stream(stream)));
+  PVGLU_CUDA(cudaMemsetAsync(h->status, 0, sizeof(hs), as_stream(stream)));
+  PVGLU_CUDA(cudaStreamSynchronize(as_stream(stream)));
+  if (code) *code = hs.code;
+  if (column) *column = hs.code ? hs.column : -1;
+  if (scenario) *scenario = hs.code ? hs.scenario : -1;
+  return PVGLU_OK;
+}
+
+int pvglu_refactor_host(pvglu_numeric* h, double* csc_values) {
+  if (!h || !csc_values || h->precision != PVGLU_FP64 || h->S != 1)
+    return fail(PVGLU_ERR_BAD_ARG, "needs a single-scenario FP64 handle");
+  PVGLU_CUDA(cudaMemcpy(h->values, csc_values, (size_t)h->nnz * sizeof(double),
+                        cudaMemcpyHostToDevice));
+  int rc = pvglu_refactor(h, nullptr);
+  if (rc) return rc;
+  PVGLU_CUDA(cudaMemcpy(csc_values, h->values, (size_t)h->nnz * sizeof(double),
+                        cudaMemcpyDeviceToHost));
+  int code = 0, col = -1, sc = -1;
+  rc = pvglu_numeric_check(h, nullptr, &code, &col, &sc);
+  if (rc) return rc;
+  if (code) return fail(code, "refactor failed at column " + std::to_string(col));
+  return PVGLU_OK;
+}
+
+int pvglu_solve_host(pvglu_numeric* h, double* b) {
+  if (!h || !b || h->precision != PVGLU_FP64 || h->S != 1)
+    return fail(PVGLU_ERR_BAD_ARG, "needs a single-scenario FP64 handle");
+  double* x = h->b64;
+  PVGLU_CUDA(cudaMemcpy(x, b, (size_t)h->n * sizeof(double), cudaMemcpyHostToDevice));
+  int rc = pvglu_solve(h, x, 0, nullptr);
+  if (rc) return rc;
+  PVGLU_CUDA(cudaMemcpy(b, x, (size_t)h->n * sizeof(double), cudaMemcpyDeviceToHost));
+  return PVGLU_OK;
+}
+
+int pvglu_scatter_refactor_solve_host(pvglu_numeric* h, const double* a_values_host,
+                                      const double* b_host, double* x_host, void* stream) {
+  if (!h || !a_values_host || !b_host || !x_host || h->precision != PVGLU_FP64)
+    return fail(PVGLU_ERR_BAD_ARG, "needs an FP64 handle and non-NULL buffers");
+  cudaStream_t st = as_stream(stream);
+  double* a = h->work64;
+  double* x = h->b64;
+  PVGLU_CUDA(cudaMemcpyAsync(a, a_values_host, (size_t)h->nnz_a * h->ld * sizeof(double),
+                             cudaMemcpyHostToDevice, st));
+  PVGLU_CUDA(cudaMemcpyAsync(x, b_host, (size_t)h->n * h->ld * sizeof(double),
+                             cudaMemcpyHostToDevice, st));
+  int rc = pvglu_scatter(h, a, stream);
+  if (!rc) rc = pvglu_refactor(h, stream);
+  if (!rc) rc = pvglu_solve(h, x, PVGLU_SOLVE_ORIGINAL, stream);
+  if (rc) return rc;
+  PVGLU_CUDA(cudaMemcpyAsync(x_host, x, (size_t)h->n * h->ld * sizeof(double),
+                             cudaMemcpyDeviceToHost, st));
+  return PVGLU_OK;
+}
+
+int pvglu_solve_refined(pvglu_numeric* h, const double* a_values, const double* b,
+                        double* x, double tol, int max_sweeps, int* sweeps_out,
+                        void* stream) {
+  if (!h || !a_values || !b || !x || max_sweeps <= 0 || !(tol > 0.0))
+    return fail(PVGLU_ERR_BAD_ARG, "bad solve_refined arguments");
+  if (h->precision != PVGLU_FP32) return fail(PVGLU_ERR_BAD_ARG, "needs an FP32 handle");
+  cudaStream_t st = as_stream(stream);
+  const int64_t nv = (int64_t)h->n * h->ld;
+  float* w = static_cast<float*>(h->work);
+  PVGLU_CUDA(cudaMemsetAsync(x, 0, nv * sizeof(double), st));
+  PVGLU_CUDA(cudaMemsetAsync(h->ir_done, 0, h->ld * sizeof(int), st));
+  PVGLU_CUDA(cudaMemsetAsync(h->ir_max_dx, 0, h->ld * sizeof(unsigned long long), st));
+  PVGLU_CUDA(cudaMemsetAsync(h->ir_max_x, 0, h->ld * sizeof(unsigned long long), st));
+  if (sweeps_out) PVGLU_CUDA(cudaMemsetAsync(sweeps_out, 0, h->ld * sizeof(int), st));
+  for (int sweep = 1; sweep <= max_sweeps; sweep++) {
+    pvglu::k_residual<<<launch_blocks(nv, 256), 256, 0, st>>>(
+        h->d.a_rowptr, h->d.a_colidx, h->n, h->ld, h->S, a_values, b, x, h->ir_done, w,
+        h->row_pos);
+    int rc = solve_permuted<float>(h, w, false, st);
+    if (rc) return rc;
+    dim3 blk(32, 8), grd((unsigned)std::min(1024, (h->n + 7) / 8), (unsigned)(h->ld + 31) / 32);
+    pvglu::k_ir_update<<<grd, blk, 0, st>>>(h->d.col_orig, h->n, h->ld, h->S, w, x,
+                                            h->ir_done, h->ir_max_dx, h->ir_max_x);
+    pvglu::k_ir_check<<<(h->S + 127) / 128, 128, 0, st>>>(h->S, sweep, max_sweeps, tol,
+                                                          h->ir_done, sweeps_out,
+                                                          h->ir_max_dx, h->ir_max_x);
+  }
+  PVGLU_CUDA(cudaGetLastError());
+  return PVGLU_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,264 @@
+// sm_103a kernels of the hot path: value scatter, left-looking GLU
+// refactorization, triangular solves (forward, backward, transposed),
+// permutations and the FP64 residual of iterative refinement.
+//
+// Layout: the value of LU slot q for scenario s lives at V[q * ld + s] (slot
+// major, scenario fastest).  A warp therefore walks one column for 32
+// scenarios and every value access is a coalesced 128/256-byte transaction,
+// while the structure indices it reads are warp-uniform broadcasts.  With a
+// single scenario (ld = 1) the same code runs one thread per chain, which is
+// the reference's launch shape (factorize_electrical_system_CUDA.cu:72-98).
+//
+// Refactorization is LEFT-looking: processing column k reads only final
+// columns j < k (its U-column dependencies, which are exactly the reference's
+// GLU dependency sets, 006_get_dependencies_GLU.cpp:5-47) and writes only
+// column k.  That needs no atomics (the reference's right-looking update
+// uses atomicAdd, factorize_matrix_GLU_CUDA.cuh:99) and makes every result
+// independent of thread scheduling.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace pvglu {
+
+struct DevStruct {
+  int n;
+  int nnz;
+  const int* colptr;     // [n+1] CSC column starts
+  const int* csc_row;    // [nnz]
+  const int* diag;       // [n] slot of M(j,j)
+  const int* slot_src;   // [nnz] A-entry feeding the slot, -1 for fill
+  const int* upd_ptr;    // [nnz+1] left-looking update ranges per U slot
+  const int* upd_tgt;    // targets in the column being factorized
+  const int* lrow_ptr;   // [n+1] strictly lower part by rows
+  const int* lrow_slot;
+  const int* lrow_col;
+  const int* urow_ptr;   // [n+1] strictly upper part by rows
+  const int* urow_slot;
+  const int* urow_col;
+  const int* row_orig;   // [n]
+  const int* col_orig;   // [n]
+  // A's own pattern (caller order) for the FP64 residual.
+  const int* a_rowptr;   // [n+1]
+  const int* a_colidx;   // [nnz_a]
+  // Level sets: start_chains / columns on the device (start_levels host-side).
+  const int* lu_sc; const int* lu_cols;
+  const int* l_sc;  const int* l_cols;
+  const int* u_sc;  const int* u_cols;
+  const int* lt_sc; const int* lt_cols;
+};
+
+struct DevStatus {
+  int code;      // 0 or first error code
+  int column;
+  int scenario;
+  int pad;
+};
+
+__device__ __forceinline__ void report_error(DevStatus* st, int code, int col, int s) {
+  if (atomicCAS(&st->code, 0, code) == 0) {
+    st->column = col;
+    st->scenario = s;
+  }
+}
+
+// Loads of values written by other blocks of the same launch bypass L1
+// (persistent kernel); in per-level launches a plain load is equally safe.
+template <typename T>
+__device__ __forceinline__ T ldv(const T* p) { return __ldcg(p); }
+
+// ----------------------------------------------------------------------------
+// (a) scatter: LU(q, s) = A(slot_src[q], s), zero at fill slots.
+template <typename T>
+__global__ void k_scatter(const int* __restrict__ slot_src, int nnz, int ld, int S,
+                          const double* __restrict__ a, T* __restrict__ v) {
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t total = (int64_t)nnz * ld;
+  for (int64_t e = tid; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int q = (int)(e / ld);
+    const int s = (int)(e - (int64_t)q * ld);
+    const int src = slot_src[q];
+    T val = T(0);
+    if (src >= 0 && s < S) val = (T)a[(int64_t)src * ld + s];
+    v[e] = val;
+  }
+}
+
+// ----------------------------------------------------------------------------
+// (b) left-looking GLU column k for scenario s.
+//   for every U slot p of column k (rows j < k, ascending):
+//     u = U(j,k); for every L slot q of column j: M(i,k) -= L(i,j) * u
+//   then L(:,k) /= U(k,k).
+// Same arithmetic as factorize_one_column_GLU_CSC_CPU
+// (GLU_CSC_CPU_levels_strings.cpp:3-63), applied in gather order.
+template <typename T>
+__device__ __forceinline__ void refactor_column(const DevStruct& d, int k, int s, int ld,
+                                                T* __restrict__ v, double pivot_tol,
+                                                DevStatus* st) {
+  const int c0 = d.colptr[k], dk = d.diag[k], c1 = d.colptr[k + 1];
+  for (int p = c0; p < dk; p++) {
+    const int j = d.csc_row[p];
+    const T u = ldv(v + (int64_t)p * ld + s);
+    const int q0 = d.diag[j] + 1, q1 = d.colptr[j + 1];
+    const int* tg = d.upd_tgt + d.upd_ptr[p] - q0;
+    for (int q = q0; q < q1; q++) {
+      T* tp = v + (int64_t)tg[q] * ld + s;
+      *tp = ldv(tp) - ldv(v + (int64_t)q * ld + s) * u;
+    }
+  }
+  const T piv = ldv(v + (int64_t)dk * ld + s);
+  if (!(fabs((double)piv) >= pivot_tol)) report_error(st, 3, k, s);
+  for (int q = dk + 1; q < c1; q++) {
+    T* tp = v + (int64_t)q * ld + s;
+    *tp = ldv(tp) / piv;
+  }
+}
+
+// One LU level: threads = chains_in_level * ld, scenario fastest.
+template <typename T>
+__global__ void k_refactor_level(DevStruct d, T* __restrict__ v, int ld, int S,
+                                 int chain_begin, int chain_end, double pivot_tol,
+                                 DevStatus* st) {
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = chain_begin + (int)(tid / ld);
+  const int s = (int)(tid % ld);
+  if (c >= chain_end || s >= S) return;
+  for (int t = d.lu_sc[c]; t < d.lu_sc[c + 1]; t++)
+    refactor_column<T>(d, d.lu_cols[t], s, ld, v, pivot_tol, st);
+}
+
+// ----------------------------------------------------------------------------
+// (c) triangular solves, gather form (no atomics).
+// kind 0: L y = b, rows by L levels       (Process_Column_L_CSC, GLU_CSC_CPU_Triangular.cpp:3-12)
+// kind 1: U x = y, rows by U levels       (Process_Column_U_CSC, :14-25)
+// kind 2: U^T z = b, columns by LU levels (adjoint, first half)
+// kind 3: L^T w = z, columns by LT levels (adjoint, second half)
+template <typename T, int KIND>
+__device__ __forceinline__ void solve_unknown(const DevStruct& d, int i, int s, int ld,
+                                              const T* __restrict__ v, T* __restrict__ x) {
+  T acc = ldv(x + (int64_t)i * ld + s);
+  if (KIND == 0) {
+    for (int e = d.lrow_ptr[i]; e < d.lrow_ptr[i + 1]; e++)
+      acc -= ldv(v + (int64_t)d.lrow_slot[e] * ld + s) * ldv(x + (int64_t)d.lrow_col[e] * ld + s);
+  } else if (KIND == 1) {
+    for (int e = d.urow_ptr[i]; e < d.urow_ptr[i + 1]; e++)
+      acc -= ldv(v + (int64_t)d.urow_slot[e] * ld + s) * ldv(x + (int64_t)d.urow_col[e] * ld + s);
+    acc /= ldv(v + (int64_t)d.diag[i] * ld + s);
+  } else if (KIND == 2) {
+    const int dg = d.diag[i];
+    for (int p = d.colptr[i]; p < dg; p++)
+      acc -= ldv(v + (int64_t)p * ld + s) * ldv(x + (int64_t)d.csc_row[p] * ld + s);
+    acc /= ldv(v + (int64_t)dg * ld + s);
+  } else {
+    for (int q = d.diag[i] + 1; q < d.colptr[i + 1]; q++)
+      acc -= ldv(v + (int64_t)q * ld + s) * ldv(x + (int64_t)d.csc_row[q] * ld + s);
+  }
+  x[(int64_t)i * ld + s] = acc;
+}
+
+template <typename T, int KIND>
+__global__ void k_solve_level(DevStruct d, const T* __restrict__ v, T* __restrict__ x,
+                              int ld, int S, int chain_begin, int chain_end) {
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = chain_begin + (int)(tid / ld);
+  const int s = (int)(tid % ld);
+  if (c >= chain_end || s >= S) return;
+  const int* sc = KIND == 0 ? d.l_sc : KIND == 1 ? d.u_sc : KIND == 2 ? d.lu_sc : d.lt_sc;
+  const int* cols = KIND == 0 ? d.l_cols : KIND == 1 ? d.u_cols : KIND == 2 ? d.lu_cols : d.lt_cols;
+  for (int t = sc[c]; t < sc[c + 1]; t++) solve_unknown<T, KIND>(d, cols[t], s, ld, v, x);
+}
+
+// ----------------------------------------------------------------------------
+// Permutations between the caller's order and the pivot order.
+// gather:  y[r] = x[perm[r]]        scatter: y[perm[r]] = x[r]
+template <typename TI, typename TO>
+__global__ void k_permute(const int* __restrict__ perm, int n, int ld, int S,
+                          const TI* __restrict__ x, TO* __restrict__ y, int gather) {
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t total = (int64_t)n * ld;
+  for (int64_t e = tid; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int r = (int)(e / ld);
+    const int s = (int)(e - (int64_t)r * ld);
+    if (s >= S) continue;
+    const int pr = perm[r];
+    if (gather) y[e] = (TO)x[(int64_t)pr * ld + s];
+    else y[(int64_t)pr * ld + s] = (TO)x[e];
+  }
+}
+
+// ----------------------------------------------------------------------------
+// Iterative refinement pieces (FP64 residual, FP32 correction).
+// r = b - A x in the caller's order; skipped for converged scenarios.
+__global__ void k_residual(const int* __restrict__ a_rowptr, const int* __restrict__ a_colidx,
+                           int n, int ld, int S, const double* __restrict__ a,
+                           const double* __restrict__ b, const double* __restrict__ x,
+                           const int* __restrict__ done, float* __restrict__ r_perm,
+                           const int* __restrict__ row_pos) {
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t total = (int64_t)n * ld;
+  for (int64_t e = tid; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(e / ld);
+    const int s = (int)(e - (int64_t)i * ld);
+    if (s >= S || done[s]) continue;
+    double acc = b[e];
+    for (int p = a_rowptr[i]; p < a_rowptr[i + 1]; p++)
+      acc -= a[(int64_t)p * ld + s] * x[(int64_t)a_colidx[p] * ld + s];
+    // Row i of J is row row_pos[i] of the pivot-ordered system.
+    r_perm[(int64_t)row_pos[i] * ld + s] = (float)acc;
+  }
+}
+
+// x[col_orig[c]] += dx[c]; per-scenario max |dx| and max |x| (non-negative
+// doubles order like their bit patterns, so atomicMax on the bits works).
+__global__ void k_ir_update(const int* __restrict__ col_orig, int n, int ld, int S,
+                            const float* __restrict__ dx, double* __restrict__ x,
+                            const int* __restrict__ done,
+                            unsigned long long* __restrict__ max_dx,
+                            unsigned long long* __restrict__ max_x) {
+  // block = (32 scenarios) x (8 rows); grid-stride over row tiles.
+  const int s = blockIdx.y * 32 + threadIdx.x;
+  __shared__ double sdx[8][33], sx[8][33];
+  double mdx = 0.0, mx = 0.0;
+  if (s < S && !done[s]) {
+    for (int c = blockIdx.x * 8 + threadIdx.y; c < n; c += gridDim.x * 8) {
+      const double d = (double)dx[(int64_t)c * ld + s];
+      double* xp = x + (int64_t)col_orig[c] * ld + s;
+      const double nx = *xp + d;
+      *xp = nx;
+      mdx = fmax(mdx, fabs(d));
+      mx = fmax(mx, fabs(nx));
+    }
+  }
+  sdx[threadIdx.y][threadIdx.x] = mdx;
+  sx[threadIdx.y][threadIdx.x] = mx;
+  __syncthreads();
+  if (threadIdx.y == 0 && s < S) {
+    for (int k = 1; k < 8; k++) {
+      mdx = fmax(mdx, sdx[k][threadIdx.x]);
+      mx = fmax(mx, sx[k][threadIdx.x]);
+    }
+    atomicMax(max_dx + s, (unsigned long long)__double_as_longlong(mdx));
+    atomicMax(max_x + s, (unsigned long long)__double_as_longlong(mx));
+  }
+}
+
+// Convergence bookkeeping after sweep `sweep` (1-based).
+__global__ void k_ir_check(int S, int sweep, int last_sweep, double tol, int* done,
+                           int* sweeps_out, unsigned long long* max_dx,
+                           unsigned long long* max_x) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= S || done[s]) return;
+  const double mdx = __longlong_as_double((long long)max_dx[s]);
+  const double mx = __longlong_as_double((long long)max_x[s]);
+  max_dx[s] = 0ull;
+  max_x[s] = 0ull;
+  const bool ok = mdx <= tol * mx;
+  if (ok) {
+    done[s] = 1;
+    if (sweeps_out) sweeps_out[s] = sweep;
+  } else if (sweep == last_sweep) {
+    if (sweeps_out) sweeps_out[s] = -1;
+  }
+}
+
+}  // namespace pvglu

@@ -1,0 +1,169 @@
+"""Python view of the pvglu C ABI.
+
+`Symbolic` mirrors the reference's `prepare_matrices`
+(PVPP_Plant_Simulator/000_PVPP_simulator.cpp:10-93) and exposes the arrays of
+`struct_CPU_CUDA_arrays` (factorize_electrical_system.h:3-61).  `Numeric`
+owns the device state and runs the hot path: `scatter` (fill_values_CSC_only,
+010_create_CSR_CSC.cpp:142-155), `refactor` (factorize_electrical_system_CUDA,
+factorize_electrical_system_CUDA.cu:61-152) and `solve`
+(triangular_substitution_LU_CUDA, triangular_substitution.cu:232-271).
+Device buffers are torch CUDA tensors passed by pointer; torch is plumbing
+only, every computation runs in libpvglu.so.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _native as N
+
+SYMBOLIC_ARRAYS = (
+    "perm_amd", "perm_rows", "row_orig", "col_orig", "fill_rowptr", "fill_col",
+    "csr_rowptr", "csr_col", "csc_colptr", "csc_row", "csr_to_csc", "csc_to_csr",
+    "csr_diag_start", "csc_diag_start", "lu_sl", "lu_sc", "lu_cols", "l_sl", "l_sc",
+    "l_cols", "u_sl", "u_sc", "u_cols", "lt_sl", "lt_sc", "lt_cols",
+    "max_elements_per_column", "slot_src", "diag_slot", "a_rowptr", "a_colidx",
+)
+
+
+def _stream_ptr(stream) -> C.c_void_p:
+    if stream is None:
+        return C.c_void_p(0)
+    if isinstance(stream, int):
+        return C.c_void_p(stream)
+    return C.c_void_p(stream.cuda_stream)
+
+
+def _ptr(t) -> C.c_void_p:
+    if t is None:
+        return C.c_void_p(0)
+    if isinstance(t, np.ndarray):
+        return C.c_void_p(t.ctypes.data)
+    return C.c_void_p(t.data_ptr())
+
+
+class Symbolic:
+    """Host symbolic analysis of one Jacobian pattern (caller's unknown order)."""
+
+    def __init__(self, rowptr, colidx, perm=None):
+        rowptr = np.ascontiguousarray(rowptr, dtype=np.int32)
+        colidx = np.ascontiguousarray(colidx, dtype=np.int32)
+        n = len(rowptr) - 1
+        self._keep = [rowptr, colidx]
+        p = None
+        if perm is not None:
+            p = np.ascontiguousarray(perm, dtype=np.int32)
+            self._keep.append(p)
+        h = C.c_void_p()
+        N.check(N.lib().pvglu_symbolic_create(n, _ptr(rowptr), _ptr(colidx), _ptr(p),
+                                              C.byref(h)), "pvglu_symbolic_create")
+        self.handle = h
+        info = N.SymbolicInfo()
+        N.check(N.lib().pvglu_symbolic_get_info(h, C.byref(info)), "pvglu_symbolic_get_info")
+        self.info = {f: getattr(info, f) for f, _ in N.SymbolicInfo._fields_}
+        self.n = info.n
+        self.nnz_a = info.nnz_a
+        self.nnz_lu = info.nnz_lu
+
+    def array(self, name: str) -> np.ndarray:
+        ptr = C.POINTER(C.c_int)()
+        ln = C.c_int64()
+        N.check(N.lib().pvglu_symbolic_get_array(self.handle, name.encode(), C.byref(ptr),
+                                                 C.byref(ln)), "pvglu_symbolic_get_array")
+        if ln.value == 0:
+            return np.zeros(0, dtype=np.int32)
+        return np.ctypeslib.as_array(ptr, shape=(ln.value,)).copy()
+
+    def arrays(self) -> dict[str, np.ndarray]:
+        return {k: self.array(k) for k in SYMBOLIC_ARRAYS}
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h and N._lib is not None:
+            N.lib().pvglu_symbolic_destroy(h)
+            self.handle = None
+
+
+class Numeric:
+    """Device LU state for `n_scenarios` Jacobians sharing one `Symbolic`."""
+
+    def __init__(self, sym: Symbolic, n_scenarios: int = 1, precision: int = N.FP64,
+                 schedule: int = N.SCHED_LEVELS):
+        self.sym = sym
+        h = C.c_void_p()
+        N.check(N.lib().pvglu_numeric_create(sym.handle, n_scenarios, precision, C.byref(h)),
+                "pvglu_numeric_create")
+        self.handle = h
+        self.S = n_scenarios
+        self.ld = N.lib().pvglu_numeric_ld(h)
+        self.precision = precision
+        self.set_schedule(schedule)
+
+    def set_schedule(self, schedule: int) -> None:
+        N.check(N.lib().pvglu_numeric_set_schedule(self.handle, schedule),
+                "pvglu_numeric_set_schedule")
+        self.schedule = schedule
+
+    def set_pivot_tol(self, tol: float) -> None:
+        N.check(N.lib().pvglu_numeric_set_pivot_tol(self.handle, tol), "pvglu_numeric_set_pivot_tol")
+
+    def values_ptr(self) -> int:
+        return N.lib().pvglu_numeric_values(self.handle)
+
+    def scatter(self, a_values, stream=None) -> None:
+        N.check(N.lib().pvglu_scatter(self.handle, _ptr(a_values), _stream_ptr(stream)),
+                "pvglu_scatter")
+
+    def refactor(self, stream=None) -> None:
+        N.check(N.lib().pvglu_refactor(self.handle, _stream_ptr(stream)), "pvglu_refactor")
+
+    def solve(self, x, transpose: bool = False, original: bool = False, stream=None) -> None:
+        flags = (N.SOLVE_TRANSPOSE if transpose else 0) | (N.SOLVE_ORIGINAL if original else 0)
+        N.check(N.lib().pvglu_solve(self.handle, _ptr(x), flags, _stream_ptr(stream)),
+                "pvglu_solve")
+
+    def solve_refined(self, a_values, b, x, tol=1e-12, max_sweeps=10, sweeps=None,
+                      stream=None) -> None:
+        N.check(N.lib().pvglu_solve_refined(self.handle, _ptr(a_values), _ptr(b), _ptr(x),
+                                            float(tol), int(max_sweeps), _ptr(sweeps),
+                                            _stream_ptr(stream)), "pvglu_solve_refined")
+
+    def check(self, stream=None) -> tuple[int, int, int]:
+        code, col, sc = C.c_int(), C.c_int(), C.c_int()
+        N.check(N.lib().pvglu_numeric_check(self.handle, _stream_ptr(stream), C.byref(code),
+                                            C.byref(col), C.byref(sc)), "pvglu_numeric_check")
+        return code.value, col.value, sc.value
+
+    def refactor_host(self, csc_values: np.ndarray) -> None:
+        N.check(N.lib().pvglu_refactor_host(self.handle, _ptr(csc_values)), "pvglu_refactor_host")
+
+    def solve_host(self, b: np.ndarray) -> None:
+        N.check(N.lib().pvglu_solve_host(self.handle, _ptr(b)), "pvglu_solve_host")
+
+    def scatter_refactor_solve_host(self, a_values, b, x, stream=None) -> None:
+        N.check(N.lib().pvglu_scatter_refactor_solve_host(self.handle, _ptr(a_values), _ptr(b),
+                                                          _ptr(x), _stream_ptr(stream)),
+                "pvglu_scatter_refactor_solve_host")
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h and N._lib is not None:
+            N.lib().pvglu_numeric_destroy(h)
+            self.handle = None
+
+
+# Names of the reference's entry points, for callers porting a driver.
+def prepare_matrices(rowptr, colidx, perm=None) -> Symbolic:
+    """prepare_matrices (000_PVPP_simulator.cpp:10-93)."""
+    return Symbolic(rowptr, colidx, perm)
+
+
+def factorize_electrical_system_CUDA(num: Numeric, stream=None) -> None:  # noqa: N802
+    """factorize_electrical_system_CUDA (factorize_electrical_system_CUDA.cu:61-152)."""
+    num.refactor(stream)
+
+
+def triangular_substitution_LU_CUDA(num: Numeric, solution, stream=None) -> None:  # noqa: N802
+    """triangular_substitution_LU_CUDA (triangular_substitution.cu:232-271); permuted space."""
+    num.solve(solution, stream=stream)
