@@ -173,6 +173,25 @@ int pvglu_solve_refined(pvglu_numeric* h, const double* a_values, const double* 
                         double* x, double tol, int max_sweeps, int* sweeps_out,
                         void* stream);
 
+/* Host-buffer form of one refined linear step on an FP32 handle: H2D of A's
+ * values ([nnz_a * ld], FP64) and b ([n * ld], FP64, original order),
+ * scatter, FP32 refactor, pvglu_solve_refined, D2H of x ([n * ld], FP64).
+ * sweeps_out: device int[ld] or NULL.  Asynchronous on `stream`. */
+int pvglu_refine_system_host(pvglu_numeric* h, const double* a_values_host,
+                             const double* b_host, double* x_host, double tol, int max_sweeps,
+                             int* sweeps_out, void* stream);
+
+/* ---------------- failure-path self-test --------------------------------- */
+
+/* Runs one bounded grid barrier that waits for one block more than it
+ * launches, so that it can only end by its spin limit (max_spins polls of
+ * ~64 ns; at most 2^24).  Synchronous.  status_code receives the recorded
+ * status (PVGLU_ERR_BARRIER_TIMEOUT expected), blocks_returned the number of
+ * blocks that came back reporting the abort.  No reference counterpart: the
+ * reference has no bounded waits (it aborts, gpu_util.h:39-47). */
+int pvglu_selftest_barrier_timeout(int blocks, long long max_spins, int* status_code,
+                                   int* blocks_returned);
+
 #ifdef __cplusplus
 }
 #endif

@@ -57,6 +57,7 @@ struct pvglu_numeric {
   void* work = nullptr;         // [n * ld] T
   double* work64 = nullptr;     // [nnz_a * ld] staging / [n * ld] vectors
   double* b64 = nullptr;        // [n * ld]
+  double* x64 = nullptr;        // [n * ld]
   int* row_pos = nullptr;       // inverse of row_orig
   pvglu::DevStatus* status = nullptr;
   int* ir_done = nullptr;
@@ -111,32 +112,35 @@ int refactor_levels(pvglu_numeric* h, cudaStream_t st) {
 }
 
 template <typename T, int KIND>
-void solve_phase(pvglu_numeric* h, const std::vector<int>& sl, T* x, cudaStream_t st) {
+void solve_phase(pvglu_numeric* h, const std::vector<int>& sl, T* x, const int* done,
+                 cudaStream_t st) {
   const T* v = static_cast<const T*>(h->values);
   for (size_t lv = 0; lv + 1 < sl.size(); lv++) {
     const int cb = sl[lv], ce = sl[lv + 1];
     const int64_t threads = (int64_t)(ce - cb) * h->ld;
     pvglu::k_solve_level<T, KIND><<<launch_blocks(threads, 128), 128, 0, st>>>(
-        h->d, v, x, h->ld, h->S, cb, ce);
+        h->d, v, x, h->ld, h->S, cb, ce, done);
   }
 }
 
+// skip: per-scenario convergence flags of iterative refinement (or none).
 template <typename T>
-int solve_permuted(pvglu_numeric* h, T* x, bool transpose, cudaStream_t st) {
+int solve_permuted(pvglu_numeric* h, T* x, bool transpose, cudaStream_t st,
+                   pvglu::SkipDone skip = pvglu::SkipDone{nullptr, nullptr}) {
   if (h->schedule == PVGLU_SCHED_PERSISTENT) {
     const int st_code = pvglu::launch_persistent<T>(
         h->plan, h->d, static_cast<T*>(h->values), x, h->ld, h->S, h->pivot_tol,
         h->status, h->barrier, h->persistent_grid,
-        transpose ? pvglu::PHASE_SOLVE_T : pvglu::PHASE_SOLVE, st);
+        transpose ? pvglu::PHASE_SOLVE_T : pvglu::PHASE_SOLVE, st, skip);
     if (st_code) return fail(PVGLU_ERR_CUDA, "persistent solve launch failed");
     return PVGLU_OK;
   }
   if (!transpose) {
-    solve_phase<T, 0>(h, h->l_sl, x, st);
-    solve_phase<T, 1>(h, h->u_sl, x, st);
+    solve_phase<T, 0>(h, h->l_sl, x, skip.done, st);
+    solve_phase<T, 1>(h, h->u_sl, x, skip.done, st);
   } else {
-    solve_phase<T, 2>(h, h->lu_sl, x, st);
-    solve_phase<T, 3>(h, h->lt_sl, x, st);
+    solve_phase<T, 2>(h, h->lu_sl, x, skip.done, st);
+    solve_phase<T, 3>(h, h->lt_sl, x, skip.done, st);
   }
   PVGLU_CUDA(cudaGetLastError());
   return PVGLU_OK;
@@ -303,8 +307,9 @@ int pvglu_numeric_create(const pvglu_symbolic* sym, int n_scenarios, int precisi
   rc |= h->alloc((size_t)h->n * h->ld * es, (char**)&h->work);
   rc |= h->alloc((size_t)std::max(h->nnz_a, h->n) * h->ld, &h->work64);
   rc |= h->alloc((size_t)h->n * h->ld, &h->b64);
+  rc |= h->alloc((size_t)h->n * h->ld, &h->x64);
   rc |= h->alloc(1, &h->status);
-  rc |= h->alloc((size_t)h->ld, &h->ir_done);
+  rc |= h->alloc((size_t)h->ld + 1, &h->ir_done);  // [ld] flags + converged count
   rc |= h->alloc((size_t)h->ld, &h->ir_max_dx);
   rc |= h->alloc((size_t)h->ld, &h->ir_max_x);
   rc |= h->alloc(4, &h->barrier);
@@ -460,6 +465,55 @@ int pvglu_scatter_refactor_solve_host(pvglu_numeric* h, const double* a_values_h
   return PVGLU_OK;
 }
 
+int pvglu_refine_system_host(pvglu_numeric* h, const double* a_values_host,
+                             const double* b_host, double* x_host, double tol, int max_sweeps,
+                             int* sweeps_out, void* stream) {
+  if (!h || !a_values_host || !b_host || !x_host || h->precision != PVGLU_FP32)
+    return fail(PVGLU_ERR_BAD_ARG, "needs an FP32 handle and non-NULL buffers");
+  cudaStream_t st = as_stream(stream);
+  double* a = h->work64;
+  PVGLU_CUDA(cudaMemcpyAsync(a, a_values_host, (size_t)h->nnz_a * h->ld * sizeof(double),
+                             cudaMemcpyHostToDevice, st));
+  PVGLU_CUDA(cudaMemcpyAsync(h->b64, b_host, (size_t)h->n * h->ld * sizeof(double),
+                             cudaMemcpyHostToDevice, st));
+  int rc = pvglu_scatter(h, a, stream);
+  if (!rc) rc = pvglu_refactor(h, stream);
+  if (!rc) rc = pvglu_solve_refined(h, a, h->b64, h->x64, tol, max_sweeps, sweeps_out, stream);
+  if (rc) return rc;
+  PVGLU_CUDA(cudaMemcpyAsync(x_host, h->x64, (size_t)h->n * h->ld * sizeof(double),
+                             cudaMemcpyDeviceToHost, st));
+  return PVGLU_OK;
+}
+
+int pvglu_selftest_barrier_timeout(int blocks, long long max_spins, int* status_code,
+                                   int* blocks_returned) {
+  if (blocks <= 0 || blocks > 4096 || max_spins <= 0 || max_spins > (1LL << 24) ||
+      !status_code || !blocks_returned)
+    return fail(PVGLU_ERR_BAD_ARG, "bad self-test arguments");
+  unsigned int* bar = nullptr;
+  pvglu::DevStatus* st = nullptr;
+  int* passed = nullptr;
+  PVGLU_CUDA(cudaMalloc((void**)&bar, 4 * sizeof(unsigned int)));
+  PVGLU_CUDA(cudaMalloc((void**)&st, sizeof(pvglu::DevStatus)));
+  PVGLU_CUDA(cudaMalloc((void**)&passed, sizeof(int)));
+  PVGLU_CUDA(cudaMemset(bar, 0, 4 * sizeof(unsigned int)));
+  PVGLU_CUDA(cudaMemset(st, 0, sizeof(pvglu::DevStatus)));
+  PVGLU_CUDA(cudaMemset(passed, 0, sizeof(int)));
+  void* args[] = {(void*)&bar, (void*)&st, (void*)&max_spins, (void*)&passed};
+  cudaError_t e = cudaLaunchCooperativeKernel((const void*)pvglu::k_barrier_timeout_probe,
+                                              dim3(blocks), dim3(64), args, 0, nullptr);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  pvglu::DevStatus hs{};
+  if (e == cudaSuccess) e = cudaMemcpy(&hs, st, sizeof(hs), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(blocks_returned, passed, sizeof(int), cudaMemcpyDeviceToHost);
+  cudaFree(bar);
+  cudaFree(st);
+  cudaFree(passed);
+  if (e != cudaSuccess) return fail(PVGLU_ERR_CUDA, cudaGetErrorString(e));
+  *status_code = hs.code;
+  return PVGLU_OK;
+}
+
 int pvglu_solve_refined(pvglu_numeric* h, const double* a_values, const double* b,
                         double* x, double tol, int max_sweeps, int* sweeps_out,
                         void* stream) {
@@ -470,21 +524,23 @@ int pvglu_solve_refined(pvglu_numeric* h, const double* a_values, const double* 
   const int64_t nv = (int64_t)h->n * h->ld;
   float* w = static_cast<float*>(h->work);
   PVGLU_CUDA(cudaMemsetAsync(x, 0, nv * sizeof(double), st));
-  PVGLU_CUDA(cudaMemsetAsync(h->ir_done, 0, h->ld * sizeof(int), st));
+  int* ndone = h->ir_done + h->ld;
+  PVGLU_CUDA(cudaMemsetAsync(h->ir_done, 0, (h->ld + 1) * sizeof(int), st));
   PVGLU_CUDA(cudaMemsetAsync(h->ir_max_dx, 0, h->ld * sizeof(unsigned long long), st));
   PVGLU_CUDA(cudaMemsetAsync(h->ir_max_x, 0, h->ld * sizeof(unsigned long long), st));
   if (sweeps_out) PVGLU_CUDA(cudaMemsetAsync(sweeps_out, 0, h->ld * sizeof(int), st));
+  const pvglu::SkipDone skip{h->ir_done, ndone};
   for (int sweep = 1; sweep <= max_sweeps; sweep++) {
     pvglu::k_residual<<<launch_blocks(nv, 256), 256, 0, st>>>(
         h->d.a_rowptr, h->d.a_colidx, h->n, h->ld, h->S, a_values, b, x, h->ir_done, w,
         h->row_pos);
-    int rc = solve_permuted<float>(h, w, false, st);
+    int rc = solve_permuted<float>(h, w, false, st, skip);
     if (rc) return rc;
     dim3 blk(32, 8), grd((unsigned)std::min(1024, (h->n + 7) / 8), (unsigned)(h->ld + 31) / 32);
     pvglu::k_ir_update<<<grd, blk, 0, st>>>(h->d.col_orig, h->n, h->ld, h->S, w, x,
                                             h->ir_done, h->ir_max_dx, h->ir_max_x);
     pvglu::k_ir_check<<<(h->S + 127) / 128, 128, 0, st>>>(h->S, sweep, max_sweeps, tol,
-                                                          h->ir_done, sweeps_out,
+                                                          h->ir_done, ndone, sweeps_out,
                                                           h->ir_max_dx, h->ir_max_x);
   }
   PVGLU_CUDA(cudaGetLastError());

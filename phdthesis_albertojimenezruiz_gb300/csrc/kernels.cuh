@@ -158,11 +158,12 @@ __device__ __forceinline__ void solve_unknown(const DevStruct& d, int i, int s, 
 
 template <typename T, int KIND>
 __global__ void k_solve_level(DevStruct d, const T* __restrict__ v, T* __restrict__ x,
-                              int ld, int S, int chain_begin, int chain_end) {
+                              int ld, int S, int chain_begin, int chain_end,
+                              const int* __restrict__ done) {
   const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int c = chain_begin + (int)(tid / ld);
   const int s = (int)(tid % ld);
-  if (c >= chain_end || s >= S) return;
+  if (c >= chain_end || s >= S || (done && done[s])) return;
   const int* sc = KIND == 0 ? d.l_sc : KIND == 1 ? d.u_sc : KIND == 2 ? d.lu_sc : d.lt_sc;
   const int* cols = KIND == 0 ? d.l_cols : KIND == 1 ? d.u_cols : KIND == 2 ? d.lu_cols : d.lt_cols;
   for (int t = sc[c]; t < sc[c + 1]; t++) solve_unknown<T, KIND>(d, cols[t], s, ld, v, x);
@@ -244,7 +245,7 @@ __global__ void k_ir_update(const int* __restrict__ col_orig, int n, int ld, int
 
 // Convergence bookkeeping after sweep `sweep` (1-based).
 __global__ void k_ir_check(int S, int sweep, int last_sweep, double tol, int* done,
-                           int* sweeps_out, unsigned long long* max_dx,
+                           int* ndone, int* sweeps_out, unsigned long long* max_dx,
                            unsigned long long* max_x) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= S || done[s]) return;
@@ -255,6 +256,7 @@ __global__ void k_ir_check(int S, int sweep, int last_sweep, double tol, int* do
   const bool ok = mdx <= tol * mx;
   if (ok) {
     done[s] = 1;
+    atomicAdd(ndone, 1);
     if (sweeps_out) sweeps_out[s] = sweep;
   } else if (sweep == last_sweep) {
     if (sweeps_out) sweeps_out[s] = -1;

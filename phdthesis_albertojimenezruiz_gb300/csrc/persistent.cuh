@@ -65,7 +65,10 @@ inline PersistentPlan make_plan(const Symbolic& s, std::vector<void*>& allocs, i
 
 // Bounded sense-by-generation grid barrier.  bar[0] = arrivals, bar[1] =
 // generation, bar[2] = abort word.  Returns false when the launch must stop.
-__device__ __forceinline__ bool grid_barrier(unsigned int* bar, DevStatus* st) {
+// `expected` is the number of arriving blocks (gridDim.x in every production
+// launch; the timeout self-test asks for one more block than exists).
+__device__ __forceinline__ bool grid_barrier(unsigned int* bar, DevStatus* st,
+                                             unsigned int expected, long long max_spins) {
   __shared__ int ok;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -75,7 +78,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned int* bar, DevStatus* st) {
     __threadfence();
     const unsigned int arrived = atomicAdd(bar, 1u) + 1u;
     int good = 1;
-    if (arrived == gridDim.x) {
+    if (arrived == expected) {
       atomicExch(bar, 0u);
       __threadfence();
       atomicAdd(bar + 1, 1u);
@@ -86,7 +89,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned int* bar, DevStatus* st) {
           good = 0;
           break;
         }
-        if (++spins > kBarrierMaxSpins) {
+        if (++spins > max_spins) {
           report_error(st, 6, -1, -1);
           atomicExch(bar + 2, 1u);
           good = 0;
@@ -102,59 +105,69 @@ __device__ __forceinline__ bool grid_barrier(unsigned int* bar, DevStatus* st) {
   return ok != 0;
 }
 
+// Scenario skipping for iterative refinement: done[s] != 0 skips scenario s;
+// *ndone >= S (read once at entry, identical for every block) skips the
+// launch.  Both NULL outside refinement.
+struct SkipDone {
+  const int* done;
+  const int* ndone;
+};
+
+// One phase (a level set) of the persistent walk.  A barrier precedes every
+// level except the very first one of the launch (*need_sync false).
+// KIND -1 = refactorization, 0..3 = solve kinds of solve_unknown.
+template <typename T, int KIND>
+__device__ __forceinline__ bool run_phase(const int* sl, int nl, const int* sc, const int* cols,
+                                          const DevStruct& d, T* __restrict__ v,
+                                          T* __restrict__ x, int ld, int S, double pivot_tol,
+                                          DevStatus* st, unsigned int* bar, const int* done,
+                                          bool* need_sync) {
+  const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
+  const int64_t gtid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  for (int lv = 0; lv < nl; lv++) {
+    if (*need_sync && !grid_barrier(bar, st, gridDim.x, kBarrierMaxSpins)) return false;
+    *need_sync = true;
+    const int cb = sl[lv], ce = sl[lv + 1];
+    const int64_t items = (int64_t)(ce - cb) * ld;
+    for (int64_t it = gtid; it < items; it += nthreads) {
+      const int c = cb + (int)(it / ld);
+      const int s = (int)(it % ld);
+      if (s >= S || (done && done[s])) continue;
+      for (int t = sc[c]; t < sc[c + 1]; t++) {
+        if constexpr (KIND < 0) refactor_column<T>(d, cols[t], s, ld, v, pivot_tol, st);
+        else solve_unknown<T, KIND>(d, cols[t], s, ld, v, x);
+      }
+    }
+  }
+  return true;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kPersistentBlock)
 k_persistent(PersistentPlan plan, DevStruct d, T* __restrict__ v, T* __restrict__ x,
              int ld, int S, double pivot_tol, DevStatus* st, unsigned int* bar,
-             int phases) {
-  const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
-  const int64_t gtid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  bool first = true;
-  auto sync = [&]() -> bool {
-    if (first) {
-      first = false;
-      return true;
-    }
-    return grid_barrier(bar, st);
-  };
-  if (phases & PHASE_REFACTOR) {
-    for (int lv = 0; lv < plan.lu_nl; lv++) {
-      if (!sync()) return;
-      const int cb = plan.lu_sl[lv], ce = plan.lu_sl[lv + 1];
-      const int64_t items = (int64_t)(ce - cb) * ld;
-      for (int64_t it = gtid; it < items; it += nthreads) {
-        const int c = cb + (int)(it / ld);
-        const int s = (int)(it % ld);
-        if (s >= S) continue;
-        for (int t = d.lu_sc[c]; t < d.lu_sc[c + 1]; t++)
-          refactor_column<T>(d, d.lu_cols[t], s, ld, v, pivot_tol, st);
-      }
-    }
-  }
-  auto run_solve = [&](const int* sl, int nl, auto kind_tag) -> bool {
-    constexpr int KIND = decltype(kind_tag)::value;
-    const int* sc = KIND == 0 ? d.l_sc : KIND == 1 ? d.u_sc : KIND == 2 ? d.lu_sc : d.lt_sc;
-    const int* cols = KIND == 0 ? d.l_cols : KIND == 1 ? d.u_cols : KIND == 2 ? d.lu_cols : d.lt_cols;
-    for (int lv = 0; lv < nl; lv++) {
-      if (!sync()) return false;
-      const int cb = sl[lv], ce = sl[lv + 1];
-      const int64_t items = (int64_t)(ce - cb) * ld;
-      for (int64_t it = gtid; it < items; it += nthreads) {
-        const int c = cb + (int)(it / ld);
-        const int s = (int)(it % ld);
-        if (s >= S) continue;
-        for (int t = sc[c]; t < sc[c + 1]; t++) solve_unknown<T, KIND>(d, cols[t], s, ld, v, x);
-      }
-    }
-    return true;
-  };
+             int phases, SkipDone skip) {
+  if (skip.ndone && __ldcg(skip.ndone) >= S) return;
+  bool need_sync = false;
+  if (phases & PHASE_REFACTOR)
+    if (!run_phase<T, -1>(plan.lu_sl, plan.lu_nl, d.lu_sc, d.lu_cols, d, v, x, ld, S,
+                          pivot_tol, st, bar, nullptr, &need_sync))
+      return;
   if (phases & PHASE_SOLVE) {
-    if (!run_solve(plan.l_sl, plan.l_nl, std::integral_constant<int, 0>())) return;
-    if (!run_solve(plan.u_sl, plan.u_nl, std::integral_constant<int, 1>())) return;
+    if (!run_phase<T, 0>(plan.l_sl, plan.l_nl, d.l_sc, d.l_cols, d, v, x, ld, S, pivot_tol,
+                         st, bar, skip.done, &need_sync))
+      return;
+    if (!run_phase<T, 1>(plan.u_sl, plan.u_nl, d.u_sc, d.u_cols, d, v, x, ld, S, pivot_tol,
+                         st, bar, skip.done, &need_sync))
+      return;
   }
   if (phases & PHASE_SOLVE_T) {
-    if (!run_solve(plan.lu_sl, plan.lu_nl, std::integral_constant<int, 2>())) return;
-    if (!run_solve(plan.lt_sl, plan.lt_nl, std::integral_constant<int, 3>())) return;
+    if (!run_phase<T, 2>(plan.lu_sl, plan.lu_nl, d.lu_sc, d.lu_cols, d, v, x, ld, S,
+                         pivot_tol, st, bar, skip.done, &need_sync))
+      return;
+    if (!run_phase<T, 3>(plan.lt_sl, plan.lt_nl, d.lt_sc, d.lt_cols, d, v, x, ld, S,
+                         pivot_tol, st, bar, skip.done, &need_sync))
+      return;
   }
 }
 
@@ -176,17 +189,27 @@ int persistent_grid() {
 template <typename T>
 int launch_persistent(const PersistentPlan& plan, const DevStruct& d, T* v, T* x, int ld,
                       int S, double pivot_tol, DevStatus* st, unsigned int* bar,
-                      int max_grid, int phases, cudaStream_t stream) {
+                      int max_grid, int phases, cudaStream_t stream,
+                      SkipDone skip = SkipDone{nullptr, nullptr}) {
   if (max_grid <= 0) return 1;
   const int64_t want = ((int64_t)plan.max_chains * ld + kPersistentBlock - 1) / kPersistentBlock;
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(want, max_grid));
   if (cudaMemsetAsync(bar, 0, 3 * sizeof(unsigned int), stream) != cudaSuccess) return 1;
   void* args[] = {(void*)&plan, (void*)&d, (void*)&v, (void*)&x, (void*)&ld, (void*)&S,
-                  (void*)&pivot_tol, (void*)&st, (void*)&bar, (void*)&phases};
+                  (void*)&pivot_tol, (void*)&st, (void*)&bar, (void*)&phases, (void*)&skip};
   if (cudaLaunchCooperativeKernel((const void*)k_persistent<T>, dim3(grid),
                                   dim3(kPersistentBlock), args, 0, stream) != cudaSuccess)
     return 1;
   return 0;
+}
+
+// Failure-path self-test: one barrier that waits for one block more than the
+// launch has, so the wait can only end by its spin limit.  Every block must
+// come back with PVGLU_ERR_BARRIER_TIMEOUT recorded and the abort word set.
+__global__ void k_barrier_timeout_probe(unsigned int* bar, DevStatus* st, long long max_spins,
+                                        int* passed) {
+  const bool ok = grid_barrier(bar, st, gridDim.x + 1u, max_spins);
+  if (threadIdx.x == 0 && !ok) atomicAdd(passed, 1);
 }
 
 }  // namespace pvglu

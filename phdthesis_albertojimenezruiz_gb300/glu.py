@@ -146,6 +146,13 @@ class Numeric:
                                                           _ptr(x), _stream_ptr(stream)),
                 "pvglu_scatter_refactor_solve_host")
 
+    def refine_system_host(self, a_values, b, x, tol=1e-12, max_sweeps=10, sweeps=None,
+                           stream=None) -> None:
+        N.check(N.lib().pvglu_refine_system_host(self.handle, _ptr(a_values), _ptr(b), _ptr(x),
+                                                 float(tol), int(max_sweeps), _ptr(sweeps),
+                                                 _stream_ptr(stream)),
+                "pvglu_refine_system_host")
+
     def __del__(self):
         h = getattr(self, "handle", None)
         if h and N._lib is not None:

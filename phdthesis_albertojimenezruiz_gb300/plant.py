@@ -106,6 +106,26 @@ class Plant:
                   -self.inc_sign * ieq[self.inc_panel])
         return gpan, ieq, a, b
 
+    def companion_batch(self, g_irr: np.ndarray, v_panel: np.ndarray, ld: int | None = None):
+        """`companion` for S scenarios at once: g_irr, v_panel [n_panels, S].
+
+        Returns A values [nnz_a, ld] and b [n, ld] (columns past S zero)."""
+        npan, S = g_irr.shape
+        ld = ld or S
+        cur, didv = self.panel_iv(self.iph(g_irr).ravel(), v_panel.ravel())
+        gpan = (-didv).reshape(npan, S)
+        ieq = (-cur).reshape(npan, S) - gpan * v_panel
+        counts = np.diff(self.contrib_ptr)
+        entry = np.repeat(np.arange(len(self.a_lin)), counts)
+        a = np.zeros((len(self.a_lin), ld))
+        a[:, :S] = self.a_lin[:, None]
+        np.add.at(a[:, :S], entry, self.contrib_sign[:, None] * gpan[self.contrib_panel])
+        b = np.zeros((self.n, ld))
+        b[:, :S] = self.b_lin[:, None]
+        node = np.repeat(np.arange(self.n), np.diff(self.inc_ptr))
+        np.add.at(b[:, :S], node, -self.inc_sign[:, None] * ieq[self.inc_panel])
+        return a, b
+
     def __del__(self):
         h = getattr(self, "handle", None)
         if h and N._lib is not None:

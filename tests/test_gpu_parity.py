@@ -1,0 +1,272 @@
+"""GPU parity: the sm_103a scatter / refactor / solve kernels against the
+reference's outputs (golden fixtures) and the CPU oracle, through the C ABI.
+
+Tolerances: FP64 factors and solutions 1e-12 componentwise relative (floor
+1e-6 x max|ref|, see conftest.rel_err); FP32 factors + FP64 refinement 1e-10
+normwise relative against the FP64 oracle solution.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import pytest
+from conftest import golden_names, load_golden, rel_err
+
+import matrices as M
+from oracle import oracle as O
+from phdthesis_albertojimenezruiz_gb300 import (FP32, FP64, SCHED_LEVELS, SCHED_PERSISTENT,
+                                                Numeric, Plant, Symbolic)
+from phdthesis_albertojimenezruiz_gb300 import _native as N
+
+pytestmark = pytest.mark.gpu
+SCHEDULES = [SCHED_LEVELS, SCHED_PERSISTENT]
+TOL64 = 1e-12
+
+
+class _DevView:
+    """A CUDA array interface over library-owned device memory."""
+
+    def __init__(self, ptr, shape, typestr):
+        self.__cuda_array_interface__ = {"shape": shape, "typestr": typestr,
+                                         "data": (ptr, False), "version": 3}
+
+
+def values_of(num: Numeric, count: int) -> np.ndarray:
+    import torch
+
+    ts = "<f8" if num.precision == FP64 else "<f4"
+    t = torch.as_tensor(_DevView(num.values_ptr(), (count * num.ld,), ts), device="cuda")
+    torch.cuda.synchronize()
+    return t.cpu().numpy().astype(np.float64).reshape(count, num.ld)
+
+
+def dev(a, dtype=None):
+    import torch
+
+    t = torch.from_numpy(np.ascontiguousarray(a, dtype=dtype)).cuda()
+    return t
+
+
+def pad_cols(a: np.ndarray, ld: int) -> np.ndarray:
+    """[rows, S] -> [rows, ld] (padding columns zero)."""
+    out = np.zeros((a.shape[0], ld))
+    out[:, : a.shape[1]] = a
+    return out
+
+
+def to_perm(g, b):
+    n = len(b)
+    t = np.empty(n)
+    t[np.argsort(g["perm_amd"])] = b
+    w = np.empty(n)
+    w[g["perm_rows"]] = t
+    return w
+
+
+@pytest.mark.parametrize("schedule", SCHEDULES)
+@pytest.mark.parametrize("name", golden_names())
+def test_golden_single_fp64(cuda, name, schedule):
+    import torch
+
+    g = load_golden(name)
+    s = Symbolic(g["rowptr"], g["colidx"], g["perm_amd"])
+    num = Numeric(s, 1, FP64, schedule)
+    nnz = int(s.nnz_lu)
+    num.scatter(dev(g["a"]))
+    assert np.array_equal(values_of(num, nnz)[:, 0], g["csc_in"])  # (a) exact copy
+    num.refactor()
+    assert num.check() == (0, -1, -1)
+    lu = values_of(num, nnz)[:, 0]
+    assert rel_err(lu, g["lu_seq"]) <= TOL64
+    # (c) permuted-space solve: triangular_substitution_LU_CUDA semantics
+    x = dev(to_perm(g, g["b"]))
+    num.solve(x)
+    assert rel_err(x.cpu().numpy(), g["x_perm"]) <= TOL64
+    # original-order solve
+    x = dev(g["b"])
+    num.solve(x, original=True)
+    torch.cuda.synchronize()
+    assert rel_err(x.cpu().numpy(), g["x"]) <= TOL64
+
+
+@pytest.mark.parametrize("schedule", SCHEDULES)
+@pytest.mark.parametrize("name", golden_names())
+def test_transposed_solve_fp64(cuda, name, schedule):
+    g = load_golden(name)
+    s = Symbolic(g["rowptr"], g["colidx"], g["perm_amd"])
+    o = O.Port(g["rowptr"], g["colidx"], g["perm_amd"])
+    num = Numeric(s, 1, FP64, schedule)
+    num.scatter(dev(g["a"]))
+    num.refactor()
+    rng = np.random.default_rng(7)
+    b = rng.uniform(-1, 1, s.n)
+    x = dev(b)
+    num.solve(x, transpose=True)
+    want = o.solve_transposed(g["lu_seq"], b)
+    assert rel_err(x.cpu().numpy(), want) <= TOL64
+    # original order: J^T lam = b
+    import scipy.sparse as sp
+
+    J = sp.csr_matrix((g["a"], g["colidx"], g["rowptr"]), shape=(s.n, s.n))
+    lam = dev(b)
+    num.solve(lam, transpose=True, original=True)
+    lam = lam.cpu().numpy()
+    assert np.abs(J.T @ lam - b).max() <= 1e-10 * (np.abs(J).max() * np.abs(lam).max() + 1)
+
+
+@pytest.mark.parametrize("schedule", SCHEDULES)
+@pytest.mark.parametrize("case", ["mesh_30x30", "random_1500"])
+def test_fill_heavy_vs_oracle(cuda, case, schedule):
+    rp, ci, a, b = M.CASES[case]()
+    s = Symbolic(rp, ci)
+    o = O.Port(rp, ci, s.array("perm_amd"))
+    num = Numeric(s, 1, FP64, schedule)
+    num.scatter(dev(a))
+    num.refactor()
+    lu_ref = o.refactor(o.scatter(a), sequential=True)
+    assert rel_err(values_of(num, int(s.nnz_lu))[:, 0], lu_ref) <= TOL64
+    x = dev(b)
+    num.solve(x, original=True)
+    _, x_ref = o.scatter_refactor_solve(a, b)
+    assert rel_err(x.cpu().numpy(), x_ref) <= TOL64
+
+
+@pytest.mark.parametrize("schedule", SCHEDULES)
+@pytest.mark.parametrize("dims,S", [((10, 16, 20), 37), ((4, 8, 20), 64)])
+def test_batched_plant_fp64(cuda, dims, S, schedule):
+    p = Plant(*dims)
+    s = Symbolic(p.rowptr, p.colidx)
+    o = O.Port(p.rowptr, p.colidx, s.array("perm_amd"))
+    num = Numeric(s, S, FP64, schedule)
+    a, b = M.plant_batch(p, S, seed0=11, preset="c3")
+    num.scatter(dev(pad_cols(a, num.ld)))
+    num.refactor()
+    assert num.check()[0] == 0
+    lu = values_of(num, int(s.nnz_lu))
+    x = dev(pad_cols(b, num.ld))
+    num.solve(x, original=True)
+    x = x.cpu().numpy().reshape(s.n, num.ld)
+    for k in range(S):
+        lu_ref, x_ref = o.scatter_refactor_solve(a[:, k], b[:, k])
+        assert rel_err(lu[:, k], lu_ref) <= TOL64, k
+        assert rel_err(x[:, k], x_ref) <= TOL64, k
+
+
+@pytest.mark.parametrize("schedule", SCHEDULES)
+def test_plant_35k_fp64(cuda, schedule):
+    """The ~35k-unknown plant (50 x 24 x 28): single instance and a batch."""
+    p = Plant(50, 24, 28)
+    s = Symbolic(p.rowptr, p.colidx)
+    o = O.Port(p.rowptr, p.colidx, s.array("perm_amd"))
+    S = 8
+    a, b = M.plant_batch(p, S, seed0=100, preset="c2")
+    for count in (1, S):
+        num = Numeric(s, count, FP64, schedule)
+        num.scatter(dev(pad_cols(a[:, :count], num.ld)))
+        num.refactor()
+        x = dev(pad_cols(b[:, :count], num.ld))
+        num.solve(x, original=True)
+        x = x.cpu().numpy().reshape(s.n, num.ld)
+        lu = values_of(num, int(s.nnz_lu))
+        for k in range(count):
+            lu_ref, x_ref = o.scatter_refactor_solve(a[:, k], b[:, k])
+            assert rel_err(lu[:, k], lu_ref) <= TOL64
+            assert rel_err(x[:, k], x_ref) <= TOL64
+
+
+@pytest.mark.parametrize("schedule", SCHEDULES)
+def test_fp32_refinement_35k(cuda, schedule):
+    import torch
+
+    p = Plant(50, 24, 28)
+    s = Symbolic(p.rowptr, p.colidx)
+    o = O.Port(p.rowptr, p.colidx, s.array("perm_amd"))
+    S = 40
+    a, b = M.plant_batch(p, S, seed0=300, preset="c3")
+    num = Numeric(s, S, FP32, schedule)
+    a_dev = dev(pad_cols(a, num.ld))
+    b_dev = dev(pad_cols(b, num.ld))
+    num.scatter(a_dev)
+    num.refactor()
+    x = torch.zeros_like(b_dev)
+    sweeps = torch.zeros(num.ld, dtype=torch.int32, device="cuda")
+    num.solve_refined(a_dev, b_dev, x, tol=1e-13, max_sweeps=30, sweeps=sweeps)
+    torch.cuda.synchronize()
+    x = x.cpu().numpy()
+    sw = sweeps.cpu().numpy()[:S]
+    assert (sw > 0).all(), sw
+    for k in range(S):
+        _, x_ref = o.scatter_refactor_solve(a[:, k], b[:, k])
+        err = np.abs(x[:, k] - x_ref).max() / np.abs(x_ref).max()
+        assert err <= 1e-10, (k, err, sw[k])
+
+
+def test_zero_pivot_reported_per_scenario(cuda):
+    p = Plant(4, 8, 20)
+    s = Symbolic(p.rowptr, p.colidx)
+    S = 33
+    a, b = M.plant_batch(p, S, seed0=5)
+    bad = 17
+    # zero every entry of one row in scenario `bad`: its pivot collapses
+    row = int(s.array("row_orig")[0])
+    a[p.rowptr[row]:p.rowptr[row + 1], bad] = 0.0
+    for schedule in SCHEDULES:
+        num = Numeric(s, S, FP64, schedule)
+        num.scatter(dev(pad_cols(a, num.ld)))
+        num.refactor()
+        code, col, sc = num.check()
+        assert code == N.OK + 3 and sc == bad, (code, col, sc)
+        assert num.check() == (0, -1, -1)  # cleared
+        # the other scenarios are unaffected
+        o = O.Port(p.rowptr, p.colidx, s.array("perm_amd"))
+        lu = values_of(num, int(s.nnz_lu))
+        for k in (0, bad - 1, bad + 1, S - 1):
+            lu_ref, _ = o.scatter_refactor_solve(a[:, k], b[:, k])
+            assert rel_err(lu[:, k], lu_ref) <= TOL64
+
+
+def test_host_dropin_entry_points(cuda):
+    """pvglu_refactor_host / pvglu_solve_host: the reference's host-in,
+    host-out semantics of factorize_electrical_system_CUDA and
+    triangular_substitution_LU_CUDA."""
+    g = load_golden("plant_c1")
+    s = Symbolic(g["rowptr"], g["colidx"], g["perm_amd"])
+    num = Numeric(s, 1, FP64)
+    v = g["csc_in"].copy()
+    num.refactor_host(v)
+    assert rel_err(v, g["lu_seq"]) <= TOL64
+    b = to_perm(g, g["b"])
+    num.solve_host(b)
+    assert rel_err(b, g["x_perm"]) <= TOL64
+
+
+def test_scatter_refactor_solve_host_buffers(cuda):
+    import torch
+
+    p = Plant(10, 16, 20)
+    s = Symbolic(p.rowptr, p.colidx)
+    o = O.Port(p.rowptr, p.colidx, s.array("perm_amd"))
+    S = 32
+    a, b = M.plant_batch(p, S, seed0=900)
+    num = Numeric(s, S, FP64, SCHED_PERSISTENT)
+    a_h = torch.from_numpy(pad_cols(a, num.ld)).pin_memory()
+    b_h = torch.from_numpy(pad_cols(b, num.ld)).pin_memory()
+    x_h = torch.empty_like(b_h).pin_memory()
+    stream = torch.cuda.current_stream()
+    num.scatter_refactor_solve_host(a_h, b_h, x_h, stream=stream)
+    stream.synchronize()
+    x = x_h.numpy()
+    for k in range(0, S, 5):
+        _, x_ref = o.scatter_refactor_solve(a[:, k], b[:, k])
+        assert rel_err(x[:, k], x_ref) <= TOL64
+
+
+def test_barrier_timeout_is_reported_not_hung(cuda):
+    code, ret = C.c_int(-1), C.c_int(-1)
+    N.check(N.lib().pvglu_selftest_barrier_timeout(4, 20000, C.byref(code), C.byref(ret)),
+            "selftest")
+    assert code.value == 6  # PVGLU_ERR_BARRIER_TIMEOUT
+    assert ret.value == 4   # every block returned
+    # the context is still usable afterwards
+    test_host_dropin_entry_points(cuda)
