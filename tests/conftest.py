@@ -17,9 +17,9 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (sm_103a)")
     # The product library and the CPU oracle are built before collection so
     # that every test runs against freshly compiled native code.
-    from phdthesis_albertojimenezruiz_gb300 import build as B
+    import __graft_entry__ as G
 
-    B.build()
+    G._load_build_module().build()
     from oracle import oracle as O
 
     O.build_port()
