@@ -203,6 +203,8 @@ def main() -> None:
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--scenarios", type=int, default=512)
     ap.add_argument("--cpu-budget", type=float, default=10.0)
+    ap.add_argument("--only-batched", action="store_true",
+                    help="time the batched FP32+IR path only (profiling runs)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -281,6 +283,14 @@ def main() -> None:
     refactor_ms = float(np.mean([s.elapsed_time(e) for s, e in rf]))
     sw = sweeps.cpu().numpy()[:S]
     value = S * world * args.steps / (ms / 1000.0)
+    if args.only_batched:  # profiling runs: the batched path alone
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT,
+                              "ms_per_step": ms / args.steps, "refactor_ms": refactor_ms,
+                              "scenarios": S, "sweeps_max": int(sw.max())}))
+        if dist:
+            dist.destroy_process_group()
+        return
 
     # Accuracy of the refined solutions against the FP64 GPU factors.
     num64 = Numeric(sym, S, FP64, SCHED_PERSISTENT)

@@ -45,6 +45,13 @@ def rel_err(x: np.ndarray, ref: np.ndarray, floor: float = 1e-6) -> float:
     return float(np.max(np.abs(x - ref) / scale)) if ref.size else 0.0
 
 
+def norm_err(x: np.ndarray, ref: np.ndarray) -> float:
+    """Normwise relative error max|x - ref| / max|ref| (solution vectors)."""
+    x = np.asarray(x, dtype=np.float64)
+    ref = np.asarray(ref, dtype=np.float64)
+    return float(np.max(np.abs(x - ref)) / max(np.abs(ref).max(), 1e-300)) if ref.size else 0.0
+
+
 def has_gpu() -> bool:
     try:
         import torch
