@@ -73,7 +73,8 @@ class _Base:
 
     def solve(self, lu: np.ndarray, b: np.ndarray) -> np.ndarray:
         x = np.array(b, dtype=np.float64, copy=True)
-        getattr(self.lib, self.prefix + "solve")(self.h, _p(np.ascontiguousarray(lu)), _p(x))
+        lu = np.ascontiguousarray(lu, dtype=np.float64)  # keep alive across the call
+        getattr(self.lib, self.prefix + "solve")(self.h, _p(lu), _p(x))
         return x
 
     def __del__(self):
@@ -103,7 +104,7 @@ class Port(_Base):
                 getattr(lib, f).argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
             for f in ("oracle_refactor_levels", "oracle_refactor_sequential"):
                 getattr(lib, f).argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
-            lib.oracle_scatter_refactor_solve.argtypes = [C.c_void_p] * 4
+            lib.oracle_scatter_refactor_solve.argtypes = [C.c_void_p] * 4 + [C.c_int]
             lib.oracle_free.argtypes = [C.c_void_p]
             cls._lib = lib
         return cls._lib
@@ -131,14 +132,18 @@ class Port(_Base):
 
     def solve_transposed(self, lu: np.ndarray, b: np.ndarray) -> np.ndarray:
         x = np.array(b, dtype=np.float64, copy=True)
-        self.lib.oracle_solve_transposed(self.h, _p(np.ascontiguousarray(lu)), _p(x))
+        lu = np.ascontiguousarray(lu, dtype=np.float64)
+        self.lib.oracle_solve_transposed(self.h, _p(lu), _p(x))
         return x
 
-    def scatter_refactor_solve(self, a_vals: np.ndarray, b: np.ndarray):
+    def scatter_refactor_solve(self, a_vals: np.ndarray, b: np.ndarray, sequential=True):
+        """Scatter, refactor (sequential GLU by default: the valid LU on every
+        pattern; level order reproduces the reference's level path), solve."""
         lu = np.empty(len(self.get("csc_row")))
         x = np.array(b, dtype=np.float64, copy=True)
-        rc = self.lib.oracle_scatter_refactor_solve(self.h, _p(np.ascontiguousarray(a_vals)),
-                                                    _p(lu), _p(x))
+        a = np.ascontiguousarray(a_vals, dtype=np.float64)
+        rc = self.lib.oracle_scatter_refactor_solve(self.h, _p(a), _p(lu), _p(x),
+                                                    1 if sequential else 0)
         if rc:
             raise ZeroDivisionError("oracle pivot failure")
         return lu, x

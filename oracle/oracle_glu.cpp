@@ -606,15 +606,18 @@ int oracle_solve_transposed(void* h, const double* v, double* b) {
 }
 
 // Full drop-in sequence of one Newton iteration on the CPU: scatter,
-// level-ordered refactor, permute b (000:198-201), solve, unpermute x
-// (000:233).  b (length n, original order) is overwritten with x.
+// refactor (sequential column order, GLU_CSC_CPU_sequential, when
+// `sequential` is set, else the level order), permute b (000:198-201),
+// solve, unpermute x (000:233).  b (length n, original order) is overwritten
+// with x.
 int oracle_scatter_refactor_solve(void* h, const double* a_vals, double* lu_out,
-                                  double* b) {
+                                  double* b, int sequential) {
   auto* o = static_cast<Oracle*>(h);
   const int n = o->n;
   oracle_scatter(h, a_vals, lu_out);
   int bad = -1;
-  const int st = oracle_refactor_levels(h, lu_out, &bad);
+  const int st = sequential ? oracle_refactor_sequential(h, lu_out, &bad)
+                            : oracle_refactor_levels(h, lu_out, &bad);
   if (st) return st;
   std::vector<double> w(b, b + n), t(n);
   for (int i = 0; i < n; i++) t[o->perm_amd_rev[i]] = w[i];  // apply_permutation(Pinv)

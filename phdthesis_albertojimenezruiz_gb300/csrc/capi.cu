@@ -150,7 +150,8 @@ template <typename TI, typename TO>
 void permute(pvglu_numeric* h, const int* perm, const TI* x, TO* y, bool gather,
              cudaStream_t st) {
   const int64_t total = (int64_t)h->n * h->ld;
-  pvglu::k_permute<TI, TO><<<launch_blocks(total, 256), 256, 0, st>>>(
+  (void)total;
+  pvglu::k_permute<TI, TO><<<pvglu::rows_grid(h->n, h->ld, 256), 256, 0, st>>>(
       perm, h->n, h->ld, h->S, x, y, gather ? 1 : 0);
 }
 
@@ -363,7 +364,8 @@ int pvglu_scatter(pvglu_numeric* h, const double* a_values, void* stream) {
   if (!h || !a_values) return fail(PVGLU_ERR_BAD_ARG, "NULL argument");
   cudaStream_t st = as_stream(stream);
   const int64_t total = (int64_t)h->nnz * h->ld;
-  const int blocks = launch_blocks(total, 256);
+  (void)total;
+  const int blocks = pvglu::rows_grid(h->nnz, h->ld, 256);
   if (h->precision == PVGLU_FP64)
     pvglu::k_scatter<double><<<blocks, 256, 0, st>>>(h->d.slot_src, h->nnz, h->ld, h->S,
                                                      a_values, (double*)h->values);
@@ -531,7 +533,7 @@ int pvglu_solve_refined(pvglu_numeric* h, const double* a_values, const double* 
   if (sweeps_out) PVGLU_CUDA(cudaMemsetAsync(sweeps_out, 0, h->ld * sizeof(int), st));
   const pvglu::SkipDone skip{h->ir_done, ndone};
   for (int sweep = 1; sweep <= max_sweeps; sweep++) {
-    pvglu::k_residual<<<launch_blocks(nv, 256), 256, 0, st>>>(
+    pvglu::k_residual<<<pvglu::rows_grid(h->n, h->ld, 256), 256, 0, st>>>(
         h->d.a_rowptr, h->d.a_colidx, h->n, h->ld, h->S, a_values, b, x, h->ir_done, w,
         h->row_pos);
     int rc = solve_permuted<float>(h, w, false, st, skip);

@@ -68,20 +68,38 @@ template <typename T>
 __device__ __forceinline__ T ldv(const T* p) { return __ldcg(p); }
 
 // ----------------------------------------------------------------------------
+// Row x scenario iteration without integer division: with one scenario a
+// thread owns a row; with a batch a warp owns a row and its lanes stride over
+// the scenarios (coalesced, ld is a multiple of 32).
+template <typename F>
+__device__ __forceinline__ void for_rows(int nrows, int ld, F&& f) {
+  if (ld == 1) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nrows; r += gridDim.x * blockDim.x)
+      f(r, 0);
+  } else {
+    const int lane = threadIdx.x & 31;
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    for (int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < nrows; r += warps)
+      for (int s = lane; s < ld; s += 32) f(r, s);
+  }
+}
+
+inline int rows_grid(int64_t nrows, int ld, int block) {
+  const int64_t threads = ld == 1 ? nrows : nrows * 32;
+  const int64_t b = (threads + block - 1) / block;
+  return (int)(b < 1 ? 1 : (b > 65536 ? 65536 : b));
+}
+
 // (a) scatter: LU(q, s) = A(slot_src[q], s), zero at fill slots.
 template <typename T>
 __global__ void k_scatter(const int* __restrict__ slot_src, int nnz, int ld, int S,
                           const double* __restrict__ a, T* __restrict__ v) {
-  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t total = (int64_t)nnz * ld;
-  for (int64_t e = tid; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-    const int q = (int)(e / ld);
-    const int s = (int)(e - (int64_t)q * ld);
+  for_rows(nnz, ld, [&](int q, int s) {
     const int src = slot_src[q];
     T val = T(0);
     if (src >= 0 && s < S) val = (T)a[(int64_t)src * ld + s];
-    v[e] = val;
-  }
+    v[(int64_t)q * ld + s] = val;
+  });
 }
 
 // ----------------------------------------------------------------------------
@@ -175,16 +193,13 @@ __global__ void k_solve_level(DevStruct d, const T* __restrict__ v, T* __restric
 template <typename TI, typename TO>
 __global__ void k_permute(const int* __restrict__ perm, int n, int ld, int S,
                           const TI* __restrict__ x, TO* __restrict__ y, int gather) {
-  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t total = (int64_t)n * ld;
-  for (int64_t e = tid; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-    const int r = (int)(e / ld);
-    const int s = (int)(e - (int64_t)r * ld);
-    if (s >= S) continue;
+  for_rows(n, ld, [&](int r, int s) {
+    if (s >= S) return;
+    const int64_t e = (int64_t)r * ld + s;
     const int pr = perm[r];
     if (gather) y[e] = (TO)x[(int64_t)pr * ld + s];
     else y[(int64_t)pr * ld + s] = (TO)x[e];
-  }
+  });
 }
 
 // ----------------------------------------------------------------------------
@@ -195,18 +210,14 @@ __global__ void k_residual(const int* __restrict__ a_rowptr, const int* __restri
                            const double* __restrict__ b, const double* __restrict__ x,
                            const int* __restrict__ done, float* __restrict__ r_perm,
                            const int* __restrict__ row_pos) {
-  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t total = (int64_t)n * ld;
-  for (int64_t e = tid; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-    const int i = (int)(e / ld);
-    const int s = (int)(e - (int64_t)i * ld);
-    if (s >= S || done[s]) continue;
-    double acc = b[e];
+  for_rows(n, ld, [&](int i, int s) {
+    if (s >= S || done[s]) return;
+    double acc = b[(int64_t)i * ld + s];
     for (int p = a_rowptr[i]; p < a_rowptr[i + 1]; p++)
       acc -= a[(int64_t)p * ld + s] * x[(int64_t)a_colidx[p] * ld + s];
     // Row i of J is row row_pos[i] of the pivot-ordered system.
     r_perm[(int64_t)row_pos[i] * ld + s] = (float)acc;
-  }
+  });
 }
 
 // x[col_orig[c]] += dx[c]; per-scenario max |dx| and max |x| (non-negative

@@ -194,7 +194,9 @@ def test_fp32_refinement_35k(cuda, schedule):
     num.refactor()
     x = torch.zeros_like(b_dev)
     sweeps = torch.zeros(num.ld, dtype=torch.int32, device="cuda")
-    num.solve_refined(a_dev, b_dev, x, tol=1e-13, max_sweeps=30, sweeps=sweeps)
+    # tol sits above the FP64 rounding floor of the residual (about cond x eps64
+    # relative for this plant); below it the corrections stop shrinking.
+    num.solve_refined(a_dev, b_dev, x, tol=1e-12, max_sweeps=10, sweeps=sweeps)
     torch.cuda.synchronize()
     x = x.cpu().numpy()
     sw = sweeps.cpu().numpy()[:S]
