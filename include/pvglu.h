@@ -48,10 +48,14 @@ enum {
                                  triangular_substitution_LU_CUDA expects */
 };
 
-/* Refactor/solve schedules. */
+/* Refactor/solve schedules.  LEVELS and PERSISTENT execute compiled chain
+ * programs (each chain staged through shared memory); THREAD_CHAIN is the
+ * reference's launch shape (one thread walks one chain through global memory,
+ * one launch per level, factorize_electrical_system_CUDA.cu:72-115). */
 enum {
-  PVGLU_SCHED_LEVELS = 0,     /* one launch per level (the reference's shape)   */
-  PVGLU_SCHED_PERSISTENT = 1  /* one cooperative launch, bounded grid barriers  */
+  PVGLU_SCHED_LEVELS = 0,      /* one launch per level                          */
+  PVGLU_SCHED_PERSISTENT = 1,  /* one cooperative launch, bounded grid barriers */
+  PVGLU_SCHED_THREAD_CHAIN = 2 /* thread per chain, one launch per level        */
 };
 
 typedef struct pvglu_symbolic pvglu_symbolic;
@@ -137,6 +141,11 @@ int pvglu_refactor(pvglu_numeric* h, void* stream);
  * Replaces triangular_substitution_LU_CUDA (triangular_substitution.cu:232-271);
  * with PVGLU_SOLVE_TRANSPOSE it solves the adjoint system. */
 int pvglu_solve(pvglu_numeric* h, void* x, int flags, void* stream);
+
+/* (b) + (c) in one call: with the persistent schedule and a permuted-space
+ * solve, a single cooperative launch walks the refactorization levels and
+ * then the solve levels; otherwise pvglu_refactor then pvglu_solve. */
+int pvglu_refactor_solve(pvglu_numeric* h, void* x, int flags, void* stream);
 
 /* Error state of the last refactor (synchronizes the stream): status code,
  * first failing column and scenario (-1 if none).  Clears the state. */

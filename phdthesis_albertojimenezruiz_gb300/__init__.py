@@ -6,11 +6,12 @@ the GLU refactorization and the triangular solves.  This package is its
 Python view; importing it loads the library and fails if it is missing.
 """
 from . import _native
-from ._native import FP32, FP64, SCHED_LEVELS, SCHED_PERSISTENT, PvgluError
+from ._native import (FP32, FP64, SCHED_LEVELS, SCHED_PERSISTENT, SCHED_THREAD_CHAIN,
+                      PvgluError)
 from .glu import Numeric, Symbolic
 from .plant import Plant
 
 _native.lib()  # fail loudly at import when the native library is absent
 
-__all__ = ["FP32", "FP64", "SCHED_LEVELS", "SCHED_PERSISTENT", "Numeric", "PvgluError",
-           "Plant", "Symbolic"]
+__all__ = ["FP32", "FP64", "SCHED_LEVELS", "SCHED_PERSISTENT", "SCHED_THREAD_CHAIN", "Numeric",
+           "PvgluError", "Plant", "Symbolic"]

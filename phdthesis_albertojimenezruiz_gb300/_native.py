@@ -17,7 +17,7 @@ ERR_NAMES = {
 }
 FP64, FP32 = 0, 1
 SOLVE_TRANSPOSE, SOLVE_ORIGINAL = 1, 2
-SCHED_LEVELS, SCHED_PERSISTENT = 0, 1
+SCHED_LEVELS, SCHED_PERSISTENT, SCHED_THREAD_CHAIN = 0, 1, 2
 
 
 class PvgluError(RuntimeError):
@@ -67,6 +67,7 @@ _SIGS = {
     "pvglu_scatter": ([_P, _P, _P], _I),
     "pvglu_refactor": ([_P, _P], _I),
     "pvglu_solve": ([_P, _P, _I, _P], _I),
+    "pvglu_refactor_solve": ([_P, _P, _I, _P], _I),
     "pvglu_numeric_check": ([_P, _P, _IP, _IP, _IP], _I),
     "pvglu_refactor_host": ([_P, _P], _I),
     "pvglu_solve_host": ([_P, _P], _I),

@@ -24,7 +24,7 @@ CXXFLAGS = ["-std=c++17", "-O2", "-fPIC", "-Wall", "-Wextra", "-Wno-unused-param
 NVCCFLAGS = ["-std=c++17", "-O3", "-lineinfo", "--expt-relaxed-constexpr",
              "-Xcompiler", "-fPIC", "-Xptxas", "-warn-spills"] + ARCH
 
-HOST_SOURCES = ["symbolic.cpp", "plant.cpp", "plant_capi.cpp"]
+HOST_SOURCES = ["symbolic.cpp", "programs.cpp", "plant.cpp", "plant_capi.cpp"]
 CUDA_SOURCES = ["capi.cu"]
 
 

@@ -66,8 +66,14 @@ struct pvglu_numeric {
   // Host copies of the level starts (launch ranges).
   std::vector<int> lu_sl, l_sl, u_sl, lt_sl;
   // Persistent schedule.
-  pvglu::PersistentPlan plan{};
-  int persistent_grid = 0;
+  // Chain programs: refactor, L, U, U^T, L^T (programs.hpp).
+  bool batch = false;              // ld > 1: lane = scenario
+  int max_locals = 0;
+  pvglu::ProgSetDev progs{};
+  std::vector<int> prog_level_chain[5];
+  int prog_max_chains = 1;
+  int prog_grid = 0;               // co-resident blocks of k_prog_persistent
+  int64_t prog_ops = 0, prog_loads = 0, prog_direct = 0;
   unsigned int* barrier = nullptr;  // [2]: count, generation
   ~pvglu_numeric() {
     for (void* p : allocs) cudaFree(p);
@@ -123,18 +129,77 @@ void solve_phase(pvglu_numeric* h, const std::vector<int>& sl, T* x, const int* 
   }
 }
 
+// Kernel attributes (dynamic shared memory above 48 KB) and the persistent
+// grid size of the chain-program kernels of one handle.
+template <typename T, bool B>
+int prog_prepare(pvglu_numeric* h) {
+  const int smem = (int)pvglu::prog_smem_bytes<T, B>(h->max_locals);
+  const void* fns[] = {(const void*)pvglu::k_prog_level<T, -1, B>,
+                       (const void*)pvglu::k_prog_level<T, 0, B>,
+                       (const void*)pvglu::k_prog_level<T, 1, B>,
+                       (const void*)pvglu::k_prog_level<T, 2, B>,
+                       (const void*)pvglu::k_prog_level<T, 3, B>};
+  for (const void* f : fns)
+    if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+      return 1;
+  h->prog_grid = pvglu::prog_persistent_grid<T, B>(h->max_locals);
+  return 0;
+}
+
+// One phase of chain programs with one launch per level.
+template <typename T, bool B, int KIND>
+void prog_levels(pvglu_numeric* h, T* x, const int* done, cudaStream_t st) {
+  const int ph = KIND + 1;
+  const auto& lc = h->prog_level_chain[ph];
+  const size_t smem = pvglu::prog_smem_bytes<T, B>(h->max_locals);
+  const int groups = B ? h->ld / 32 : 1;
+  const int warps = pvglu::kProgBlock / 32;
+  for (size_t lv = 0; lv + 1 < lc.size(); lv++) {
+    const int cb = lc[lv], ce = lc[lv + 1];
+    const int64_t items = (int64_t)(ce - cb) * groups;
+    pvglu::k_prog_level<T, KIND, B><<<launch_blocks(items, warps), pvglu::kProgBlock, smem, st>>>(
+        h->progs.p[ph], h->d, cb, ce, static_cast<T*>(h->values), x, h->ld, h->S,
+        h->pivot_tol, h->status, done);
+  }
+}
+
+template <typename T, bool B>
+int prog_dispatch(pvglu_numeric* h, int phases, T* x, pvglu::SkipDone skip, cudaStream_t st) {
+  if (h->schedule == PVGLU_SCHED_PERSISTENT) {
+    if (pvglu::launch_prog_persistent<T, B>(h->progs, h->prog_max_chains, h->d,
+                                            static_cast<T*>(h->values), x, h->ld, h->S,
+                                            h->pivot_tol, h->status, h->barrier, h->prog_grid,
+                                            phases, st, skip))
+      return fail(PVGLU_ERR_CUDA, std::string("persistent launch failed: ") +
+                                      cudaGetErrorString(cudaGetLastError()));
+    return PVGLU_OK;
+  }
+  if (phases & pvglu::PHASE_REFACTOR) prog_levels<T, B, -1>(h, x, nullptr, st);
+  if (phases & pvglu::PHASE_SOLVE) {
+    prog_levels<T, B, 0>(h, x, skip.done, st);
+    prog_levels<T, B, 1>(h, x, skip.done, st);
+  }
+  if (phases & pvglu::PHASE_SOLVE_T) {
+    prog_levels<T, B, 2>(h, x, skip.done, st);
+    prog_levels<T, B, 3>(h, x, skip.done, st);
+  }
+  PVGLU_CUDA(cudaGetLastError());
+  return PVGLU_OK;
+}
+
+template <typename T>
+int run_phases(pvglu_numeric* h, int phases, T* x, cudaStream_t st,
+               pvglu::SkipDone skip = pvglu::SkipDone{nullptr, nullptr}) {
+  return h->batch ? prog_dispatch<T, true>(h, phases, x, skip, st)
+                  : prog_dispatch<T, false>(h, phases, x, skip, st);
+}
+
 // skip: per-scenario convergence flags of iterative refinement (or none).
 template <typename T>
 int solve_permuted(pvglu_numeric* h, T* x, bool transpose, cudaStream_t st,
                    pvglu::SkipDone skip = pvglu::SkipDone{nullptr, nullptr}) {
-  if (h->schedule == PVGLU_SCHED_PERSISTENT) {
-    const int st_code = pvglu::launch_persistent<T>(
-        h->plan, h->d, static_cast<T*>(h->values), x, h->ld, h->S, h->pivot_tol,
-        h->status, h->barrier, h->persistent_grid,
-        transpose ? pvglu::PHASE_SOLVE_T : pvglu::PHASE_SOLVE, st, skip);
-    if (st_code) return fail(PVGLU_ERR_CUDA, "persistent solve launch failed");
-    return PVGLU_OK;
-  }
+  if (h->schedule != PVGLU_SCHED_THREAD_CHAIN)
+    return run_phases<T>(h, transpose ? pvglu::PHASE_SOLVE_T : pvglu::PHASE_SOLVE, x, st, skip);
   if (!transpose) {
     solve_phase<T, 0>(h, h->l_sl, x, skip.done, st);
     solve_phase<T, 1>(h, h->u_sl, x, skip.done, st);
@@ -325,14 +390,46 @@ int pvglu_numeric_create(const pvglu_symbolic* sym, int n_scenarios, int precisi
     delete h;
     return fail(PVGLU_ERR_CUDA, "cudaMemset failed");
   }
-  // Persistent schedule plan (level ranges in one table).
-  h->plan = pvglu::make_plan(s, h->allocs, &rc);
+  // Chain programs for the shared-memory schedules.  Table budget: a warp's
+  // tile is max_locals x 32 scenarios (batched) or max_locals (single).
+  h->batch = h->ld > 1;
+  h->max_locals = h->batch ? (precision == PVGLU_FP32 ? 96 : 64) : 1024;
+  for (int ph = 0; ph < 5; ph++) {
+    pvglu::ChainProgram prog;
+    pvglu::build_chain_program(s, ph - 1, h->max_locals, prog);
+    std::vector<int4> seg(prog.seg.size()), ops(prog.ops.size());
+    for (size_t i = 0; i < seg.size(); i++)
+      seg[i] = make_int4(prog.seg[i].load_begin, prog.seg[i].n_load, prog.seg[i].op_begin,
+                         prog.seg[i].n_op);
+    for (size_t i = 0; i < ops.size(); i++)
+      ops[i] = make_int4(prog.ops[i].code, prog.ops[i].a, prog.ops[i].b, prog.ops[i].c);
+    pvglu::ProgDev& P = h->progs.p[ph];
+    rc |= h->put(prog.level_chain, &P.level_chain);
+    rc |= h->put(prog.chain_seg, &P.chain_seg);
+    rc |= h->put(seg, &P.seg);
+    rc |= h->put(prog.loads, &P.loads);
+    rc |= h->put(ops, &P.ops);
+    P.n_levels = (int)prog.level_chain.size() - 1;
+    P.max_locals = h->max_locals;
+    h->prog_level_chain[ph] = prog.level_chain;
+    for (int lv = 0; lv < P.n_levels; lv++)
+      h->prog_max_chains = std::max(h->prog_max_chains,
+                                    prog.level_chain[lv + 1] - prog.level_chain[lv]);
+    h->prog_ops += (int64_t)prog.ops.size();
+    h->prog_loads += (int64_t)prog.loads.size();
+    h->prog_direct += prog.direct_segments;
+  }
   if (rc) {
     delete h;
-    return fail(PVGLU_ERR_NO_MEMORY, "persistent plan upload failed");
+    return fail(PVGLU_ERR_NO_MEMORY, "chain program upload failed");
   }
-  h->persistent_grid = precision == PVGLU_FP64 ? pvglu::persistent_grid<double>()
-                                               : pvglu::persistent_grid<float>();
+  const int smem_rc = precision == PVGLU_FP64
+                          ? (h->batch ? prog_prepare<double, true>(h) : prog_prepare<double, false>(h))
+                          : (h->batch ? prog_prepare<float, true>(h) : prog_prepare<float, false>(h));
+  if (smem_rc) {
+    delete h;
+    return fail(PVGLU_ERR_CUDA, "cannot configure the chain-program kernels");
+  }
   *out = h;
   return PVGLU_OK;
 }
@@ -346,9 +443,10 @@ int pvglu_numeric_ld(const pvglu_numeric* h) { return h ? h->ld : 0; }
 void* pvglu_numeric_values(pvglu_numeric* h) { return h ? h->values : nullptr; }
 
 int pvglu_numeric_set_schedule(pvglu_numeric* h, int schedule) {
-  if (!h || (schedule != PVGLU_SCHED_LEVELS && schedule != PVGLU_SCHED_PERSISTENT))
+  if (!h || (schedule != PVGLU_SCHED_LEVELS && schedule != PVGLU_SCHED_PERSISTENT &&
+             schedule != PVGLU_SCHED_THREAD_CHAIN))
     return fail(PVGLU_ERR_BAD_ARG, "bad schedule");
-  if (schedule == PVGLU_SCHED_PERSISTENT && h->persistent_grid <= 0)
+  if (schedule == PVGLU_SCHED_PERSISTENT && h->prog_grid <= 0)
     return fail(PVGLU_ERR_CUDA, "cooperative launch unavailable on this device");
   h->schedule = schedule;
   return PVGLU_OK;
@@ -379,23 +477,25 @@ int pvglu_scatter(pvglu_numeric* h, const double* a_values, void* stream) {
 int pvglu_refactor(pvglu_numeric* h, void* stream) {
   if (!h) return fail(PVGLU_ERR_BAD_ARG, "NULL handle");
   cudaStream_t st = as_stream(stream);
-  if (h->schedule == PVGLU_SCHED_PERSISTENT) {
-    int rc = h->precision == PVGLU_FP64
-                 ? pvglu::launch_persistent<double>(h->plan, h->d, (double*)h->values,
-                                                    nullptr, h->ld, h->S, h->pivot_tol,
-                                                    h->status, h->barrier,
-                                                    h->persistent_grid,
-                                                    pvglu::PHASE_REFACTOR, st)
-                 : pvglu::launch_persistent<float>(h->plan, h->d, (float*)h->values,
-                                                   nullptr, h->ld, h->S, h->pivot_tol,
-                                                   h->status, h->barrier,
-                                                   h->persistent_grid,
-                                                   pvglu::PHASE_REFACTOR, st);
-    if (rc) return fail(PVGLU_ERR_CUDA, "persistent refactor launch failed");
-    return PVGLU_OK;
+  if (h->schedule == PVGLU_SCHED_THREAD_CHAIN)
+    return h->precision == PVGLU_FP64 ? refactor_levels<double>(h, st)
+                                      : refactor_levels<float>(h, st);
+  return h->precision == PVGLU_FP64
+             ? run_phases<double>(h, pvglu::PHASE_REFACTOR, (double*)nullptr, st)
+             : run_phases<float>(h, pvglu::PHASE_REFACTOR, (float*)nullptr, st);
+}
+
+int pvglu_refactor_solve(pvglu_numeric* h, void* x, int flags, void* stream) {
+  if (!h || !x) return fail(PVGLU_ERR_BAD_ARG, "NULL argument");
+  if ((flags & PVGLU_SOLVE_ORIGINAL) || h->schedule != PVGLU_SCHED_PERSISTENT) {
+    int rc = pvglu_refactor(h, stream);
+    return rc ? rc : pvglu_solve(h, x, flags, stream);
   }
-  return h->precision == PVGLU_FP64 ? refactor_levels<double>(h, st)
-                                    : refactor_levels<float>(h, st);
+  const int phases = pvglu::PHASE_REFACTOR |
+                     ((flags & PVGLU_SOLVE_TRANSPOSE) ? pvglu::PHASE_SOLVE_T : pvglu::PHASE_SOLVE);
+  cudaStream_t st = as_stream(stream);
+  return h->precision == PVGLU_FP64 ? run_phases<double>(h, phases, (double*)x, st)
+                                    : run_phases<float>(h, phases, (float*)x, st);
 }
 
 int pvglu_solve(pvglu_numeric* h, void* x, int flags, void* stream) {
@@ -533,9 +633,12 @@ int pvglu_solve_refined(pvglu_numeric* h, const double* a_values, const double* 
   if (sweeps_out) PVGLU_CUDA(cudaMemsetAsync(sweeps_out, 0, h->ld * sizeof(int), st));
   const pvglu::SkipDone skip{h->ir_done, ndone};
   for (int sweep = 1; sweep <= max_sweeps; sweep++) {
-    pvglu::k_residual<<<pvglu::rows_grid(h->n, h->ld, 256), 256, 0, st>>>(
-        h->d.a_rowptr, h->d.a_colidx, h->n, h->ld, h->S, a_values, b, x, h->ir_done, w,
-        h->row_pos);
+    if (sweep == 1)  // x = 0: the residual is b itself
+      permute<double, float>(h, h->d.row_orig, b, w, true, st);
+    else
+      pvglu::k_residual<<<pvglu::rows_grid(h->n, h->ld, 256), 256, 0, st>>>(
+          h->d.a_rowptr, h->d.a_colidx, h->n, h->ld, h->S, a_values, b, x, h->ir_done, w,
+          h->row_pos);
     int rc = solve_permuted<float>(h, w, false, st, skip);
     if (rc) return rc;
     dim3 blk(32, 8), grd((unsigned)std::min(1024, (h->n + 7) / 8), (unsigned)(h->ld + 31) / 32);

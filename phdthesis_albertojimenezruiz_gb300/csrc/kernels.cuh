@@ -67,6 +67,16 @@ __device__ __forceinline__ void report_error(DevStatus* st, int code, int col, i
 template <typename T>
 __device__ __forceinline__ T ldv(const T* p) { return __ldcg(p); }
 
+// a - b * c.  FP64 rounds the product and the difference separately, as the
+// reference's CPU code does (GLU_CSC_CPU_levels_strings.cpp:56,
+// GLU_CSC_CPU_Triangular.cpp:8,21); with the same update order per entry the
+// FP64 factors and solutions are then bit-identical to the reference's
+// sequential path.  FP32 (refined afterwards in FP64) keeps the fused form.
+__device__ __forceinline__ double fnms(double a, double b, double c) {
+  return __dsub_rn(a, __dmul_rn(b, c));
+}
+__device__ __forceinline__ float fnms(float a, float b, float c) { return a - b * c; }
+
 // ----------------------------------------------------------------------------
 // Row x scenario iteration without integer division: with one scenario a
 // thread owns a row; with a batch a warp owns a row and its lanes stride over
@@ -121,7 +131,7 @@ __device__ __forceinline__ void refactor_column(const DevStruct& d, int k, int s
     const int* tg = d.upd_tgt + d.upd_ptr[p] - q0;
     for (int q = q0; q < q1; q++) {
       T* tp = v + (int64_t)tg[q] * ld + s;
-      *tp = ldv(tp) - ldv(v + (int64_t)q * ld + s) * u;
+      *tp = fnms(ldv(tp), ldv(v + (int64_t)q * ld + s), u);
     }
   }
   const T piv = ldv(v + (int64_t)dk * ld + s);
@@ -155,21 +165,23 @@ template <typename T, int KIND>
 __device__ __forceinline__ void solve_unknown(const DevStruct& d, int i, int s, int ld,
                                               const T* __restrict__ v, T* __restrict__ x) {
   T acc = ldv(x + (int64_t)i * ld + s);
-  if (KIND == 0) {
+  if (KIND == 0) {  // updates arrive in ascending column order, as in the reference
     for (int e = d.lrow_ptr[i]; e < d.lrow_ptr[i + 1]; e++)
-      acc -= ldv(v + (int64_t)d.lrow_slot[e] * ld + s) * ldv(x + (int64_t)d.lrow_col[e] * ld + s);
-  } else if (KIND == 1) {
-    for (int e = d.urow_ptr[i]; e < d.urow_ptr[i + 1]; e++)
-      acc -= ldv(v + (int64_t)d.urow_slot[e] * ld + s) * ldv(x + (int64_t)d.urow_col[e] * ld + s);
+      acc = fnms(acc, ldv(v + (int64_t)d.lrow_slot[e] * ld + s),
+                 ldv(x + (int64_t)d.lrow_col[e] * ld + s));
+  } else if (KIND == 1) {  // descending: the reference's backward sweep order
+    for (int e = d.urow_ptr[i + 1] - 1; e >= d.urow_ptr[i]; e--)
+      acc = fnms(acc, ldv(v + (int64_t)d.urow_slot[e] * ld + s),
+                 ldv(x + (int64_t)d.urow_col[e] * ld + s));
     acc /= ldv(v + (int64_t)d.diag[i] * ld + s);
   } else if (KIND == 2) {
     const int dg = d.diag[i];
     for (int p = d.colptr[i]; p < dg; p++)
-      acc -= ldv(v + (int64_t)p * ld + s) * ldv(x + (int64_t)d.csc_row[p] * ld + s);
+      acc = fnms(acc, ldv(v + (int64_t)p * ld + s), ldv(x + (int64_t)d.csc_row[p] * ld + s));
     acc /= ldv(v + (int64_t)dg * ld + s);
   } else {
     for (int q = d.diag[i] + 1; q < d.colptr[i + 1]; q++)
-      acc -= ldv(v + (int64_t)q * ld + s) * ldv(x + (int64_t)d.csc_row[q] * ld + s);
+      acc = fnms(acc, ldv(v + (int64_t)q * ld + s), ldv(x + (int64_t)d.csc_row[q] * ld + s));
   }
   x[(int64_t)i * ld + s] = acc;
 }

@@ -14,6 +14,7 @@
 #include <type_traits>
 #include <vector>
 
+#include "chainprog.cuh"
 #include "kernels.cuh"
 #include "symbolic.hpp"
 
@@ -21,47 +22,7 @@ namespace pvglu {
 
 enum : int { PHASE_REFACTOR = 1, PHASE_SOLVE = 2, PHASE_SOLVE_T = 4 };
 
-struct PersistentPlan {
-  const int* lu_sl; int lu_nl;
-  const int* l_sl;  int l_nl;
-  const int* u_sl;  int u_nl;
-  const int* lt_sl; int lt_nl;
-  int max_chains;   // widest level over all phases
-};
-
-constexpr int kPersistentBlock = 128;
 constexpr long long kBarrierMaxSpins = 1LL << 22;  // x ~100-1000 ns => ~0.4-4 s
-
-inline PersistentPlan make_plan(const Symbolic& s, std::vector<void*>& allocs, int* rc) {
-  PersistentPlan p{};
-  auto up = [&](const std::vector<int>& v, const int** out) {
-    int* d = nullptr;
-    if (cudaMalloc((void**)&d, std::max<size_t>(v.size(), 1) * sizeof(int)) != cudaSuccess) {
-      *rc = 1;
-      return;
-    }
-    allocs.push_back(d);
-    if (!v.empty() &&
-        cudaMemcpy(d, v.data(), v.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess)
-      *rc = 1;
-    *out = d;
-  };
-  up(s.lu.start_levels, &p.lu_sl);
-  up(s.l.start_levels, &p.l_sl);
-  up(s.u.start_levels, &p.u_sl);
-  up(s.lt.start_levels, &p.lt_sl);
-  p.lu_nl = s.lu.num_levels();
-  p.l_nl = s.l.num_levels();
-  p.u_nl = s.u.num_levels();
-  p.lt_nl = s.lt.num_levels();
-  int mx = 1;
-  const LevelSet* sets[4] = {&s.lu, &s.l, &s.u, &s.lt};
-  for (const LevelSet* ls : sets)
-    for (int lv = 0; lv < ls->num_levels(); lv++)
-      mx = std::max(mx, ls->start_levels[lv + 1] - ls->start_levels[lv]);
-  p.max_chains = mx;
-  return p;
-}
 
 // Bounded sense-by-generation grid barrier.  bar[0] = arrivals, bar[1] =
 // generation, bar[2] = abort word.  Returns false when the launch must stop.
@@ -113,92 +74,101 @@ struct SkipDone {
   const int* ndone;
 };
 
-// One phase (a level set) of the persistent walk.  A barrier precedes every
-// level except the very first one of the launch (*need_sync false).
-// KIND -1 = refactorization, 0..3 = solve kinds of solve_unknown.
-template <typename T, int KIND>
-__device__ __forceinline__ bool run_phase(const int* sl, int nl, const int* sc, const int* cols,
-                                          const DevStruct& d, T* __restrict__ v,
-                                          T* __restrict__ x, int ld, int S, double pivot_tol,
-                                          DevStatus* st, unsigned int* bar, const int* done,
-                                          bool* need_sync) {
-  const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
-  const int64_t gtid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  for (int lv = 0; lv < nl; lv++) {
+// ---------------------------------------------------------------------------
+// Persistent walk over chain programs (chainprog.cuh): same phases and
+// barriers as k_persistent, each chain executed from a shared-memory table.
+struct ProgSetDev {
+  ProgDev p[5];  // refactor, L, U, U^T, L^T
+};
+
+constexpr int kProgBlock = 128;
+
+template <typename T, int KIND, bool BATCH>
+__device__ __forceinline__ bool prog_phase(const ProgDev& P, const DevStruct& d, T* v, T* x,
+                                           int ld, int S, T* sm, double pivot_tol,
+                                           DevStatus* st, unsigned int* bar, const int* done,
+                                           bool* need_sync) {
+  const int64_t warp_id = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int lv = 0; lv < P.n_levels; lv++) {
     if (*need_sync && !grid_barrier(bar, st, gridDim.x, kBarrierMaxSpins)) return false;
     *need_sync = true;
-    const int cb = sl[lv], ce = sl[lv + 1];
-    const int64_t items = (int64_t)(ce - cb) * ld;
-    for (int64_t it = gtid; it < items; it += nthreads) {
-      const int c = cb + (int)(it / ld);
-      const int s = (int)(it % ld);
-      if (s >= S || (done && done[s])) continue;
-      for (int t = sc[c]; t < sc[c + 1]; t++) {
-        if constexpr (KIND < 0) refactor_column<T>(d, cols[t], s, ld, v, pivot_tol, st);
-        else solve_unknown<T, KIND>(d, cols[t], s, ld, v, x);
-      }
-    }
+    prog_run_level<T, KIND, BATCH>(P, d, P.level_chain[lv], P.level_chain[lv + 1], v, x, ld,
+                                   S, sm, pivot_tol, st, done, warp_id, n_warps);
   }
   return true;
 }
 
-template <typename T>
-__global__ void __launch_bounds__(kPersistentBlock)
-k_persistent(PersistentPlan plan, DevStruct d, T* __restrict__ v, T* __restrict__ x,
-             int ld, int S, double pivot_tol, DevStatus* st, unsigned int* bar,
-             int phases, SkipDone skip) {
+template <typename T, bool BATCH>
+__global__ void __launch_bounds__(kProgBlock)
+k_prog_persistent(ProgSetDev PS, DevStruct d, T* __restrict__ v, T* __restrict__ x, int ld,
+                  int S, double pivot_tol, DevStatus* st, unsigned int* bar, int phases,
+                  SkipDone skip) {
   if (skip.ndone && __ldcg(skip.ndone) >= S) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int ml = PS.p[0].max_locals;
+  T* sm = reinterpret_cast<T*>(smem_raw) + (threadIdx.x >> 5) * ml * (BATCH ? 32 : 1);
   bool need_sync = false;
   if (phases & PHASE_REFACTOR)
-    if (!run_phase<T, -1>(plan.lu_sl, plan.lu_nl, d.lu_sc, d.lu_cols, d, v, x, ld, S,
-                          pivot_tol, st, bar, nullptr, &need_sync))
+    if (!prog_phase<T, -1, BATCH>(PS.p[0], d, v, x, ld, S, sm, pivot_tol, st, bar, nullptr,
+                                  &need_sync))
       return;
   if (phases & PHASE_SOLVE) {
-    if (!run_phase<T, 0>(plan.l_sl, plan.l_nl, d.l_sc, d.l_cols, d, v, x, ld, S, pivot_tol,
-                         st, bar, skip.done, &need_sync))
+    if (!prog_phase<T, 0, BATCH>(PS.p[1], d, v, x, ld, S, sm, pivot_tol, st, bar, skip.done,
+                                 &need_sync))
       return;
-    if (!run_phase<T, 1>(plan.u_sl, plan.u_nl, d.u_sc, d.u_cols, d, v, x, ld, S, pivot_tol,
-                         st, bar, skip.done, &need_sync))
+    if (!prog_phase<T, 1, BATCH>(PS.p[2], d, v, x, ld, S, sm, pivot_tol, st, bar, skip.done,
+                                 &need_sync))
       return;
   }
   if (phases & PHASE_SOLVE_T) {
-    if (!run_phase<T, 2>(plan.lu_sl, plan.lu_nl, d.lu_sc, d.lu_cols, d, v, x, ld, S,
-                         pivot_tol, st, bar, skip.done, &need_sync))
+    if (!prog_phase<T, 2, BATCH>(PS.p[3], d, v, x, ld, S, sm, pivot_tol, st, bar, skip.done,
+                                 &need_sync))
       return;
-    if (!run_phase<T, 3>(plan.lt_sl, plan.lt_nl, d.lt_sc, d.lt_cols, d, v, x, ld, S,
-                         pivot_tol, st, bar, skip.done, &need_sync))
+    if (!prog_phase<T, 3, BATCH>(PS.p[4], d, v, x, ld, S, sm, pivot_tol, st, bar, skip.done,
+                                 &need_sync))
       return;
   }
 }
 
-// Largest co-resident grid for the persistent kernel (0 if cooperative
-// launches are unsupported).
-template <typename T>
-int persistent_grid() {
+template <typename T, bool BATCH>
+size_t prog_smem_bytes(int max_locals) {
+  return (size_t)(kProgBlock / 32) * max_locals * (BATCH ? 32 : 1) * sizeof(T);
+}
+
+// Largest co-resident grid of k_prog_persistent for the given table size.
+template <typename T, bool BATCH>
+int prog_persistent_grid(int max_locals) {
   int dev = 0, coop = 0, sms = 0, per_sm = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return 0;
   if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop)
     return 0;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_persistent<T>,
-                                                    kPersistentBlock, 0) != cudaSuccess)
+  const size_t smem = prog_smem_bytes<T, BATCH>(max_locals);
+  if (cudaFuncSetAttribute(k_prog_persistent<T, BATCH>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_prog_persistent<T, BATCH>,
+                                                    kProgBlock, smem) != cudaSuccess)
     return 0;
   return sms * per_sm;
 }
 
-template <typename T>
-int launch_persistent(const PersistentPlan& plan, const DevStruct& d, T* v, T* x, int ld,
-                      int S, double pivot_tol, DevStatus* st, unsigned int* bar,
-                      int max_grid, int phases, cudaStream_t stream,
-                      SkipDone skip = SkipDone{nullptr, nullptr}) {
+template <typename T, bool BATCH>
+int launch_prog_persistent(const ProgSetDev& PS, int max_chains, const DevStruct& d, T* v,
+                           T* x, int ld, int S, double pivot_tol, DevStatus* st,
+                           unsigned int* bar, int max_grid, int phases, cudaStream_t stream,
+                           SkipDone skip) {
   if (max_grid <= 0) return 1;
-  const int64_t want = ((int64_t)plan.max_chains * ld + kPersistentBlock - 1) / kPersistentBlock;
+  const int64_t items = (int64_t)max_chains * (BATCH ? ld / 32 : 1);
+  const int64_t want = (items + kProgBlock / 32 - 1) / (kProgBlock / 32);
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(want, max_grid));
   if (cudaMemsetAsync(bar, 0, 3 * sizeof(unsigned int), stream) != cudaSuccess) return 1;
-  void* args[] = {(void*)&plan, (void*)&d, (void*)&v, (void*)&x, (void*)&ld, (void*)&S,
+  void* args[] = {(void*)&PS, (void*)&d, (void*)&v, (void*)&x, (void*)&ld, (void*)&S,
                   (void*)&pivot_tol, (void*)&st, (void*)&bar, (void*)&phases, (void*)&skip};
-  if (cudaLaunchCooperativeKernel((const void*)k_persistent<T>, dim3(grid),
-                                  dim3(kPersistentBlock), args, 0, stream) != cudaSuccess)
+  const size_t smem = prog_smem_bytes<T, BATCH>(PS.p[0].max_locals);
+  if (cudaLaunchCooperativeKernel((const void*)k_prog_persistent<T, BATCH>, dim3(grid),
+                                  dim3(kProgBlock), args, smem, stream) != cudaSuccess)
     return 1;
   return 0;
 }

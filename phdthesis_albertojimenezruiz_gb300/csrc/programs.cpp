@@ -1,0 +1,208 @@
+// Chain program compiler (see programs.hpp).
+#include "programs.hpp"
+
+#include <algorithm>
+
+namespace pvglu {
+
+namespace {
+
+// Local table under construction for one segment.
+struct Table {
+  std::vector<int> loc_of_x, loc_of_v;  // -1 when absent
+  std::vector<int> used_x, used_v;      // for resetting
+  std::vector<int> loads;
+  std::vector<Op> ops;
+  std::vector<int> units;               // units computed in this segment
+  void init(int n, int64_t nnz) {
+    loc_of_x.assign(n, -1);
+    loc_of_v.assign(nnz, -1);
+  }
+  int size() const { return (int)loads.size(); }
+  void reset() {
+    for (int i : used_x) loc_of_x[i] = -1;
+    for (int q : used_v) loc_of_v[q] = -1;
+    used_x.clear();
+    used_v.clear();
+    loads.clear();
+    ops.clear();
+    units.clear();
+  }
+  // Refactor tables hold LU slots only: ref = slot * 2 + store.
+  int slot_refactor(int q, bool own) {
+    if (loc_of_v[q] >= 0) return loc_of_v[q];
+    loc_of_v[q] = size();
+    used_v.push_back(q);
+    loads.push_back(q * 2 + (own ? 1 : 0));
+    return loc_of_v[q];
+  }
+  // Solve tables: x entries (ref = i * 2 + store) and read-only slots
+  // (ref = -(q + 1)).
+  int x(int i, bool own) {
+    if (loc_of_x[i] >= 0) return loc_of_x[i];
+    loc_of_x[i] = size();
+    used_x.push_back(i);
+    loads.push_back(i * 2 + (own ? 1 : 0));
+    return loc_of_x[i];
+  }
+  int v(int q) {
+    if (loc_of_v[q] >= 0) return loc_of_v[q];
+    loc_of_v[q] = size();
+    used_v.push_back(q);
+    loads.push_back(-(q + 1));
+    return loc_of_v[q];
+  }
+};
+
+const LevelSet& level_set(const Symbolic& s, int kind) {
+  switch (kind) {
+    case 0: return s.l;
+    case 1: return s.u;
+    case 3: return s.lt;
+    default: return s.lu;
+  }
+}
+
+// Values a unit needs that are not yet in the table (upper bound: counts
+// distinct new entries).
+int new_locals(const Symbolic& s, int kind, int u, const Table& t) {
+  int cnt = 0;
+  std::vector<int> seen_x, seen_v;
+  auto need_x = [&](int i) {
+    if (t.loc_of_x[i] < 0 && std::find(seen_x.begin(), seen_x.end(), i) == seen_x.end()) {
+      seen_x.push_back(i);
+      cnt++;
+    }
+  };
+  auto need_v = [&](int q) {
+    if (t.loc_of_v[q] < 0 && std::find(seen_v.begin(), seen_v.end(), q) == seen_v.end()) {
+      seen_v.push_back(q);
+      cnt++;
+    }
+  };
+  if (kind == -1) {
+    const int c0 = s.csc_colptr[u], dk = s.diag_slot[u], c1 = s.csc_colptr[u + 1];
+    for (int q = c0; q < c1; q++) need_v(q);
+    for (int p = c0; p < dk; p++) {
+      const int j = s.csc_row[p];
+      for (int q = s.diag_slot[j] + 1; q < s.csc_colptr[j + 1]; q++) need_v(q);
+    }
+  } else if (kind == 0 || kind == 1) {
+    need_x(u);
+    const auto& ptr = kind == 0 ? s.lrow_ptr : s.urow_ptr;
+    const auto& slot = kind == 0 ? s.lrow_slot : s.urow_slot;
+    const auto& col = kind == 0 ? s.lrow_col : s.urow_col;
+    for (int e = ptr[u]; e < ptr[u + 1]; e++) {
+      need_x(col[e]);
+      need_v(slot[e]);
+    }
+    if (kind == 1) need_v(s.diag_slot[u]);
+  } else {
+    need_x(u);
+    const int b = kind == 2 ? s.csc_colptr[u] : s.diag_slot[u] + 1;
+    const int e = kind == 2 ? s.diag_slot[u] : s.csc_colptr[u + 1];
+    for (int q = b; q < e; q++) {
+      need_x(s.csc_row[q]);
+      need_v(q);
+    }
+    if (kind == 2) need_v(s.diag_slot[u]);
+  }
+  return cnt;
+}
+
+void emit_unit(const Symbolic& s, int kind, int u, Table& t) {
+  if (kind == -1) {
+    const int c0 = s.csc_colptr[u], dk = s.diag_slot[u], c1 = s.csc_colptr[u + 1];
+    for (int q = c0; q < c1; q++) t.slot_refactor(q, true);  // own slots, CSC order
+    for (int p = c0; p < dk; p++) {
+      const int j = s.csc_row[p];
+      const int q0 = s.diag_slot[j] + 1;
+      const int up = t.slot_refactor(p, true);
+      for (int q = q0; q < s.csc_colptr[j + 1]; q++) {
+        const int tgt = s.upd_tgt[s.upd_ptr[p] + (q - q0)];
+        const int lq = t.slot_refactor(q, false);
+        t.ops.push_back(Op{OP_FNMA, t.loc_of_v[tgt], lq, up});
+      }
+    }
+    const int cnt = c1 - dk - 1;
+    t.ops.push_back(Op{OP_SCALE | (cnt << 4), t.loc_of_v[dk], cnt > 0 ? t.loc_of_v[dk + 1] : 0, u});
+  } else if (kind == 0 || kind == 1) {
+    const int xi = t.x(u, true);
+    const auto& ptr = kind == 0 ? s.lrow_ptr : s.urow_ptr;
+    const auto& slot = kind == 0 ? s.lrow_slot : s.urow_slot;
+    const auto& col = kind == 0 ? s.lrow_col : s.urow_col;
+    // L rows take their updates in ascending column order, U rows in
+    // descending order: the order in which the reference's column sweeps
+    // deliver them (GLU_CSC_CPU_Triangular.cpp:27-43).
+    const int n_e = ptr[u + 1] - ptr[u];
+    for (int k = 0; k < n_e; k++) {
+      const int e = kind == 0 ? ptr[u] + k : ptr[u + 1] - 1 - k;
+      const int xj = t.x(col[e], false);
+      const int vq = t.v(slot[e]);
+      t.ops.push_back(Op{OP_FNMA, xi, vq, xj});
+    }
+    if (kind == 1) t.ops.push_back(Op{OP_DIV, xi, t.v(s.diag_slot[u]), 0});
+  } else {
+    const int xj = t.x(u, true);
+    const int b = kind == 2 ? s.csc_colptr[u] : s.diag_slot[u] + 1;
+    const int e = kind == 2 ? s.diag_slot[u] : s.csc_colptr[u + 1];
+    for (int q = b; q < e; q++) {
+      const int xi = t.x(s.csc_row[q], false);
+      const int vq = t.v(q);
+      t.ops.push_back(Op{OP_FNMA, xj, vq, xi});
+    }
+    if (kind == 2) t.ops.push_back(Op{OP_DIV, xj, t.v(s.diag_slot[u]), 0});
+  }
+  t.units.push_back(u);
+}
+
+}  // namespace
+
+void build_chain_program(const Symbolic& s, int kind, int max_locals, ChainProgram& out) {
+  out = ChainProgram();
+  out.kind = kind;
+  out.max_locals = max_locals;
+  const LevelSet& ls = level_set(s, kind);
+  out.level_chain = ls.start_levels;
+  Table t;
+  t.init(s.n, s.nnz_lu);
+  auto close = [&]() {
+    if (t.units.empty()) return;
+    Segment g;
+    g.load_begin = (int)out.loads.size();
+    g.n_load = t.size();
+    g.op_begin = (int)out.ops.size();
+    g.n_op = (int)t.ops.size();
+    out.loads.insert(out.loads.end(), t.loads.begin(), t.loads.end());
+    out.ops.insert(out.ops.end(), t.ops.begin(), t.ops.end());
+    out.seg.push_back(g);
+    t.reset();
+  };
+  for (int c = 0; c < ls.num_chains(); c++) {
+    out.chain_seg.push_back((int)out.seg.size());
+    const int first_seg = (int)out.seg.size();
+    for (int k = ls.start_chains[c]; k < ls.start_chains[c + 1]; k++) {
+      const int u = ls.columns[k];
+      int need = new_locals(s, kind, u, t);
+      if (t.size() + need > max_locals && !t.units.empty()) {
+        close();
+        need = new_locals(s, kind, u, t);
+      }
+      if (need > max_locals) {
+        // Too wide for the local table: executed from global memory, after
+        // the segment collected so far (chain order is execution order).
+        close();
+        out.seg.push_back(Segment{0, -1, u, 0});
+        out.direct_segments++;
+        continue;
+      }
+      emit_unit(s, kind, u, t);
+    }
+    close();
+    out.longest_chain_segments =
+        std::max(out.longest_chain_segments, (int)out.seg.size() - first_seg);
+  }
+  out.chain_seg.push_back((int)out.seg.size());
+}
+
+}  // namespace pvglu

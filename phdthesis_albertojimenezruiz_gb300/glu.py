@@ -123,6 +123,12 @@ class Numeric:
         N.check(N.lib().pvglu_solve(self.handle, _ptr(x), flags, _stream_ptr(stream)),
                 "pvglu_solve")
 
+    def refactor_solve(self, x, transpose: bool = False, original: bool = False,
+                       stream=None) -> None:
+        flags = (N.SOLVE_TRANSPOSE if transpose else 0) | (N.SOLVE_ORIGINAL if original else 0)
+        N.check(N.lib().pvglu_refactor_solve(self.handle, _ptr(x), flags, _stream_ptr(stream)),
+                "pvglu_refactor_solve")
+
     def solve_refined(self, a_values, b, x, tol=1e-12, max_sweeps=10, sweeps=None,
                       stream=None) -> None:
         N.check(N.lib().pvglu_solve_refined(self.handle, _ptr(a_values), _ptr(b), _ptr(x),

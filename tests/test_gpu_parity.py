@@ -19,11 +19,11 @@ from conftest import golden_names, load_golden, norm_err, rel_err
 import matrices as M
 from oracle import oracle as O
 from phdthesis_albertojimenezruiz_gb300 import (FP32, FP64, SCHED_LEVELS, SCHED_PERSISTENT,
-                                                Numeric, Plant, Symbolic)
+                                                SCHED_THREAD_CHAIN, Numeric, Plant, Symbolic)
 from phdthesis_albertojimenezruiz_gb300 import _native as N
 
 pytestmark = pytest.mark.gpu
-SCHEDULES = [SCHED_LEVELS, SCHED_PERSISTENT]
+SCHEDULES = [SCHED_LEVELS, SCHED_PERSISTENT, SCHED_THREAD_CHAIN]
 TOL64 = 1e-12
 
 
@@ -91,6 +91,23 @@ def test_golden_single_fp64(cuda, name, schedule):
     num.solve(x, original=True)
     torch.cuda.synchronize()
     assert norm_err(x.cpu().numpy(), g["x"]) <= TOL64
+
+
+@pytest.mark.parametrize("schedule", SCHEDULES)
+@pytest.mark.parametrize("name", golden_names())
+def test_golden_fp64_bit_exact(cuda, name, schedule):
+    """Stronger than the 1e-12 bar: the FP64 kernels apply every update to an
+    entry in the reference's sequential order with separately rounded
+    multiply and subtract, so factors and solution equal the reference's
+    GLU_CSC_CPU_sequential + Substitute_LU_Vector_b_CSC_CPU bit for bit."""
+    g = load_golden(name)
+    s = Symbolic(g["rowptr"], g["colidx"], g["perm_amd"])
+    num = Numeric(s, 1, FP64, schedule)
+    num.scatter(dev(g["a"]))
+    x = dev(to_perm(g, g["b"]))
+    num.refactor_solve(x)
+    assert np.array_equal(values_of(num, int(s.nnz_lu))[:, 0], g["lu_seq"])
+    assert np.array_equal(x.cpu().numpy(), g["x_perm"])
 
 
 @pytest.mark.parametrize("schedule", SCHEDULES)
