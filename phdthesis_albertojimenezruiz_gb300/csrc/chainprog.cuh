@@ -93,20 +93,32 @@ __device__ __forceinline__ void prog_run_chain(const ProgDev& P, const DevStruct
     const int* lr = P.loads + sg.x;
     const int nl = sg.y;
     if (BATCH) {
-      int l = 0;
-      for (; l + kLoadUnroll <= nl; l += kLoadUnroll) {
-        int r[kLoadUnroll];
-        T val[kLoadUnroll];
+      // kChunk refs per coalesced load, broadcast by shuffles: kChunk
+      // independent value loads in flight per lane before the first use.
+      constexpr int kChunk = sizeof(T) == 8 ? 16 : 32;
+      for (int base = 0; base < nl; base += kChunk) {
+        const int cnt = min(kChunk, nl - base);
+        const int my_ref = lane < cnt ? __ldg(lr + base + lane) : 0;
+        T val[kChunk];
 #pragma unroll
-        for (int k = 0; k < kLoadUnroll; k++) r[k] = __ldg(lr + l + k);
+        for (int k = 0; k < kChunk; k++) {
+          const int r = __shfl_sync(0xffffffffu, my_ref, k);
+          if (k < cnt) val[k] = prog_fetch<T, KIND>(r, v, x, ld, s);
+        }
 #pragma unroll
-        for (int k = 0; k < kLoadUnroll; k++) val[k] = prog_fetch<T, KIND>(r[k], v, x, ld, s);
-#pragma unroll
-        for (int k = 0; k < kLoadUnroll; k++) sm[(l + k) * 32 + lane] = val[k];
+        for (int k = 0; k < kChunk; k++)
+          if (k < cnt) sm[(base + k) * 32 + lane] = val[k];
       }
-      for (; l < nl; l++) sm[l * 32 + lane] = prog_fetch<T, KIND>(__ldg(lr + l), v, x, ld, s);
       prog_exec_ops<T, KIND, true>(P.ops + sg.z, sg.w, sm, lane, s, S, pivot_tol, st);
-      for (int l2 = 0; l2 < nl; l2++) prog_store<T, KIND>(__ldg(lr + l2), sm[l2 * 32 + lane], v, x, ld, s);
+      for (int base = 0; base < nl; base += 32) {
+        const int cnt = min(32, nl - base);
+        const int my_ref = lane < cnt ? __ldg(lr + base + lane) : 0;
+#pragma unroll 4
+        for (int k = 0; k < cnt; k++) {
+          const int r = __shfl_sync(0xffffffffu, my_ref, k);
+          prog_store<T, KIND>(r, sm[(base + k) * 32 + lane], v, x, ld, s);
+        }
+      }
     } else {
       for (int l = lane; l < nl; l += 32) sm[l] = prog_fetch<T, KIND>(__ldg(lr + l), v, x, 1, 0);
       __syncwarp();
