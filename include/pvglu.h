@@ -190,6 +190,27 @@ int pvglu_refine_system_host(pvglu_numeric* h, const double* a_values_host,
                              const double* b_host, double* x_host, double tol, int max_sweeps,
                              int* sweeps_out, void* stream);
 
+/* ---------------- allocation-free solve ---------------------------------- */
+
+/* The original-order solve of pvglu_solve (flags: PVGLU_SOLVE_TRANSPOSE
+ * optional, PVGLU_SOLVE_ORIGINAL implied) for FP64 handles, with its permuted
+ * work vector in a static device array owned by the library instead of the
+ * handle's work buffer.  It calls no cudaMalloc or cudaFree and no other
+ * allocating routine.  It is meant for callers whose solve path must not
+ * allocate device memory, for example an application that reserves the GPU's
+ * memory up front and forbids further allocation, or a real-time loop where
+ * an allocation's implicit synchronisation is not acceptable.  (The handle
+ * itself is still created beforehand with pvglu_numeric_create.)
+ * Limit: n * ld <= 1,048,576 FP64 entries (8 MiB, reserved on every GPU
+ * that loads the library until the process exits); larger handles get
+ * PVGLU_ERR_TOO_LARGE.  The first call on a device looks the array up with
+ * cudaGetSymbolAddress for that device, so make that first call before any
+ * stream capture.  All calls share the array and it keeps the last call's
+ * contents; nothing in it needs to start at zero.  Calls whose work overlaps
+ * on the GPU (other streams, other threads) race on the array.
+ * No counterpart in the reference. */
+int pvglu_solve_noalloc(pvglu_numeric* h, double* x, int flags, void* stream);
+
 /* ---------------- failure-path self-test --------------------------------- */
 
 /* Runs one bounded grid barrier that waits for one block more than it

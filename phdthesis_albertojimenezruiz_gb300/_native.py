@@ -75,6 +75,7 @@ _SIGS = {
     "pvglu_solve_refined": ([_P, _P, _P, _P, C.c_double, _I, _P, _P], _I),
     "pvglu_selftest_barrier_timeout": ([_I, C.c_longlong, _IP, _IP], _I),
     "pvglu_refine_system_host": ([_P, _P, _P, _P, C.c_double, _I, _P, _P], _I),
+    "pvglu_solve_noalloc": ([_P, _P, _I, _P], _I),
     "pvglu_plant_create": ([_I, _I, _I, C.POINTER(_P)], _I),
     "pvglu_plant_destroy": ([_P], _I),
     "pvglu_plant_get_info": ([_P, C.POINTER(PlantInfo)], _I),

@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -584,6 +585,65 @@ int pvglu_refine_system_host(pvglu_numeric* h, const double* a_values_host,
   if (rc) return rc;
   PVGLU_CUDA(cudaMemcpyAsync(x_host, h->x64, (size_t)h->n * h->ld * sizeof(double),
                              cudaMemcpyDeviceToHost, st));
+  return PVGLU_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free solve.  Its permuted work vector lives in this file-scope
+// device array instead of the handle's work buffer.  Every GPU that loads
+// the library reserves the array until the process exits.  Host code must not
+// use the array's name as a device address: the address is obtained once per
+// device with cudaGetSymbolAddress.
+constexpr int64_t kNoAllocScratchElems = int64_t(1) << 20;  // 8 MiB of FP64
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocScratchElems];
+
+namespace {
+std::mutex g_noalloc_mu;
+double* g_noalloc_ptr[128] = {};  // per device ordinal
+
+int noalloc_scratch(double** out) {
+  int dev = 0;
+  PVGLU_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 128) return fail(PVGLU_ERR_BAD_ARG, "device ordinal out of range");
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess)
+      return fail(PVGLU_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    g_noalloc_ptr[dev] = static_cast<double*>(p);
+  }
+  *out = g_noalloc_ptr[dev];
+  return PVGLU_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int pvglu_solve_noalloc(pvglu_numeric* h, double* x, int flags, void* stream) {
+  if (!h || !x) return fail(PVGLU_ERR_BAD_ARG, "NULL argument");
+  if (h->precision != PVGLU_FP64) return fail(PVGLU_ERR_BAD_ARG, "needs an FP64 handle");
+  const int64_t need = (int64_t)h->n * h->ld;
+  if (need > kNoAllocScratchElems)
+    return fail(PVGLU_ERR_TOO_LARGE,
+                "n * ld = " + std::to_string(need) + " exceeds the static scratch of " +
+                    std::to_string(kNoAllocScratchElems) + " FP64 entries");
+  double* w = nullptr;
+  int rc = noalloc_scratch(&w);
+  if (rc) return rc;
+  cudaStream_t st = as_stream(stream);
+  const bool tr = (flags & PVGLU_SOLVE_TRANSPOSE) != 0;
+  // Same sequence as the original-order pvglu_solve; every entry of w that a
+  // solve reads is written by the gather first, so nothing needs clearing.
+  const int* in_perm = tr ? h->d.col_orig : h->d.row_orig;
+  const int* out_perm = tr ? h->d.row_orig : h->d.col_orig;
+  permute<double, double>(h, in_perm, x, w, true, st);
+  rc = solve_permuted<double>(h, w, tr, st);
+  if (rc) return rc;
+  permute<double, double>(h, out_perm, w, x, false, st);
+  PVGLU_CUDA(cudaGetLastError());
   return PVGLU_OK;
 }
 
