@@ -321,6 +321,13 @@ int pvglu_numeric_create(const pvglu_symbolic* sym, int n_scenarios, int precisi
   *out = nullptr;
   const auto& s = sym->s;
   if (s.update_count > 0x7fffffffLL) return fail(PVGLU_ERR_TOO_LARGE, "update list > 2^31");
+  {
+    // The chain programs address values with 32-bit offsets.
+    const int64_t ld_max = n_scenarios == 1 ? 1 : ((n_scenarios + 31) / 32) * 32;
+    if (s.nnz_lu * ld_max >= 0x7fffffffLL || (int64_t)s.n * ld_max >= 0x7fffffffLL ||
+        s.nnz_a * ld_max >= 0x7fffffffLL)
+      return fail(PVGLU_ERR_TOO_LARGE, "nnz x scenarios exceeds 2^31 values per handle");
+  }
   auto* h = new pvglu_numeric();
   h->sym = sym;
   h->n = s.n;
@@ -394,22 +401,24 @@ int pvglu_numeric_create(const pvglu_symbolic* sym, int n_scenarios, int precisi
   // Chain programs for the shared-memory schedules.  Table budget: a warp's
   // tile is max_locals x 32 scenarios (batched) or max_locals (single).
   h->batch = h->ld > 1;
-  h->max_locals = h->batch ? (precision == PVGLU_FP32 ? 96 : 64) : 1024;
+  h->max_locals = h->batch ? (precision == PVGLU_FP32 ? 64 : 40) : pvglu::kMaxLocals;
   for (int ph = 0; ph < 5; ph++) {
     pvglu::ChainProgram prog;
     pvglu::build_chain_program(s, ph - 1, h->max_locals, prog);
-    std::vector<int4> seg(prog.seg.size()), ops(prog.ops.size());
-    for (size_t i = 0; i < seg.size(); i++)
-      seg[i] = make_int4(prog.seg[i].load_begin, prog.seg[i].n_load, prog.seg[i].op_begin,
-                         prog.seg[i].n_op);
-    for (size_t i = 0; i < ops.size(); i++)
-      ops[i] = make_int4(prog.ops[i].code, prog.ops[i].a, prog.ops[i].b, prog.ops[i].c);
+    std::vector<int4> seg(prog.seg.size()), ops(prog.ops.size() / 4);
+    for (size_t i = 0; i < seg.size(); i++) {
+      const auto& g = prog.seg[i];
+      seg[i] = make_int4(g.load_begin, g.n_load < 0 ? -1 : (g.n_load | (g.n_own << 16)),
+                         g.op_begin, g.n_op);
+    }
+    std::memcpy(ops.data(), prog.ops.data(), ops.size() * sizeof(int4));
     pvglu::ProgDev& P = h->progs.p[ph];
     rc |= h->put(prog.level_chain, &P.level_chain);
     rc |= h->put(prog.chain_seg, &P.chain_seg);
     rc |= h->put(seg, &P.seg);
     rc |= h->put(prog.loads, &P.loads);
     rc |= h->put(ops, &P.ops);
+    rc |= h->put(prog.op_col, &P.op_col);
     P.n_levels = (int)prog.level_chain.size() - 1;
     P.max_locals = h->max_locals;
     h->prog_level_chain[ph] = prog.level_chain;

@@ -4,8 +4,8 @@
 // = scenario; its local table is a [max_locals][32] tile of shared memory, so
 // every table access is bank-conflict free and every global access of the
 // load/store phases is one coalesced 128-byte (FP32) or 256-byte (FP64) row.
-// The load phase issues kUnroll independent loads per lane before the first
-// use, which keeps many requests in flight per warp.
+// The load phase fetches 32 refs with one coalesced load and broadcasts them
+// with shuffles, keeping kChunk independent value loads in flight per lane.
 //
 // Single mode (BATCH = false): a warp runs one chain of the one scenario; the
 // lanes split the loads and stores of each segment, lane 0 executes the
@@ -22,53 +22,59 @@ struct ProgDev {
   const int* level_chain;  // [levels + 1]
   int n_levels;
   const int* chain_seg;    // [chains + 1]
-  const int4* seg;         // Segment records
+  const int4* seg;         // {load_begin, n_load | n_own << 16 (or -1: DIRECT), op_begin, n_op}
   const int* loads;
-  const int4* ops;
+  const int4* ops;         // packed operations, 4 per int4
+  const int* op_col;       // column of each SCALE operation
   int max_locals;
 };
 
-constexpr int kLoadUnroll = 8;
-
-// Fetch / store of one table entry.  Refactor (KIND < 0): LU slots,
-// ref = slot * 2 + own.  Solves: x entries (ref = i * 2 + own) or read-only
-// LU slots (ref = -(slot + 1)).
+// Offsets are 32-bit: the handle guarantees nnz_lu * ld and n * ld < 2^31.
 template <typename T, int KIND>
-__device__ __forceinline__ T prog_fetch(int ref, const T* __restrict__ v,
-                                        const T* __restrict__ x, int ld, int s) {
-  if (KIND < 0) return ldv(v + (int64_t)(ref >> 1) * ld + s);
-  if (ref >= 0) return ldv(x + (int64_t)(ref >> 1) * ld + s);
-  return ldv(v + (int64_t)(-ref - 1) * ld + s);
+__device__ __forceinline__ T prog_fetch(int ref, const T* __restrict__ vs,
+                                        const T* __restrict__ xs, int ld) {
+  if (KIND < 0) return ldv(vs + (unsigned)ref * (unsigned)ld);
+  if (ref >= 0) return ldv(xs + (unsigned)ref * (unsigned)ld);
+  return ldv(vs + (unsigned)(-ref - 1) * (unsigned)ld);
 }
 
 template <typename T, int KIND>
-__device__ __forceinline__ void prog_store(int ref, T val, T* __restrict__ v,
-                                           T* __restrict__ x, int ld, int s) {
-  if (!(ref & 1) || ref < 0) return;
-  if (KIND < 0) v[(int64_t)(ref >> 1) * ld + s] = val;
-  else x[(int64_t)(ref >> 1) * ld + s] = val;
+__device__ __forceinline__ void prog_store(int ref, T val, T* __restrict__ vs,
+                                           T* __restrict__ xs, int ld) {
+  if (KIND < 0) vs[(unsigned)ref * (unsigned)ld] = val;
+  else xs[(unsigned)ref * (unsigned)ld] = val;
 }
 
-template <typename T, int KIND, bool BATCH>
-__device__ __forceinline__ void prog_exec_ops(const int4* __restrict__ ops, int n_op, T* sm,
-                                              int lane, int s, int S, double pivot_tol,
-                                              DevStatus* st) {
-#define PVGLU_L(i) sm[BATCH ? (i) * 32 + lane : (i)]
-  for (int o = 0; o < n_op; o++) {
-    const int4 q = __ldg(ops + o);
-    const int code = q.x & 15;
-    if (code == OP_FNMA) {
-      PVGLU_L(q.y) = fnms(PVGLU_L(q.y), PVGLU_L(q.z), PVGLU_L(q.w));
-    } else if (code == OP_SCALE) {
-      const T p = PVGLU_L(q.y);
-      if (!(fabs((double)p) >= pivot_tol) && s < S) report_error(st, 3, q.w, s);
-      const int cnt = q.x >> 4;
-      for (int i = 0; i < cnt; i++) PVGLU_L(q.z + i) = PVGLU_L(q.z + i) / p;
-    } else {
-      PVGLU_L(q.y) = PVGLU_L(q.y) / PVGLU_L(q.z);
-    }
+template <typename T, bool BATCH>
+__device__ __forceinline__ void prog_exec_op(uint32_t op, int op_index, const int* op_col,
+                                             T* sml, int s, int S, double pivot_tol,
+                                             DevStatus* st) {
+  constexpr int SH = BATCH ? 5 : 0;
+  const int code = op & 3;
+  const int a = (op >> 2) & 1023, b = (op >> 12) & 1023, c = (op >> 22) & 1023;
+  if (code == OP_FNMA) {
+    sml[a << SH] = fnms(sml[a << SH], sml[b << SH], sml[c << SH]);
+  } else if (code == OP_SCALE) {
+    const T p = sml[a << SH];
+    if (!(fabs((double)p) >= pivot_tol) && s < S) report_error(st, 3, op_col[op_index], s);
+    for (int i = 0; i < c; i++) sml[(b + i) << SH] = sml[(b + i) << SH] / p;
+  } else if (code == OP_DIV) {
+    sml[a << SH] = sml[a << SH] / sml[b << SH];
   }
-#undef PVGLU_L
+}
+
+template <typename T, bool BATCH>
+__device__ __forceinline__ void prog_exec_ops(const ProgDev& P, int op_begin, int n_op, T* sml,
+                                              int s, int S, double pivot_tol, DevStatus* st) {
+  const int4* o4 = P.ops + (op_begin >> 2);
+  for (int k = 0; k < (n_op >> 2); k++) {
+    const int4 w = __ldg(o4 + k);
+    const int base = op_begin + 4 * k;
+    prog_exec_op<T, BATCH>((uint32_t)w.x, base, P.op_col, sml, s, S, pivot_tol, st);
+    prog_exec_op<T, BATCH>((uint32_t)w.y, base + 1, P.op_col, sml, s, S, pivot_tol, st);
+    prog_exec_op<T, BATCH>((uint32_t)w.z, base + 2, P.op_col, sml, s, S, pivot_tol, st);
+    prog_exec_op<T, BATCH>((uint32_t)w.w, base + 3, P.op_col, sml, s, S, pivot_tol, st);
+  }
 }
 
 // Runs every segment of `chain` for scenario s (BATCH) or the single
@@ -79,6 +85,8 @@ __device__ __forceinline__ void prog_run_chain(const ProgDev& P, const DevStruct
                                                int s, int S, T* sm, double pivot_tol,
                                                DevStatus* st) {
   const int lane = threadIdx.x & 31;
+  T* vs = v + s;
+  T* xs = KIND < 0 ? nullptr : x + s;
   const int g_end = __ldg(P.chain_seg + chain + 1);
   for (int g = __ldg(P.chain_seg + chain); g < g_end; g++) {
     const int4 sg = __ldg(P.seg + g);
@@ -91,11 +99,10 @@ __device__ __forceinline__ void prog_run_chain(const ProgDev& P, const DevStruct
       continue;
     }
     const int* lr = P.loads + sg.x;
-    const int nl = sg.y;
+    const int nl = sg.y & 0xffff, n_own = sg.y >> 16;
     if (BATCH) {
-      // kChunk refs per coalesced load, broadcast by shuffles: kChunk
-      // independent value loads in flight per lane before the first use.
-      constexpr int kChunk = sizeof(T) == 8 ? 16 : 32;
+      constexpr int kChunk = 16;
+      T* sml = sm + lane;
       for (int base = 0; base < nl; base += kChunk) {
         const int cnt = min(kChunk, nl - base);
         const int my_ref = lane < cnt ? __ldg(lr + base + lane) : 0;
@@ -103,28 +110,28 @@ __device__ __forceinline__ void prog_run_chain(const ProgDev& P, const DevStruct
 #pragma unroll
         for (int k = 0; k < kChunk; k++) {
           const int r = __shfl_sync(0xffffffffu, my_ref, k);
-          if (k < cnt) val[k] = prog_fetch<T, KIND>(r, v, x, ld, s);
+          if (k < cnt) val[k] = prog_fetch<T, KIND>(r, vs, xs, ld);
         }
 #pragma unroll
         for (int k = 0; k < kChunk; k++)
-          if (k < cnt) sm[(base + k) * 32 + lane] = val[k];
+          if (k < cnt) sml[(base + k) << 5] = val[k];
       }
-      prog_exec_ops<T, KIND, true>(P.ops + sg.z, sg.w, sm, lane, s, S, pivot_tol, st);
-      for (int base = 0; base < nl; base += 32) {
-        const int cnt = min(32, nl - base);
+      prog_exec_ops<T, true>(P, sg.z, sg.w, sml, s, S, pivot_tol, st);
+      for (int base = 0; base < n_own; base += 32) {
+        const int cnt = min(32, n_own - base);
         const int my_ref = lane < cnt ? __ldg(lr + base + lane) : 0;
 #pragma unroll 4
         for (int k = 0; k < cnt; k++) {
           const int r = __shfl_sync(0xffffffffu, my_ref, k);
-          prog_store<T, KIND>(r, sm[(base + k) * 32 + lane], v, x, ld, s);
+          prog_store<T, KIND>(r, sml[(base + k) << 5], vs, xs, ld);
         }
       }
     } else {
-      for (int l = lane; l < nl; l += 32) sm[l] = prog_fetch<T, KIND>(__ldg(lr + l), v, x, 1, 0);
+      for (int l = lane; l < nl; l += 32) sm[l] = prog_fetch<T, KIND>(__ldg(lr + l), v, x, 1);
       __syncwarp();
-      if (lane == 0) prog_exec_ops<T, KIND, false>(P.ops + sg.z, sg.w, sm, 0, 0, S, pivot_tol, st);
+      if (lane == 0) prog_exec_ops<T, false>(P, sg.z, sg.w, sm, 0, S, pivot_tol, st);
       __syncwarp();
-      for (int l = lane; l < nl; l += 32) prog_store<T, KIND>(__ldg(lr + l), sm[l], v, x, 1, 0);
+      for (int l = lane; l < n_own; l += 32) prog_store<T, KIND>(__ldg(lr + l), sm[l], v, x, 1);
       __syncwarp();
     }
   }
@@ -136,14 +143,15 @@ template <typename T, int KIND, bool BATCH>
 __device__ __forceinline__ void prog_run_level(const ProgDev& P, const DevStruct& d, int cb,
                                                int ce, T* __restrict__ v, T* __restrict__ x,
                                                int ld, int S, T* sm_warp, double pivot_tol,
-                                               DevStatus* st, const int* done,
-                                               int64_t warp_id, int64_t n_warps) {
-  const int groups = BATCH ? ld / 32 : 1;
-  const int64_t items = (int64_t)(ce - cb) * groups;
+                                               DevStatus* st, const int* done, int warp_id,
+                                               int n_warps) {
+  const int groups = BATCH ? ld >> 5 : 1;
+  const int items = (ce - cb) * groups;
   const int lane = threadIdx.x & 31;
-  for (int64_t it = warp_id; it < items; it += n_warps) {
-    const int c = cb + (int)(it / groups);
-    const int s = BATCH ? (int)(it % groups) * 32 + lane : 0;
+  for (int it = warp_id; it < items; it += n_warps) {
+    const int ci = BATCH ? it / groups : it;
+    const int c = cb + ci;
+    const int s = BATCH ? ((it - ci * groups) << 5) + lane : 0;
     if (BATCH && done && __all_sync(0xffffffffu, s >= S || done[s])) continue;
     prog_run_chain<T, KIND, BATCH>(P, d, c, v, x, ld, s, S, sm_warp, pivot_tol, st);
   }
@@ -156,8 +164,8 @@ __global__ void k_prog_level(ProgDev P, DevStruct d, int cb, int ce, T* __restri
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* sm = reinterpret_cast<T*>(smem_raw) +
           (threadIdx.x >> 5) * P.max_locals * (BATCH ? 32 : 1);
-  const int64_t warp_id = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int warp_id = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int n_warps = (gridDim.x * blockDim.x) >> 5;
   prog_run_level<T, KIND, BATCH>(P, d, cb, ce, v, x, ld, S, sm, pivot_tol, st, done, warp_id,
                                  n_warps);
 }

@@ -88,8 +88,8 @@ __device__ __forceinline__ bool prog_phase(const ProgDev& P, const DevStruct& d,
                                            int ld, int S, T* sm, double pivot_tol,
                                            DevStatus* st, unsigned int* bar, const int* done,
                                            bool* need_sync) {
-  const int64_t warp_id = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int warp_id = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int n_warps = (gridDim.x * blockDim.x) >> 5;
   for (int lv = 0; lv < P.n_levels; lv++) {
     if (*need_sync && !grid_barrier(bar, st, gridDim.x, kBarrierMaxSpins)) return false;
     *need_sync = true;

@@ -7,49 +7,59 @@ namespace pvglu {
 
 namespace {
 
+struct RawOp {
+  int code, a, b, c, col;
+};
+
 // Local table under construction for one segment.
 struct Table {
   std::vector<int> loc_of_x, loc_of_v;  // -1 when absent
   std::vector<int> used_x, used_v;      // for resetting
-  std::vector<int> loads;
-  std::vector<Op> ops;
+  std::vector<int> refs;
+  std::vector<char> own;
+  std::vector<RawOp> ops;
   std::vector<int> units;               // units computed in this segment
   void init(int n, int64_t nnz) {
     loc_of_x.assign(n, -1);
     loc_of_v.assign(nnz, -1);
   }
-  int size() const { return (int)loads.size(); }
+  int size() const { return (int)refs.size(); }
   void reset() {
     for (int i : used_x) loc_of_x[i] = -1;
     for (int q : used_v) loc_of_v[q] = -1;
     used_x.clear();
     used_v.clear();
-    loads.clear();
+    refs.clear();
+    own.clear();
     ops.clear();
     units.clear();
   }
-  // Refactor tables hold LU slots only: ref = slot * 2 + store.
-  int slot_refactor(int q, bool own) {
-    if (loc_of_v[q] >= 0) return loc_of_v[q];
-    loc_of_v[q] = size();
-    used_v.push_back(q);
-    loads.push_back(q * 2 + (own ? 1 : 0));
+  int add(int ref, bool is_own) {
+    refs.push_back(ref);
+    own.push_back(is_own ? 1 : 0);
+    return size() - 1;
+  }
+  // Refactor tables hold LU slots only (ref = slot).
+  int slot_refactor(int q, bool is_own) {
+    if (loc_of_v[q] < 0) {
+      loc_of_v[q] = add(q, is_own);
+      used_v.push_back(q);
+    }
     return loc_of_v[q];
   }
-  // Solve tables: x entries (ref = i * 2 + store) and read-only slots
-  // (ref = -(q + 1)).
-  int x(int i, bool own) {
-    if (loc_of_x[i] >= 0) return loc_of_x[i];
-    loc_of_x[i] = size();
-    used_x.push_back(i);
-    loads.push_back(i * 2 + (own ? 1 : 0));
+  // Solve tables: x entries (ref = i) and read-only slots (ref = -(q + 1)).
+  int x(int i, bool is_own) {
+    if (loc_of_x[i] < 0) {
+      loc_of_x[i] = add(i, is_own);
+      used_x.push_back(i);
+    }
     return loc_of_x[i];
   }
   int v(int q) {
-    if (loc_of_v[q] >= 0) return loc_of_v[q];
-    loc_of_v[q] = size();
-    used_v.push_back(q);
-    loads.push_back(-(q + 1));
+    if (loc_of_v[q] < 0) {
+      loc_of_v[q] = add(-(q + 1), false);
+      used_v.push_back(q);
+    }
     return loc_of_v[q];
   }
 };
@@ -63,8 +73,7 @@ const LevelSet& level_set(const Symbolic& s, int kind) {
   }
 }
 
-// Values a unit needs that are not yet in the table (upper bound: counts
-// distinct new entries).
+// Number of values a unit needs that are not yet in the table.
 int new_locals(const Symbolic& s, int kind, int u, const Table& t) {
   int cnt = 0;
   std::vector<int> seen_x, seen_v;
@@ -117,15 +126,16 @@ void emit_unit(const Symbolic& s, int kind, int u, Table& t) {
     for (int p = c0; p < dk; p++) {
       const int j = s.csc_row[p];
       const int q0 = s.diag_slot[j] + 1;
-      const int up = t.slot_refactor(p, true);
+      const int up = t.loc_of_v[p];
       for (int q = q0; q < s.csc_colptr[j + 1]; q++) {
         const int tgt = s.upd_tgt[s.upd_ptr[p] + (q - q0)];
         const int lq = t.slot_refactor(q, false);
-        t.ops.push_back(Op{OP_FNMA, t.loc_of_v[tgt], lq, up});
+        t.ops.push_back(RawOp{OP_FNMA, t.loc_of_v[tgt], lq, up, -1});
       }
     }
+    // The L slots of column u are consecutive own locals (added in CSC order).
     const int cnt = c1 - dk - 1;
-    t.ops.push_back(Op{OP_SCALE | (cnt << 4), t.loc_of_v[dk], cnt > 0 ? t.loc_of_v[dk + 1] : 0, u});
+    t.ops.push_back(RawOp{OP_SCALE, t.loc_of_v[dk], cnt > 0 ? t.loc_of_v[dk + 1] : 0, cnt, u});
   } else if (kind == 0 || kind == 1) {
     const int xi = t.x(u, true);
     const auto& ptr = kind == 0 ? s.lrow_ptr : s.urow_ptr;
@@ -139,9 +149,9 @@ void emit_unit(const Symbolic& s, int kind, int u, Table& t) {
       const int e = kind == 0 ? ptr[u] + k : ptr[u + 1] - 1 - k;
       const int xj = t.x(col[e], false);
       const int vq = t.v(slot[e]);
-      t.ops.push_back(Op{OP_FNMA, xi, vq, xj});
+      t.ops.push_back(RawOp{OP_FNMA, xi, vq, xj, -1});
     }
-    if (kind == 1) t.ops.push_back(Op{OP_DIV, xi, t.v(s.diag_slot[u]), 0});
+    if (kind == 1) t.ops.push_back(RawOp{OP_DIV, xi, t.v(s.diag_slot[u]), 0, -1});
   } else {
     const int xj = t.x(u, true);
     const int b = kind == 2 ? s.csc_colptr[u] : s.diag_slot[u] + 1;
@@ -149,9 +159,9 @@ void emit_unit(const Symbolic& s, int kind, int u, Table& t) {
     for (int q = b; q < e; q++) {
       const int xi = t.x(s.csc_row[q], false);
       const int vq = t.v(q);
-      t.ops.push_back(Op{OP_FNMA, xj, vq, xi});
+      t.ops.push_back(RawOp{OP_FNMA, xj, vq, xi, -1});
     }
-    if (kind == 2) t.ops.push_back(Op{OP_DIV, xj, t.v(s.diag_slot[u]), 0});
+    if (kind == 2) t.ops.push_back(RawOp{OP_DIV, xj, t.v(s.diag_slot[u]), 0, -1});
   }
   t.units.push_back(u);
 }
@@ -159,6 +169,7 @@ void emit_unit(const Symbolic& s, int kind, int u, Table& t) {
 }  // namespace
 
 void build_chain_program(const Symbolic& s, int kind, int max_locals, ChainProgram& out) {
+  max_locals = std::min(max_locals, kMaxLocals);
   out = ChainProgram();
   out.kind = kind;
   out.max_locals = max_locals;
@@ -166,15 +177,40 @@ void build_chain_program(const Symbolic& s, int kind, int max_locals, ChainProgr
   out.level_chain = ls.start_levels;
   Table t;
   t.init(s.n, s.nnz_lu);
+  std::vector<int> remap;
   auto close = [&]() {
     if (t.units.empty()) return;
+    // Own entries first (in load order), then the read-only ones.
+    const int nl = t.size();
+    remap.assign(nl, -1);
     Segment g;
     g.load_begin = (int)out.loads.size();
-    g.n_load = t.size();
+    g.n_load = nl;
+    g.n_own = 0;
+    for (int l = 0; l < nl; l++)
+      if (t.own[l]) {
+        remap[l] = g.n_own++;
+        out.loads.push_back(t.refs[l]);
+      }
+    int next = g.n_own;
+    for (int l = 0; l < nl; l++)
+      if (!t.own[l]) {
+        remap[l] = next++;
+        out.loads.push_back(t.refs[l]);
+      }
     g.op_begin = (int)out.ops.size();
-    g.n_op = (int)t.ops.size();
-    out.loads.insert(out.loads.end(), t.loads.begin(), t.loads.end());
-    out.ops.insert(out.ops.end(), t.ops.begin(), t.ops.end());
+    for (const RawOp& o : t.ops) {
+      const int a = remap[o.a];
+      const int b = (o.code == OP_SCALE && o.c == 0) ? 0 : remap[o.b];
+      const int c = (o.code == OP_FNMA) ? remap[o.c] : o.c;
+      out.ops.push_back(pack_op(o.code, a, b, c));
+      out.op_col.push_back(o.col);
+    }
+    while ((out.ops.size() - g.op_begin) % 4) {
+      out.ops.push_back(pack_op(OP_NOP, 0, 0, 0));
+      out.op_col.push_back(-1);
+    }
+    g.n_op = (int)out.ops.size() - g.op_begin;
     out.seg.push_back(g);
     t.reset();
   };
@@ -192,7 +228,7 @@ void build_chain_program(const Symbolic& s, int kind, int max_locals, ChainProgr
         // Too wide for the local table: executed from global memory, after
         // the segment collected so far (chain order is execution order).
         close();
-        out.seg.push_back(Segment{0, -1, u, 0});
+        out.seg.push_back(Segment{0, -1, 0, u, 0});
         out.direct_segments++;
         continue;
       }

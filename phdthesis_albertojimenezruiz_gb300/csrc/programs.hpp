@@ -21,24 +21,28 @@
 
 namespace pvglu {
 
-// Operation codes (low 4 bits of Op::code).
+// Operations are packed in 32 bits: code (2) | a (10) | b (10) | c (10),
+// so a local table holds at most kMaxLocals entries.
 enum : int {
   OP_FNMA = 0,   // t[a] = t[a] - t[b] * t[c]
-  OP_SCALE = 1,  // p = t[a]; pivot check (column c); t[b + i] /= p, i < code >> 4
+  OP_SCALE = 1,  // p = t[a]; pivot check; t[b + i] /= p for i < c
   OP_DIV = 2,    // t[a] = t[a] / t[b]
+  OP_NOP = 3,    // padding to a multiple of 4 operations per segment
 };
+constexpr int kMaxLocals = 1023;
 
-struct Op {
-  int code, a, b, c;
-};
+inline uint32_t pack_op(int code, int a, int b, int c) {
+  return (uint32_t)code | ((uint32_t)a << 2) | ((uint32_t)b << 12) | ((uint32_t)c << 22);
+}
 
-// Segment header.  load refs: refactor programs reference LU slots
-// (ref = slot * 2 + store_back); solve programs reference solution entries
-// (ref = index * 2 + store_back, index >= 0) or LU slots (ref = -(slot + 1),
-// read only).  A segment with n_load < 0 is DIRECT: column/row `op_begin`
-// is executed straight from global memory (too wide for the local table).
+// Segment header.  Loads: refactor programs reference LU slots (ref =
+// slot); solve programs reference solution entries (ref = i >= 0) or
+// read-only LU slots (ref = -(slot + 1)).  The first n_own loads are the
+// segment's own entries, written back after the operations.
+// A segment with n_load < 0 is DIRECT: unit `op_begin` (a column or row
+// too wide for the table) is executed straight from global memory.
 struct Segment {
-  int load_begin, n_load, op_begin, n_op;
+  int load_begin, n_load, n_own, op_begin, n_op;
 };
 
 struct ChainProgram {
@@ -48,7 +52,8 @@ struct ChainProgram {
   std::vector<int> chain_seg;    // [chains + 1] -> segment index
   std::vector<Segment> seg;
   std::vector<int> loads;
-  std::vector<Op> ops;
+  std::vector<uint32_t> ops;     // packed, each segment's run padded to 4
+  std::vector<int> op_col;       // column of each SCALE operation (error reports)
   int longest_chain_segments = 0;
   int direct_segments = 0;
 };
