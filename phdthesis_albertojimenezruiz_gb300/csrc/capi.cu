@@ -148,8 +148,11 @@ int prog_prepare(pvglu_numeric* h) {
 }
 
 // One phase of chain programs with one launch per level.
+constexpr pvglu::IrFuse kNoFuse{nullptr, nullptr, nullptr, nullptr, nullptr};
+
 template <typename T, bool B, int KIND>
-void prog_levels(pvglu_numeric* h, T* x, const int* done, cudaStream_t st) {
+void prog_levels(pvglu_numeric* h, T* x, const int* done, const pvglu::IrFuse& ir,
+                 cudaStream_t st) {
   const int ph = KIND + 1;
   const auto& lc = h->prog_level_chain[ph];
   const size_t smem = pvglu::prog_smem_bytes<T, B>(h->max_locals);
@@ -160,29 +163,30 @@ void prog_levels(pvglu_numeric* h, T* x, const int* done, cudaStream_t st) {
     const int64_t items = (int64_t)(ce - cb) * groups;
     pvglu::k_prog_level<T, KIND, B><<<launch_blocks(items, warps), pvglu::kProgBlock, smem, st>>>(
         h->progs.p[ph], h->d, cb, ce, static_cast<T*>(h->values), x, h->ld, h->S,
-        h->pivot_tol, h->status, done);
+        h->pivot_tol, h->status, done, KIND == 1 ? ir : kNoFuse);
   }
 }
 
 template <typename T, bool B>
-int prog_dispatch(pvglu_numeric* h, int phases, T* x, pvglu::SkipDone skip, cudaStream_t st) {
+int prog_dispatch(pvglu_numeric* h, int phases, T* x, pvglu::SkipDone skip,
+                  const pvglu::IrFuse& ir, cudaStream_t st) {
   if (h->schedule == PVGLU_SCHED_PERSISTENT) {
     if (pvglu::launch_prog_persistent<T, B>(h->progs, h->prog_max_chains, h->d,
                                             static_cast<T*>(h->values), x, h->ld, h->S,
                                             h->pivot_tol, h->status, h->barrier, h->prog_grid,
-                                            phases, st, skip))
+                                            phases, st, skip, ir))
       return fail(PVGLU_ERR_CUDA, std::string("persistent launch failed: ") +
                                       cudaGetErrorString(cudaGetLastError()));
     return PVGLU_OK;
   }
-  if (phases & pvglu::PHASE_REFACTOR) prog_levels<T, B, -1>(h, x, nullptr, st);
+  if (phases & pvglu::PHASE_REFACTOR) prog_levels<T, B, -1>(h, x, nullptr, kNoFuse, st);
   if (phases & pvglu::PHASE_SOLVE) {
-    prog_levels<T, B, 0>(h, x, skip.done, st);
-    prog_levels<T, B, 1>(h, x, skip.done, st);
+    prog_levels<T, B, 0>(h, x, skip.done, kNoFuse, st);
+    prog_levels<T, B, 1>(h, x, skip.done, ir, st);
   }
   if (phases & pvglu::PHASE_SOLVE_T) {
-    prog_levels<T, B, 2>(h, x, skip.done, st);
-    prog_levels<T, B, 3>(h, x, skip.done, st);
+    prog_levels<T, B, 2>(h, x, skip.done, kNoFuse, st);
+    prog_levels<T, B, 3>(h, x, skip.done, kNoFuse, st);
   }
   PVGLU_CUDA(cudaGetLastError());
   return PVGLU_OK;
@@ -190,17 +194,22 @@ int prog_dispatch(pvglu_numeric* h, int phases, T* x, pvglu::SkipDone skip, cuda
 
 template <typename T>
 int run_phases(pvglu_numeric* h, int phases, T* x, cudaStream_t st,
-               pvglu::SkipDone skip = pvglu::SkipDone{nullptr, nullptr}) {
-  return h->batch ? prog_dispatch<T, true>(h, phases, x, skip, st)
-                  : prog_dispatch<T, false>(h, phases, x, skip, st);
+               pvglu::SkipDone skip = pvglu::SkipDone{nullptr, nullptr},
+               const pvglu::IrFuse& ir = kNoFuse) {
+  return h->batch ? prog_dispatch<T, true>(h, phases, x, skip, ir, st)
+                  : prog_dispatch<T, false>(h, phases, x, skip, ir, st);
 }
 
-// skip: per-scenario convergence flags of iterative refinement (or none).
+// skip: per-scenario convergence flags of iterative refinement (or none);
+// ir: accumulation of the correction into the FP64 solution, fused into the
+// U phase (chain-program schedules only).
 template <typename T>
 int solve_permuted(pvglu_numeric* h, T* x, bool transpose, cudaStream_t st,
-                   pvglu::SkipDone skip = pvglu::SkipDone{nullptr, nullptr}) {
+                   pvglu::SkipDone skip = pvglu::SkipDone{nullptr, nullptr},
+                   const pvglu::IrFuse& ir = kNoFuse) {
   if (h->schedule != PVGLU_SCHED_THREAD_CHAIN)
-    return run_phases<T>(h, transpose ? pvglu::PHASE_SOLVE_T : pvglu::PHASE_SOLVE, x, st, skip);
+    return run_phases<T>(h, transpose ? pvglu::PHASE_SOLVE_T : pvglu::PHASE_SOLVE, x, st, skip,
+                         ir);
   if (!transpose) {
     solve_phase<T, 0>(h, h->l_sl, x, skip.done, st);
     solve_phase<T, 1>(h, h->u_sl, x, skip.done, st);
@@ -708,11 +717,17 @@ int pvglu_solve_refined(pvglu_numeric* h, const double* a_values, const double* 
       pvglu::k_residual<<<pvglu::rows_grid(h->n, h->ld, 256), 256, 0, st>>>(
           h->d.a_rowptr, h->d.a_colidx, h->n, h->ld, h->S, a_values, b, x, h->ir_done, w,
           h->row_pos);
-    int rc = solve_permuted<float>(h, w, false, st, skip);
+    // Chain-program schedules accumulate x += dx inside the U phase; the
+    // thread-chain schedule uses the separate update kernel.
+    const bool fused = h->schedule != PVGLU_SCHED_THREAD_CHAIN;
+    const pvglu::IrFuse ir{x, h->d.col_orig, h->ir_done, h->ir_max_dx, h->ir_max_x};
+    int rc = solve_permuted<float>(h, w, false, st, skip, fused ? ir : kNoFuse);
     if (rc) return rc;
-    dim3 blk(32, 8), grd((unsigned)std::min(1024, (h->n + 7) / 8), (unsigned)(h->ld + 31) / 32);
-    pvglu::k_ir_update<<<grd, blk, 0, st>>>(h->d.col_orig, h->n, h->ld, h->S, w, x,
-                                            h->ir_done, h->ir_max_dx, h->ir_max_x);
+    if (!fused) {
+      dim3 blk(32, 8), grd((unsigned)std::min(1024, (h->n + 7) / 8), (unsigned)(h->ld + 31) / 32);
+      pvglu::k_ir_update<<<grd, blk, 0, st>>>(h->d.col_orig, h->n, h->ld, h->S, w, x,
+                                              h->ir_done, h->ir_max_dx, h->ir_max_x);
+    }
     pvglu::k_ir_check<<<(h->S + 127) / 128, 128, 0, st>>>(h->S, sweep, max_sweeps, tol,
                                                           h->ir_done, ndone, sweeps_out,
                                                           h->ir_max_dx, h->ir_max_x);

@@ -29,6 +29,33 @@ struct ProgDev {
   int max_locals;
 };
 
+// Iterative-refinement accumulation fused into the U-solve store phase:
+// every own entry dx_i of the correction is also added to the FP64 solution,
+// x[col_orig[i]] += dx_i, and the per-scenario max|dx| / max|x| are kept.
+// x64 == nullptr disables it.
+struct IrFuse {
+  double* x64;
+  const int* col_orig;
+  const int* done;
+  unsigned long long* max_dx;
+  unsigned long long* max_x;
+};
+
+// Per-thread running maxima of the fused accumulation, flushed with one
+// atomicMax pair whenever the thread moves to another scenario.
+struct IrMax {
+  int s = -1;
+  double dx = 0.0, x = 0.0;
+  __device__ __forceinline__ void flush(const IrFuse& ir) {
+    if (s >= 0 && (dx > 0.0 || x > 0.0)) {
+      atomicMax(ir.max_dx + s, (unsigned long long)__double_as_longlong(dx));
+      atomicMax(ir.max_x + s, (unsigned long long)__double_as_longlong(x));
+    }
+    dx = 0.0;
+    x = 0.0;
+  }
+};
+
 // Offsets are 32-bit: the handle guarantees nnz_lu * ld and n * ld < 2^31.
 template <typename T, int KIND>
 __device__ __forceinline__ T prog_fetch(int ref, const T* __restrict__ vs,
@@ -83,7 +110,8 @@ template <typename T, int KIND, bool BATCH>
 __device__ __forceinline__ void prog_run_chain(const ProgDev& P, const DevStruct& d, int chain,
                                                T* __restrict__ v, T* __restrict__ x, int ld,
                                                int s, int S, T* sm, double pivot_tol,
-                                               DevStatus* st) {
+                                               DevStatus* st, const IrFuse& ir, IrMax& irm) {
+  const bool fuse = KIND == 1 && ir.x64 != nullptr && s < S && !(ir.done && ir.done[s]);
   const int lane = threadIdx.x & 31;
   T* vs = v + s;
   T* xs = KIND < 0 ? nullptr : x + s;
@@ -94,6 +122,14 @@ __device__ __forceinline__ void prog_run_chain(const ProgDev& P, const DevStruct
       if (BATCH || lane == 0) {
         if (KIND < 0) refactor_column<T>(d, sg.z, s, ld, v, pivot_tol, st);
         else solve_unknown<T, (KIND < 0 ? 0 : KIND)>(d, sg.z, s, ld, v, x);
+        if (fuse) {
+          const T val = x[(unsigned)sg.z * (unsigned)ld + s];
+          double* xo = ir.x64 + (unsigned)__ldg(ir.col_orig + sg.z) * (unsigned)ld + s;
+          const double nx = *xo + (double)val;
+          *xo = nx;
+          irm.dx = fmax(irm.dx, fabs((double)val));
+          irm.x = fmax(irm.x, fabs(nx));
+        }
       }
       __syncwarp();
       continue;
@@ -120,10 +156,22 @@ __device__ __forceinline__ void prog_run_chain(const ProgDev& P, const DevStruct
       for (int base = 0; base < n_own; base += 32) {
         const int cnt = min(32, n_own - base);
         const int my_ref = lane < cnt ? __ldg(lr + base + lane) : 0;
+        // col_orig of the rows (scenario independent), broadcast like refs
+        const int my_col = (KIND == 1 && ir.x64 != nullptr && lane < cnt)
+                               ? __ldg(ir.col_orig + __ldg(lr + base + lane)) : 0;
 #pragma unroll 4
         for (int k = 0; k < cnt; k++) {
           const int r = __shfl_sync(0xffffffffu, my_ref, k);
-          prog_store<T, KIND>(r, sml[(base + k) << 5], vs, xs, ld);
+          const T val = sml[(base + k) << 5];
+          prog_store<T, KIND>(r, val, vs, xs, ld);
+          const int co = __shfl_sync(0xffffffffu, my_col, k);
+          if (fuse) {
+            double* xo = ir.x64 + (unsigned)co * (unsigned)ld + s;
+            const double nx = *xo + (double)val;
+            *xo = nx;
+            irm.dx = fmax(irm.dx, fabs((double)val));
+            irm.x = fmax(irm.x, fabs(nx));
+          }
         }
       }
     } else {
@@ -131,7 +179,17 @@ __device__ __forceinline__ void prog_run_chain(const ProgDev& P, const DevStruct
       __syncwarp();
       if (lane == 0) prog_exec_ops<T, false>(P, sg.z, sg.w, sm, 0, S, pivot_tol, st);
       __syncwarp();
-      for (int l = lane; l < n_own; l += 32) prog_store<T, KIND>(__ldg(lr + l), sm[l], v, x, 1);
+      for (int l = lane; l < n_own; l += 32) {
+        const int r = __ldg(lr + l);
+        prog_store<T, KIND>(r, sm[l], v, x, 1);
+        if (fuse) {
+          double* xo = ir.x64 + __ldg(ir.col_orig + r);
+          const double nx = *xo + (double)sm[l];
+          *xo = nx;
+          irm.dx = fmax(irm.dx, fabs((double)sm[l]));
+          irm.x = fmax(irm.x, fabs(nx));
+        }
+      }
       __syncwarp();
     }
   }
@@ -144,30 +202,36 @@ __device__ __forceinline__ void prog_run_level(const ProgDev& P, const DevStruct
                                                int ce, T* __restrict__ v, T* __restrict__ x,
                                                int ld, int S, T* sm_warp, double pivot_tol,
                                                DevStatus* st, const int* done, int warp_id,
-                                               int n_warps) {
+                                               int n_warps, const IrFuse& ir) {
   const int groups = BATCH ? ld >> 5 : 1;
   const int items = (ce - cb) * groups;
   const int lane = threadIdx.x & 31;
+  IrMax irm;
   for (int it = warp_id; it < items; it += n_warps) {
     const int ci = BATCH ? it / groups : it;
     const int c = cb + ci;
     const int s = BATCH ? ((it - ci * groups) << 5) + lane : 0;
     if (BATCH && done && __all_sync(0xffffffffu, s >= S || done[s])) continue;
-    prog_run_chain<T, KIND, BATCH>(P, d, c, v, x, ld, s, S, sm_warp, pivot_tol, st);
+    if (KIND == 1 && ir.x64 && s != irm.s) {
+      irm.flush(ir);
+      irm.s = s;
+    }
+    prog_run_chain<T, KIND, BATCH>(P, d, c, v, x, ld, s, S, sm_warp, pivot_tol, st, ir, irm);
   }
+  if (KIND == 1 && ir.x64) irm.flush(ir);
 }
 
 template <typename T, int KIND, bool BATCH>
 __global__ void k_prog_level(ProgDev P, DevStruct d, int cb, int ce, T* __restrict__ v,
                              T* __restrict__ x, int ld, int S, double pivot_tol, DevStatus* st,
-                             const int* done) {
+                             const int* done, IrFuse ir) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* sm = reinterpret_cast<T*>(smem_raw) +
           (threadIdx.x >> 5) * P.max_locals * (BATCH ? 32 : 1);
   const int warp_id = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int n_warps = (gridDim.x * blockDim.x) >> 5;
   prog_run_level<T, KIND, BATCH>(P, d, cb, ce, v, x, ld, S, sm, pivot_tol, st, done, warp_id,
-                                 n_warps);
+                                 n_warps, ir);
 }
 
 }  // namespace pvglu
