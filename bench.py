@@ -227,7 +227,7 @@ def main() -> None:
                                                     SCHED_THREAD_CHAIN, Numeric, Symbolic)
 
     S = args.scenarios
-    ld = ((S + 31) // 32) * 32
+    ld = ((S + 63) // 64) * 64
     p, a, b = make_inputs(S, ld, seed0=1000 + rank * S)
     sym = Symbolic(p.rowptr, p.colidx)
     n, nnz_a, nnz_lu = sym.n, int(sym.nnz_a), int(sym.nnz_lu)

@@ -134,7 +134,7 @@ void solve_phase(pvglu_numeric* h, const std::vector<int>& sl, T* x, const int* 
 // grid size of the chain-program kernels of one handle.
 template <typename T, bool B>
 int prog_prepare(pvglu_numeric* h) {
-  const int smem = (int)pvglu::prog_smem_bytes<T, B>(h->max_locals);
+  const int smem = (int)pvglu::prog_smem_bytes<T, B>(h->max_locals, pvglu::kProgWarps);
   const void* fns[] = {(const void*)pvglu::k_prog_level<T, -1, B>,
                        (const void*)pvglu::k_prog_level<T, 0, B>,
                        (const void*)pvglu::k_prog_level<T, 1, B>,
@@ -148,45 +148,41 @@ int prog_prepare(pvglu_numeric* h) {
 }
 
 // One phase of chain programs with one launch per level.
-constexpr pvglu::IrFuse kNoFuse{nullptr, nullptr, nullptr, nullptr, nullptr};
-
 template <typename T, bool B, int KIND>
-void prog_levels(pvglu_numeric* h, T* x, const int* done, const pvglu::IrFuse& ir,
-                 cudaStream_t st) {
+void prog_levels(pvglu_numeric* h, T* x, const int* done, cudaStream_t st) {
   const int ph = KIND + 1;
   const auto& lc = h->prog_level_chain[ph];
-  const size_t smem = pvglu::prog_smem_bytes<T, B>(h->max_locals);
-  const int groups = B ? h->ld / 32 : 1;
-  const int warps = pvglu::kProgBlock / 32;
+  const size_t smem = pvglu::prog_smem_bytes<T, B>(h->max_locals, pvglu::kProgWarps);
+  const int groups = B ? h->ld / pvglu::kGroup : 1;
   for (size_t lv = 0; lv + 1 < lc.size(); lv++) {
     const int cb = lc[lv], ce = lc[lv + 1];
     const int64_t items = (int64_t)(ce - cb) * groups;
-    pvglu::k_prog_level<T, KIND, B><<<launch_blocks(items, warps), pvglu::kProgBlock, smem, st>>>(
-        h->progs.p[ph], h->d, cb, ce, static_cast<T*>(h->values), x, h->ld, h->S,
-        h->pivot_tol, h->status, done, KIND == 1 ? ir : kNoFuse);
+    pvglu::k_prog_level<T, KIND, B>
+        <<<launch_blocks(items, pvglu::kProgWarps), pvglu::kProgBlock, smem, st>>>(
+            h->progs.p[ph], h->d, cb, ce, static_cast<T*>(h->values), x, h->ld, h->S,
+            h->pivot_tol, h->status, done);
   }
 }
 
 template <typename T, bool B>
-int prog_dispatch(pvglu_numeric* h, int phases, T* x, pvglu::SkipDone skip,
-                  const pvglu::IrFuse& ir, cudaStream_t st) {
+int prog_dispatch(pvglu_numeric* h, int phases, T* x, pvglu::SkipDone skip, cudaStream_t st) {
   if (h->schedule == PVGLU_SCHED_PERSISTENT) {
     if (pvglu::launch_prog_persistent<T, B>(h->progs, h->prog_max_chains, h->d,
                                             static_cast<T*>(h->values), x, h->ld, h->S,
                                             h->pivot_tol, h->status, h->barrier, h->prog_grid,
-                                            phases, st, skip, ir))
+                                            phases, st, skip))
       return fail(PVGLU_ERR_CUDA, std::string("persistent launch failed: ") +
                                       cudaGetErrorString(cudaGetLastError()));
     return PVGLU_OK;
   }
-  if (phases & pvglu::PHASE_REFACTOR) prog_levels<T, B, -1>(h, x, nullptr, kNoFuse, st);
+  if (phases & pvglu::PHASE_REFACTOR) prog_levels<T, B, -1>(h, x, nullptr, st);
   if (phases & pvglu::PHASE_SOLVE) {
-    prog_levels<T, B, 0>(h, x, skip.done, kNoFuse, st);
-    prog_levels<T, B, 1>(h, x, skip.done, ir, st);
+    prog_levels<T, B, 0>(h, x, skip.done, st);
+    prog_levels<T, B, 1>(h, x, skip.done, st);
   }
   if (phases & pvglu::PHASE_SOLVE_T) {
-    prog_levels<T, B, 2>(h, x, skip.done, kNoFuse, st);
-    prog_levels<T, B, 3>(h, x, skip.done, kNoFuse, st);
+    prog_levels<T, B, 2>(h, x, skip.done, st);
+    prog_levels<T, B, 3>(h, x, skip.done, st);
   }
   PVGLU_CUDA(cudaGetLastError());
   return PVGLU_OK;
@@ -194,22 +190,20 @@ int prog_dispatch(pvglu_numeric* h, int phases, T* x, pvglu::SkipDone skip,
 
 template <typename T>
 int run_phases(pvglu_numeric* h, int phases, T* x, cudaStream_t st,
-               pvglu::SkipDone skip = pvglu::SkipDone{nullptr, nullptr},
-               const pvglu::IrFuse& ir = kNoFuse) {
-  return h->batch ? prog_dispatch<T, true>(h, phases, x, skip, ir, st)
-                  : prog_dispatch<T, false>(h, phases, x, skip, ir, st);
+               pvglu::SkipDone skip = pvglu::SkipDone{nullptr, nullptr}) {
+  // Batched chain programs move rows with TMA bulk copies: 16-byte alignment.
+  if (h->batch && x && (reinterpret_cast<uintptr_t>(x) & 15))
+    return fail(PVGLU_ERR_BAD_ARG, "solution vector must be 16-byte aligned");
+  return h->batch ? prog_dispatch<T, true>(h, phases, x, skip, st)
+                  : prog_dispatch<T, false>(h, phases, x, skip, st);
 }
 
-// skip: per-scenario convergence flags of iterative refinement (or none);
-// ir: accumulation of the correction into the FP64 solution, fused into the
-// U phase (chain-program schedules only).
+// skip: per-scenario convergence flags of iterative refinement (or none).
 template <typename T>
 int solve_permuted(pvglu_numeric* h, T* x, bool transpose, cudaStream_t st,
-                   pvglu::SkipDone skip = pvglu::SkipDone{nullptr, nullptr},
-                   const pvglu::IrFuse& ir = kNoFuse) {
+                   pvglu::SkipDone skip = pvglu::SkipDone{nullptr, nullptr}) {
   if (h->schedule != PVGLU_SCHED_THREAD_CHAIN)
-    return run_phases<T>(h, transpose ? pvglu::PHASE_SOLVE_T : pvglu::PHASE_SOLVE, x, st, skip,
-                         ir);
+    return run_phases<T>(h, transpose ? pvglu::PHASE_SOLVE_T : pvglu::PHASE_SOLVE, x, st, skip);
   if (!transpose) {
     solve_phase<T, 0>(h, h->l_sl, x, skip.done, st);
     solve_phase<T, 1>(h, h->u_sl, x, skip.done, st);
@@ -332,7 +326,7 @@ int pvglu_numeric_create(const pvglu_symbolic* sym, int n_scenarios, int precisi
   if (s.update_count > 0x7fffffffLL) return fail(PVGLU_ERR_TOO_LARGE, "update list > 2^31");
   {
     // The chain programs address values with 32-bit offsets.
-    const int64_t ld_max = n_scenarios == 1 ? 1 : ((n_scenarios + 31) / 32) * 32;
+    const int64_t ld_max = n_scenarios == 1 ? 1 : ((n_scenarios + 63) / 64) * 64;
     if (s.nnz_lu * ld_max >= 0x7fffffffLL || (int64_t)s.n * ld_max >= 0x7fffffffLL ||
         s.nnz_a * ld_max >= 0x7fffffffLL)
       return fail(PVGLU_ERR_TOO_LARGE, "nnz x scenarios exceeds 2^31 values per handle");
@@ -343,7 +337,8 @@ int pvglu_numeric_create(const pvglu_symbolic* sym, int n_scenarios, int precisi
   h->nnz = (int)s.nnz_lu;
   h->nnz_a = (int)s.nnz_a;
   h->S = n_scenarios;
-  h->ld = n_scenarios == 1 ? 1 : ((n_scenarios + 31) / 32) * 32;
+  // Scenario stride: one 64-scenario group per warp item in batched mode.
+  h->ld = n_scenarios == 1 ? 1 : ((n_scenarios + 63) / 64) * 64;
   h->precision = precision;
   h->lu_sl = s.lu.start_levels;
   h->l_sl = s.l.start_levels;
@@ -417,7 +412,9 @@ int pvglu_numeric_create(const pvglu_symbolic* sym, int n_scenarios, int precisi
     std::vector<int4> seg(prog.seg.size()), ops(prog.ops.size() / 4);
     for (size_t i = 0; i < seg.size(); i++) {
       const auto& g = prog.seg[i];
-      seg[i] = make_int4(g.load_begin, g.n_load < 0 ? -1 : (g.n_load | (g.n_own << 16)),
+      seg[i] = make_int4(g.load_begin,
+                         g.n_load < 0 ? -1
+                                      : (g.n_load | (g.n_own << 16) | (g.reads_own_chain << 30)),
                          g.op_begin, g.n_op);
     }
     std::memcpy(ops.data(), prog.ops.data(), ops.size() * sizeof(int4));
@@ -717,17 +714,11 @@ int pvglu_solve_refined(pvglu_numeric* h, const double* a_values, const double* 
       pvglu::k_residual<<<pvglu::rows_grid(h->n, h->ld, 256), 256, 0, st>>>(
           h->d.a_rowptr, h->d.a_colidx, h->n, h->ld, h->S, a_values, b, x, h->ir_done, w,
           h->row_pos);
-    // Chain-program schedules accumulate x += dx inside the U phase; the
-    // thread-chain schedule uses the separate update kernel.
-    const bool fused = h->schedule != PVGLU_SCHED_THREAD_CHAIN;
-    const pvglu::IrFuse ir{x, h->d.col_orig, h->ir_done, h->ir_max_dx, h->ir_max_x};
-    int rc = solve_permuted<float>(h, w, false, st, skip, fused ? ir : kNoFuse);
+    int rc = solve_permuted<float>(h, w, false, st, skip);
     if (rc) return rc;
-    if (!fused) {
-      dim3 blk(32, 8), grd((unsigned)std::min(1024, (h->n + 7) / 8), (unsigned)(h->ld + 31) / 32);
-      pvglu::k_ir_update<<<grd, blk, 0, st>>>(h->d.col_orig, h->n, h->ld, h->S, w, x,
-                                              h->ir_done, h->ir_max_dx, h->ir_max_x);
-    }
+    dim3 blk(32, 8), grd((unsigned)std::min(1024, (h->n + 7) / 8), (unsigned)(h->ld + 31) / 32);
+    pvglu::k_ir_update<<<grd, blk, 0, st>>>(h->d.col_orig, h->n, h->ld, h->S, w, x,
+                                            h->ir_done, h->ir_max_dx, h->ir_max_x);
     pvglu::k_ir_check<<<(h->S + 127) / 128, 128, 0, st>>>(h->S, sweep, max_sweeps, tol,
                                                           h->ir_done, ndone, sweeps_out,
                                                           h->ir_max_dx, h->ir_max_x);

@@ -1,15 +1,18 @@
 // Device executor of the chain programs (programs.hpp).
 //
-// Batched mode (BATCH = true): a warp runs one chain for 32 scenarios, lane
-// = scenario; its local table is a [max_locals][32] tile of shared memory, so
-// every table access is bank-conflict free and every global access of the
-// load/store phases is one coalesced 128-byte (FP32) or 256-byte (FP64) row.
-// The load phase fetches 32 refs with one coalesced load and broadcasts them
-// with shuffles, keeping kChunk independent value loads in flight per lane.
+// Batched mode (BATCH = true): a warp runs one chain for a group of 64
+// scenarios; lane l owns scenarios 2l and 2l+1 of the group, so every table
+// access is one 8-byte (FP32) or 16-byte (FP64) shared-memory access for two
+// scenarios.  The local table is [max_locals][64] values; one table row is
+// one value of the group, which in HBM is one contiguous 256/512-byte row of
+// the slot-major layout.  Rows are moved with TMA bulk copies:
+// cp.async.bulk global->shared completing on a per-warp mbarrier (loads) and
+// cp.async.bulk shared->global in bulk groups (stores).  A segment's loads
+// are all in flight at once and need no registers.
 //
 // Single mode (BATCH = false): a warp runs one chain of the one scenario; the
-// lanes split the loads and stores of each segment, lane 0 executes the
-// operations out of shared memory.
+// lanes split the loads and stores of each segment (ld.global.cg), lane 0
+// executes the operations out of shared memory.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -29,209 +32,319 @@ struct ProgDev {
   int max_locals;
 };
 
-// Iterative-refinement accumulation fused into the U-solve store phase:
-// every own entry dx_i of the correction is also added to the FP64 solution,
-// x[col_orig[i]] += dx_i, and the per-scenario max|dx| / max|x| are kept.
-// x64 == nullptr disables it.
-struct IrFuse {
-  double* x64;
-  const int* col_orig;
-  const int* done;
-  unsigned long long* max_dx;
-  unsigned long long* max_x;
+constexpr int kGroup = 64;                       // scenarios per warp item
+constexpr long long kMbarMaxPolls = 1LL << 20;   // bounded mbarrier waits
+
+// ---------------------------------------------------------------------------
+// PTX helpers: mbarrier + bulk (non-tensor) TMA copies.
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+  return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(unsigned long long* mbar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(mbar)), "r"(count)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long* mbar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* mbar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(mbar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ void bulk_load(void* smem_dst, const void* gsrc, unsigned bytes,
+                                          unsigned long long* mbar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(smem_u32(smem_dst)),
+      "l"(gsrc), "r"(bytes), "r"(smem_u32(mbar))
+      : "memory");
+}
+__device__ __forceinline__ void bulk_store(void* gdst, const void* smem_src, unsigned bytes) {
+  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(gdst),
+               "r"(smem_u32(smem_src)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_commit() {
+  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+// Source shared memory of this thread's bulk stores may be reused.
+__device__ __forceinline__ void bulk_wait_read() {
+  asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+}
+// This thread's bulk stores are complete in global memory.
+__device__ __forceinline__ void bulk_wait_all() {
+  asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+}
+// Orders this thread's generic-proxy and async-proxy memory accesses.
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async;" ::: "memory");
+}
+
+template <typename T>
+struct Vec2;
+template <>
+struct Vec2<float> {
+  using type = float2;
+};
+template <>
+struct Vec2<double> {
+  using type = double2;
 };
 
-// Per-thread running maxima of the fused accumulation, flushed with one
-// atomicMax pair whenever the thread moves to another scenario.
-struct IrMax {
-  int s = -1;
-  double dx = 0.0, x = 0.0;
-  __device__ __forceinline__ void flush(const IrFuse& ir) {
-    if (s >= 0 && (dx > 0.0 || x > 0.0)) {
-      atomicMax(ir.max_dx + s, (unsigned long long)__double_as_longlong(dx));
-      atomicMax(ir.max_x + s, (unsigned long long)__double_as_longlong(x));
-    }
-    dx = 0.0;
-    x = 0.0;
-  }
-};
-
-// Offsets are 32-bit: the handle guarantees nnz_lu * ld and n * ld < 2^31.
+// ---------------------------------------------------------------------------
+// Single-scenario table access (ld == 1).
 template <typename T, int KIND>
-__device__ __forceinline__ T prog_fetch(int ref, const T* __restrict__ vs,
-                                        const T* __restrict__ xs, int ld) {
-  if (KIND < 0) return ldv(vs + (unsigned)ref * (unsigned)ld);
-  if (ref >= 0) return ldv(xs + (unsigned)ref * (unsigned)ld);
-  return ldv(vs + (unsigned)(-ref - 1) * (unsigned)ld);
+__device__ __forceinline__ T prog_fetch1(int ref, const T* __restrict__ v,
+                                         const T* __restrict__ x) {
+  if (KIND < 0) return ldv(v + ref);
+  if (ref >= 0) return ldv(x + ref);
+  return ldv(v + (-ref - 1));
 }
 
 template <typename T, int KIND>
-__device__ __forceinline__ void prog_store(int ref, T val, T* __restrict__ vs,
-                                           T* __restrict__ xs, int ld) {
-  if (KIND < 0) vs[(unsigned)ref * (unsigned)ld] = val;
-  else xs[(unsigned)ref * (unsigned)ld] = val;
+__device__ __forceinline__ void prog_store1(int ref, T val, T* __restrict__ v,
+                                            T* __restrict__ x) {
+  if (KIND < 0) v[ref] = val;
+  else x[ref] = val;
 }
 
-template <typename T, bool BATCH>
-__device__ __forceinline__ void prog_exec_op(uint32_t op, int op_index, const int* op_col,
-                                             T* sml, int s, int S, double pivot_tol,
-                                             DevStatus* st) {
-  constexpr int SH = BATCH ? 5 : 0;
-  const int code = op & 3;
-  const int a = (op >> 2) & 1023, b = (op >> 12) & 1023, c = (op >> 22) & 1023;
+// Row pointer of entry `ref` for scenario group starting at s0 (batched).
+template <typename T, int KIND>
+__device__ __forceinline__ T* prog_row(int ref, T* v, T* x, int ld, int s0) {
+  if (KIND < 0) return v + (unsigned)ref * (unsigned)ld + s0;
+  if (ref >= 0) return x + (unsigned)ref * (unsigned)ld + s0;
+  return v + (unsigned)(-ref - 1) * (unsigned)ld + s0;
+}
+
+__device__ __forceinline__ void decode_op(uint32_t op, int& code, int& a, int& b, int& c) {
+  code = op & 3;
+  a = (op >> 2) & 1023;
+  b = (op >> 12) & 1023;
+  c = (op >> 22) & 1023;
+}
+
+// One operation on the two scenarios (x, y components) of this lane.
+template <typename T>
+__device__ __forceinline__ void exec_op2(uint32_t op, int op_index, const int* op_col,
+                                         typename Vec2<T>::type* t, int s0, int S,
+                                         double pivot_tol, DevStatus* st) {
+  int code, a, b, c;
+  decode_op(op, code, a, b, c);
   if (code == OP_FNMA) {
-    sml[a << SH] = fnms(sml[a << SH], sml[b << SH], sml[c << SH]);
+    const auto ta = t[a << 5], tb = t[b << 5], tc = t[c << 5];
+    typename Vec2<T>::type r;
+    r.x = fnms(ta.x, tb.x, tc.x);
+    r.y = fnms(ta.y, tb.y, tc.y);
+    t[a << 5] = r;
   } else if (code == OP_SCALE) {
-    const T p = sml[a << SH];
-    if (!(fabs((double)p) >= pivot_tol) && s < S) report_error(st, 3, op_col[op_index], s);
-    for (int i = 0; i < c; i++) sml[(b + i) << SH] = sml[(b + i) << SH] / p;
+    const auto p = t[a << 5];
+    if (!(fabs((double)p.x) >= pivot_tol) && s0 < S) report_error(st, 3, op_col[op_index], s0);
+    if (!(fabs((double)p.y) >= pivot_tol) && s0 + 1 < S)
+      report_error(st, 3, op_col[op_index], s0 + 1);
+    for (int i = 0; i < c; i++) {
+      auto q = t[(b + i) << 5];
+      q.x = q.x / p.x;
+      q.y = q.y / p.y;
+      t[(b + i) << 5] = q;
+    }
   } else if (code == OP_DIV) {
-    sml[a << SH] = sml[a << SH] / sml[b << SH];
+    auto q = t[a << 5];
+    const auto p = t[b << 5];
+    q.x = q.x / p.x;
+    q.y = q.y / p.y;
+    t[a << 5] = q;
   }
 }
 
-template <typename T, bool BATCH>
-__device__ __forceinline__ void prog_exec_ops(const ProgDev& P, int op_begin, int n_op, T* sml,
-                                              int s, int S, double pivot_tol, DevStatus* st) {
-  const int4* o4 = P.ops + (op_begin >> 2);
-  for (int k = 0; k < (n_op >> 2); k++) {
-    const int4 w = __ldg(o4 + k);
-    const int base = op_begin + 4 * k;
-    prog_exec_op<T, BATCH>((uint32_t)w.x, base, P.op_col, sml, s, S, pivot_tol, st);
-    prog_exec_op<T, BATCH>((uint32_t)w.y, base + 1, P.op_col, sml, s, S, pivot_tol, st);
-    prog_exec_op<T, BATCH>((uint32_t)w.z, base + 2, P.op_col, sml, s, S, pivot_tol, st);
-    prog_exec_op<T, BATCH>((uint32_t)w.w, base + 3, P.op_col, sml, s, S, pivot_tol, st);
+template <typename T>
+__device__ __forceinline__ void exec_op1(uint32_t op, int op_index, const int* op_col, T* t,
+                                         int S, double pivot_tol, DevStatus* st) {
+  int code, a, b, c;
+  decode_op(op, code, a, b, c);
+  if (code == OP_FNMA) {
+    t[a] = fnms(t[a], t[b], t[c]);
+  } else if (code == OP_SCALE) {
+    const T p = t[a];
+    if (!(fabs((double)p) >= pivot_tol) && 0 < S) report_error(st, 3, op_col[op_index], 0);
+    for (int i = 0; i < c; i++) t[b + i] = t[b + i] / p;
+  } else if (code == OP_DIV) {
+    t[a] = t[a] / t[b];
   }
 }
 
-// Runs every segment of `chain` for scenario s (BATCH) or the single
-// scenario (s = 0).  sm: this warp's local table.
+// Per-warp state of the batched path: its table, its mbarrier and phase.
+struct WarpTma {
+  unsigned long long* mbar;
+  unsigned phase;
+};
+
+// Runs every segment of `chain`, batched over the 64 scenarios starting at
+// s0 (BATCH) or for the single scenario.  sm: this warp's table.
 template <typename T, int KIND, bool BATCH>
 __device__ __forceinline__ void prog_run_chain(const ProgDev& P, const DevStruct& d, int chain,
                                                T* __restrict__ v, T* __restrict__ x, int ld,
-                                               int s, int S, T* sm, double pivot_tol,
-                                               DevStatus* st, const IrFuse& ir, IrMax& irm) {
-  const bool fuse = KIND == 1 && ir.x64 != nullptr && s < S && !(ir.done && ir.done[s]);
+                                               int s0, int S, T* sm, WarpTma& tma,
+                                               double pivot_tol, DevStatus* st) {
   const int lane = threadIdx.x & 31;
-  T* vs = v + s;
-  T* xs = KIND < 0 ? nullptr : x + s;
   const int g_end = __ldg(P.chain_seg + chain + 1);
   for (int g = __ldg(P.chain_seg + chain); g < g_end; g++) {
     const int4 sg = __ldg(P.seg + g);
-    if (sg.y < 0) {  // DIRECT unit: straight from global memory
-      if (BATCH || lane == 0) {
-        if (KIND < 0) refactor_column<T>(d, sg.z, s, ld, v, pivot_tol, st);
-        else solve_unknown<T, (KIND < 0 ? 0 : KIND)>(d, sg.z, s, ld, v, x);
-        if (fuse) {
-          const T val = x[(unsigned)sg.z * (unsigned)ld + s];
-          double* xo = ir.x64 + (unsigned)__ldg(ir.col_orig + sg.z) * (unsigned)ld + s;
-          const double nx = *xo + (double)val;
-          *xo = nx;
-          irm.dx = fmax(irm.dx, fabs((double)val));
-          irm.x = fmax(irm.x, fabs(nx));
+    if (sg.y < 0) {  // DIRECT unit: straight from global memory (generic proxy)
+      if (BATCH) {
+        bulk_wait_all();
+        fence_proxy_async();
+        __syncwarp();
+        for (int k = 0; k < 2; k++) {
+          const int s = s0 + 2 * lane + k;
+          if (KIND < 0) refactor_column<T>(d, sg.z, s, ld, v, pivot_tol, st);
+          else solve_unknown<T, (KIND < 0 ? 0 : KIND)>(d, sg.z, s, ld, v, x);
         }
+        fence_proxy_async();
+        __syncwarp();
+      } else {
+        if (lane == 0) {
+          if (KIND < 0) refactor_column<T>(d, sg.z, 0, 1, v, pivot_tol, st);
+          else solve_unknown<T, (KIND < 0 ? 0 : KIND)>(d, sg.z, 0, 1, v, x);
+        }
+        __syncwarp();
       }
-      __syncwarp();
       continue;
     }
     const int* lr = P.loads + sg.x;
-    const int nl = sg.y & 0xffff, n_own = sg.y >> 16;
+    const int nl = sg.y & 0xffff, n_own = (sg.y >> 16) & 0x3ff;
     if (BATCH) {
-      constexpr int kChunk = 16;
-      T* sml = sm + lane;
-      for (int base = 0; base < nl; base += kChunk) {
-        const int cnt = min(kChunk, nl - base);
-        const int my_ref = lane < cnt ? __ldg(lr + base + lane) : 0;
-        T val[kChunk];
-#pragma unroll
-        for (int k = 0; k < kChunk; k++) {
-          const int r = __shfl_sync(0xffffffffu, my_ref, k);
-          if (k < cnt) val[k] = prog_fetch<T, KIND>(r, vs, xs, ld);
-        }
-#pragma unroll
-        for (int k = 0; k < kChunk; k++)
-          if (k < cnt) sml[(base + k) << 5] = val[k];
-      }
-      prog_exec_ops<T, true>(P, sg.z, sg.w, sml, s, S, pivot_tol, st);
-      for (int base = 0; base < n_own; base += 32) {
-        const int cnt = min(32, n_own - base);
-        const int my_ref = lane < cnt ? __ldg(lr + base + lane) : 0;
-        // col_orig of the rows (scenario independent), broadcast like refs
-        const int my_col = (KIND == 1 && ir.x64 != nullptr && lane < cnt)
-                               ? __ldg(ir.col_orig + __ldg(lr + base + lane)) : 0;
-#pragma unroll 4
-        for (int k = 0; k < cnt; k++) {
-          const int r = __shfl_sync(0xffffffffu, my_ref, k);
-          const T val = sml[(base + k) << 5];
-          prog_store<T, KIND>(r, val, vs, xs, ld);
-          const int co = __shfl_sync(0xffffffffu, my_col, k);
-          if (fuse) {
-            double* xo = ir.x64 + (unsigned)co * (unsigned)ld + s;
-            const double nx = *xo + (double)val;
-            *xo = nx;
-            irm.dx = fmax(irm.dx, fabs((double)val));
-            irm.x = fmax(irm.x, fabs(nx));
-          }
+      using V2 = typename Vec2<T>::type;
+      constexpr unsigned kRow = kGroup * sizeof(T);
+      // The previous segment's bulk stores must have read the table; when
+      // this segment reads rows they wrote, they must also be complete.
+      if ((sg.y >> 30) & 1) bulk_wait_all();
+      else bulk_wait_read();
+      __syncwarp();
+      if (lane == 0) mbar_arrive_expect_tx(tma.mbar, (unsigned)nl * kRow);
+      __syncwarp();
+      for (int l = lane; l < nl; l += 32)
+        bulk_load(sm + l * kGroup, prog_row<T, KIND>(__ldg(lr + l), v, x, ld, s0), kRow,
+                  tma.mbar);
+      long long polls = 0;
+      while (!mbar_try_wait(tma.mbar, tma.phase)) {
+        if (++polls > kMbarMaxPolls) {
+          report_error(st, 6, -2, s0);
+          break;
         }
       }
+      tma.phase ^= 1u;
+      V2* t = reinterpret_cast<V2*>(sm) + lane;
+      const int4* o4 = P.ops + (sg.z >> 2);
+      for (int k = 0; k < (sg.w >> 2); k++) {
+        const int4 w = __ldg(o4 + k);
+        const int base = sg.z + 4 * k;
+        exec_op2<T>((uint32_t)w.x, base, P.op_col, t, s0 + 2 * lane, S, pivot_tol, st);
+        exec_op2<T>((uint32_t)w.y, base + 1, P.op_col, t, s0 + 2 * lane, S, pivot_tol, st);
+        exec_op2<T>((uint32_t)w.z, base + 2, P.op_col, t, s0 + 2 * lane, S, pivot_tol, st);
+        exec_op2<T>((uint32_t)w.w, base + 3, P.op_col, t, s0 + 2 * lane, S, pivot_tol, st);
+      }
+      // Make this lane's table writes visible to the async proxy, then let
+      // lanes write back the own rows with bulk stores.
+      fence_proxy_async();
+      __syncwarp();
+      for (int l = lane; l < n_own; l += 32)
+        bulk_store(prog_row<T, KIND>(__ldg(lr + l), v, x, ld, s0), sm + l * kGroup, kRow);
+      bulk_commit();
     } else {
-      for (int l = lane; l < nl; l += 32) sm[l] = prog_fetch<T, KIND>(__ldg(lr + l), v, x, 1);
+      for (int l = lane; l < nl; l += 32) sm[l] = prog_fetch1<T, KIND>(__ldg(lr + l), v, x);
       __syncwarp();
-      if (lane == 0) prog_exec_ops<T, false>(P, sg.z, sg.w, sm, 0, S, pivot_tol, st);
-      __syncwarp();
-      for (int l = lane; l < n_own; l += 32) {
-        const int r = __ldg(lr + l);
-        prog_store<T, KIND>(r, sm[l], v, x, 1);
-        if (fuse) {
-          double* xo = ir.x64 + __ldg(ir.col_orig + r);
-          const double nx = *xo + (double)sm[l];
-          *xo = nx;
-          irm.dx = fmax(irm.dx, fabs((double)sm[l]));
-          irm.x = fmax(irm.x, fabs(nx));
+      if (lane == 0) {
+        const int4* o4 = P.ops + (sg.z >> 2);
+        for (int k = 0; k < (sg.w >> 2); k++) {
+          const int4 w = __ldg(o4 + k);
+          const int base = sg.z + 4 * k;
+          exec_op1<T>((uint32_t)w.x, base, P.op_col, sm, S, pivot_tol, st);
+          exec_op1<T>((uint32_t)w.y, base + 1, P.op_col, sm, S, pivot_tol, st);
+          exec_op1<T>((uint32_t)w.z, base + 2, P.op_col, sm, S, pivot_tol, st);
+          exec_op1<T>((uint32_t)w.w, base + 3, P.op_col, sm, S, pivot_tol, st);
         }
       }
+      __syncwarp();
+      for (int l = lane; l < n_own; l += 32) prog_store1<T, KIND>(__ldg(lr + l), sm[l], v, x);
       __syncwarp();
     }
   }
 }
 
-// Chains [cb, ce) of one level: work item = (chain, 32-scenario group) in
-// batched mode, chain alone in single mode; one warp per item.
+// Chains [cb, ce) of one level: work item = (chain, 64-scenario group) in
+// batched mode, chain alone in single mode; one warp per item.  In batched
+// mode every bulk store of the warp is complete when this returns.
 template <typename T, int KIND, bool BATCH>
 __device__ __forceinline__ void prog_run_level(const ProgDev& P, const DevStruct& d, int cb,
                                                int ce, T* __restrict__ v, T* __restrict__ x,
-                                               int ld, int S, T* sm_warp, double pivot_tol,
-                                               DevStatus* st, const int* done, int warp_id,
-                                               int n_warps, const IrFuse& ir) {
-  const int groups = BATCH ? ld >> 5 : 1;
+                                               int ld, int S, T* sm_warp, WarpTma& tma,
+                                               double pivot_tol, DevStatus* st,
+                                               const int* done, int warp_id, int n_warps) {
+  const int groups = BATCH ? ld / kGroup : 1;
   const int items = (ce - cb) * groups;
   const int lane = threadIdx.x & 31;
-  IrMax irm;
   for (int it = warp_id; it < items; it += n_warps) {
     const int ci = BATCH ? it / groups : it;
     const int c = cb + ci;
-    const int s = BATCH ? ((it - ci * groups) << 5) + lane : 0;
-    if (BATCH && done && __all_sync(0xffffffffu, s >= S || done[s])) continue;
-    if (KIND == 1 && ir.x64 && s != irm.s) {
-      irm.flush(ir);
-      irm.s = s;
+    const int s0 = BATCH ? (it - ci * groups) * kGroup : 0;
+    if (BATCH && done) {
+      const int sa = s0 + 2 * lane;
+      const bool idle = (sa >= S || done[sa]) && (sa + 1 >= S || done[sa + 1]);
+      if (__all_sync(0xffffffffu, idle)) continue;
     }
-    prog_run_chain<T, KIND, BATCH>(P, d, c, v, x, ld, s, S, sm_warp, pivot_tol, st, ir, irm);
+    prog_run_chain<T, KIND, BATCH>(P, d, c, v, x, ld, s0, S, sm_warp, tma, pivot_tol, st);
   }
-  if (KIND == 1 && ir.x64) irm.flush(ir);
+  if (BATCH) {
+    bulk_wait_all();
+    fence_proxy_async();
+  }
+}
+
+// Table layout of a block: warps_per_block tables, then one mbarrier per
+// warp.  Returns this warp's table and initialises its mbarrier.
+template <typename T, bool BATCH>
+__device__ __forceinline__ T* prog_setup_warp(unsigned char* smem_raw, int max_locals,
+                                              WarpTma& tma) {
+  const int w = threadIdx.x >> 5;
+  const int nw = blockDim.x >> 5;
+  const size_t table = (size_t)max_locals * (BATCH ? kGroup : 1) * sizeof(T);
+  T* sm = reinterpret_cast<T*>(smem_raw + (size_t)w * table);
+  tma.mbar = reinterpret_cast<unsigned long long*>(smem_raw + (size_t)nw * table) + w;
+  tma.phase = 0;
+  if (BATCH) {
+    if ((threadIdx.x & 31) == 0) mbar_init(tma.mbar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    __syncwarp();
+  }
+  return sm;
+}
+
+template <typename T, bool BATCH>
+size_t prog_smem_bytes(int max_locals, int warps_per_block) {
+  return (size_t)warps_per_block * max_locals * (BATCH ? kGroup : 1) * sizeof(T) +
+         (size_t)warps_per_block * sizeof(unsigned long long);
 }
 
 template <typename T, int KIND, bool BATCH>
 __global__ void k_prog_level(ProgDev P, DevStruct d, int cb, int ce, T* __restrict__ v,
                              T* __restrict__ x, int ld, int S, double pivot_tol, DevStatus* st,
-                             const int* done, IrFuse ir) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* sm = reinterpret_cast<T*>(smem_raw) +
-          (threadIdx.x >> 5) * P.max_locals * (BATCH ? 32 : 1);
+                             const int* done) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  WarpTma tma;
+  T* sm = prog_setup_warp<T, BATCH>(smem_raw, P.max_locals, tma);
   const int warp_id = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int n_warps = (gridDim.x * blockDim.x) >> 5;
-  prog_run_level<T, KIND, BATCH>(P, d, cb, ce, v, x, ld, S, sm, pivot_tol, st, done, warp_id,
-                                 n_warps, ir);
+  prog_run_level<T, KIND, BATCH>(P, d, cb, ce, v, x, ld, S, sm, tma, pivot_tol, st, done,
+                                 warp_id, n_warps);
 }
 
 }  // namespace pvglu

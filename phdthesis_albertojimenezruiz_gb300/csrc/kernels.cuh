@@ -222,49 +222,14 @@ __global__ void k_residual(const int* __restrict__ a_rowptr, const int* __restri
                            const double* __restrict__ b, const double* __restrict__ x,
                            const int* __restrict__ done, float* __restrict__ r_perm,
                            const int* __restrict__ row_pos) {
-  if (ld == 1) {
-    for_rows(n, ld, [&](int i, int s) {
-      if (s >= S || done[s]) return;
-      double acc = b[i];
-      for (int p = a_rowptr[i]; p < a_rowptr[i + 1]; p++) acc -= a[p] * x[a_colidx[p]];
-      r_perm[row_pos[i]] = (float)acc;  // row i of J is row row_pos[i] of M
-    });
-    return;
-  }
-  // A warp owns a row: its pattern (up to kCache entries) is read once into
-  // registers, then the scenario loop issues independent coalesced loads.
-  constexpr int kCache = 8;
-  const int lane = threadIdx.x & 31;
-  const int warps = (gridDim.x * blockDim.x) >> 5;
-  for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
-    const int p0 = a_rowptr[i], np = a_rowptr[i + 1] - p0;
-    const unsigned ro = (unsigned)row_pos[i] * (unsigned)ld;
-    if (np <= kCache) {
-      unsigned col_off[kCache], a_off[kCache];
-#pragma unroll
-      for (int k = 0; k < kCache; k++) {
-        col_off[k] = k < np ? (unsigned)a_colidx[p0 + k] * (unsigned)ld : 0u;
-        a_off[k] = (unsigned)(p0 + k) * (unsigned)ld;
-      }
-#pragma unroll 2
-      for (int s = lane; s < ld; s += 32) {
-        if (s >= S || done[s]) continue;
-        double acc = b[(unsigned)i * (unsigned)ld + s];
-#pragma unroll
-        for (int k = 0; k < kCache; k++)
-          if (k < np) acc -= a[a_off[k] + s] * x[col_off[k] + s];
-        r_perm[ro + s] = (float)acc;
-      }
-    } else {
-      for (int s = lane; s < ld; s += 32) {
-        if (s >= S || done[s]) continue;
-        double acc = b[(unsigned)i * (unsigned)ld + s];
-        for (int p = p0; p < p0 + np; p++)
-          acc -= a[(unsigned)p * (unsigned)ld + s] * x[(unsigned)a_colidx[p] * (unsigned)ld + s];
-        r_perm[ro + s] = (float)acc;
-      }
-    }
-  }
+  for_rows(n, ld, [&](int i, int s) {
+    if (s >= S || done[s]) return;
+    double acc = b[(int64_t)i * ld + s];
+    for (int p = a_rowptr[i]; p < a_rowptr[i + 1]; p++)
+      acc -= a[(int64_t)p * ld + s] * x[(int64_t)a_colidx[p] * ld + s];
+    // Row i of J is row row_pos[i] of the pivot-ordered system.
+    r_perm[(int64_t)row_pos[i] * ld + s] = (float)acc;
+  });
 }
 
 // x[col_orig[c]] += dx[c]; per-scenario max |dx| and max |x| (non-negative

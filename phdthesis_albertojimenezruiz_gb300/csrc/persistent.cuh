@@ -75,26 +75,33 @@ struct SkipDone {
 };
 
 // ---------------------------------------------------------------------------
-// Persistent walk over chain programs (chainprog.cuh): same phases and
-// barriers as k_persistent, each chain executed from a shared-memory table.
+// Persistent walk over chain programs (chainprog.cuh): the levels of each
+// requested phase in order, a bounded grid barrier between levels, each chain
+// executed from a shared-memory table.
 struct ProgSetDev {
   ProgDev p[5];  // refactor, L, U, U^T, L^T
 };
 
 constexpr int kProgBlock = 128;
+constexpr int kProgWarps = kProgBlock / 32;
 
 template <typename T, int KIND, bool BATCH>
 __device__ __forceinline__ bool prog_phase(const ProgDev& P, const DevStruct& d, T* v, T* x,
-                                           int ld, int S, T* sm, double pivot_tol,
-                                           DevStatus* st, unsigned int* bar, const int* done,
-                                           bool* need_sync, const IrFuse& ir) {
+                                           int ld, int S, T* sm, WarpTma& tma,
+                                           double pivot_tol, DevStatus* st, unsigned int* bar,
+                                           const int* done, bool* need_sync) {
   const int warp_id = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int n_warps = (gridDim.x * blockDim.x) >> 5;
   for (int lv = 0; lv < P.n_levels; lv++) {
-    if (*need_sync && !grid_barrier(bar, st, gridDim.x, kBarrierMaxSpins)) return false;
+    if (*need_sync) {
+      if (!grid_barrier(bar, st, gridDim.x, kBarrierMaxSpins)) return false;
+      // Bulk copies issued after the barrier must see what other blocks
+      // wrote before it.
+      if (BATCH) fence_proxy_async();
+    }
     *need_sync = true;
     prog_run_level<T, KIND, BATCH>(P, d, P.level_chain[lv], P.level_chain[lv + 1], v, x, ld,
-                                   S, sm, pivot_tol, st, done, warp_id, n_warps, ir);
+                                   S, sm, tma, pivot_tol, st, done, warp_id, n_warps);
   }
   return true;
 }
@@ -103,38 +110,32 @@ template <typename T, bool BATCH>
 __global__ void __launch_bounds__(kProgBlock)
 k_prog_persistent(ProgSetDev PS, DevStruct d, T* __restrict__ v, T* __restrict__ x, int ld,
                   int S, double pivot_tol, DevStatus* st, unsigned int* bar, int phases,
-                  SkipDone skip, IrFuse ir) {
+                  SkipDone skip) {
   if (skip.ndone && __ldcg(skip.ndone) >= S) return;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int ml = PS.p[0].max_locals;
-  T* sm = reinterpret_cast<T*>(smem_raw) + (threadIdx.x >> 5) * ml * (BATCH ? 32 : 1);
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  WarpTma tma;
+  T* sm = prog_setup_warp<T, BATCH>(smem_raw, PS.p[0].max_locals, tma);
   bool need_sync = false;
-  const IrFuse none{nullptr, nullptr, nullptr, nullptr, nullptr};
   if (phases & PHASE_REFACTOR)
-    if (!prog_phase<T, -1, BATCH>(PS.p[0], d, v, x, ld, S, sm, pivot_tol, st, bar, nullptr,
-                                  &need_sync, none))
+    if (!prog_phase<T, -1, BATCH>(PS.p[0], d, v, x, ld, S, sm, tma, pivot_tol, st, bar,
+                                  nullptr, &need_sync))
       return;
   if (phases & PHASE_SOLVE) {
-    if (!prog_phase<T, 0, BATCH>(PS.p[1], d, v, x, ld, S, sm, pivot_tol, st, bar, skip.done,
-                                 &need_sync, none))
+    if (!prog_phase<T, 0, BATCH>(PS.p[1], d, v, x, ld, S, sm, tma, pivot_tol, st, bar,
+                                 skip.done, &need_sync))
       return;
-    if (!prog_phase<T, 1, BATCH>(PS.p[2], d, v, x, ld, S, sm, pivot_tol, st, bar, skip.done,
-                                 &need_sync, ir))
+    if (!prog_phase<T, 1, BATCH>(PS.p[2], d, v, x, ld, S, sm, tma, pivot_tol, st, bar,
+                                 skip.done, &need_sync))
       return;
   }
   if (phases & PHASE_SOLVE_T) {
-    if (!prog_phase<T, 2, BATCH>(PS.p[3], d, v, x, ld, S, sm, pivot_tol, st, bar, skip.done,
-                                 &need_sync, none))
+    if (!prog_phase<T, 2, BATCH>(PS.p[3], d, v, x, ld, S, sm, tma, pivot_tol, st, bar,
+                                 skip.done, &need_sync))
       return;
-    if (!prog_phase<T, 3, BATCH>(PS.p[4], d, v, x, ld, S, sm, pivot_tol, st, bar, skip.done,
-                                 &need_sync, none))
+    if (!prog_phase<T, 3, BATCH>(PS.p[4], d, v, x, ld, S, sm, tma, pivot_tol, st, bar,
+                                 skip.done, &need_sync))
       return;
   }
-}
-
-template <typename T, bool BATCH>
-size_t prog_smem_bytes(int max_locals) {
-  return (size_t)(kProgBlock / 32) * max_locals * (BATCH ? 32 : 1) * sizeof(T);
 }
 
 // Largest co-resident grid of k_prog_persistent for the given table size.
@@ -145,7 +146,7 @@ int prog_persistent_grid(int max_locals) {
   if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop)
     return 0;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
-  const size_t smem = prog_smem_bytes<T, BATCH>(max_locals);
+  const size_t smem = prog_smem_bytes<T, BATCH>(max_locals, kProgWarps);
   if (cudaFuncSetAttribute(k_prog_persistent<T, BATCH>,
                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return 0;
@@ -159,27 +160,15 @@ template <typename T, bool BATCH>
 int launch_prog_persistent(const ProgSetDev& PS, int max_chains, const DevStruct& d, T* v,
                            T* x, int ld, int S, double pivot_tol, DevStatus* st,
                            unsigned int* bar, int max_grid, int phases, cudaStream_t stream,
-                           SkipDone skip, IrFuse ir) {
+                           SkipDone skip) {
   if (max_grid <= 0) return 1;
-  const int64_t items = (int64_t)max_chains * (BATCH ? ld / 32 : 1);
-  const int64_t want = (items + kProgBlock / 32 - 1) / (kProgBlock / 32);
-  int grid = (int)std::max<int64_t>(1, std::min<int64_t>(want, max_grid));
-  if (BATCH) {
-    // Make the warp count a multiple of the scenario groups so that each
-    // warp keeps one scenario group through every level (the fused
-    // refinement then flushes its running maxima once per level).
-    const int warps_per_block = kProgBlock / 32;
-    const int groups = ld / 32;
-    int g = groups, w = warps_per_block;
-    while (w) { const int t = g % w; g = w; w = t; }  // gcd(groups, warps_per_block)
-    const int step = groups / g;
-    if (grid >= step) grid = grid / step * step;
-  }
+  const int64_t items = (int64_t)max_chains * (BATCH ? ld / kGroup : 1);
+  const int64_t want = (items + kProgWarps - 1) / kProgWarps;
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(want, max_grid));
   if (cudaMemsetAsync(bar, 0, 3 * sizeof(unsigned int), stream) != cudaSuccess) return 1;
   void* args[] = {(void*)&PS, (void*)&d, (void*)&v, (void*)&x, (void*)&ld, (void*)&S,
-                  (void*)&pivot_tol, (void*)&st, (void*)&bar, (void*)&phases, (void*)&skip,
-                  (void*)&ir};
-  const size_t smem = prog_smem_bytes<T, BATCH>(PS.p[0].max_locals);
+                  (void*)&pivot_tol, (void*)&st, (void*)&bar, (void*)&phases, (void*)&skip};
+  const size_t smem = prog_smem_bytes<T, BATCH>(PS.p[0].max_locals, kProgWarps);
   if (cudaLaunchCooperativeKernel((const void*)k_prog_persistent<T, BATCH>, dim3(grid),
                                   dim3(kProgBlock), args, smem, stream) != cudaSuccess)
     return 1;

@@ -178,6 +178,12 @@ void build_chain_program(const Symbolic& s, int kind, int max_locals, ChainProgr
   Table t;
   t.init(s.n, s.nnz_lu);
   std::vector<int> remap;
+  // Entries written by the segments of the current chain so far (by ref).
+  std::vector<char> written_x(s.n, 0), written_v(s.nnz_lu, 0);
+  std::vector<int> written_list;
+  auto written = [&](int ref) -> char& {
+    return (kind >= 0 && ref >= 0) ? written_x[ref] : written_v[kind < 0 ? ref : -ref - 1];
+  };
   auto close = [&]() {
     if (t.units.empty()) return;
     // Own entries first (in load order), then the read-only ones.
@@ -187,6 +193,14 @@ void build_chain_program(const Symbolic& s, int kind, int max_locals, ChainProgr
     g.load_begin = (int)out.loads.size();
     g.n_load = nl;
     g.n_own = 0;
+    g.reads_own_chain = 0;
+    for (int l = 0; l < nl; l++)
+      if (!t.own[l] && written(t.refs[l])) g.reads_own_chain = 1;
+    for (int l = 0; l < nl; l++)
+      if (t.own[l] && !written(t.refs[l])) {
+        written(t.refs[l]) = 1;
+        written_list.push_back(t.refs[l]);
+      }
     for (int l = 0; l < nl; l++)
       if (t.own[l]) {
         remap[l] = g.n_own++;
@@ -215,6 +229,8 @@ void build_chain_program(const Symbolic& s, int kind, int max_locals, ChainProgr
     t.reset();
   };
   for (int c = 0; c < ls.num_chains(); c++) {
+    for (int r : written_list) written(r) = 0;
+    written_list.clear();
     out.chain_seg.push_back((int)out.seg.size());
     const int first_seg = (int)out.seg.size();
     for (int k = ls.start_chains[c]; k < ls.start_chains[c + 1]; k++) {
@@ -228,7 +244,19 @@ void build_chain_program(const Symbolic& s, int kind, int max_locals, ChainProgr
         // Too wide for the local table: executed from global memory, after
         // the segment collected so far (chain order is execution order).
         close();
-        out.seg.push_back(Segment{0, -1, 0, u, 0});
+        out.seg.push_back(Segment{0, -1, 0, u, 0, 1});
+        // A DIRECT unit writes its own entries through global memory.
+        const int own_ref = kind < 0 ? -1 : u;
+        if (own_ref >= 0 && !written(own_ref)) {
+          written(own_ref) = 1;
+          written_list.push_back(own_ref);
+        }
+        if (kind < 0)
+          for (int q = s.csc_colptr[u]; q < s.csc_colptr[u + 1]; q++)
+            if (!written(q)) {
+              written(q) = 1;
+              written_list.push_back(q);
+            }
         out.direct_segments++;
         continue;
       }

@@ -43,6 +43,7 @@ inline uint32_t pack_op(int code, int a, int b, int c) {
 // too wide for the table) is executed straight from global memory.
 struct Segment {
   int load_begin, n_load, n_own, op_begin, n_op;
+  int reads_own_chain = 0;  // reads entries written by an earlier segment of the chain
 };
 
 struct ChainProgram {
