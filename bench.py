@@ -203,10 +203,15 @@ def main() -> None:
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--scenarios", type=int, default=512)
     ap.add_argument("--cpu-budget", type=float, default=10.0)
+    ap.add_argument("--ir-tol", type=float, default=IR_TOL,
+                    help="refinement stop: max|dx| <= tol * max|x| per scenario")
+    ap.add_argument("--ir-sweeps", type=int, default=IR_MAX_SWEEPS)
     ap.add_argument("--only-batched", action="store_true",
                     help="time the batched FP32+IR path only (profiling runs)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    global IR_TOL, IR_MAX_SWEEPS
+    IR_TOL, IR_MAX_SWEEPS = args.ir_tol, args.ir_sweeps
     if args.impl == "reference":
         run_reference(args)
         return
@@ -374,7 +379,8 @@ def main() -> None:
         return
     cpu = cpu_baseline(a[:, :S], b[:, :S], p, sym.array("perm_amd"), args.cpu_budget,
                        os.cpu_count() or 1, prefer_ref=True)
-    launches = args.steps * (2 + 4 * IR_MAX_SWEEPS)
+    # per step: scatter, refactor, permute b, then per sweep solve + step + check
+    launches = args.steps * (3 + 3 * IR_MAX_SWEEPS)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
