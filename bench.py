@@ -196,6 +196,7 @@ def run_reference(args) -> None:
 
 
 def main() -> None:
+    global IR_TOL, IR_MAX_SWEEPS
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
@@ -210,7 +211,6 @@ def main() -> None:
                     help="time the batched FP32+IR path only (profiling runs)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
-    global IR_TOL, IR_MAX_SWEEPS
     IR_TOL, IR_MAX_SWEEPS = args.ir_tol, args.ir_sweeps
     if args.impl == "reference":
         run_reference(args)
