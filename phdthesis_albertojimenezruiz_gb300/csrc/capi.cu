@@ -59,8 +59,6 @@ struct pvglu_numeric {
   double* work64 = nullptr;     // [nnz_a * ld] staging / [n * ld] vectors
   double* b64 = nullptr;        // [n * ld]
   double* x64 = nullptr;        // [n * ld]
-  double* ir_x2 = nullptr;      // [n * ld] second solution buffer (FP32 handles)
-  float* ir_w2 = nullptr;       // [n * ld] second correction buffer (FP32 handles)
   int* col_pos = nullptr;       // inverse of col_orig
   int* row_pos = nullptr;       // inverse of row_orig
   pvglu::DevStatus* status = nullptr;
@@ -69,7 +67,6 @@ struct pvglu_numeric {
   unsigned long long* ir_max_x = nullptr;
   // Host copies of the level starts (launch ranges).
   std::vector<int> lu_sl, l_sl, u_sl, lt_sl;
-  // Persistent schedule.
   // Chain programs: refactor, L, U, U^T, L^T (programs.hpp).
   bool batch = false;              // ld > 1: lane = scenario
   int max_locals = 0;
@@ -131,12 +128,6 @@ void solve_phase(pvglu_numeric* h, const std::vector<int>& sl, T* x, const int* 
     pvglu::k_solve_level<T, KIND><<<launch_blocks(threads, 128), 128, 0, st>>>(
         h->d, v, x, h->ld, h->S, cb, ce, done);
   }
-}
-
-int ensure_ir_buffers(pvglu_numeric* h) {
-  if (!h->ir_x2 || !h->ir_w2 || !h->col_pos)
-    return fail(PVGLU_ERR_BAD_ARG, "refinement buffers missing (FP32 handles only)");
-  return PVGLU_OK;
 }
 
 // Kernel attributes (dynamic shared memory above 48 KB) and the persistent
@@ -395,10 +386,6 @@ int pvglu_numeric_create(const pvglu_symbolic* sym, int n_scenarios, int precisi
   rc |= h->alloc((size_t)std::max(h->nnz_a, h->n) * h->ld, &h->work64);
   rc |= h->alloc((size_t)h->n * h->ld, &h->b64);
   rc |= h->alloc((size_t)h->n * h->ld, &h->x64);
-  if (precision == PVGLU_FP32) {
-    rc |= h->alloc((size_t)h->n * h->ld, &h->ir_x2);
-    rc |= h->alloc((size_t)h->n * h->ld, &h->ir_w2);
-  }
   {
     std::vector<int> col_pos(s.n);
     for (int c = 0; c < s.n; c++) col_pos[s.col_orig[c]] = c;
@@ -719,12 +706,7 @@ int pvglu_solve_refined(pvglu_numeric* h, const double* a_values, const double* 
   if (h->precision != PVGLU_FP32) return fail(PVGLU_ERR_BAD_ARG, "needs an FP32 handle");
   cudaStream_t st = as_stream(stream);
   const int64_t nv = (int64_t)h->n * h->ld;
-  int rc = ensure_ir_buffers(h);
-  if (rc) return rc;
-  // x and the handle's second solution buffer alternate; the correction dx
-  // and the next residual alternate between the two FP32 work vectors.
-  double* xb[2] = {x, h->ir_x2};
-  float* wb[2] = {static_cast<float*>(h->work), h->ir_w2};
+  float* w = static_cast<float*>(h->work);
   PVGLU_CUDA(cudaMemsetAsync(x, 0, nv * sizeof(double), st));
   int* ndone = h->ir_done + h->ld;
   PVGLU_CUDA(cudaMemsetAsync(h->ir_done, 0, (h->ld + 1) * sizeof(int), st));
@@ -733,26 +715,22 @@ int pvglu_solve_refined(pvglu_numeric* h, const double* a_values, const double* 
   if (sweeps_out) PVGLU_CUDA(cudaMemsetAsync(sweeps_out, 0, h->ld * sizeof(int), st));
   const pvglu::SkipDone skip{h->ir_done, ndone};
   // x = 0: the first residual is b itself.
-  permute<double, float>(h, h->d.row_orig, b, wb[0], true, st);
-  int cx = 0, cw = 0;
+  permute<double, float>(h, h->d.row_orig, b, w, true, st);
   const dim3 blk(32, 8);
   const dim3 grd((unsigned)std::min(1024, (h->n + 7) / 8), (unsigned)(h->ld + 31) / 32);
   for (int sweep = 1; sweep <= max_sweeps; sweep++) {
-    rc = solve_permuted<float>(h, wb[cw], false, st, skip);  // dx of this sweep
+    int rc = solve_permuted<float>(h, w, false, st, skip);  // dx of this sweep
     if (rc) return rc;
-    // x <- x + dx, and the residual of the next sweep unless this is the last.
-    pvglu::k_ir_step<<<grd, blk, 0, st>>>(h->d.a_rowptr, h->d.a_colidx, h->col_pos, h->row_pos,
-                                          h->n, h->ld, h->S, a_values, b, xb[cx], xb[1 - cx],
-                                          wb[cw], wb[1 - cw], sweep < max_sweeps ? 1 : 0,
-                                          h->ir_done, ndone, h->ir_max_dx, h->ir_max_x);
+    pvglu::k_ir_update<<<grd, blk, 0, st>>>(h->d.col_orig, h->n, h->ld, h->S, w, x,
+                                            h->ir_done, h->ir_max_dx, h->ir_max_x);
     pvglu::k_ir_check<<<(h->S + 127) / 128, 128, 0, st>>>(h->S, sweep, max_sweeps, tol,
-                                                          1 - cx, h->ir_done, ndone, sweeps_out,
+                                                          h->ir_done, ndone, sweeps_out,
                                                           h->ir_max_dx, h->ir_max_x);
-    cx = 1 - cx;
-    cw = 1 - cw;
+    if (sweep < max_sweeps)  // residual of the scenarios still refining
+      pvglu::k_residual<<<pvglu::rows_grid(h->n, h->ld, 256), 256, 0, st>>>(
+          h->d.a_rowptr, h->d.a_colidx, h->n, h->ld, h->S, a_values, b, x, h->ir_done, w,
+          h->row_pos);
   }
-  pvglu::k_ir_finalize<<<pvglu::rows_grid(h->n, h->ld, 256), 256, 0, st>>>(
-      h->n, h->ld, h->S, cx, h->ir_done, x, h->ir_x2);
   PVGLU_CUDA(cudaGetLastError());
   return PVGLU_OK;
 }

@@ -232,73 +232,6 @@ __global__ void k_residual(const int* __restrict__ a_rowptr, const int* __restri
   });
 }
 
-// One refinement step in one pass: apply the correction and form the next
-// residual.  For unknown i (caller order) with column position c = col_pos[i]:
-//   x_new[i] = x_old[i] + dx[c]
-//   r[row_pos[i]] = b[i] - sum_e A[e] * (x_old[j_e] + dx[col_pos[j_e]])
-// (the neighbours' updated values are formed on the fly, so x is
-// double-buffered instead of updated in place).  Per-scenario max |dx| and
-// max |x_new| feed the convergence test.  Converged scenarios are skipped
-// (done[s] records which buffer holds their result).  block = 32 scenarios x
-// 8 rows.
-__global__ void k_ir_step(const int* __restrict__ a_rowptr, const int* __restrict__ a_colidx,
-                          const int* __restrict__ col_pos, const int* __restrict__ row_pos,
-                          int n, int ld, int S, const double* __restrict__ a,
-                          const double* __restrict__ b, const double* __restrict__ x_old,
-                          double* __restrict__ x_new, const float* __restrict__ dx,
-                          float* __restrict__ r_perm, int want_residual,
-                          const int* __restrict__ done, const int* __restrict__ ndone,
-                          unsigned long long* __restrict__ max_dx,
-                          unsigned long long* __restrict__ max_x) {
-  if (__ldcg(ndone) >= S) return;  // every scenario converged
-  const int s = blockIdx.y * 32 + threadIdx.x;
-  __shared__ double sdx[8][33], sx[8][33];
-  double mdx = 0.0, mx = 0.0;
-  const bool active = s < S && !done[s];
-  if (active) {
-    for (int i = blockIdx.x * 8 + threadIdx.y; i < n; i += gridDim.x * 8) {
-      const int64_t ii = (int64_t)i * ld + s;
-      const double d = (double)dx[(int64_t)col_pos[i] * ld + s];
-      const double nx = x_old[ii] + d;
-      x_new[ii] = nx;
-      mdx = fmax(mdx, fabs(d));
-      mx = fmax(mx, fabs(nx));
-      if (want_residual) {
-        double acc = b[ii];
-        for (int p = a_rowptr[i]; p < a_rowptr[i + 1]; p++) {
-          const int j = a_colidx[p];
-          const double xj = x_old[(int64_t)j * ld + s] + (double)dx[(int64_t)col_pos[j] * ld + s];
-          acc -= a[(int64_t)p * ld + s] * xj;
-        }
-        r_perm[(int64_t)row_pos[i] * ld + s] = (float)acc;
-      }
-    }
-  }
-  sdx[threadIdx.y][threadIdx.x] = mdx;
-  sx[threadIdx.y][threadIdx.x] = mx;
-  __syncthreads();
-  if (threadIdx.y == 0 && active) {
-    for (int k = 1; k < 8; k++) {
-      mdx = fmax(mdx, sdx[k][threadIdx.x]);
-      mx = fmax(mx, sx[k][threadIdx.x]);
-    }
-    atomicMax(max_dx + s, (unsigned long long)__double_as_longlong(mdx));
-    atomicMax(max_x + s, (unsigned long long)__double_as_longlong(mx));
-  }
-}
-
-// Gathers every scenario's refined solution into x (buffer 0): scenarios
-// whose result sits in buffer 1 (done[s] == 2, or not converged and the last
-// sweep wrote buffer 1) are copied from x2.
-__global__ void k_ir_finalize(int n, int ld, int S, int last_buf, const int* __restrict__ done,
-                              double* __restrict__ x, const double* __restrict__ x2) {
-  for_rows(n, ld, [&](int i, int s) {
-    if (s >= S) return;
-    const int buf = done[s] ? done[s] - 1 : last_buf;
-    if (buf == 1) x[(int64_t)i * ld + s] = x2[(int64_t)i * ld + s];
-  });
-}
-
 // x[col_orig[c]] += dx[c]; per-scenario max |dx| and max |x| (non-negative
 // doubles order like their bit patterns, so atomicMax on the bits works).
 __global__ void k_ir_update(const int* __restrict__ col_orig, int n, int ld, int S,
@@ -333,10 +266,8 @@ __global__ void k_ir_update(const int* __restrict__ col_orig, int n, int ld, int
   }
 }
 
-// Convergence bookkeeping after sweep `sweep` (1-based).  The sweep's
-// updated solution sits in buffer `new_buf`; a converged scenario records it
-// as done[s] = 1 + new_buf.
-__global__ void k_ir_check(int S, int sweep, int last_sweep, double tol, int new_buf, int* done,
+// Convergence bookkeeping after sweep `sweep` (1-based).
+__global__ void k_ir_check(int S, int sweep, int last_sweep, double tol, int* done,
                            int* ndone, int* sweeps_out, unsigned long long* max_dx,
                            unsigned long long* max_x) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -347,7 +278,7 @@ __global__ void k_ir_check(int S, int sweep, int last_sweep, double tol, int new
   max_x[s] = 0ull;
   const bool ok = mdx <= tol * mx;
   if (ok) {
-    done[s] = 1 + new_buf;
+    done[s] = 1;
     atomicAdd(ndone, 1);
     if (sweeps_out) sweeps_out[s] = sweep;
   } else if (sweep == last_sweep) {
