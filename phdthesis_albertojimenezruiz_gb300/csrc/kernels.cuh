@@ -112,6 +112,61 @@ __global__ void k_scatter(const int* __restrict__ slot_src, int nnz, int ld, int
   });
 }
 
+// Structured Jacobian: value of A entry e for scenario s,
+//   base[e] + sum_c sign[c] * g[elem[c]],
+// the companion stamps of every nonlinear element on entry e
+// (002b_sistema_electrico_base_matriz.cpp:183-197) over the linear part.
+struct Stamps {
+  const double* base;
+  const int* ptr;
+  const int* elem;
+  const int* sign;
+};
+
+__device__ __forceinline__ double stamp_value(const Stamps& st, int e, const double* g, int ld,
+                                              int s) {
+  double val = st.base[e];
+  for (int c = st.ptr[e]; c < st.ptr[e + 1]; c++)
+    val += (double)st.sign[c] * g[(int64_t)st.elem[c] * ld + s];
+  return val;
+}
+
+// (a) scatter from stamps: LU(q, s) = A(slot_src[q], s) assembled on the fly.
+template <typename T>
+__global__ void k_scatter_stamps(const int* __restrict__ slot_src, int nnz, int ld, int S,
+                                 Stamps st, const double* __restrict__ g, T* __restrict__ v) {
+  for_rows(nnz, ld, [&](int q, int s) {
+    const int src = slot_src[q];
+    T val = T(0);
+    if (src >= 0 && s < S) val = (T)stamp_value(st, src, g, ld, s);
+    v[(int64_t)q * ld + s] = val;
+  });
+}
+
+// A's entry values from stamps (caller order), for callers that need them.
+__global__ void k_assemble_stamps(int nnz_a, int ld, int S, Stamps st,
+                                  const double* __restrict__ g, double* __restrict__ a) {
+  for_rows(nnz_a, ld, [&](int e, int s) {
+    a[(int64_t)e * ld + s] = s < S ? stamp_value(st, e, g, ld, s) : 0.0;
+  });
+}
+
+// FP64 residual r = b - A x with A from stamps (see k_residual).
+__global__ void k_residual_stamps(const int* __restrict__ a_rowptr,
+                                  const int* __restrict__ a_colidx, int n, int ld, int S,
+                                  Stamps st, const double* __restrict__ g,
+                                  const double* __restrict__ b, const double* __restrict__ x,
+                                  const int* __restrict__ done, float* __restrict__ r_perm,
+                                  const int* __restrict__ row_pos) {
+  for_rows(n, ld, [&](int i, int s) {
+    if (s >= S || done[s]) return;
+    double acc = b[(int64_t)i * ld + s];
+    for (int p = a_rowptr[i]; p < a_rowptr[i + 1]; p++)
+      acc -= stamp_value(st, p, g, ld, s) * x[(int64_t)a_colidx[p] * ld + s];
+    r_perm[(int64_t)row_pos[i] * ld + s] = (float)acc;
+  });
+}
+
 // ----------------------------------------------------------------------------
 // (b) left-looking GLU column k for scenario s.
 //   for every U slot p of column k (rows j < k, ascending):
