@@ -132,6 +132,25 @@ int pvglu_numeric_set_pivot_tol(pvglu_numeric* h, double tol);
  * (000_PVPP_simulator.cpp:193-210, 010_create_CSR_CSC.cpp:142-155). */
 int pvglu_scatter(pvglu_numeric* h, const double* a_values, void* stream);
 
+/* Structured Jacobian ("stamps").  A Newton Jacobian is a fixed linear part
+ * plus the companion conductance of every nonlinear two-terminal element
+ * stamped on up to four entries (002b_sistema_electrico_base_matriz.cpp:5-38
+ * admittance stamp, :183-202 per-element G and convergence conductance).
+ * Registering that structure once lets the scatter, the refinement residual
+ * and the Newton driver read one FP64 conductance per element and scenario
+ * instead of nnz_a FP64 values per scenario.
+ * Host arrays, copied: base[nnz_a] linear values; entry e receives
+ * sum over c in [entry_ptr[e], entry_ptr[e+1]) of entry_sign[c] * g[entry_elem[c]]
+ * (entry_sign = +1 / -1), added after base in that order.  Replaces any
+ * earlier registration on the handle. */
+int pvglu_numeric_set_stamps(pvglu_numeric* h, int n_elems, const double* base,
+                             const int* entry_ptr, const int* entry_elem,
+                             const int* entry_sign);
+/* (a) from stamps: g device FP64 [n_elems * ld] element conductances; gmin
+ * device FP64 [ld] per-scenario convergence conductance added to every
+ * element stamp where it is > 0, or NULL. */
+int pvglu_scatter_stamps(pvglu_numeric* h, const double* g, const double* gmin, void* stream);
+
 /* (b) GLU numeric refactorization in place, every scenario.
  * Replaces factorize_electrical_system_CUDA (factorize_electrical_system_CUDA.cu:61-152). */
 int pvglu_refactor(pvglu_numeric* h, void* stream);
@@ -181,6 +200,14 @@ int pvglu_scatter_refactor_solve_host(pvglu_numeric* h, const double* a_values_h
 int pvglu_solve_refined(pvglu_numeric* h, const double* a_values, const double* b,
                         double* x, double tol, int max_sweeps, int* sweeps_out,
                         void* stream);
+
+/* General form of pvglu_solve_refined: A's values either explicit
+ * (a_values, g NULL) or from the registered stamps (g [n_elems * ld] and
+ * optional gmin [ld], a_values NULL).  flags: PVGLU_SOLVE_TRANSPOSE refines
+ * J^T x = b (the adjoint system) with an FP64 residual over J's columns. */
+int pvglu_refine(pvglu_numeric* h, const double* a_values, const double* g, const double* gmin,
+                 const double* b, double* x, int flags, double tol, int max_sweeps,
+                 int* sweeps_out, void* stream);
 
 /* Host-buffer form of one refined linear step on an FP32 handle: H2D of A's
  * values ([nnz_a * ld], FP64) and b ([n * ld], FP64, original order),

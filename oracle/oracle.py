@@ -105,6 +105,12 @@ class Port(_Base):
             for f in ("oracle_refactor_levels", "oracle_refactor_sequential"):
                 getattr(lib, f).argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
             lib.oracle_scatter_refactor_solve.argtypes = [C.c_void_p] * 4 + [C.c_int]
+            D = C.c_double
+            lib.oracle_newton.argtypes = ([C.c_void_p, C.c_int] + [C.c_void_p] * 4 + [C.c_int] +
+                                          [C.c_void_p] * 2 + [D] * 4 + [C.c_void_p] * 3 +
+                                          [C.c_int, D, C.c_int] + [C.c_void_p] * 3)
+            lib.oracle_adjoint.argtypes = ([C.c_void_p, C.c_int] + [C.c_void_p] * 4 + [C.c_int] +
+                                           [C.c_void_p] * 2 + [D] * 4 + [C.c_void_p] * 4)
             lib.oracle_free.argtypes = [C.c_void_p]
             cls._lib = lib
         return cls._lib
@@ -147,6 +153,49 @@ class Port(_Base):
         if rc:
             raise ZeroDivisionError("oracle pivot failure")
         return lu, x
+
+
+    # ---- Newton loop and adjoint (oracle_newton.cpp) -------------------------
+    def _circuit(self, plant):
+        i = plant.info
+        keep = [np.ascontiguousarray(plant.rowptr, dtype=np.int32),
+                np.ascontiguousarray(plant.colidx, dtype=np.int32),
+                np.ascontiguousarray(plant.a_lin, dtype=np.float64),
+                np.ascontiguousarray(plant.b_lin, dtype=np.float64),
+                np.ascontiguousarray(plant.pan_hi, dtype=np.int32),
+                np.ascontiguousarray(plant.pan_lo, dtype=np.int32)]
+        args = [self.h, plant.n, _p(keep[0]), _p(keep[1]), _p(keep[2]), _p(keep[3]),
+                plant.n_panels, _p(keep[4]), _p(keep[5]), i["panel_i0"], i["panel_a"],
+                i["panel_rs"], i["panel_rsh"]]
+        return keep, args
+
+    def newton(self, plant, iph, v0, gmin, tol, max_iterations=5000):
+        """One scenario of the simulator's Newton loop.  Returns
+        (outcome, iterations, last diff, element voltages, node solution)."""
+        keep, args = self._circuit(plant)
+        iph = np.ascontiguousarray(iph, dtype=np.float64)
+        v = np.array(v0, dtype=np.float64, copy=True)
+        g = np.ascontiguousarray(gmin, dtype=np.float64)
+        x = np.zeros(plant.n)
+        it = C.c_int(0)
+        diff = C.c_double(0.0)
+        rc = self.lib.oracle_newton(*args, _p(iph), _p(v), _p(g), len(g), float(tol),
+                                    int(max_iterations), _p(x), C.byref(it), C.byref(diff))
+        del keep
+        return rc, it.value, diff.value, v, x
+
+    def adjoint(self, plant, iph, v, dpdx):
+        """dP/dIph per element at the iterate v for P = dpdx . x."""
+        keep, args = self._circuit(plant)
+        iph = np.ascontiguousarray(iph, dtype=np.float64)
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        dpdx = np.ascontiguousarray(dpdx, dtype=np.float64)
+        out = np.zeros(plant.n_panels)
+        rc = self.lib.oracle_adjoint(*args, _p(iph), _p(v), _p(dpdx), _p(out))
+        del keep
+        if rc:
+            raise RuntimeError(f"oracle adjoint failed ({rc})")
+        return out
 
 
 class Ref(_Base):

@@ -1,0 +1,192 @@
+// ORACLE — test infrastructure only.
+//
+// CPU restatement of the PV plant simulator's Newton loop, one scenario at a
+// time, over the oracle's own symbolic analysis and sequential GLU
+// (oracle_glu.cpp):
+//   stages of convergence conductance, a stage ends once diff < tol
+//     (PVPP_Plant_Simulator/000_PVPP_simulator.cpp:163-236),
+//   A and b assembled entry by entry as create_matrix_and_vector does
+//     (002b_sistema_electrico_base_matriz.cpp:141-240: linear part, then per
+//     nonlinear element the admittance G, the current source -Ieq and, while
+//     positive, the convergence admittance),
+//   permutation, scatter, GLU, substitution, unpermutation (000:193-233),
+//   damped update with a global halving loop (011_calculate_new_iteration.cpp:
+//   37-90) and a long double diff.
+// The element law is the plant's own definition (panel_model.h), an input of
+// the check like the plant's pattern and linear part.
+#include <cmath>
+#include <map>
+#include <vector>
+
+#include "panel_model.h"
+
+extern "C" {
+int oracle_get(void* h, const char* name, const int** ptr, long long* len);
+int oracle_scatter_refactor_solve(void* h, const double* a_vals, double* lu_out, double* b,
+                                  int sequential);
+int oracle_scatter(void* h, const double* a_vals, double* csc_vals);
+int oracle_refactor_sequential(void* h, double* v, int* bad_col);
+int oracle_solve_transposed(void* h, const double* v, double* b);
+}
+
+namespace {
+
+using Row = std::map<int, double>;
+
+struct Circuit {
+  int n, n_elems;
+  const int *rowptr, *colidx, *hi, *lo;
+  const double *a_lin, *b_lin;
+  pvglu_panel_params panel;
+};
+
+// 002b:5-38 (admittance between n1 and n2, ground = -1).
+void add_admittance(std::vector<Row>& A, int n1, int n2, double g) {
+  if (n1 >= 0) A[n1][n1] += g;
+  if (n1 >= 0 && n2 >= 0) {
+    A[n1][n2] += -g;
+    A[n2][n1] += -g;
+  }
+  if (n2 >= 0) A[n2][n2] += g;
+}
+
+// 002b:100-110 (current source val from n1 to n2).
+void add_current_source(std::vector<double>& b, int n1, int n2, double val) {
+  if (n1 >= 0) b[n1] += val;
+  if (n2 >= 0) b[n2] -= val;
+}
+
+// create_matrix_and_vector at the voltage iterate v; A's values returned in
+// the pattern's CSR order.  Returns false if a stamp falls outside it.
+bool assemble(const Circuit& c, const double* iph, const double* v, double gmin,
+              std::vector<double>& a_vals, std::vector<double>& b, std::vector<double>* didiph) {
+  std::vector<Row> A(c.n);
+  for (int i = 0; i < c.n; i++)
+    for (int p = c.rowptr[i]; p < c.rowptr[i + 1]; p++) A[i][c.colidx[p]] = c.a_lin[p];
+  b.assign(c.b_lin, c.b_lin + c.n);
+  for (int k = 0; k < c.n_elems; k++) {
+    double cur, didv, dphi;
+    pvglu_panel_iv3(&c.panel, iph[k], v[k], &cur, &didv, &dphi);
+    const double f = -cur, G = -didv;
+    const double ieq = f - G * v[k];
+    add_admittance(A, c.hi[k], c.lo[k], G);
+    add_current_source(b, c.hi[k], c.lo[k], -ieq);
+    if (gmin > 0) add_admittance(A, c.hi[k], c.lo[k], gmin);
+    if (didiph) (*didiph)[k] = dphi;
+  }
+  a_vals.assign(c.rowptr[c.n], 0.0);
+  size_t count = 0;
+  for (int i = 0; i < c.n; i++) {
+    count += A[i].size();
+    for (int p = c.rowptr[i]; p < c.rowptr[i + 1]; p++) a_vals[p] = A[i][c.colidx[p]];
+  }
+  return count == (size_t)c.rowptr[c.n];
+}
+
+}  // namespace
+
+extern "C" {
+
+// Outcome: 0 converged, 2 iteration limit, 3 damping below 1e-13, 4 pivot
+// failure, 5 stamp outside the pattern.  v: element voltages in/out; x: the
+// last linear solution (caller order); iterations and the last diff out.
+int oracle_newton(void* sym, int n, const int* rowptr, const int* colidx, const double* a_lin,
+                  const double* b_lin, int n_elems, const int* hi, const int* lo, double i0,
+                  double a, double rs, double rsh, const double* iph, double* v,
+                  const double* gmin, int n_stages, double tol, int max_iterations, double* x,
+                  int* iterations, double* last_diff) {
+  const Circuit c{n, n_elems, rowptr, colidx, hi, lo, a_lin, b_lin, {i0, a, rs, rsh}};
+  const int* csc_row = nullptr;
+  long long nnz_lu = 0;
+  oracle_get(sym, "csc_row", &csc_row, &nnz_lu);
+  std::vector<double> lu(nnz_lu), a_vals, b, sol(n, 0.0);
+  std::vector<double> movement(n_elems), cand(n_elems), newv(n_elems);
+  int it = 0;
+  long double diff = 0;
+  for (int stage = 0; stage < n_stages; stage++) {
+    diff = 1e10L;
+    for (;;) {
+      if (diff < (long double)tol) break;
+      if (++it > max_iterations) {
+        *iterations = it - 1;
+        *last_diff = (double)diff;
+        return 2;
+      }
+      if (!assemble(c, iph, v, gmin[stage], a_vals, b, nullptr)) return 5;
+      if (oracle_scatter_refactor_solve(sym, a_vals.data(), lu.data(), b.data(), 1)) {
+        *iterations = it;
+        return 4;
+      }
+      sol = b;
+      for (int k = 0; k < n_elems; k++) {
+        newv[k] = (hi[k] >= 0 ? sol[hi[k]] : 0.0) - (lo[k] >= 0 ? sol[lo[k]] : 0.0);
+        movement[k] = 1.0;
+      }
+      for (;;) {
+        for (int k = 0; k < n_elems; k++)
+          cand[k] = v[k] * (1.0 - movement[k]) + newv[k] * movement[k];
+        for (int k = 0; k < n_elems; k++)
+          if (movement[k] < 1e-13) {
+            *iterations = it;
+            for (int i = 0; i < n; i++) x[i] = sol[i];
+            return 3;
+          }
+        bool reduce = false;
+        for (int k = 0; k < n_elems; k++) {
+          const bool ok = !std::isnan(v[k]) && !std::isnan(cand[k]) &&
+                          !(std::fabs(v[k] - cand[k]) > 1.0);
+          if (ok) continue;
+          movement[k] /= 2.0;
+          reduce = true;
+        }
+        if (!reduce) break;
+      }
+      diff = 0;
+      for (int k = 0; k < n_elems; k++) {
+        diff += std::fabs(cand[k] - v[k]);
+        v[k] = cand[k];
+      }
+    }
+  }
+  for (int i = 0; i < n; i++) x[i] = sol[i];
+  *iterations = it;
+  *last_diff = (double)diff;
+  return 0;
+}
+
+// Adjoint check: J at the iterate v without convergence conductance,
+// J^T lambda = dpdx through the oracle's factors and permutations, then
+// dP/dIph[k] = dI/dIph * (lambda[hi] - lambda[lo]).  Returns 0, 4 (pivot) or 5.
+int oracle_adjoint(void* sym, int n, const int* rowptr, const int* colidx, const double* a_lin,
+                   const double* b_lin, int n_elems, const int* hi, const int* lo, double i0,
+                   double a, double rs, double rsh, const double* iph, const double* v,
+                   const double* dpdx, double* dpdiph) {
+  const Circuit c{n, n_elems, rowptr, colidx, hi, lo, a_lin, b_lin, {i0, a, rs, rsh}};
+  const int *csc_row = nullptr, *perm_amd = nullptr, *perm_rows = nullptr;
+  long long nnz_lu = 0, len = 0;
+  oracle_get(sym, "csc_row", &csc_row, &nnz_lu);
+  oracle_get(sym, "perm_amd", &perm_amd, &len);
+  oracle_get(sym, "perm_rows", &perm_rows, &len);
+  std::vector<double> lu(nnz_lu), a_vals, b, dphi(n_elems);
+  if (!assemble(c, iph, v, -1.0, a_vals, b, &dphi)) return 5;
+  oracle_scatter(sym, a_vals.data(), lu.data());
+  int bad = -1;
+  if (oracle_refactor_sequential(sym, lu.data(), &bad)) return 4;
+  // J x = b is M y = R b, x = C y (x[perm_amd[i]] = y[i]); so J^T l = g is
+  // M^T z = C^T g with l = R^T z.
+  std::vector<int> perm_amd_rev(n);
+  for (int i = 0; i < n; i++) perm_amd_rev[perm_amd[i]] = i;
+  std::vector<double> w(n), t(n), lam(n);
+  for (int i = 0; i < n; i++) w[i] = dpdx[perm_amd[i]];
+  oracle_solve_transposed(sym, lu.data(), w.data());
+  for (int i = 0; i < n; i++) t[i] = w[perm_rows[i]];
+  for (int i = 0; i < n; i++) lam[i] = t[perm_amd_rev[i]];
+  for (int k = 0; k < n_elems; k++) {
+    const double lh = hi[k] >= 0 ? lam[hi[k]] : 0.0;
+    const double ll = lo[k] >= 0 ? lam[lo[k]] : 0.0;
+    dpdiph[k] = dphi[k] * (lh - ll);
+  }
+  return 0;
+}
+
+}  // extern "C"

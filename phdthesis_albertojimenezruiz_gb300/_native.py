@@ -1,4 +1,5 @@
-"""ctypes binding of libpvglu.so (include/pvglu.h, include/pvglu_plant.h).
+"""ctypes binding of libpvglu.so (include/pvglu.h, include/pvglu_plant.h,
+include/pvglu_newton.h).
 
 Loading fails loudly when the native library is missing: there is no Python
 or CPU fallback for any hot-path operation.
@@ -18,6 +19,7 @@ ERR_NAMES = {
 FP64, FP32 = 0, 1
 SOLVE_TRANSPOSE, SOLVE_ORIGINAL = 1, 2
 SCHED_LEVELS, SCHED_PERSISTENT, SCHED_THREAD_CHAIN = 0, 1, 2
+NEWTON_CONVERGED, NEWTON_RUNNING, NEWTON_MAX_ITERATIONS, NEWTON_DAMPING = 0, 1, 2, 3
 
 
 class PvgluError(RuntimeError):
@@ -43,6 +45,14 @@ class PlantInfo(C.Structure):
         ("voc_panel", C.c_double), ("v_mppt", C.c_double), ("extent_x", C.c_double),
         ("extent_y", C.c_double), ("panel_i0", C.c_double), ("panel_a", C.c_double),
         ("panel_rs", C.c_double), ("panel_rsh", C.c_double), ("iph_stc", C.c_double),
+    ]
+
+
+class Circuit(C.Structure):
+    _fields_ = [
+        ("n_elems", C.c_int), ("elem_hi", C.c_void_p), ("elem_lo", C.c_void_p),
+        ("a_lin", C.c_void_p), ("b_lin", C.c_void_p), ("i0", C.c_double), ("a", C.c_double),
+        ("rs", C.c_double), ("rsh", C.c_double),
     ]
 
 
@@ -76,6 +86,20 @@ _SIGS = {
     "pvglu_selftest_barrier_timeout": ([_I, C.c_longlong, _IP, _IP], _I),
     "pvglu_refine_system_host": ([_P, _P, _P, _P, C.c_double, _I, _P, _P], _I),
     "pvglu_solve_noalloc": ([_P, _P, _I, _P], _I),
+    "pvglu_numeric_set_stamps": ([_P, _I, _P, _P, _P, _P], _I),
+    "pvglu_scatter_stamps": ([_P, _P, _P, _P], _I),
+    "pvglu_refine": ([_P, _P, _P, _P, _P, _P, _I, C.c_double, _I, _P, _P], _I),
+    "pvglu_newton_create": ([_P, C.POINTER(Circuit), C.POINTER(_P)], _I),
+    "pvglu_newton_destroy": ([_P], _I),
+    "pvglu_newton_set_iph": ([_P, _P, _P], _I),
+    "pvglu_newton_set_voltages": ([_P, _P, _P], _I),
+    "pvglu_newton_set_refinement": ([_P, C.c_double, _I], _I),
+    "pvglu_newton_run": ([_P, _P, _I, C.c_double, _I, _I, _P], _I),
+    "pvglu_newton_results": ([_P, _P, _P, _P], _I),
+    "pvglu_newton_voltages": ([_P], _P),
+    "pvglu_newton_solution": ([_P, _P, _P], _I),
+    "pvglu_newton_last_run": ([_P, _IP, _IP], _I),
+    "pvglu_newton_adjoint": ([_P, _P, _P, _P], _I),
     "pvglu_plant_create": ([_I, _I, _I, C.POINTER(_P)], _I),
     "pvglu_plant_destroy": ([_P], _I),
     "pvglu_plant_get_info": ([_P, C.POINTER(PlantInfo)], _I),

@@ -20,12 +20,15 @@ BUILD = ROOT / "_build"
 LIB = PKG / "libpvglu.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CXXFLAGS = ["-std=c++17", "-O2", "-fPIC", "-Wall", "-Wextra", "-Wno-unused-parameter"]
+# Host code contracts no a*b+c into FMA, so x86-64 and aarch64 builds round alike.
+CXXFLAGS = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-Wall", "-Wextra",
+            "-Wno-unused-parameter"]
 NVCCFLAGS = ["-std=c++17", "-O3", "-lineinfo", "--expt-relaxed-constexpr",
-             "-Xcompiler", "-fPIC", "-Xptxas", "-warn-spills"] + ARCH
+             "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+             "-Xptxas", "-warn-spills"] + ARCH
 
 HOST_SOURCES = ["symbolic.cpp", "programs.cpp", "plant.cpp", "plant_capi.cpp"]
-CUDA_SOURCES = ["capi.cu"]
+CUDA_SOURCES = ["capi.cu", "newton.cu"]
 
 
 def _nvcc() -> str:

@@ -170,6 +170,98 @@ int solve_any(pvglu_numeric* h, T* x, int flags, cudaStream_t st) {
 
 }  // namespace
 
+namespace pvglu {
+
+int run_scatter(pvglu_numeric* h, const AValues& A, const int* ndone, cudaStream_t st) {
+  const int blocks = rows_grid(h->nnz, h->ld, 256);
+  if (h->precision == PVGLU_FP64)
+    k_scatter<double><<<blocks, 256, 0, st>>>(h->d.slot_src, h->nnz, h->ld, h->S, A,
+                                              (double*)h->values, ndone);
+  else
+    k_scatter<float><<<blocks, 256, 0, st>>>(h->d.slot_src, h->nnz, h->ld, h->S, A,
+                                             (float*)h->values, ndone);
+  PVGLU_CUDA(cudaGetLastError());
+  return PVGLU_OK;
+}
+
+int run_refactor(pvglu_numeric* h, cudaStream_t st) {
+  if (h->schedule == PVGLU_SCHED_THREAD_CHAIN)
+    return h->precision == PVGLU_FP64 ? refactor_levels<double>(h, st)
+                                      : refactor_levels<float>(h, st);
+  return h->precision == PVGLU_FP64
+             ? run_phases<double>(h, PHASE_REFACTOR, (double*)nullptr, st)
+             : run_phases<float>(h, PHASE_REFACTOR, (float*)nullptr, st);
+}
+
+int run_solve_perm(pvglu_numeric* h, void* x, bool transpose, SkipDone skip, cudaStream_t st) {
+  return h->precision == PVGLU_FP64 ? solve_permuted<double>(h, (double*)x, transpose, st, skip)
+                                    : solve_permuted<float>(h, (float*)x, transpose, st, skip);
+}
+
+int run_refactor_solve_perm(pvglu_numeric* h, void* x, bool transpose, SkipDone skip,
+                            cudaStream_t st) {
+  if (h->schedule != PVGLU_SCHED_PERSISTENT) {
+    const int rc = run_refactor(h, st);
+    return rc ? rc : run_solve_perm(h, x, transpose, skip, st);
+  }
+  const int phases = PHASE_REFACTOR | (transpose ? PHASE_SOLVE_T : PHASE_SOLVE);
+  return h->precision == PVGLU_FP64 ? run_phases<double>(h, phases, (double*)x, st, skip)
+                                    : run_phases<float>(h, phases, (float*)x, st, skip);
+}
+
+// Mixed-precision refinement on factors already in the handle: x0 = 0, then
+// per sweep dx = M^-1 r (FP32), x += dx (FP64), r = b - A x (FP64), until
+// max|dx| <= tol * max|x| per scenario or max_sweeps.  Converged scenarios
+// drop out of every later kernel (done flags; the whole launch once all are).
+int run_refine(pvglu_numeric* h, const AValues& A, const double* b, double* x, bool transpose,
+               double tol, int max_sweeps, int* sweeps_out, cudaStream_t st,
+               const int* init_done) {
+  if (h->precision != PVGLU_FP32) return fail(PVGLU_ERR_BAD_ARG, "needs an FP32 handle");
+  const int64_t nv = (int64_t)h->n * h->ld;
+  float* w = static_cast<float*>(h->work);
+  int* ndone = h->ir_done + h->ld;
+  if (init_done) {
+    PVGLU_CUDA(cudaMemsetAsync(ndone, 0, sizeof(int), st));
+    k_ir_init<<<rows_grid(h->n, h->ld, 256), 256, 0, st>>>(h->n, h->ld, h->S, init_done,
+                                                           h->ir_done, ndone, x);
+  } else {
+    PVGLU_CUDA(cudaMemsetAsync(x, 0, nv * sizeof(double), st));
+    PVGLU_CUDA(cudaMemsetAsync(h->ir_done, 0, (h->ld + 1) * sizeof(int), st));
+  }
+  PVGLU_CUDA(cudaMemsetAsync(h->ir_max_dx, 0, h->ld * sizeof(unsigned long long), st));
+  PVGLU_CUDA(cudaMemsetAsync(h->ir_max_x, 0, h->ld * sizeof(unsigned long long), st));
+  if (sweeps_out) PVGLU_CUDA(cudaMemsetAsync(sweeps_out, 0, h->ld * sizeof(int), st));
+  const SkipDone skip{h->ir_done, ndone};
+  // J x = b:   w = b[row_orig], M y = w, x[col_orig] = y, residual rows by A.
+  // J^T x = b: w = b[col_orig], M^T z = w, x[row_orig] = z, rows by A^T.
+  const int* in_perm = transpose ? h->d.col_orig : h->d.row_orig;
+  const int* out_perm = transpose ? h->d.row_orig : h->d.col_orig;
+  const int* r_ptr = transpose ? h->at_ptr : h->d.a_rowptr;
+  const int* r_idx = transpose ? h->at_row : h->d.a_colidx;
+  const int* r_ent = transpose ? h->at_entry : nullptr;
+  const int* r_pos = transpose ? h->col_pos : h->row_pos;
+  // x = 0: the first residual is b itself.
+  permute<double, float>(h, in_perm, b, w, true, st);
+  const dim3 blk(32, 8);
+  const dim3 grd((unsigned)std::min(1024, (h->n + 7) / 8), (unsigned)(h->ld + 31) / 32);
+  for (int sweep = 1; sweep <= max_sweeps; sweep++) {
+    int rc = solve_permuted<float>(h, w, transpose, st, skip);  // dx of this sweep
+    if (rc) return rc;
+    k_ir_update<<<grd, blk, 0, st>>>(out_perm, h->n, h->ld, h->S, w, x, h->ir_done,
+                                     h->ir_max_dx, h->ir_max_x);
+    k_ir_check<<<(h->S + 127) / 128, 128, 0, st>>>(h->S, sweep, max_sweeps, tol, h->ir_done,
+                                                   ndone, sweeps_out, h->ir_max_dx,
+                                                   h->ir_max_x);
+    if (sweep < max_sweeps)  // residual of the scenarios still refining
+      k_residual<<<rows_grid(h->n, h->ld, 256), 256, 0, st>>>(
+          r_ptr, r_idx, r_ent, h->n, h->ld, h->S, A, b, x, h->ir_done, w, r_pos);
+  }
+  PVGLU_CUDA(cudaGetLastError());
+  return PVGLU_OK;
+}
+
+}  // namespace pvglu
+
 extern "C" {
 
 const char* pvglu_last_error(void) { return g_err.c_str(); }
@@ -314,6 +406,26 @@ int pvglu_numeric_create(const pvglu_symbolic* sym, int n_scenarios, int precisi
   rc |= h->alloc((size_t)h->n * h->ld, &h->b64);
   rc |= h->alloc((size_t)h->n * h->ld, &h->x64);
   {
+    // A^T by rows: counting sort of A's entries by column.
+    std::vector<int> at_ptr(s.n + 1, 0), at_row(s.nnz_a), at_entry(s.nnz_a);
+    for (int64_t p = 0; p < s.nnz_a; p++) at_ptr[s.a_colidx[p] + 1]++;
+    for (int j = 0; j < s.n; j++) at_ptr[j + 1] += at_ptr[j];
+    std::vector<int> fillp(at_ptr.begin(), at_ptr.end() - 1);
+    for (int i = 0; i < s.n; i++)
+      for (int p = s.a_rowptr[i]; p < s.a_rowptr[i + 1]; p++) {
+        const int q = fillp[s.a_colidx[p]]++;
+        at_row[q] = i;
+        at_entry[q] = p;
+      }
+    const int *a0 = nullptr, *a1 = nullptr, *a2 = nullptr;
+    rc |= h->put(at_ptr, &a0);
+    rc |= h->put(at_row, &a1);
+    rc |= h->put(at_entry, &a2);
+    h->at_ptr = const_cast<int*>(a0);
+    h->at_row = const_cast<int*>(a1);
+    h->at_entry = const_cast<int*>(a2);
+  }
+  {
     std::vector<int> col_pos(s.n);
     for (int c = 0; c < s.n; c++) col_pos[s.col_orig[c]] = c;
     const int* cp = nullptr;
@@ -410,42 +522,84 @@ int pvglu_numeric_set_pivot_tol(pvglu_numeric* h, double tol) {
 
 int pvglu_scatter(pvglu_numeric* h, const double* a_values, void* stream) {
   if (!h || !a_values) return fail(PVGLU_ERR_BAD_ARG, "NULL argument");
-  cudaStream_t st = as_stream(stream);
-  const int64_t total = (int64_t)h->nnz * h->ld;
-  (void)total;
-  const int blocks = pvglu::rows_grid(h->nnz, h->ld, 256);
-  if (h->precision == PVGLU_FP64)
-    pvglu::k_scatter<double><<<blocks, 256, 0, st>>>(h->d.slot_src, h->nnz, h->ld, h->S,
-                                                     a_values, (double*)h->values);
-  else
-    pvglu::k_scatter<float><<<blocks, 256, 0, st>>>(h->d.slot_src, h->nnz, h->ld, h->S,
-                                                    a_values, (float*)h->values);
-  PVGLU_CUDA(cudaGetLastError());
+  const pvglu::AValues A{a_values, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  return pvglu::run_scatter(h, A, nullptr, as_stream(stream));
+}
+
+int pvglu_numeric_set_stamps(pvglu_numeric* h, int n_elems, const double* base,
+                             const int* entry_ptr, const int* entry_elem,
+                             const int* entry_sign) {
+  if (!h || n_elems < 0 || !base || !entry_ptr || (entry_ptr[h->nnz_a] > 0 && (!entry_elem || !entry_sign)))
+    return fail(PVGLU_ERR_BAD_ARG, "bad set_stamps arguments");
+  const int nnz_a = h->nnz_a;
+  if (entry_ptr[0] != 0) return fail(PVGLU_ERR_BAD_ARG, "entry_ptr[0] must be 0");
+  for (int e = 0; e < nnz_a; e++)
+    if (entry_ptr[e + 1] < entry_ptr[e]) return fail(PVGLU_ERR_BAD_ARG, "entry_ptr not monotone");
+  const int nc = entry_ptr[nnz_a];
+  for (int c = 0; c < nc; c++) {
+    if (entry_elem[c] < 0 || entry_elem[c] >= n_elems)
+      return fail(PVGLU_ERR_BAD_ARG, "stamp element out of range");
+    if (entry_sign[c] != 1 && entry_sign[c] != -1)
+      return fail(PVGLU_ERR_BAD_ARG, "stamp sign must be +1 or -1");
+  }
+  for (void* p : h->stamp_allocs) cudaFree(p);
+  h->stamp_allocs.clear();
+  h->n_elems = 0;
+  std::vector<double> vb(base, base + nnz_a);
+  std::vector<int> vp(entry_ptr, entry_ptr + nnz_a + 1), ve(entry_elem, entry_elem + nc),
+      vs(entry_sign, entry_sign + nc);
+  int rc = 0;
+  double* db = nullptr;
+  int *dp = nullptr, *de = nullptr, *ds = nullptr;
+  rc |= upload(vb, &db);
+  h->stamp_allocs.push_back(db);
+  rc |= upload(vp, &dp);
+  h->stamp_allocs.push_back(dp);
+  rc |= upload(ve, &de);
+  h->stamp_allocs.push_back(de);
+  rc |= upload(vs, &ds);
+  h->stamp_allocs.push_back(ds);
+  if (rc) return fail(PVGLU_ERR_NO_MEMORY, "stamp upload failed: " + g_err);
+  h->st_base = db;
+  h->st_ptr = dp;
+  h->st_elem = de;
+  h->st_sign = ds;
+  h->n_elems = n_elems;
   return PVGLU_OK;
+}
+
+int pvglu_scatter_stamps(pvglu_numeric* h, const double* g, const double* gmin, void* stream) {
+  if (!h || !g) return fail(PVGLU_ERR_BAD_ARG, "NULL argument");
+  if (!h->st_ptr) return fail(PVGLU_ERR_BAD_ARG, "no stamps set on this handle");
+  return pvglu::run_scatter(h, h->stamps(g, gmin), nullptr, as_stream(stream));
+}
+
+int pvglu_refine(pvglu_numeric* h, const double* a_values, const double* g, const double* gmin,
+                 const double* b, double* x, int flags, double tol, int max_sweeps,
+                 int* sweeps_out, void* stream) {
+  if (!h || !b || !x || max_sweeps <= 0 || !(tol > 0.0) || (!a_values == !g))
+    return fail(PVGLU_ERR_BAD_ARG, "bad refine arguments");
+  if (g && !h->st_ptr) return fail(PVGLU_ERR_BAD_ARG, "no stamps set on this handle");
+  const pvglu::AValues A = a_values ? pvglu::AValues{a_values, nullptr, nullptr, nullptr,
+                                                     nullptr, nullptr, nullptr}
+                                    : h->stamps(g, gmin);
+  return pvglu::run_refine(h, A, b, x, (flags & PVGLU_SOLVE_TRANSPOSE) != 0, tol, max_sweeps,
+                           sweeps_out, as_stream(stream));
 }
 
 int pvglu_refactor(pvglu_numeric* h, void* stream) {
   if (!h) return fail(PVGLU_ERR_BAD_ARG, "NULL handle");
-  cudaStream_t st = as_stream(stream);
-  if (h->schedule == PVGLU_SCHED_THREAD_CHAIN)
-    return h->precision == PVGLU_FP64 ? refactor_levels<double>(h, st)
-                                      : refactor_levels<float>(h, st);
-  return h->precision == PVGLU_FP64
-             ? run_phases<double>(h, pvglu::PHASE_REFACTOR, (double*)nullptr, st)
-             : run_phases<float>(h, pvglu::PHASE_REFACTOR, (float*)nullptr, st);
+  return pvglu::run_refactor(h, as_stream(stream));
 }
 
 int pvglu_refactor_solve(pvglu_numeric* h, void* x, int flags, void* stream) {
   if (!h || !x) return fail(PVGLU_ERR_BAD_ARG, "NULL argument");
-  if ((flags & PVGLU_SOLVE_ORIGINAL) || h->schedule != PVGLU_SCHED_PERSISTENT) {
+  if (flags & PVGLU_SOLVE_ORIGINAL) {
     int rc = pvglu_refactor(h, stream);
     return rc ? rc : pvglu_solve(h, x, flags, stream);
   }
-  const int phases = pvglu::PHASE_REFACTOR |
-                     ((flags & PVGLU_SOLVE_TRANSPOSE) ? pvglu::PHASE_SOLVE_T : pvglu::PHASE_SOLVE);
-  cudaStream_t st = as_stream(stream);
-  return h->precision == PVGLU_FP64 ? run_phases<double>(h, phases, (double*)x, st)
-                                    : run_phases<float>(h, phases, (float*)x, st);
+  return pvglu::run_refactor_solve_perm(h, x, (flags & PVGLU_SOLVE_TRANSPOSE) != 0,
+                                        pvglu::SkipDone{nullptr, nullptr}, as_stream(stream));
 }
 
 int pvglu_solve(pvglu_numeric* h, void* x, int flags, void* stream) {
@@ -628,38 +782,9 @@ int pvglu_selftest_barrier_timeout(int blocks, long long max_spins, int* status_
 int pvglu_solve_refined(pvglu_numeric* h, const double* a_values, const double* b,
                         double* x, double tol, int max_sweeps, int* sweeps_out,
                         void* stream) {
-  if (!h || !a_values || !b || !x || max_sweeps <= 0 || !(tol > 0.0))
-    return fail(PVGLU_ERR_BAD_ARG, "bad solve_refined arguments");
-  if (h->precision != PVGLU_FP32) return fail(PVGLU_ERR_BAD_ARG, "needs an FP32 handle");
-  cudaStream_t st = as_stream(stream);
-  const int64_t nv = (int64_t)h->n * h->ld;
-  float* w = static_cast<float*>(h->work);
-  PVGLU_CUDA(cudaMemsetAsync(x, 0, nv * sizeof(double), st));
-  int* ndone = h->ir_done + h->ld;
-  PVGLU_CUDA(cudaMemsetAsync(h->ir_done, 0, (h->ld + 1) * sizeof(int), st));
-  PVGLU_CUDA(cudaMemsetAsync(h->ir_max_dx, 0, h->ld * sizeof(unsigned long long), st));
-  PVGLU_CUDA(cudaMemsetAsync(h->ir_max_x, 0, h->ld * sizeof(unsigned long long), st));
-  if (sweeps_out) PVGLU_CUDA(cudaMemsetAsync(sweeps_out, 0, h->ld * sizeof(int), st));
-  const pvglu::SkipDone skip{h->ir_done, ndone};
-  // x = 0: the first residual is b itself.
-  permute<double, float>(h, h->d.row_orig, b, w, true, st);
-  const dim3 blk(32, 8);
-  const dim3 grd((unsigned)std::min(1024, (h->n + 7) / 8), (unsigned)(h->ld + 31) / 32);
-  for (int sweep = 1; sweep <= max_sweeps; sweep++) {
-    int rc = solve_permuted<float>(h, w, false, st, skip);  // dx of this sweep
-    if (rc) return rc;
-    pvglu::k_ir_update<<<grd, blk, 0, st>>>(h->d.col_orig, h->n, h->ld, h->S, w, x,
-                                            h->ir_done, h->ir_max_dx, h->ir_max_x);
-    pvglu::k_ir_check<<<(h->S + 127) / 128, 128, 0, st>>>(h->S, sweep, max_sweeps, tol,
-                                                          h->ir_done, ndone, sweeps_out,
-                                                          h->ir_max_dx, h->ir_max_x);
-    if (sweep < max_sweeps)  // residual of the scenarios still refining
-      pvglu::k_residual<<<pvglu::rows_grid(h->n, h->ld, 256), 256, 0, st>>>(
-          h->d.a_rowptr, h->d.a_colidx, h->n, h->ld, h->S, a_values, b, x, h->ir_done, w,
-          h->row_pos);
-  }
-  PVGLU_CUDA(cudaGetLastError());
-  return PVGLU_OK;
+  if (!a_values) return fail(PVGLU_ERR_BAD_ARG, "bad solve_refined arguments");
+  return pvglu_refine(h, a_values, nullptr, nullptr, b, x, 0, tol, max_sweeps, sweeps_out,
+                      stream);
 }
 
 }  // extern "C"

@@ -72,15 +72,24 @@ struct pvglu_numeric {
   int prog_grid = 0;               // co-resident blocks of k_prog_persistent
   int64_t prog_ops = 0, prog_loads = 0, prog_direct = 0;
   unsigned int* barrier = nullptr;  // [2]: count, generation
-  // Structured Jacobian (pvglu_numeric_set_stamps): entry e of A is
-  // st_base[e] + sum over c in [st_ptr[e], st_ptr[e+1]) of st_sign[c] * g[st_elem[c]].
+  // A^T by rows (caller order): entries at_ptr[j]..at_ptr[j+1] of column j
+  // of A, in row order, with their row and A-entry index.
+  int* at_ptr = nullptr;
+  int* at_row = nullptr;
+  int* at_entry = nullptr;
+  // Structured Jacobian (pvglu_numeric_set_stamps); n_elems = 0 until set.
   int n_elems = 0;
-  const double* st_base = nullptr;
-  const int* st_ptr = nullptr;
-  const int* st_elem = nullptr;
-  const int* st_sign = nullptr;
+  std::vector<void*> stamp_allocs;
+  double* st_base = nullptr;
+  int* st_ptr = nullptr;
+  int* st_elem = nullptr;
+  int* st_sign = nullptr;
+  pvglu::AValues stamps(const double* g, const double* gmin) const {
+    return pvglu::AValues{nullptr, st_base, st_ptr, st_elem, st_sign, g, gmin};
+  }
   ~pvglu_numeric() {
     for (void* p : allocs) cudaFree(p);
+    for (void* p : stamp_allocs) cudaFree(p);
   }
   template <typename T>
   int put(const std::vector<T>& h, const T** out) {
@@ -99,3 +108,20 @@ struct pvglu_numeric {
   }
 };
 
+
+// Launch sequences of capi.cu shared with newton.cu.  All are asynchronous on
+// `st`; vectors are [n x ld] in pivot order ("perm") or the caller's order.
+namespace pvglu {
+int run_scatter(pvglu_numeric* h, const AValues& A, const int* ndone, cudaStream_t st);
+int run_refactor(pvglu_numeric* h, cudaStream_t st);
+// Solve in pivot order in place (x: T = double or float per the handle).
+int run_solve_perm(pvglu_numeric* h, void* x, bool transpose, SkipDone skip, cudaStream_t st);
+// Refactor + pivot-order solve; one persistent launch where the schedule has it.
+int run_refactor_solve_perm(pvglu_numeric* h, void* x, bool transpose, SkipDone skip,
+                            cudaStream_t st);
+// FP32 factors + FP64 refinement of J x = b (J^T x = b): x, b in caller order.
+// init_done (or NULL): scenarios flagged there are left alone, x included.
+int run_refine(pvglu_numeric* h, const AValues& A, const double* b, double* x, bool transpose,
+               double tol, int max_sweeps, int* sweeps_out, cudaStream_t st,
+               const int* init_done = nullptr);
+}  // namespace pvglu

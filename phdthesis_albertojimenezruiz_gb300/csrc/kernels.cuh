@@ -100,71 +100,51 @@ inline int rows_grid(int64_t nrows, int ld, int block) {
   return (int)(b < 1 ? 1 : (b > 65536 ? 65536 : b));
 }
 
-// (a) scatter: LU(q, s) = A(slot_src[q], s), zero at fill slots.
-template <typename T>
-__global__ void k_scatter(const int* __restrict__ slot_src, int nnz, int ld, int S,
-                          const double* __restrict__ a, T* __restrict__ v) {
-  for_rows(nnz, ld, [&](int q, int s) {
-    const int src = slot_src[q];
-    T val = T(0);
-    if (src >= 0 && s < S) val = (T)a[(int64_t)src * ld + s];
-    v[(int64_t)q * ld + s] = val;
-  });
-}
-
-// Structured Jacobian: value of A entry e for scenario s,
-//   base[e] + sum_c sign[c] * g[elem[c]],
-// the companion stamps of every nonlinear element on entry e
-// (002b_sistema_electrico_base_matriz.cpp:183-197) over the linear part.
-struct Stamps {
-  const double* base;
-  const int* ptr;
+// Values of A's entries for one batch, in the caller's CSR order: either an
+// explicit [nnz_a x ld] array, or a structured Jacobian whose entry e is
+//   base[e] + sum over c in [ptr[e], ptr[e+1]) of sign[c] * (g[elem[c]] (+ gmin)),
+// the companion stamps of the nonlinear elements on entry e over the linear
+// part, added element by element in the order of
+// 002b_sistema_electrico_base_matriz.cpp:183-202 (conductance G, then the
+// convergence conductance gmin when it is positive).
+struct AValues {
+  const double* a;      // explicit values, or NULL for stamps
+  const double* base;   // [nnz_a]
+  const int* ptr;       // [nnz_a + 1]
   const int* elem;
-  const int* sign;
+  const int* sign;      // +1 / -1
+  const double* g;      // [n_elems x ld] element conductances
+  const double* gmin;   // [ld] per-scenario convergence conductance, or NULL
+  __device__ __forceinline__ double operator()(int e, int ld, int s) const {
+    if (a) return a[(int64_t)e * ld + s];
+    double val = base[e];
+    const double gm = gmin ? gmin[s] : 0.0;
+    for (int c = ptr[e]; c < ptr[e + 1]; c++) {
+      const double sg = (double)sign[c];
+      val += sg * g[(int64_t)elem[c] * ld + s];
+      if (gm > 0.0) val += sg * gm;
+    }
+    return val;
+  }
 };
 
-__device__ __forceinline__ double stamp_value(const Stamps& st, int e, const double* g, int ld,
-                                              int s) {
-  double val = st.base[e];
-  for (int c = st.ptr[e]; c < st.ptr[e + 1]; c++)
-    val += (double)st.sign[c] * g[(int64_t)st.elem[c] * ld + s];
-  return val;
-}
-
-// (a) scatter from stamps: LU(q, s) = A(slot_src[q], s) assembled on the fly.
+// (a) scatter: LU(q, s) = A(slot_src[q], s), zero at fill slots.  `ndone`
+// (or NULL): the launch does nothing once every scenario has converged.
 template <typename T>
-__global__ void k_scatter_stamps(const int* __restrict__ slot_src, int nnz, int ld, int S,
-                                 Stamps st, const double* __restrict__ g, T* __restrict__ v) {
+__global__ void k_scatter(const int* __restrict__ slot_src, int nnz, int ld, int S, AValues A,
+                          T* __restrict__ v, const int* __restrict__ ndone) {
+  if (ndone && __ldcg(ndone) >= S) return;
   for_rows(nnz, ld, [&](int q, int s) {
     const int src = slot_src[q];
     T val = T(0);
-    if (src >= 0 && s < S) val = (T)stamp_value(st, src, g, ld, s);
+    if (src >= 0 && s < S) val = (T)A(src, ld, s);
     v[(int64_t)q * ld + s] = val;
   });
 }
 
-// A's entry values from stamps (caller order), for callers that need them.
-__global__ void k_assemble_stamps(int nnz_a, int ld, int S, Stamps st,
-                                  const double* __restrict__ g, double* __restrict__ a) {
-  for_rows(nnz_a, ld, [&](int e, int s) {
-    a[(int64_t)e * ld + s] = s < S ? stamp_value(st, e, g, ld, s) : 0.0;
-  });
-}
-
-// FP64 residual r = b - A x with A from stamps (see k_residual).
-__global__ void k_residual_stamps(const int* __restrict__ a_rowptr,
-                                  const int* __restrict__ a_colidx, int n, int ld, int S,
-                                  Stamps st, const double* __restrict__ g,
-                                  const double* __restrict__ b, const double* __restrict__ x,
-                                  const int* __restrict__ done, float* __restrict__ r_perm,
-                                  const int* __restrict__ row_pos) {
-  for_rows(n, ld, [&](int i, int s) {
-    if (s >= S || done[s]) return;
-    double acc = b[(int64_t)i * ld + s];
-    for (int p = a_rowptr[i]; p < a_rowptr[i + 1]; p++)
-      acc -= stamp_value(st, p, g, ld, s) * x[(int64_t)a_colidx[p] * ld + s];
-    r_perm[(int64_t)row_pos[i] * ld + s] = (float)acc;
-  });
+// A's entry values (caller order) from any AValues source.
+static __global__ void k_assemble(int nnz_a, int ld, int S, AValues A, double* __restrict__ a) {
+  for_rows(nnz_a, ld, [&](int e, int s) { a[(int64_t)e * ld + s] = s < S ? A(e, ld, s) : 0.0; });
 }
 
 // ----------------------------------------------------------------------------
@@ -271,25 +251,29 @@ __global__ void k_permute(const int* __restrict__ perm, int n, int ld, int S,
 
 // ----------------------------------------------------------------------------
 // Iterative refinement pieces (FP64 residual, FP32 correction).
-// r = b - A x in the caller's order; skipped for converged scenarios.
-__global__ void k_residual(const int* __restrict__ a_rowptr, const int* __restrict__ a_colidx,
-                           int n, int ld, int S, const double* __restrict__ a,
+// r = b - A x (or b - A^T x) in the caller's order; skipped for converged
+// scenarios.  Rows of the product come from a CSR (ptr, idx) whose entry p
+// has A-value index ent[p] (NULL: p itself, A's own rows).  Row i of the
+// product is row pos[i] of the pivot-ordered system (row_pos for A,
+// col_pos for A^T).
+static __global__ void k_residual(const int* __restrict__ ptr, const int* __restrict__ idx,
+                           const int* __restrict__ ent, int n, int ld, int S, AValues A,
                            const double* __restrict__ b, const double* __restrict__ x,
                            const int* __restrict__ done, float* __restrict__ r_perm,
-                           const int* __restrict__ row_pos) {
+                           const int* __restrict__ pos) {
   for_rows(n, ld, [&](int i, int s) {
     if (s >= S || done[s]) return;
     double acc = b[(int64_t)i * ld + s];
-    for (int p = a_rowptr[i]; p < a_rowptr[i + 1]; p++)
-      acc -= a[(int64_t)p * ld + s] * x[(int64_t)a_colidx[p] * ld + s];
-    // Row i of J is row row_pos[i] of the pivot-ordered system.
-    r_perm[(int64_t)row_pos[i] * ld + s] = (float)acc;
+    for (int p = ptr[i]; p < ptr[i + 1]; p++)
+      acc -= A(ent ? ent[p] : p, ld, s) * x[(int64_t)idx[p] * ld + s];
+    r_perm[(int64_t)pos[i] * ld + s] = (float)acc;
   });
 }
 
-// x[col_orig[c]] += dx[c]; per-scenario max |dx| and max |x| (non-negative
-// doubles order like their bit patterns, so atomicMax on the bits works).
-__global__ void k_ir_update(const int* __restrict__ col_orig, int n, int ld, int S,
+// x[out_perm[c]] += dx[c] (out_perm = col_orig for A, row_orig for A^T);
+// per-scenario max |dx| and max |x| (non-negative doubles order like their
+// bit patterns, so atomicMax on the bits works).
+static __global__ void k_ir_update(const int* __restrict__ out_perm, int n, int ld, int S,
                             const float* __restrict__ dx, double* __restrict__ x,
                             const int* __restrict__ done,
                             unsigned long long* __restrict__ max_dx,
@@ -301,7 +285,7 @@ __global__ void k_ir_update(const int* __restrict__ col_orig, int n, int ld, int
   if (s < S && !done[s]) {
     for (int c = blockIdx.x * 8 + threadIdx.y; c < n; c += gridDim.x * 8) {
       const double d = (double)dx[(int64_t)c * ld + s];
-      double* xp = x + (int64_t)col_orig[c] * ld + s;
+      double* xp = x + (int64_t)out_perm[c] * ld + s;
       const double nx = *xp + d;
       *xp = nx;
       mdx = fmax(mdx, fabs(d));
@@ -321,8 +305,23 @@ __global__ void k_ir_update(const int* __restrict__ col_orig, int n, int ld, int
   }
 }
 
+// Refinement start for a subset: done[s] = src[s] (s < S), ndone counts them,
+// x = 0 for the scenarios that will refine.  *ndone must be 0 on entry.
+static __global__ void k_ir_init(int n, int ld, int S, const int* __restrict__ src,
+                          int* __restrict__ done, int* __restrict__ ndone,
+                          double* __restrict__ x) {
+  for_rows(n, ld, [&](int i, int s) {
+    const int d = s < S ? src[s] : 1;
+    if (i == 0) {
+      done[s] = d;
+      if (d && s < S) atomicAdd(ndone, 1);
+    }
+    if (!d) x[(int64_t)i * ld + s] = 0.0;
+  });
+}
+
 // Convergence bookkeeping after sweep `sweep` (1-based).
-__global__ void k_ir_check(int S, int sweep, int last_sweep, double tol, int* done,
+static __global__ void k_ir_check(int S, int sweep, int last_sweep, double tol, int* done,
                            int* ndone, int* sweeps_out, unsigned long long* max_dx,
                            unsigned long long* max_x) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;

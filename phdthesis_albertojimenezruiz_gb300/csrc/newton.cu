@@ -1,0 +1,635 @@
+// Device Newton driver and adjoint (include/pvglu_newton.h) over the hot path
+// of capi.cu.  Every Newton iteration is a fixed sequence of launches with no
+// host decision inside, so it is captured once as a CUDA graph and replayed;
+// per-scenario progress (gmin stage, iteration count, outcome) lives on the
+// device.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "../../include/pvglu_newton.h"
+#include "handle.hpp"
+#include "panel_model.h"
+
+namespace pvglu {
+namespace {
+
+constexpr int kMaxStages = 16;
+
+struct NewtonParams {
+  double gmin[kMaxStages];
+  double tol;
+  int n_stages;
+  int max_iterations;
+};
+
+// Device view of the driver's state.
+struct NtDev {
+  int n, n_elems, ld, S;
+  const int* hi;          // [n_elems]
+  const int* lo;
+  const int* inc_ptr;     // [n+1] elements incident to each unknown
+  const int* inc_elem;
+  const int* inc_sign;    // +1: + terminal, -1: - terminal
+  const double* b_lin;    // [n]
+  pvglu_panel_params panel;
+  double* iph;            // [n_elems x ld] photocurrent
+  double* v;              // voltage iterate
+  double* g;              // companion conductance G
+  double* ieq;            // companion current Ieq (dI/dIph in the adjoint)
+  double* gmin_s;         // [ld] gmin of each scenario's current stage (0: none)
+  int* stage;             // [ld]
+  int* iters;             // [ld]
+  int* outcome;           // [ld] PVGLU_NEWTON_*
+  int* damp_fail;         // [ld]
+  int* done;              // [ld + 1]: flags, then the stopped count
+  double* diff;           // [ld]
+  double* partial;        // [n_chunks x ld] per-chunk sums of |dv|
+  const NewtonParams* prm;
+};
+
+constexpr int kUpdRows = 8;            // update block: 32 scenarios x 8 element rows
+constexpr int kUpdChunk = 1024;        // elements per partial sum
+
+__device__ __forceinline__ bool all_stopped(const NtDev& D) {
+  return __ldcg(D.done + D.ld) >= D.S;
+}
+
+// Companion model of every element (002b_sistema_electrico_base_matriz.cpp:
+// 183-197): f(V) = -I(V) is the current from the + to the - terminal,
+// G = f'(V), Ieq = f(V) - G*V.  Row 0 also publishes the scenario's gmin.
+__global__ void k_nt_companion(NtDev D) {
+  if (all_stopped(D)) return;
+  for_rows(D.n_elems, D.ld, [&](int k, int s) {
+    if (s >= D.S || D.done[s]) return;
+    if (k == 0) {
+      const double gm = D.prm->gmin[D.stage[s]];
+      D.gmin_s[s] = gm > 0.0 ? gm : 0.0;
+    }
+    const int64_t e = (int64_t)k * D.ld + s;
+    const double v = D.v[e];
+    double cur, didv;
+    pvglu_panel_iv(&D.panel, D.iph[e], v, &cur, &didv);
+    const double G = -didv;
+    D.g[e] = G;
+    D.ieq[e] = __dsub_rn(-cur, __dmul_rn(G, v));
+  });
+}
+
+// b = b_lin, then per incident element in element order the current-source
+// stamp of -Ieq (002b:100-110, :196): + terminal b -= Ieq, - terminal b += Ieq.
+// Written at pos[i] (pivot order) or i (pos NULL).
+__global__ void k_nt_rhs(NtDev D, double* __restrict__ out, const int* __restrict__ pos) {
+  if (all_stopped(D)) return;
+  for_rows(D.n, D.ld, [&](int i, int s) {
+    if (s >= D.S || D.done[s]) return;
+    double acc = D.b_lin[i];
+    for (int c = D.inc_ptr[i]; c < D.inc_ptr[i + 1]; c++) {
+      const double q = D.ieq[(int64_t)D.inc_elem[c] * D.ld + s];
+      acc = D.inc_sign[c] > 0 ? __dsub_rn(acc, q) : __dadd_rn(acc, q);
+    }
+    out[(int64_t)(pos ? pos[i] : i) * D.ld + s] = acc;
+  });
+}
+
+// Damped update of one element (011_calculate_new_iteration.cpp:37-90): the
+// step factor m starts at 1 and halves while the candidate moves the voltage
+// by more than 1 V or is NaN; below 1e-13 the element keeps its voltage and
+// the scenario is flagged.
+__device__ __forceinline__ double damped_step(double old, double nv, bool* bad) {
+  double m = 1.0;
+  for (;;) {
+    const double t = __dadd_rn(__dmul_rn(old, __dsub_rn(1.0, m)), __dmul_rn(nv, m));
+    if (m < 1e-13) {
+      *bad = true;
+      return old;
+    }
+    if (!isnan(old) && !isnan(t) && !(fabs(__dsub_rn(old, t)) > 1.0)) return t;
+    m *= 0.5;
+  }
+}
+
+// New voltage drops from the solution X (pivot order through xpos, or caller
+// order when xpos is NULL), damped update, per-chunk sums of |change| in a
+// fixed order (deterministic).  Block: 32 scenarios x 8 element rows; grid:
+// (chunks, ld / 32).  With one scenario the 256 threads split the elements.
+__global__ void __launch_bounds__(256) k_nt_update(NtDev D, const double* __restrict__ X,
+                                                   const int* __restrict__ xpos) {
+  if (all_stopped(D)) return;
+  __shared__ double red[kUpdRows][33];
+  const bool single = D.ld == 1;
+  const int s = single ? 0 : blockIdx.y * 32 + threadIdx.x;
+  const int kb = blockIdx.x * kUpdChunk;
+  const int ke = min(D.n_elems, kb + kUpdChunk);
+  double sum = 0.0;
+  bool bad = false;
+  if (s < D.S && !D.done[s]) {
+    const int k0 = single ? kb + threadIdx.y * 32 + threadIdx.x : kb + threadIdx.y;
+    const int dk = single ? 32 * kUpdRows : kUpdRows;
+    for (int k = k0; k < ke; k += dk) {
+      const int64_t e = (int64_t)k * D.ld + s;
+      const int h = D.hi[k], l = D.lo[k];
+      const double xh = h >= 0 ? X[(int64_t)(xpos ? xpos[h] : h) * D.ld + s] : 0.0;
+      const double xl = l >= 0 ? X[(int64_t)(xpos ? xpos[l] : l) * D.ld + s] : 0.0;
+      const double old = D.v[e];
+      const double t = damped_step(old, __dsub_rn(xh, xl), &bad);
+      D.v[e] = t;
+      sum = __dadd_rn(sum, fabs(__dsub_rn(t, old)));
+    }
+  }
+  if (bad) D.damp_fail[s] = 1;
+  if (single) {
+    // 256 partial sums of one scenario, added in thread order.
+    __shared__ double all[32 * kUpdRows];
+    all[threadIdx.y * 32 + threadIdx.x] = sum;
+    __syncthreads();
+    if (threadIdx.x == 0 && threadIdx.y == 0 && !D.done[0]) {
+      double t = 0.0;
+      for (int i = 0; i < 32 * kUpdRows; i++) t += all[i];
+      D.partial[blockIdx.x] = t;
+    }
+    return;
+  }
+  red[threadIdx.y][threadIdx.x] = sum;
+  __syncthreads();
+  if (threadIdx.y == 0 && s < D.S && !D.done[s]) {
+    double t = 0.0;
+    for (int r = 0; r < kUpdRows; r++) t += red[r][threadIdx.x];
+    D.partial[(int64_t)blockIdx.x * D.ld + s] = t;
+  }
+}
+
+// End of an iteration for every running scenario: diff, stage advance
+// (000_PVPP_simulator.cpp:172-176: a stage ends once diff < tol), outcome.
+__global__ void k_nt_check(NtDev D, int n_chunks) {
+  if (all_stopped(D)) return;
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= D.S || D.done[s]) return;
+  double diff = 0.0;
+  for (int c = 0; c < n_chunks; c++) diff += D.partial[(int64_t)c * D.ld + s];
+  D.diff[s] = diff;
+  const int it = ++D.iters[s];
+  int out = PVGLU_NEWTON_RUNNING;
+  if (D.damp_fail[s]) {
+    out = PVGLU_NEWTON_DAMPING;
+  } else if (diff < D.prm->tol) {
+    const int st = ++D.stage[s];
+    if (st >= D.prm->n_stages) out = PVGLU_NEWTON_CONVERGED;
+  }
+  if (out == PVGLU_NEWTON_RUNNING && it >= D.prm->max_iterations)
+    out = PVGLU_NEWTON_MAX_ITERATIONS;
+  D.outcome[s] = out;
+  if (out != PVGLU_NEWTON_RUNNING) {
+    D.done[s] = 1;
+    atomicAdd(D.done + D.ld, 1);
+  }
+}
+
+__global__ void k_nt_reset(NtDev D) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s == 0) D.done[D.ld] = 0;
+  if (s >= D.ld) return;
+  D.stage[s] = 0;
+  D.iters[s] = 0;
+  D.outcome[s] = s < D.S ? PVGLU_NEWTON_RUNNING : PVGLU_NEWTON_CONVERGED;
+  D.damp_fail[s] = 0;
+  D.done[s] = s < D.S ? 0 : 1;
+  D.diff[s] = 0.0;
+  D.gmin_s[s] = 0.0;
+}
+
+// Adjoint: companion conductance at the iterate without gmin, and
+// dI/dIph (kept in ieq) for the sensitivity.
+__global__ void k_nt_adjoint_companion(NtDev D) {
+  for_rows(D.n_elems, D.ld, [&](int k, int s) {
+    if (s >= D.S) return;
+    const int64_t e = (int64_t)k * D.ld + s;
+    double cur, didv, didiph;
+    pvglu_panel_iv3(&D.panel, D.iph[e], D.v[e], &cur, &didv, &didiph);
+    D.g[e] = -didv;
+    D.ieq[e] = didiph;
+  });
+}
+
+// dP/dIph[k] = dI/dIph * (lambda[hi] - lambda[lo]); lambda in pivot order
+// through lpos, or caller order when lpos is NULL.
+__global__ void k_nt_adjoint_reduce(NtDev D, const double* __restrict__ lam,
+                                    const int* __restrict__ lpos, double* __restrict__ out) {
+  for_rows(D.n_elems, D.ld, [&](int k, int s) {
+    const int64_t e = (int64_t)k * D.ld + s;
+    if (s >= D.S) {
+      out[e] = 0.0;
+      return;
+    }
+    const int h = D.hi[k], l = D.lo[k];
+    const double lh = h >= 0 ? lam[(int64_t)(lpos ? lpos[h] : h) * D.ld + s] : 0.0;
+    const double ll = l >= 0 ? lam[(int64_t)(lpos ? lpos[l] : l) * D.ld + s] : 0.0;
+    out[e] = D.ieq[e] * (lh - ll);
+  });
+}
+
+}  // namespace
+}  // namespace pvglu
+
+struct pvglu_newton {
+  pvglu_numeric* num = nullptr;
+  int n_elems = 0, n_chunks = 1;
+  std::vector<void*> allocs;
+  pvglu::NtDev D{};
+  pvglu::NewtonParams* prm_dev = nullptr;
+  pvglu::NewtonParams prm_host{};
+  double* w64 = nullptr;        // FP64 handles: right-hand side / solution, pivot order
+  double* rhs64 = nullptr;      // FP32 handles: right-hand side, caller order
+  double* x64 = nullptr;        // FP32 handles: refined solution, caller order
+  double* lam = nullptr;        // adjoint vector
+  int* pinned_ndone = nullptr;  // host-pinned copy of the stopped count
+  double ir_tol = 1e-12;
+  int ir_sweeps = 8;
+  // Captured iteration body and what it was captured with.
+  cudaStream_t cap_stream = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  int graph_schedule = -1, graph_sweeps = -1;
+  double graph_tol = -1.0;
+  bool graph_failed = false;
+  int last_bodies = 0, last_graph = 0;
+  ~pvglu_newton() {
+    if (graph) cudaGraphExecDestroy(graph);
+    if (cap_stream) cudaStreamDestroy(cap_stream);
+    if (pinned_ndone) cudaFreeHost(pinned_ndone);
+    for (void* p : allocs) cudaFree(p);
+  }
+  template <typename T>
+  int alloc(size_t count, T** out) {
+    PVGLU_CUDA(cudaMalloc((void**)out, std::max<size_t>(count, 1) * sizeof(T)));
+    allocs.push_back(*out);
+    return PVGLU_OK;
+  }
+  template <typename T>
+  int put(const std::vector<T>& h, T** out) {
+    int st = upload(h, out);
+    if (st) return st;
+    allocs.push_back(*out);
+    return PVGLU_OK;
+  }
+};
+
+namespace {
+
+cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// One Newton iteration for every running scenario (no host synchronization).
+int newton_body(pvglu_newton* nw, cudaStream_t st) {
+  pvglu_numeric* h = nw->num;
+  const pvglu::NtDev& D = nw->D;
+  const int* ndone = D.done + D.ld;
+  const pvglu::SkipDone skip{D.done, ndone};
+  const bool fp64 = h->precision == PVGLU_FP64;
+  pvglu::k_nt_companion<<<pvglu::rows_grid(D.n_elems, D.ld, 256), 256, 0, st>>>(D);
+  pvglu::k_nt_rhs<<<pvglu::rows_grid(D.n, D.ld, 256), 256, 0, st>>>(
+      D, fp64 ? nw->w64 : nw->rhs64, fp64 ? h->row_pos : nullptr);
+  const pvglu::AValues A = h->stamps(D.g, D.gmin_s);
+  int rc = pvglu::run_scatter(h, A, ndone, st);
+  if (rc) return rc;
+  const double* X;
+  const int* xpos;
+  if (fp64) {
+    rc = pvglu::run_refactor_solve_perm(h, nw->w64, false, skip, st);
+    X = nw->w64;
+    xpos = h->col_pos;
+  } else {
+    rc = pvglu::run_refactor(h, st);
+    if (!rc)
+      rc = pvglu::run_refine(h, A, nw->rhs64, nw->x64, false, nw->ir_tol, nw->ir_sweeps,
+                             nullptr, st, D.done);
+    X = nw->x64;
+    xpos = nullptr;
+  }
+  if (rc) return rc;
+  const dim3 ublk(32, pvglu::kUpdRows);
+  const dim3 ugrd((unsigned)nw->n_chunks, D.ld == 1 ? 1u : (unsigned)(D.ld / 32));
+  pvglu::k_nt_update<<<ugrd, ublk, 0, st>>>(D, X, xpos);
+  pvglu::k_nt_check<<<(D.S + 127) / 128, 128, 0, st>>>(D, nw->n_chunks);
+  PVGLU_CUDA(cudaGetLastError());
+  return PVGLU_OK;
+}
+
+// Captures newton_body into an executable graph; on any capture failure the
+// driver falls back to direct launches for good.
+void capture_body(pvglu_newton* nw) {
+  if (nw->graph_failed) return;
+  pvglu_numeric* h = nw->num;
+  if (nw->graph && nw->graph_schedule == h->schedule && nw->graph_sweeps == nw->ir_sweeps &&
+      nw->graph_tol == nw->ir_tol)
+    return;
+  if (nw->graph) {
+    cudaGraphExecDestroy(nw->graph);
+    nw->graph = nullptr;
+  }
+  if (!nw->cap_stream &&
+      cudaStreamCreateWithFlags(&nw->cap_stream, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    nw->graph_failed = true;
+    return;
+  }
+  cudaGraph_t g = nullptr;
+  if (cudaStreamBeginCapture(nw->cap_stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    cudaGetLastError();
+    nw->graph_failed = true;
+    return;
+  }
+  const int rc = newton_body(nw, nw->cap_stream);
+  const cudaError_t e = cudaStreamEndCapture(nw->cap_stream, &g);
+  cudaGraphExec_t ex = nullptr;
+  if (rc || e != cudaSuccess || !g ||
+      cudaGraphInstantiate(&ex, g, 0) != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    nw->graph_failed = true;
+    return;
+  }
+  cudaGraphDestroy(g);
+  nw->graph = ex;
+  nw->graph_schedule = h->schedule;
+  nw->graph_sweeps = nw->ir_sweeps;
+  nw->graph_tol = nw->ir_tol;
+}
+
+// Position of entry (r, c) in A's CSR (sorted rows), -1 if absent.
+int find_entry(const pvglu::Symbolic& s, int r, int c) {
+  const int* b = s.a_colidx.data() + s.a_rowptr[r];
+  const int* e = s.a_colidx.data() + s.a_rowptr[r + 1];
+  const int* p = std::lower_bound(b, e, c);
+  return (p != e && *p == c) ? (int)(p - s.a_colidx.data()) : -1;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pvglu_newton_create(pvglu_numeric* num, const pvglu_circuit* c, pvglu_newton** out) {
+  if (!num || !c || !out || c->n_elems < 0 || (c->n_elems > 0 && (!c->elem_hi || !c->elem_lo)) ||
+      !c->a_lin || !c->b_lin || !(c->i0 > 0) || !(c->a > 0) || !(c->rs > 0) || !(c->rsh > 0))
+    return fail(PVGLU_ERR_BAD_ARG, "bad newton_create arguments");
+  *out = nullptr;
+  const pvglu::Symbolic& s = num->sym->s;
+  const int n = s.n, ne = c->n_elems;
+  for (int k = 0; k < ne; k++)
+    if (c->elem_hi[k] < -1 || c->elem_hi[k] >= n || c->elem_lo[k] < -1 || c->elem_lo[k] >= n)
+      return fail(PVGLU_ERR_BAD_ARG, "element terminal out of range");
+  // Stamps: per A entry, the elements touching it in element order
+  // (admittance stamp of 002b:5-38 at (hi,hi)+, (hi,lo)-, (lo,hi)-, (lo,lo)+).
+  const int nnz_a = (int)s.nnz_a;
+  std::vector<std::vector<std::pair<int, int>>> per(nnz_a);
+  for (int k = 0; k < ne; k++) {
+    const int hi = c->elem_hi[k], lo = c->elem_lo[k];
+    const int rr[4] = {hi, hi, lo, lo}, cc[4] = {hi, lo, hi, lo}, sg[4] = {1, -1, -1, 1};
+    for (int q = 0; q < 4; q++) {
+      if (rr[q] < 0 || cc[q] < 0) continue;
+      const int e = find_entry(s, rr[q], cc[q]);
+      if (e < 0)
+        return fail(PVGLU_ERR_STRUCTURAL, "element " + std::to_string(k) + " stamps (" +
+                                              std::to_string(rr[q]) + "," +
+                                              std::to_string(cc[q]) + ") outside the pattern");
+      per[e].push_back({k, sg[q]});
+    }
+  }
+  std::vector<int> eptr(nnz_a + 1, 0), eelem, esign;
+  for (int e = 0; e < nnz_a; e++) {
+    for (const auto& ks : per[e]) {
+      eelem.push_back(ks.first);
+      esign.push_back(ks.second);
+    }
+    eptr[e + 1] = (int)eelem.size();
+  }
+  int rc = pvglu_numeric_set_stamps(num, ne, c->a_lin, eptr.data(), eelem.data(), esign.data());
+  if (rc) return rc;
+  // Incidence: unknown i <- elements with a terminal there, element order.
+  std::vector<std::vector<std::pair<int, int>>> inc(n);
+  for (int k = 0; k < ne; k++) {
+    if (c->elem_hi[k] >= 0) inc[c->elem_hi[k]].push_back({k, 1});
+    if (c->elem_lo[k] >= 0) inc[c->elem_lo[k]].push_back({k, -1});
+  }
+  std::vector<int> iptr(n + 1, 0), ielem, isign;
+  for (int i = 0; i < n; i++) {
+    for (const auto& ks : inc[i]) {
+      ielem.push_back(ks.first);
+      isign.push_back(ks.second);
+    }
+    iptr[i + 1] = (int)ielem.size();
+  }
+  auto* nw = new pvglu_newton();
+  nw->num = num;
+  nw->n_elems = ne;
+  nw->n_chunks = std::max(1, (ne + pvglu::kUpdChunk - 1) / pvglu::kUpdChunk);
+  pvglu::NtDev& D = nw->D;
+  D.n = n;
+  D.n_elems = ne;
+  D.ld = num->ld;
+  D.S = num->S;
+  D.panel = pvglu_panel_params{c->i0, c->a, c->rs, c->rsh};
+  const size_t ev = (size_t)std::max(ne, 1) * D.ld, nv = (size_t)n * D.ld;
+  std::vector<int> hi(c->elem_hi, c->elem_hi + ne), lo(c->elem_lo, c->elem_lo + ne);
+  std::vector<double> bl(c->b_lin, c->b_lin + n);
+  int* tmp = nullptr;
+  double* dtmp = nullptr;
+  rc = 0;
+  rc |= nw->put(hi, &tmp);
+  D.hi = tmp;
+  rc |= nw->put(lo, &tmp);
+  D.lo = tmp;
+  rc |= nw->put(iptr, &tmp);
+  D.inc_ptr = tmp;
+  rc |= nw->put(ielem, &tmp);
+  D.inc_elem = tmp;
+  rc |= nw->put(isign, &tmp);
+  D.inc_sign = tmp;
+  rc |= nw->put(bl, &dtmp);
+  D.b_lin = dtmp;
+  rc |= nw->alloc(ev, &dtmp);
+  D.iph = dtmp;
+  rc |= nw->alloc(ev, &D.v);
+  rc |= nw->alloc(ev, &D.g);
+  rc |= nw->alloc(ev, &D.ieq);
+  rc |= nw->alloc(D.ld, &D.gmin_s);
+  rc |= nw->alloc(D.ld, &D.stage);
+  rc |= nw->alloc(D.ld, &D.iters);
+  rc |= nw->alloc(D.ld, &D.outcome);
+  rc |= nw->alloc(D.ld, &D.damp_fail);
+  rc |= nw->alloc(D.ld + 1, &D.done);
+  rc |= nw->alloc(D.ld, &D.diff);
+  rc |= nw->alloc((size_t)nw->n_chunks * D.ld, &D.partial);
+  rc |= nw->alloc(1, &nw->prm_dev);
+  D.prm = nw->prm_dev;
+  rc |= nw->alloc(nv, &nw->lam);
+  if (num->precision == PVGLU_FP64) {
+    rc |= nw->alloc(nv, &nw->w64);
+  } else {
+    rc |= nw->alloc(nv, &nw->rhs64);
+    rc |= nw->alloc(nv, &nw->x64);
+  }
+  if (!rc && cudaMallocHost((void**)&nw->pinned_ndone, sizeof(int)) != cudaSuccess)
+    rc = fail(PVGLU_ERR_NO_MEMORY, "pinned allocation failed");
+  if (rc) {
+    const std::string e = pvglu_last_error();
+    delete nw;
+    return fail(PVGLU_ERR_NO_MEMORY, "device allocation failed: " + e);
+  }
+  if (cudaMemset(D.iph, 0, ev * sizeof(double)) != cudaSuccess ||
+      cudaMemset(D.v, 0, ev * sizeof(double)) != cudaSuccess ||
+      cudaMemset(D.g, 0, ev * sizeof(double)) != cudaSuccess ||
+      cudaMemset(D.ieq, 0, ev * sizeof(double)) != cudaSuccess ||
+      cudaMemset(nw->lam, 0, nv * sizeof(double)) != cudaSuccess ||
+      (nw->w64 && cudaMemset(nw->w64, 0, nv * sizeof(double)) != cudaSuccess) ||
+      (nw->x64 && cudaMemset(nw->x64, 0, nv * sizeof(double)) != cudaSuccess) ||
+      (nw->rhs64 && cudaMemset(nw->rhs64, 0, nv * sizeof(double)) != cudaSuccess)) {
+    delete nw;
+    return fail(PVGLU_ERR_CUDA, "cudaMemset failed");
+  }
+  pvglu::k_nt_reset<<<(D.ld + 127) / 128, 128>>>(D);
+  if (cudaDeviceSynchronize() != cudaSuccess) {
+    delete nw;
+    return fail(PVGLU_ERR_CUDA, "Newton state reset failed");
+  }
+  *out = nw;
+  return PVGLU_OK;
+}
+
+int pvglu_newton_destroy(pvglu_newton* nw) {
+  delete nw;
+  return PVGLU_OK;
+}
+
+int pvglu_newton_set_iph(pvglu_newton* nw, const double* iph, void* stream) {
+  if (!nw || !iph) return fail(PVGLU_ERR_BAD_ARG, "NULL argument");
+  PVGLU_CUDA(cudaMemcpyAsync(nw->D.iph, iph, (size_t)nw->n_elems * nw->D.ld * sizeof(double),
+                             cudaMemcpyDeviceToDevice, as_stream(stream)));
+  return PVGLU_OK;
+}
+
+int pvglu_newton_set_voltages(pvglu_newton* nw, const double* v, void* stream) {
+  if (!nw || !v) return fail(PVGLU_ERR_BAD_ARG, "NULL argument");
+  PVGLU_CUDA(cudaMemcpyAsync(nw->D.v, v, (size_t)nw->n_elems * nw->D.ld * sizeof(double),
+                             cudaMemcpyDeviceToDevice, as_stream(stream)));
+  return PVGLU_OK;
+}
+
+int pvglu_newton_set_refinement(pvglu_newton* nw, double tol, int max_sweeps) {
+  if (!nw || !(tol > 0.0) || max_sweeps <= 0 || max_sweeps > 64)
+    return fail(PVGLU_ERR_BAD_ARG, "bad refinement settings");
+  nw->ir_tol = tol;
+  nw->ir_sweeps = max_sweeps;
+  return PVGLU_OK;
+}
+
+int pvglu_newton_run(pvglu_newton* nw, const double* gmin, int n_stages, double tol,
+                     int max_iterations, int check_every, void* stream) {
+  if (!nw || !gmin || n_stages <= 0 || n_stages > pvglu::kMaxStages || !(tol > 0.0) ||
+      max_iterations <= 0 || check_every <= 0)
+    return fail(PVGLU_ERR_BAD_ARG, "bad newton_run arguments");
+  cudaStream_t st = as_stream(stream);
+  pvglu::NewtonParams& P = nw->prm_host;
+  P = pvglu::NewtonParams{};
+  for (int i = 0; i < n_stages; i++) P.gmin[i] = gmin[i];
+  P.tol = tol;
+  P.n_stages = n_stages;
+  P.max_iterations = max_iterations;
+  // The parameters live in the handle, so the copy may complete after return.
+  PVGLU_CUDA(cudaMemcpyAsync(nw->prm_dev, &P, sizeof(P), cudaMemcpyHostToDevice, st));
+  const pvglu::NtDev& D = nw->D;
+  pvglu::k_nt_reset<<<(D.ld + 127) / 128, 128, 0, st>>>(D);
+  PVGLU_CUDA(cudaGetLastError());
+  PVGLU_CUDA(cudaStreamSynchronize(st));
+  capture_body(nw);
+  nw->last_bodies = 0;
+  nw->last_graph = nw->graph ? 1 : 0;
+  while (nw->last_bodies < max_iterations) {
+    const int k = std::min(check_every, max_iterations - nw->last_bodies);
+    for (int i = 0; i < k; i++) {
+      if (nw->graph) {
+        PVGLU_CUDA(cudaGraphLaunch(nw->graph, st));
+      } else {
+        const int rc = newton_body(nw, st);
+        if (rc) return rc;
+      }
+    }
+    nw->last_bodies += k;
+    PVGLU_CUDA(cudaMemcpyAsync(nw->pinned_ndone, D.done + D.ld, sizeof(int),
+                               cudaMemcpyDeviceToHost, st));
+    PVGLU_CUDA(cudaStreamSynchronize(st));
+    if (*nw->pinned_ndone >= D.S) break;
+  }
+  return PVGLU_OK;
+}
+
+int pvglu_newton_results(pvglu_newton* nw, int* iterations, int* outcome, double* diff) {
+  if (!nw) return fail(PVGLU_ERR_BAD_ARG, "NULL handle");
+  const int S = nw->D.S;
+  PVGLU_CUDA(cudaDeviceSynchronize());
+  if (iterations)
+    PVGLU_CUDA(cudaMemcpy(iterations, nw->D.iters, S * sizeof(int), cudaMemcpyDeviceToHost));
+  if (outcome)
+    PVGLU_CUDA(cudaMemcpy(outcome, nw->D.outcome, S * sizeof(int), cudaMemcpyDeviceToHost));
+  if (diff) PVGLU_CUDA(cudaMemcpy(diff, nw->D.diff, S * sizeof(double), cudaMemcpyDeviceToHost));
+  return PVGLU_OK;
+}
+
+const double* pvglu_newton_voltages(const pvglu_newton* nw) { return nw ? nw->D.v : nullptr; }
+
+int pvglu_newton_last_run(const pvglu_newton* nw, int* bodies, int* graph) {
+  if (!nw) return fail(PVGLU_ERR_BAD_ARG, "NULL handle");
+  if (bodies) *bodies = nw->last_bodies;
+  if (graph) *graph = nw->last_graph;
+  return PVGLU_OK;
+}
+
+int pvglu_newton_solution(pvglu_newton* nw, double* x, void* stream) {
+  if (!nw || !x) return fail(PVGLU_ERR_BAD_ARG, "NULL argument");
+  pvglu_numeric* h = nw->num;
+  cudaStream_t st = as_stream(stream);
+  const size_t nv = (size_t)h->n * h->ld;
+  if (h->precision == PVGLU_FP64) {
+    // x[col_orig[c]] = w[c]
+    PVGLU_CUDA(cudaMemsetAsync(x, 0, nv * sizeof(double), st));
+    pvglu::k_permute<double, double><<<pvglu::rows_grid(h->n, h->ld, 256), 256, 0, st>>>(
+        h->d.col_orig, h->n, h->ld, h->S, nw->w64, x, 0);
+  } else {
+    PVGLU_CUDA(cudaMemcpyAsync(x, nw->x64, nv * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  }
+  PVGLU_CUDA(cudaGetLastError());
+  return PVGLU_OK;
+}
+
+int pvglu_newton_adjoint(pvglu_newton* nw, const double* dpdx, double* dpdiph, void* stream) {
+  if (!nw || !dpdx || !dpdiph) return fail(PVGLU_ERR_BAD_ARG, "NULL argument");
+  pvglu_numeric* h = nw->num;
+  cudaStream_t st = as_stream(stream);
+  const pvglu::NtDev& D = nw->D;
+  pvglu::k_nt_adjoint_companion<<<pvglu::rows_grid(D.n_elems, D.ld, 256), 256, 0, st>>>(D);
+  const pvglu::AValues A = h->stamps(D.g, nullptr);
+  int rc = pvglu::run_scatter(h, A, nullptr, st);
+  if (rc) return rc;
+  const pvglu::SkipDone none{nullptr, nullptr};
+  if (h->precision == PVGLU_FP64) {
+    // J^T lambda = dpdx: w = dpdx[col_orig], M^T z = w, lambda = z at row_pos.
+    pvglu::k_permute<double, double><<<pvglu::rows_grid(h->n, h->ld, 256), 256, 0, st>>>(
+        h->d.col_orig, h->n, h->ld, h->S, dpdx, nw->lam, 1);
+    rc = pvglu::run_refactor_solve_perm(h, nw->lam, true, none, st);
+    if (rc) return rc;
+    pvglu::k_nt_adjoint_reduce<<<pvglu::rows_grid(D.n_elems, D.ld, 256), 256, 0, st>>>(
+        D, nw->lam, h->row_pos, dpdiph);
+  } else {
+    rc = pvglu::run_refactor(h, st);
+    if (!rc)
+      rc = pvglu::run_refine(h, A, dpdx, nw->lam, true, nw->ir_tol, nw->ir_sweeps, nullptr, st);
+    if (rc) return rc;
+    pvglu::k_nt_adjoint_reduce<<<pvglu::rows_grid(D.n_elems, D.ld, 256), 256, 0, st>>>(
+        D, nw->lam, nullptr, dpdiph);
+  }
+  PVGLU_CUDA(cudaGetLastError());
+  return PVGLU_OK;
+}
+
+}  // extern "C"

@@ -64,19 +64,27 @@ PVGLU_HD double pvglu_lambert_w0_exp(double log_theta) {
   return w;
 }
 
-// Terminal current I(V) (out of the + terminal) and dI/dV.
-PVGLU_HD void pvglu_panel_iv(const pvglu_panel_params* p, double iph, double v,
-                             double* current, double* didv) {
+// Terminal current I(V) (out of the + terminal), dI/dV and dI/dIph.
+PVGLU_HD void pvglu_panel_iv3(const pvglu_panel_params* p, double iph, double v,
+                              double* current, double* didv, double* didiph) {
   const double rs = p->rs, rsh = p->rsh, a = p->a, i0 = p->i0;
   const double rsum = rs + rsh;
   const double log_theta = log(rs * rsh * i0 / (a * rsum)) +
                            rsh * (rs * (iph + i0) + v) / (a * rsum);
   const double w = pvglu_lambert_w0_exp(log_theta);
   const double i = (rsh * (iph + i0) - v) / rsum - (a / rs) * w;
-  // Implicit derivative: with gd = dIdiode/dVd + 1/Rsh at Vd = V + I*Rs,
-  // dI/dV = -gd / (1 + Rs*gd).
+  // Implicit derivatives: with gd = dIdiode/dVd + 1/Rsh at Vd = V + I*Rs,
+  // dI/dV = -gd / (1 + Rs*gd) and dI/dIph = 1 / (1 + Rs*gd).
   const double vd = v + i * rs;
   const double gd = i0 / a * exp(vd / a) + 1.0 / rsh;
   *current = i;
   *didv = -gd / (1.0 + rs * gd);
+  *didiph = 1.0 / (1.0 + rs * gd);
+}
+
+// Terminal current I(V) (out of the + terminal) and dI/dV.
+PVGLU_HD void pvglu_panel_iv(const pvglu_panel_params* p, double iph, double v,
+                             double* current, double* didv) {
+  double didiph;
+  pvglu_panel_iv3(p, iph, v, current, didv, &didiph);
 }

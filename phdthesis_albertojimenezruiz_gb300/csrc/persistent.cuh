@@ -178,7 +178,7 @@ int launch_prog_persistent(const ProgSetDev& PS, int max_chains, const DevStruct
 // Failure-path self-test: one barrier that waits for one block more than the
 // launch has, so the wait can only end by its spin limit.  Every block must
 // come back with PVGLU_ERR_BARRIER_TIMEOUT recorded and the abort word set.
-__global__ void k_barrier_timeout_probe(unsigned int* bar, DevStatus* st, long long max_spins,
+static __global__ void k_barrier_timeout_probe(unsigned int* bar, DevStatus* st, long long max_spins,
                                         int* passed) {
   const bool ok = grid_barrier(bar, st, gridDim.x + 1u, max_spins);
   if (threadIdx.x == 0 && !ok) atomicAdd(passed, 1);

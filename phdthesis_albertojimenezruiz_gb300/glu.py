@@ -135,6 +135,28 @@ class Numeric:
                                             float(tol), int(max_sweeps), _ptr(sweeps),
                                             _stream_ptr(stream)), "pvglu_solve_refined")
 
+    def refine(self, b, x, a_values=None, g=None, gmin=None, transpose=False, tol=1e-12,
+               max_sweeps=10, sweeps=None, stream=None) -> None:
+        """pvglu_refine: J from explicit `a_values` or from the stamps over `g`."""
+        flags = N.SOLVE_TRANSPOSE if transpose else 0
+        N.check(N.lib().pvglu_refine(self.handle, _ptr(a_values), _ptr(g), _ptr(gmin), _ptr(b),
+                                     _ptr(x), flags, float(tol), int(max_sweeps), _ptr(sweeps),
+                                     _stream_ptr(stream)), "pvglu_refine")
+
+    def set_stamps(self, n_elems: int, base, entry_ptr, entry_elem, entry_sign) -> None:
+        """Registers a structured Jacobian (pvglu_numeric_set_stamps)."""
+        self._stamps = [np.ascontiguousarray(base, dtype=np.float64),
+                        np.ascontiguousarray(entry_ptr, dtype=np.int32),
+                        np.ascontiguousarray(entry_elem, dtype=np.int32),
+                        np.ascontiguousarray(entry_sign, dtype=np.int32)]
+        N.check(N.lib().pvglu_numeric_set_stamps(self.handle, int(n_elems),
+                                                 *[_ptr(a) for a in self._stamps]),
+                "pvglu_numeric_set_stamps")
+
+    def scatter_stamps(self, g, gmin=None, stream=None) -> None:
+        N.check(N.lib().pvglu_scatter_stamps(self.handle, _ptr(g), _ptr(gmin),
+                                             _stream_ptr(stream)), "pvglu_scatter_stamps")
+
     def check(self, stream=None) -> tuple[int, int, int]:
         code, col, sc = C.c_int(), C.c_int(), C.c_int()
         N.check(N.lib().pvglu_numeric_check(self.handle, _stream_ptr(stream), C.byref(code),

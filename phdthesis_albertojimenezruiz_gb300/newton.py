@@ -1,0 +1,95 @@
+"""Device Newton driver of the PV plant (include/pvglu_newton.h).
+
+`Newton` binds the damped, gmin-staged Newton iteration of the reference's
+simulator (PVPP_Plant_Simulator/000_PVPP_simulator.cpp:163-236,
+002b_sistema_electrico_base_matriz.cpp:141-240,
+011_calculate_new_iteration.cpp:37-110) to a `Numeric` handle; every
+iteration runs on the device (a CUDA graph where capture works) and the
+adjoint gives dP/dIph for a linear objective P = dpdx . x.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _native as N
+from .glu import Numeric, _ptr, _stream_ptr
+
+# Convergence-conductance stages of the reference (000_PVPP_simulator.cpp:101-102).
+GMIN_STAGES = (100.0, 10.0, 1.0, 0.9, 0.8, 0.5, 0.4, 0.3, 0.2, 0.1, 0.05, -1.0)
+MAX_ITERATIONS = 5000  # 000_PVPP_simulator.cpp:152
+
+
+class Newton:
+    def __init__(self, num: Numeric, n_elems: int, elem_hi, elem_lo, a_lin, b_lin,
+                 i0: float, a: float, rs: float, rsh: float):
+        self.num = num
+        self.n_elems = int(n_elems)
+        self._keep = [np.ascontiguousarray(elem_hi, dtype=np.int32),
+                      np.ascontiguousarray(elem_lo, dtype=np.int32),
+                      np.ascontiguousarray(a_lin, dtype=np.float64),
+                      np.ascontiguousarray(b_lin, dtype=np.float64)]
+        c = N.Circuit(self.n_elems, *[k.ctypes.data for k in self._keep], float(i0), float(a),
+                      float(rs), float(rsh))
+        h = C.c_void_p()
+        N.check(N.lib().pvglu_newton_create(num.handle, C.byref(c), C.byref(h)),
+                "pvglu_newton_create")
+        self.handle = h
+
+    @classmethod
+    def for_plant(cls, num: Numeric, plant) -> "Newton":
+        i = plant.info
+        return cls(num, plant.n_panels, plant.pan_hi, plant.pan_lo, plant.a_lin, plant.b_lin,
+                   i["panel_i0"], i["panel_a"], i["panel_rs"], i["panel_rsh"])
+
+    def set_iph(self, iph, stream=None) -> None:
+        N.check(N.lib().pvglu_newton_set_iph(self.handle, _ptr(iph), _stream_ptr(stream)),
+                "pvglu_newton_set_iph")
+
+    def set_voltages(self, v, stream=None) -> None:
+        N.check(N.lib().pvglu_newton_set_voltages(self.handle, _ptr(v), _stream_ptr(stream)),
+                "pvglu_newton_set_voltages")
+
+    def set_refinement(self, tol: float, max_sweeps: int) -> None:
+        N.check(N.lib().pvglu_newton_set_refinement(self.handle, float(tol), int(max_sweeps)),
+                "pvglu_newton_set_refinement")
+
+    def run(self, tol: float, gmin=GMIN_STAGES, max_iterations: int = MAX_ITERATIONS,
+            check_every: int = 4, stream=None) -> None:
+        g = np.ascontiguousarray(gmin, dtype=np.float64)
+        N.check(N.lib().pvglu_newton_run(self.handle, _ptr(g), len(g), float(tol),
+                                         int(max_iterations), int(check_every),
+                                         _stream_ptr(stream)), "pvglu_newton_run")
+
+    def results(self):
+        S = self.num.S
+        it = np.zeros(S, np.int32)
+        out = np.zeros(S, np.int32)
+        diff = np.zeros(S)
+        N.check(N.lib().pvglu_newton_results(self.handle, _ptr(it), _ptr(out), _ptr(diff)),
+                "pvglu_newton_results")
+        return it, out, diff
+
+    def last_run(self) -> tuple[int, bool]:
+        bodies, graph = C.c_int(), C.c_int()
+        N.check(N.lib().pvglu_newton_last_run(self.handle, C.byref(bodies), C.byref(graph)),
+                "pvglu_newton_last_run")
+        return bodies.value, bool(graph.value)
+
+    def voltages_ptr(self) -> int:
+        return N.lib().pvglu_newton_voltages(self.handle)
+
+    def solution(self, x, stream=None) -> None:
+        N.check(N.lib().pvglu_newton_solution(self.handle, _ptr(x), _stream_ptr(stream)),
+                "pvglu_newton_solution")
+
+    def adjoint(self, dpdx, dpdiph, stream=None) -> None:
+        N.check(N.lib().pvglu_newton_adjoint(self.handle, _ptr(dpdx), _ptr(dpdiph),
+                                             _stream_ptr(stream)), "pvglu_newton_adjoint")
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h and N._lib is not None:
+            N.lib().pvglu_newton_destroy(h)
+            self.handle = None

@@ -1,0 +1,329 @@
+"""Newton driver and adjoint (include/pvglu_newton.h) against the CPU oracle's
+restatement of the simulator's Newton loop (oracle/oracle_newton.cpp).
+
+CPU tests pin the oracle itself: the panel law against an independent
+bisection of the implicit single-diode equation, the converged operating
+point against Kirchhoff's current law with the true element currents, and
+the oracle's adjoint against central finite differences of full Newton
+solves.  GPU tests run the device driver through the C ABI.
+
+Tolerances: FP64 voltages and node solutions 1e-12 normwise relative
+(conftest.norm_err) with equal iteration counts; FP32 factors + FP64
+refinement 1e-10; adjoint 1e-10 against the oracle's adjoint and 1e-6
+against central differences (step 1e-2 W/m^2, truncation ~1e-7).
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+from conftest import norm_err
+
+from oracle import oracle as O
+from phdthesis_albertojimenezruiz_gb300 import (FP32, FP64, GMIN_STAGES, SCHED_LEVELS,
+                                                SCHED_PERSISTENT, SCHED_THREAD_CHAIN, Newton,
+                                                Numeric, Plant, Symbolic)
+from phdthesis_albertojimenezruiz_gb300 import _native as N
+
+SCHEDULES = [SCHED_LEVELS, SCHED_PERSISTENT, SCHED_THREAD_CHAIN]
+G_TO_IPH = 8.5 / 1000.0  # Iph = 8.5 A at 1000 W/m^2
+
+
+def bright(p: Plant, seed: int) -> np.ndarray:
+    """Irradiance with per-panel variation 400-1000 W/m^2 (every panel lit)."""
+    return 1000.0 - np.random.default_rng(seed).uniform(0.0, 600.0, p.n_panels)
+
+
+def objective(p: Plant) -> np.ndarray:
+    """P = power into the MPPT sinks = -V_mppt * sum of source currents."""
+    d = np.zeros(p.n)
+    d[p.inv_current] = -p.v_mppt
+    return d
+
+
+def setup(dims):
+    p = Plant(*dims)
+    sym = Symbolic(p.rowptr, p.colidx)
+    port = O.Port(p.rowptr, p.colidx, sym.array("perm_amd"))
+    return p, sym, port
+
+
+def kcl_residual(p: Plant, iph: np.ndarray, x: np.ndarray) -> float:
+    vx = np.where(p.pan_hi >= 0, x[np.maximum(p.pan_hi, 0)], 0.0) - \
+        np.where(p.pan_lo >= 0, x[np.maximum(p.pan_lo, 0)], 0.0)
+    cur, _ = p.panel_iv(iph, vx)
+    F = -p.b_lin.copy()
+    rows = np.repeat(np.arange(p.n), np.diff(p.rowptr))
+    np.add.at(F, rows, p.a_lin * x[p.colidx])
+    hi, lo = p.pan_hi >= 0, p.pan_lo >= 0
+    np.add.at(F, p.pan_hi[hi], -cur[hi])
+    np.add.at(F, p.pan_lo[lo], cur[lo])
+    return float(np.abs(F).max())
+
+
+# --------------------------------------------------------------------------
+# CPU: the oracle pinned by physics and finite differences
+
+
+def test_panel_law_matches_bisection():
+    p = Plant(1, 1, 3)
+    i = p.info
+    rng = np.random.default_rng(3)
+    v = np.concatenate([rng.uniform(-120, 60, 400), [0.0, p.voc_panel]])
+    iph = rng.uniform(0.0, 9.0, len(v))
+    cur, didv = p.panel_iv(iph, v)
+    # Independent: bisection on the diode voltage vd of
+    #   (vd - V)/Rs = Iph - I0 (exp(vd/a) - 1) - vd/Rsh   (strictly decreasing in vd)
+    i0, a, rs, rsh = i["panel_i0"], i["panel_a"], i["panel_rs"], i["panel_rsh"]
+    h = lambda vd: iph + i0 - i0 * np.exp(vd / a) - vd / rsh - (vd - v) / rs  # noqa: E731
+    lo = np.minimum(v, 0.0) - 1e3
+    hi = np.full_like(v, 80.0)
+    for _ in range(200):
+        mid = 0.5 * (lo + hi)
+        pos = h(mid) > 0
+        lo = np.where(pos, mid, lo)
+        hi = np.where(pos, hi, mid)
+    vd = 0.5 * (lo + hi)
+    ref = (vd - v) / rs
+    assert np.max(np.abs(cur - ref) / np.maximum(np.abs(ref), 1e-3)) < 1e-10
+    gd = i0 / a * np.exp(vd / a) + 1.0 / rsh
+    assert np.max(np.abs(didv + gd / (1 + rs * gd)) / (gd / (1 + rs * gd))) < 1e-9
+
+
+@pytest.mark.parametrize("dims", [(1, 2, 5), (2, 4, 10)])
+def test_oracle_newton_satisfies_kcl(dims):
+    p, sym, port = setup(dims)
+    iph = p.iph(bright(p, 1))
+    rc, it, diff, v, x = port.newton(p, iph, p.flat_start(), GMIN_STAGES, 1e-9)
+    assert rc == 0 and 10 < it < 5000 and diff < 1e-9
+    assert kcl_residual(p, iph, x) < 1e-8 * np.abs(x).max()
+    assert objective(p) @ x > 0  # the plant delivers power
+
+
+def test_oracle_newton_iteration_cap_and_stage_tolerance():
+    p, sym, port = setup((1, 2, 5))
+    iph = p.iph(bright(p, 2))
+    rc, it, _, _, _ = port.newton(p, iph, p.flat_start(), GMIN_STAGES, 1e-9, max_iterations=7)
+    assert rc == 2 and it == 7
+    # Reference tolerance 1e-6 * n stops earlier than 1e-9.
+    _, it_loose, *_ = port.newton(p, iph, p.flat_start(), GMIN_STAGES, 1e-6 * p.n)
+    _, it_tight, *_ = port.newton(p, iph, p.flat_start(), GMIN_STAGES, 1e-9)
+    assert it_loose < it_tight
+
+
+@pytest.mark.parametrize("dims", [(1, 2, 5), (2, 4, 10)])
+def test_oracle_adjoint_matches_finite_differences(dims):
+    p, sym, port = setup(dims)
+    g = bright(p, 1)
+    dpdx = objective(p)
+
+    def solve(gg):
+        rc, _, _, v, x = port.newton(p, p.iph(gg), p.flat_start(), GMIN_STAGES, 1e-9)
+        assert rc == 0
+        return v, x
+
+    v, _ = solve(g)
+    adj = port.adjoint(p, p.iph(g), v, dpdx) * G_TO_IPH
+    h = 1e-2
+    # A direction without sign changes keeps the derivative away from cancellation.
+    d = np.random.default_rng(5).uniform(0.5, 1.0, p.n_panels)
+    fd = (dpdx @ solve(g + h * d)[1] - dpdx @ solve(g - h * d)[1]) / (2 * h)
+    assert abs(adj @ d - fd) <= 1e-6 * abs(fd)
+    # One panel: the most sensitive one (a near-zero derivative would measure
+    # the finite-difference noise, ~1e-8 W per W/m^2, instead).
+    k = int(np.argmax(np.abs(adj)))
+    e = np.zeros(p.n_panels)
+    e[k] = 1.0
+    fd_k = (dpdx @ solve(g + h * e)[1] - dpdx @ solve(g - h * e)[1]) / (2 * h)
+    assert abs(adj[k] - fd_k) <= 1e-6 * abs(fd_k)
+
+
+# --------------------------------------------------------------------------
+# GPU: the device driver through the C ABI
+
+
+def dev(a, dtype=np.float64):
+    import torch
+
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=dtype)).cuda()
+
+
+def cols(a: np.ndarray, ld: int) -> np.ndarray:
+    """[rows, S] -> [rows, ld] (padding columns zero); 1-D = one scenario."""
+    a = a.reshape(a.shape[0], -1)
+    out = np.zeros((a.shape[0], ld))
+    out[:, : a.shape[1]] = a
+    return out
+
+
+def run_device(p, sym, g_cols, precision, schedule, tol, max_iterations=5000, check_every=4):
+    """Device Newton for the scenarios in g_cols [n_panels, S]."""
+    import torch
+
+    S = g_cols.shape[1]
+    num = Numeric(sym, S, precision, schedule)
+    nw = Newton.for_plant(num, p)
+    ld = num.ld
+    nw.set_iph(dev(cols(p.iph(g_cols), ld)))
+    nw.set_voltages(dev(cols(np.repeat(p.flat_start()[:, None], S, 1), ld)))
+    nw.run(tol, max_iterations=max_iterations, check_every=check_every)
+    it, out, diff = nw.results()
+    x = torch.zeros(p.n * ld, dtype=torch.float64, device="cuda")
+    nw.solution(x)
+    vt = torch.as_tensor(_DevView(nw.voltages_ptr(), (p.n_panels * ld,)), device="cuda")
+    torch.cuda.synchronize()
+    x = x.cpu().numpy().reshape(p.n, ld)[:, :S]
+    v = vt.cpu().numpy().reshape(p.n_panels, ld)[:, :S]
+    return num, nw, it, out, diff, v, x
+
+
+class _DevView:
+    def __init__(self, ptr, shape):
+        self.__cuda_array_interface__ = {"shape": shape, "typestr": "<f8",
+                                         "data": (ptr, False), "version": 3}
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [FP64, FP32])
+def test_scatter_stamps_equals_explicit_values(cuda, precision):
+    import torch
+
+    from test_gpu_parity import values_of
+
+    p, sym, _ = setup((2, 4, 10))
+    S = 3
+    num = Numeric(sym, S, precision, SCHED_LEVELS)
+    Newton.for_plant(num, p)  # registers the stamps
+    ld = num.ld
+    rng = np.random.default_rng(0)
+    gel = rng.uniform(0.01, 2.0, (p.n_panels, S))
+    gmin = np.array([0.0, 0.5, 100.0])
+    num.scatter_stamps(dev(cols(gel, ld)), dev(np.pad(gmin, (0, ld - S))))
+    stamped = values_of(num, int(sym.nnz_lu))
+    # Same additions in the same order on the host: base, then per element
+    # in element order +-G and, if positive, +-gmin.
+    a = np.repeat(p.a_lin[:, None], S, 1)
+    ptr = p.contrib_ptr
+    for e in range(len(p.a_lin)):
+        for c in range(ptr[e], ptr[e + 1]):
+            sg = float(p.contrib_sign[c])
+            for s in range(S):
+                a[e, s] = a[e, s] + sg * gel[p.contrib_panel[c], s]
+                if gmin[s] > 0:
+                    a[e, s] = a[e, s] + sg * gmin[s]
+    num.scatter(dev(cols(a, ld)))
+    explicit = values_of(num, int(sym.nnz_lu))
+    assert np.array_equal(stamped, explicit)
+    torch.cuda.synchronize()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("schedule", SCHEDULES)
+@pytest.mark.parametrize("dims,S", [((2, 4, 10), 1), ((1, 8, 20), 3)])
+def test_newton_fp64_matches_oracle(cuda, dims, S, schedule):
+    p, sym, port = setup(dims)
+    g = np.stack([bright(p, 10 + s) for s in range(S)], 1)
+    tol = 1e-6 * p.n
+    num, nw, it, out, diff, v, x = run_device(p, sym, g, FP64, schedule, tol)
+    assert num.check()[0] == 0
+    for s in range(S):
+        rc, it_o, diff_o, v_o, x_o = port.newton(p, p.iph(g[:, s]), p.flat_start(),
+                                                 GMIN_STAGES, tol)
+        assert rc == 0 and out[s] == N.NEWTON_CONVERGED
+        assert it[s] == it_o
+        assert norm_err(v[:, s], v_o) <= 1e-12
+        assert norm_err(x[:, s], x_o) <= 1e-12
+    if schedule == SCHED_LEVELS:
+        assert nw.last_run()[1], "iteration body did not run as a CUDA graph"
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("schedule", [SCHED_LEVELS, SCHED_PERSISTENT])
+def test_newton_fp32_refined_matches_oracle(cuda, schedule):
+    p, sym, port = setup((2, 4, 10))
+    S = 3
+    g = np.stack([bright(p, 20 + s) for s in range(S)], 1)
+    tol = 1e-9
+    num, nw, it, out, diff, v, x = run_device(p, sym, g, FP32, schedule, tol)
+    for s in range(S):
+        rc, it_o, _, v_o, x_o = port.newton(p, p.iph(g[:, s]), p.flat_start(), GMIN_STAGES, tol)
+        assert rc == 0 and out[s] == N.NEWTON_CONVERGED
+        assert abs(int(it[s]) - it_o) <= 2
+        assert norm_err(v[:, s], v_o) <= 1e-10
+        assert norm_err(x[:, s], x_o) <= 1e-10
+
+
+@pytest.mark.gpu
+def test_newton_iteration_cap(cuda):
+    p, sym, _ = setup((1, 2, 5))
+    g = bright(p, 3)[:, None]
+    _, nw, it, out, _, _, _ = run_device(p, sym, g, FP64, SCHED_LEVELS, 1e-9, max_iterations=7,
+                                         check_every=3)
+    assert it[0] == 7 and out[0] == N.NEWTON_MAX_ITERATIONS
+    assert nw.last_run()[0] <= 7 + 3
+
+
+@pytest.mark.gpu
+def test_newton_bad_arguments(cuda):
+    p, sym, _ = setup((1, 2, 5))
+    num = Numeric(sym, 1, FP64)
+    nw = Newton.for_plant(num, p)
+    with pytest.raises(N.PvgluError):
+        nw.run(1e-6, gmin=[])
+    with pytest.raises(N.PvgluError):
+        nw.run(1e-6, gmin=list(range(17)))
+    with pytest.raises(N.PvgluError):
+        nw.run(0.0)
+    with pytest.raises(N.PvgluError):  # a terminal outside the pattern's unknowns
+        Newton(num, 1, [p.n], [-1], p.a_lin, p.b_lin, 1e-9, 2.0, 0.3, 300.0)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [FP64, FP32])
+def test_adjoint_matches_oracle_and_finite_differences(cuda, precision):
+    import torch
+
+    p, sym, port = setup((2, 4, 10))
+    g0 = bright(p, 1)
+    h = 1e-2
+    d = np.random.default_rng(5).uniform(0.5, 1.0, p.n_panels)
+    g = np.stack([g0, g0 + h * d, g0 - h * d], 1)
+    num, nw, it, out, diff, v, x = run_device(p, sym, g, precision, SCHED_PERSISTENT, 1e-9)
+    assert (out == N.NEWTON_CONVERGED).all()
+    dpdx = objective(p)
+    ld = num.ld
+    dpdiph = torch.zeros(p.n_panels * ld, dtype=torch.float64, device="cuda")
+    nw.adjoint(dev(cols(np.repeat(dpdx[:, None], 3, 1), ld)), dpdiph)
+    torch.cuda.synchronize()
+    adj = dpdiph.cpu().numpy().reshape(p.n_panels, ld)[:, 0]
+    ref = port.adjoint(p, p.iph(g0), v[:, 0], dpdx)
+    assert norm_err(adj, ref) <= (1e-10 if precision == FP64 else 1e-8)
+    fd = (dpdx @ x[:, 1] - dpdx @ x[:, 2]) / (2 * h)
+    assert abs(G_TO_IPH * adj @ d - fd) <= 1e-6 * abs(fd)
+
+
+@pytest.mark.gpu
+def test_refine_transposed_and_stamped(cuda):
+    import torch
+
+    p, sym, port = setup((2, 4, 10))
+    S = 2
+    rng = np.random.default_rng(9)
+    gel = rng.uniform(0.01, 1.0, (p.n_panels, S))
+    num = Numeric(sym, S, FP32, SCHED_LEVELS)
+    Newton.for_plant(num, p)
+    ld = num.ld
+    gd = dev(cols(gel, ld))
+    num.scatter_stamps(gd)
+    num.refactor()
+    b = rng.standard_normal((p.n, S))
+    xt = torch.zeros(p.n * ld, dtype=torch.float64, device="cuda")
+    num.refine(dev(cols(b, ld)), xt, g=gd, transpose=True, tol=1e-13, max_sweeps=12)
+    torch.cuda.synchronize()
+    xt = xt.cpu().numpy().reshape(p.n, ld)
+    for s in range(S):
+        a = p.jacobian_values(gel[:, s])
+        A = np.zeros((p.n, p.n))
+        rows = np.repeat(np.arange(p.n), np.diff(p.rowptr))
+        np.add.at(A, (rows, p.colidx), a)
+        ref = np.linalg.solve(A.T, b[:, s])
+        assert norm_err(xt[:, s], ref) <= 1e-10
