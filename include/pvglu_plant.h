@@ -60,6 +60,11 @@ int pvglu_plant_irradiance(const pvglu_plant* p, int min_shadows, int max_shadow
 int pvglu_plant_panel_iv(const pvglu_plant* p, int count, const double* iph,
                          const double* v, double* current, double* didv);
 
+/* The panel model's own exponential and logarithm (the same code runs on
+ * the device), for accuracy checks: exp_out[i] = exp(x[i]),
+ * log_out[i] = log(x[i]); either output may be NULL. */
+int pvglu_plant_exp_log(int count, const double* x, double* exp_out, double* log_out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -107,6 +107,7 @@ _SIGS = {
     "pvglu_plant_get_darray": ([_P, C.c_char_p, C.POINTER(_DP), C.POINTER(C.c_int64)], _I),
     "pvglu_plant_irradiance": ([_P, _I, _I, C.c_double, C.c_double, C.c_uint64, C.c_double, _P], _I),
     "pvglu_plant_panel_iv": ([_P, _I, _P, _P, _P, _P], _I),
+    "pvglu_plant_exp_log": ([_I, _P, _P, _P], _I),
 }
 
 

@@ -29,6 +29,9 @@ NVCCFLAGS = ["-std=c++17", "-O3", "-lineinfo", "--expt-relaxed-constexpr",
 
 HOST_SOURCES = ["symbolic.cpp", "programs.cpp", "plant.cpp", "plant_capi.cpp"]
 CUDA_SOURCES = ["capi.cu", "newton.cu"]
+# newton.cu evaluates the panel model (panel_model.h) on the device; without
+# multiply-add contraction it rounds exactly like the host code.
+EXTRA_NVCCFLAGS = {"newton.cu": ["--fmad=false"]}
 
 
 def _nvcc() -> str:
@@ -66,7 +69,8 @@ def build(verbose: bool = False, force: bool = False) -> Path:
         obj = BUILD / (src + ".o")
         objs.append(obj)
         if force or _stale(obj, [CSRC / src] + headers):
-            jobs.append([nvcc, *NVCCFLAGS, "-I", str(CSRC), "-c", str(CSRC / src), "-o", str(obj)])
+            jobs.append([nvcc, *NVCCFLAGS, *EXTRA_NVCCFLAGS.get(src, []), "-I", str(CSRC), "-c",
+                         str(CSRC / src), "-o", str(obj)])
     with ThreadPoolExecutor(max_workers=max(2, len(jobs))) as ex:
         for cmd, _ in zip(jobs, ex.map(_run, jobs)):
             if verbose:

@@ -33,13 +33,13 @@ int launch_blocks(int64_t threads, int block) {
 }
 
 template <typename T>
-int refactor_levels(pvglu_numeric* h, cudaStream_t st) {
+int refactor_levels(pvglu_numeric* h, cudaStream_t st, const int* ndone) {
   T* v = static_cast<T*>(h->values);
   for (size_t lv = 0; lv + 1 < h->lu_sl.size(); lv++) {
     const int cb = h->lu_sl[lv], ce = h->lu_sl[lv + 1];
     const int64_t threads = (int64_t)(ce - cb) * h->ld;
     pvglu::k_refactor_level<T><<<launch_blocks(threads, 128), 128, 0, st>>>(
-        h->d, v, h->ld, h->S, cb, ce, h->pivot_tol, h->status);
+        h->d, v, h->ld, h->S, cb, ce, h->pivot_tol, h->status, ndone);
   }
   PVGLU_CUDA(cudaGetLastError());
   return PVGLU_OK;
@@ -76,7 +76,7 @@ int prog_prepare(pvglu_numeric* h) {
 
 // One phase of chain programs with one launch per level.
 template <typename T, bool B, int KIND>
-void prog_levels(pvglu_numeric* h, T* x, const int* done, cudaStream_t st) {
+void prog_levels(pvglu_numeric* h, T* x, const int* done, const int* ndone, cudaStream_t st) {
   const int ph = KIND + 1;
   const auto& lc = h->prog_level_chain[ph];
   const size_t smem = pvglu::prog_smem_bytes<T, B>(h->max_locals, pvglu::kProgWarps);
@@ -87,7 +87,7 @@ void prog_levels(pvglu_numeric* h, T* x, const int* done, cudaStream_t st) {
     pvglu::k_prog_level<T, KIND, B>
         <<<launch_blocks(items, pvglu::kProgWarps), pvglu::kProgBlock, smem, st>>>(
             h->progs.p[ph], h->d, cb, ce, static_cast<T*>(h->values), x, h->ld, h->S,
-            h->pivot_tol, h->status, done);
+            h->pivot_tol, h->status, done, ndone);
   }
 }
 
@@ -102,14 +102,14 @@ int prog_dispatch(pvglu_numeric* h, int phases, T* x, pvglu::SkipDone skip, cuda
                                       cudaGetErrorString(cudaGetLastError()));
     return PVGLU_OK;
   }
-  if (phases & pvglu::PHASE_REFACTOR) prog_levels<T, B, -1>(h, x, nullptr, st);
+  if (phases & pvglu::PHASE_REFACTOR) prog_levels<T, B, -1>(h, x, nullptr, skip.ndone, st);
   if (phases & pvglu::PHASE_SOLVE) {
-    prog_levels<T, B, 0>(h, x, skip.done, st);
-    prog_levels<T, B, 1>(h, x, skip.done, st);
+    prog_levels<T, B, 0>(h, x, skip.done, skip.ndone, st);
+    prog_levels<T, B, 1>(h, x, skip.done, skip.ndone, st);
   }
   if (phases & pvglu::PHASE_SOLVE_T) {
-    prog_levels<T, B, 2>(h, x, skip.done, st);
-    prog_levels<T, B, 3>(h, x, skip.done, st);
+    prog_levels<T, B, 2>(h, x, skip.done, skip.ndone, st);
+    prog_levels<T, B, 3>(h, x, skip.done, skip.ndone, st);
   }
   PVGLU_CUDA(cudaGetLastError());
   return PVGLU_OK;
@@ -184,13 +184,13 @@ int run_scatter(pvglu_numeric* h, const AValues& A, const int* ndone, cudaStream
   return PVGLU_OK;
 }
 
-int run_refactor(pvglu_numeric* h, cudaStream_t st) {
+int run_refactor(pvglu_numeric* h, cudaStream_t st, SkipDone skip) {
   if (h->schedule == PVGLU_SCHED_THREAD_CHAIN)
-    return h->precision == PVGLU_FP64 ? refactor_levels<double>(h, st)
-                                      : refactor_levels<float>(h, st);
+    return h->precision == PVGLU_FP64 ? refactor_levels<double>(h, st, skip.ndone)
+                                      : refactor_levels<float>(h, st, skip.ndone);
   return h->precision == PVGLU_FP64
-             ? run_phases<double>(h, PHASE_REFACTOR, (double*)nullptr, st)
-             : run_phases<float>(h, PHASE_REFACTOR, (float*)nullptr, st);
+             ? run_phases<double>(h, PHASE_REFACTOR, (double*)nullptr, st, skip)
+             : run_phases<float>(h, PHASE_REFACTOR, (float*)nullptr, st, skip);
 }
 
 int run_solve_perm(pvglu_numeric* h, void* x, bool transpose, SkipDone skip, cudaStream_t st) {
@@ -201,7 +201,7 @@ int run_solve_perm(pvglu_numeric* h, void* x, bool transpose, SkipDone skip, cud
 int run_refactor_solve_perm(pvglu_numeric* h, void* x, bool transpose, SkipDone skip,
                             cudaStream_t st) {
   if (h->schedule != PVGLU_SCHED_PERSISTENT) {
-    const int rc = run_refactor(h, st);
+    const int rc = run_refactor(h, st, skip);
     return rc ? rc : run_solve_perm(h, x, transpose, skip, st);
   }
   const int phases = PHASE_REFACTOR | (transpose ? PHASE_SOLVE_T : PHASE_SOLVE);
@@ -589,7 +589,7 @@ int pvglu_refine(pvglu_numeric* h, const double* a_values, const double* g, cons
 
 int pvglu_refactor(pvglu_numeric* h, void* stream) {
   if (!h) return fail(PVGLU_ERR_BAD_ARG, "NULL handle");
-  return pvglu::run_refactor(h, as_stream(stream));
+  return pvglu::run_refactor(h, as_stream(stream), pvglu::SkipDone{nullptr, nullptr});
 }
 
 int pvglu_refactor_solve(pvglu_numeric* h, void* x, int flags, void* stream) {

@@ -334,10 +334,13 @@ size_t prog_smem_bytes(int max_locals, int warps_per_block) {
          (size_t)warps_per_block * sizeof(unsigned long long);
 }
 
+// done: per-scenario skip of the solves (NULL for the refactorization);
+// ndone (or NULL): the launch does nothing once every scenario is done.
 template <typename T, int KIND, bool BATCH>
 __global__ void k_prog_level(ProgDev P, DevStruct d, int cb, int ce, T* __restrict__ v,
                              T* __restrict__ x, int ld, int S, double pivot_tol, DevStatus* st,
-                             const int* done) {
+                             const int* done, const int* ndone) {
+  if (ndone && __ldcg(ndone) >= S) return;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   WarpTma tma;
   T* sm = prog_setup_warp<T, BATCH>(smem_raw, P.max_locals, tma);

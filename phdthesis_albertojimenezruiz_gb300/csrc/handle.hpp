@@ -113,7 +113,9 @@ struct pvglu_numeric {
 // `st`; vectors are [n x ld] in pivot order ("perm") or the caller's order.
 namespace pvglu {
 int run_scatter(pvglu_numeric* h, const AValues& A, const int* ndone, cudaStream_t st);
-int run_refactor(pvglu_numeric* h, cudaStream_t st);
+// skip.ndone (or NULL): nothing runs once every scenario is done; the
+// refactorization itself never skips single scenarios.
+int run_refactor(pvglu_numeric* h, cudaStream_t st, SkipDone skip = SkipDone{nullptr, nullptr});
 // Solve in pivot order in place (x: T = double or float per the handle).
 int run_solve_perm(pvglu_numeric* h, void* x, bool transpose, SkipDone skip, cudaStream_t st);
 // Refactor + pivot-order solve; one persistent launch where the schedule has it.

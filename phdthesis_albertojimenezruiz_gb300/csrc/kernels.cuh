@@ -181,7 +181,8 @@ __device__ __forceinline__ void refactor_column(const DevStruct& d, int k, int s
 template <typename T>
 __global__ void k_refactor_level(DevStruct d, T* __restrict__ v, int ld, int S,
                                  int chain_begin, int chain_end, double pivot_tol,
-                                 DevStatus* st) {
+                                 DevStatus* st, const int* __restrict__ ndone) {
+  if (ndone && __ldcg(ndone) >= S) return;
   const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int c = chain_begin + (int)(tid / ld);
   const int s = (int)(tid % ld);

@@ -46,6 +46,7 @@ struct NtDev {
   int* outcome;           // [ld] PVGLU_NEWTON_*
   int* damp_fail;         // [ld]
   int* done;              // [ld + 1]: flags, then the stopped count
+  int* just_done;         // [ld] stopped in the current iteration
   double* diff;           // [ld]
   double* partial;        // [n_chunks x ld] per-chunk sums of |dv|
   const NewtonParams* prm;
@@ -165,9 +166,12 @@ __global__ void __launch_bounds__(256) k_nt_update(NtDev D, const double* __rest
 // End of an iteration for every running scenario: diff, stage advance
 // (000_PVPP_simulator.cpp:172-176: a stage ends once diff < tol), outcome.
 __global__ void k_nt_check(NtDev D, int n_chunks) {
-  if (all_stopped(D)) return;
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= D.S || D.done[s]) return;
+  if (s >= D.S) return;
+  if (D.done[s]) {
+    D.just_done[s] = 0;
+    return;
+  }
   double diff = 0.0;
   for (int c = 0; c < n_chunks; c++) diff += D.partial[(int64_t)c * D.ld + s];
   D.diff[s] = diff;
@@ -182,10 +186,22 @@ __global__ void k_nt_check(NtDev D, int n_chunks) {
   if (out == PVGLU_NEWTON_RUNNING && it >= D.prm->max_iterations)
     out = PVGLU_NEWTON_MAX_ITERATIONS;
   D.outcome[s] = out;
+  D.just_done[s] = out != PVGLU_NEWTON_RUNNING;
   if (out != PVGLU_NEWTON_RUNNING) {
     D.done[s] = 1;
     atomicAdd(D.done + D.ld, 1);
   }
+}
+
+// FP64 handles solve in place in pivot order, and later iterations of other
+// scenarios reuse that vector (a 64-scenario group solves as a whole), so a
+// scenario's node solution is saved, in caller order, in the iteration where
+// it stops: x[col_orig[c]] = w[c].
+__global__ void k_nt_keep(NtDev D, const double* __restrict__ w, const int* __restrict__ col_pos,
+                          double* __restrict__ x) {
+  for_rows(D.n, D.ld, [&](int i, int s) {
+    if (s < D.S && D.just_done[s]) x[(int64_t)i * D.ld + s] = w[(int64_t)col_pos[i] * D.ld + s];
+  });
 }
 
 __global__ void k_nt_reset(NtDev D) {
@@ -196,6 +212,7 @@ __global__ void k_nt_reset(NtDev D) {
   D.iters[s] = 0;
   D.outcome[s] = s < D.S ? PVGLU_NEWTON_RUNNING : PVGLU_NEWTON_CONVERGED;
   D.damp_fail[s] = 0;
+  D.just_done[s] = 0;
   D.done[s] = s < D.S ? 0 : 1;
   D.diff[s] = 0.0;
   D.gmin_s[s] = 0.0;
@@ -243,7 +260,8 @@ struct pvglu_newton {
   pvglu::NewtonParams prm_host{};
   double* w64 = nullptr;        // FP64 handles: right-hand side / solution, pivot order
   double* rhs64 = nullptr;      // FP32 handles: right-hand side, caller order
-  double* x64 = nullptr;        // FP32 handles: refined solution, caller order
+  double* x64 = nullptr;        // node solution, caller order (FP32: refined in place;
+                                // FP64: saved when a scenario stops)
   double* lam = nullptr;        // adjoint vector
   int* pinned_ndone = nullptr;  // host-pinned copy of the stopped count
   double ir_tol = 1e-12;
@@ -300,7 +318,7 @@ int newton_body(pvglu_newton* nw, cudaStream_t st) {
     X = nw->w64;
     xpos = h->col_pos;
   } else {
-    rc = pvglu::run_refactor(h, st);
+    rc = pvglu::run_refactor(h, st, skip);
     if (!rc)
       rc = pvglu::run_refine(h, A, nw->rhs64, nw->x64, false, nw->ir_tol, nw->ir_sweeps,
                              nullptr, st, D.done);
@@ -312,6 +330,9 @@ int newton_body(pvglu_newton* nw, cudaStream_t st) {
   const dim3 ugrd((unsigned)nw->n_chunks, D.ld == 1 ? 1u : (unsigned)(D.ld / 32));
   pvglu::k_nt_update<<<ugrd, ublk, 0, st>>>(D, X, xpos);
   pvglu::k_nt_check<<<(D.S + 127) / 128, 128, 0, st>>>(D, nw->n_chunks);
+  if (fp64)
+    pvglu::k_nt_keep<<<pvglu::rows_grid(D.n, D.ld, 256), 256, 0, st>>>(D, nw->w64, h->col_pos,
+                                                                         nw->x64);
   PVGLU_CUDA(cudaGetLastError());
   return PVGLU_OK;
 }
@@ -459,17 +480,17 @@ int pvglu_newton_create(pvglu_numeric* num, const pvglu_circuit* c, pvglu_newton
   rc |= nw->alloc(D.ld, &D.outcome);
   rc |= nw->alloc(D.ld, &D.damp_fail);
   rc |= nw->alloc(D.ld + 1, &D.done);
+  rc |= nw->alloc(D.ld, &D.just_done);
   rc |= nw->alloc(D.ld, &D.diff);
   rc |= nw->alloc((size_t)nw->n_chunks * D.ld, &D.partial);
   rc |= nw->alloc(1, &nw->prm_dev);
   D.prm = nw->prm_dev;
   rc |= nw->alloc(nv, &nw->lam);
-  if (num->precision == PVGLU_FP64) {
+  rc |= nw->alloc(nv, &nw->x64);
+  if (num->precision == PVGLU_FP64)
     rc |= nw->alloc(nv, &nw->w64);
-  } else {
+  else
     rc |= nw->alloc(nv, &nw->rhs64);
-    rc |= nw->alloc(nv, &nw->x64);
-  }
   if (!rc && cudaMallocHost((void**)&nw->pinned_ndone, sizeof(int)) != cudaSuccess)
     rc = fail(PVGLU_ERR_NO_MEMORY, "pinned allocation failed");
   if (rc) {
@@ -588,17 +609,9 @@ int pvglu_newton_last_run(const pvglu_newton* nw, int* bodies, int* graph) {
 int pvglu_newton_solution(pvglu_newton* nw, double* x, void* stream) {
   if (!nw || !x) return fail(PVGLU_ERR_BAD_ARG, "NULL argument");
   pvglu_numeric* h = nw->num;
-  cudaStream_t st = as_stream(stream);
   const size_t nv = (size_t)h->n * h->ld;
-  if (h->precision == PVGLU_FP64) {
-    // x[col_orig[c]] = w[c]
-    PVGLU_CUDA(cudaMemsetAsync(x, 0, nv * sizeof(double), st));
-    pvglu::k_permute<double, double><<<pvglu::rows_grid(h->n, h->ld, 256), 256, 0, st>>>(
-        h->d.col_orig, h->n, h->ld, h->S, nw->w64, x, 0);
-  } else {
-    PVGLU_CUDA(cudaMemcpyAsync(x, nw->x64, nv * sizeof(double), cudaMemcpyDeviceToDevice, st));
-  }
-  PVGLU_CUDA(cudaGetLastError());
+  PVGLU_CUDA(cudaMemcpyAsync(x, nw->x64, nv * sizeof(double), cudaMemcpyDeviceToDevice,
+                             as_stream(stream)));
   return PVGLU_OK;
 }
 

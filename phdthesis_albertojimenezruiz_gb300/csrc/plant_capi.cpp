@@ -114,4 +114,13 @@ int pvglu_plant_panel_iv(const pvglu_plant* h, int count, const double* iph, con
   return PVGLU_OK;
 }
 
+int pvglu_plant_exp_log(int count, const double* x, double* exp_out, double* log_out) {
+  if (count < 0 || (count > 0 && !x)) return PVGLU_ERR_BAD_ARG;
+  for (int i = 0; i < count; i++) {
+    if (exp_out) exp_out[i] = pvglu_exp(x[i]);
+    if (log_out) log_out[i] = pvglu_log(x[i]);
+  }
+  return PVGLU_OK;
+}
+
 }  // extern "C"
