@@ -163,6 +163,95 @@ def cpu_baseline(a: np.ndarray, b: np.ndarray, p, sym_perm, budget_s: float, thr
                       f"one scenario per thread"}
 
 
+def newton_section(p, sym, stream, S: int, seed0: int, fd_check: bool = True) -> dict:
+    """Device Newton driver over the reference's gmin stages (tolerance
+    1e-6 * n, the reference's) for S scenarios with FP32 factors + FP64
+    refinement, then the adjoint dP/dG of the plant power for every panel;
+    the adjoint is checked against a central difference of two more Newton
+    solves (3-scenario handle, tolerance 1e-7 on the summed voltage change)."""
+    import torch
+
+    from phdthesis_albertojimenezruiz_gb300 import FP32, SCHED_PERSISTENT, Newton, Numeric
+
+    dev = torch.device("cuda", torch.cuda.current_device())
+    g_to_iph = p.info["iph_stc"] / 1000.0
+
+    def setup(g_cols, tol_ir=1e-10):
+        num = Numeric(sym, g_cols.shape[1], FP32, SCHED_PERSISTENT)
+        nw = Newton.for_plant(num, p)
+        ld = num.ld
+        iph = np.zeros((p.n_panels, ld))
+        iph[:, : g_cols.shape[1]] = p.iph(g_cols)
+        v0 = np.zeros((p.n_panels, ld))
+        v0[:, : g_cols.shape[1]] = p.flat_start()[:, None]
+        iph_d = torch.from_numpy(iph).to(dev)
+        v0_d = torch.from_numpy(v0).to(dev)
+        nw.set_iph(iph_d, stream=stream)
+        nw.set_refinement(tol_ir, IR_MAX_SWEEPS)
+        return num, nw, v0_d, iph_d
+
+    g = np.stack([p.irradiance(seed=seed0 + s, preset="c2") for s in range(S)], axis=1)
+    num, nw, v0_d, _ = setup(g)
+    dpdx = np.zeros((p.n, num.ld))
+    dpdx[p.inv_current, :S] = -p.v_mppt
+    dpdx_d = torch.from_numpy(dpdx).to(dev)
+    dpdiph = torch.zeros(p.n_panels * num.ld, dtype=torch.float64, device=dev)
+    tol = 1e-6 * p.n
+    # warm-up solve (graph capture, first-touch)
+    nw.set_voltages(v0_d, stream=stream)
+    nw.run(tol, stream=stream)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e2 = torch.cuda.Event(enable_timing=True)
+    nw.set_voltages(v0_d, stream=stream)
+    e0.record(stream)
+    nw.run(tol, check_every=8, stream=stream)
+    e1.record(stream)
+    nw.adjoint(dpdx_d, dpdiph, stream=stream)
+    e2.record(stream)
+    torch.cuda.synchronize()
+    it, out, _ = nw.results()
+    bodies, graph = nw.last_run()
+    newton_ms = e0.elapsed_time(e1)
+    res = {"workload": f"plant_{DIMS[0]}x{DIMS[1]}x{DIMS[2]}, {S} scenarios, FP32 LU + FP64 "
+                       "refinement, gmin stages 100..0.05,off, tol 1e-6*n",
+           "scenarios": S, "iterations_min": int(it.min()), "iterations_max": int(it.max()),
+           "converged": int((out == 0).sum()), "bodies_launched": bodies, "cuda_graph": graph,
+           "newton_ms": newton_ms,
+           "scenario_iterations_per_s": float(it.sum()) / (newton_ms / 1000.0),
+           "adjoint_ms": e1.elapsed_time(e2),
+           "adjoint_gradients_per_s": S * p.n_panels / (e1.elapsed_time(e2) / 1000.0)}
+    del nw, num
+    if fd_check:
+        h = 1e-2
+        d = np.random.default_rng(5).uniform(0.5, 1.0, p.n_panels)
+        g0 = g[:, 0]
+        g3 = np.stack([g0, g0 + h * d, g0 - h * d], 1)
+        num3, nw3, v3_d, _ = setup(g3)
+        nw3.set_voltages(v3_d, stream=stream)
+        nw3.run(1e-7, stream=stream)
+        x3 = torch.zeros(p.n * num3.ld, dtype=torch.float64, device=dev)
+        nw3.solution(x3, stream=stream)
+        d3 = torch.zeros(p.n_panels * num3.ld, dtype=torch.float64, device=dev)
+        dp3 = np.zeros((p.n, num3.ld))
+        dp3[p.inv_current, :3] = -p.v_mppt
+        nw3.adjoint(torch.from_numpy(dp3).to(dev), d3, stream=stream)
+        torch.cuda.synchronize()
+        it3, out3, _ = nw3.results()
+        x3 = x3.cpu().numpy().reshape(p.n, num3.ld)
+        adj = d3.cpu().numpy().reshape(p.n_panels, num3.ld)[:, 0] * g_to_iph
+        pw = -p.v_mppt * x3[p.inv_current, :3].sum(axis=0)
+        fd = (pw[1] - pw[2]) / (2 * h)
+        res["fd_check"] = {"direction": "U[0.5,1] per panel, h=1e-2 W/m^2",
+                           "adjoint": float(adj @ d), "central_difference": float(fd),
+                           "rel_err": float(abs(adj @ d - fd) / abs(fd)),
+                           "plant_power_w": float(pw[0]),
+                           "newton_iterations": [int(v) for v in it3],
+                           "converged": int((out3 == 0).sum())}
+    return res
+
+
 def run_reference(args) -> None:
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -209,6 +298,10 @@ def main() -> None:
     ap.add_argument("--ir-sweeps", type=int, default=IR_MAX_SWEEPS)
     ap.add_argument("--only-batched", action="store_true",
                     help="time the batched FP32+IR path only (profiling runs)")
+    ap.add_argument("--newton-scenarios", type=int, default=128,
+                    help="scenarios of the device Newton + adjoint section (0: skip)")
+    ap.add_argument("--only-newton", action="store_true",
+                    help="run the Newton + adjoint section alone (profiling runs)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     IR_TOL, IR_MAX_SWEEPS = args.ir_tol, args.ir_sweeps
@@ -231,6 +324,16 @@ def main() -> None:
     from phdthesis_albertojimenezruiz_gb300 import (FP32, FP64, SCHED_LEVELS, SCHED_PERSISTENT,
                                                     SCHED_THREAD_CHAIN, Numeric, Symbolic)
 
+    if args.only_newton:
+        from phdthesis_albertojimenezruiz_gb300 import Plant
+
+        p = Plant(*DIMS)
+        sym = Symbolic(p.rowptr, p.colidx)
+        res = newton_section(p, sym, torch.cuda.current_stream(), args.newton_scenarios, 5000,
+                             fd_check=False)
+        if rank == 0:
+            print(json.dumps(res))
+        return
     S = args.scenarios
     ld = ((S + 63) // 64) * 64
     p, a, b = make_inputs(S, ld, seed0=1000 + rank * S)
@@ -377,6 +480,8 @@ def main() -> None:
         if dist:
             dist.destroy_process_group()
         return
+    newton = (newton_section(p, sym, stream, args.newton_scenarios, 5000)
+              if args.newton_scenarios > 0 else None)
     cpu = cpu_baseline(a[:, :S], b[:, :S], p, sym.array("perm_amd"), args.cpu_budget,
                        os.cpu_count() or 1, prefer_ref=True)
     # per step: scatter, refactor, permute b, then per sweep solve + step + check
@@ -402,6 +507,7 @@ def main() -> None:
                 "d2h_bytes_per_step": int(8 * n * ld)},
         "roofline": roofline,
         "cpu_baseline": cpu,
+        "newton_adjoint": newton,
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }

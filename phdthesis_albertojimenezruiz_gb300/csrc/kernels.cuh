@@ -78,6 +78,47 @@ __device__ __forceinline__ double fnms(double a, double b, double c) {
 __device__ __forceinline__ float fnms(float a, float b, float c) { return a - b * c; }
 
 // ----------------------------------------------------------------------------
+// float <-> double conversions on the integer pipes.  GB300 issues FP64
+// instructions, conversions included, at a small fraction of its FP32 and
+// INT32 rates, and the refinement kernels that convert between the FP32
+// factors and the FP64 vectors would otherwise be bound by them.  Normal
+// numbers convert exactly as F2F does (double -> float rounds to nearest
+// even); magnitudes below the smallest normal float become signed zero,
+// overflow gives infinity, NaN stays NaN.
+__device__ __forceinline__ float d2f_bits(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned int sign = (unsigned int)(b >> 32) & 0x80000000u;
+  const int e = (int)((b >> 52) & 0x7ff);
+  const unsigned long long m = b & 0x000fffffffffffffull;
+  if (e == 0x7ff) return __uint_as_float(sign | 0x7f800000u | (m ? 0x400000u : 0u));
+  const int fe = e - 1023 + 127;
+  if (fe <= 0) return __uint_as_float(sign);
+  if (fe >= 255) return __uint_as_float(sign | 0x7f800000u);
+  // exponent and mantissa as one field: a rounding carry moves into the
+  // exponent (and to infinity past the largest float), as IEEE requires.
+  const unsigned long long em = ((unsigned long long)fe << 52) | m;
+  const unsigned long long r = em + 0x0fffffffull + ((em >> 29) & 1ull);
+  return __uint_as_float(sign | (unsigned int)(r >> 29));
+}
+
+__device__ __forceinline__ double f2d_bits(float f) {
+  const unsigned int b = __float_as_uint(f);
+  const unsigned long long sign = (unsigned long long)(b & 0x80000000u) << 32;
+  const unsigned int e = (b >> 23) & 0xff;
+  const unsigned long long m = (unsigned long long)(b & 0x7fffffu) << 29;
+  if (e == 0) return __longlong_as_double((long long)sign);
+  if (e == 0xff) return __longlong_as_double((long long)(sign | 0x7ff0000000000000ull | m));
+  return __longlong_as_double((long long)(sign | ((unsigned long long)(e - 127 + 1023) << 52) | m));
+}
+
+template <typename TO, typename TI>
+__device__ __forceinline__ TO convert(TI x) { return (TO)x; }
+template <>
+__device__ __forceinline__ float convert<float, double>(double x) { return d2f_bits(x); }
+template <>
+__device__ __forceinline__ double convert<double, float>(float x) { return f2d_bits(x); }
+
+// ----------------------------------------------------------------------------
 // Row x scenario iteration without integer division: with one scenario a
 // thread owns a row; with a batch a warp owns a row and its lanes stride over
 // the scenarios (coalesced, ld is a multiple of 32).
@@ -137,7 +178,7 @@ __global__ void k_scatter(const int* __restrict__ slot_src, int nnz, int ld, int
   for_rows(nnz, ld, [&](int q, int s) {
     const int src = slot_src[q];
     T val = T(0);
-    if (src >= 0 && s < S) val = (T)A(src, ld, s);
+    if (src >= 0 && s < S) val = convert<T>(A(src, ld, s));
     v[(int64_t)q * ld + s] = val;
   });
 }
@@ -245,8 +286,8 @@ __global__ void k_permute(const int* __restrict__ perm, int n, int ld, int S,
     if (s >= S) return;
     const int64_t e = (int64_t)r * ld + s;
     const int pr = perm[r];
-    if (gather) y[e] = (TO)x[(int64_t)pr * ld + s];
-    else y[(int64_t)pr * ld + s] = (TO)x[e];
+    if (gather) y[e] = convert<TO>(x[(int64_t)pr * ld + s]);
+    else y[(int64_t)pr * ld + s] = convert<TO>(x[e]);
   });
 }
 
@@ -267,13 +308,16 @@ static __global__ void k_residual(const int* __restrict__ ptr, const int* __rest
     double acc = b[(int64_t)i * ld + s];
     for (int p = ptr[i]; p < ptr[i + 1]; p++)
       acc -= A(ent ? ent[p] : p, ld, s) * x[(int64_t)idx[p] * ld + s];
-    r_perm[(int64_t)pos[i] * ld + s] = (float)acc;
+    r_perm[(int64_t)pos[i] * ld + s] = d2f_bits(acc);
   });
 }
 
 // x[out_perm[c]] += dx[c] (out_perm = col_orig for A, row_orig for A^T);
-// per-scenario max |dx| and max |x| (non-negative doubles order like their
-// bit patterns, so atomicMax on the bits works).
+// per-scenario max |dx| and max |x| as the bit patterns of non-negative
+// doubles, which order like the values, so atomicMax on the bits works.  The
+// maxima are taken on integer bits (|dx| exactly, |x| truncated to its upper
+// 32 bits, a lower bound within 2^-20): the one FP64 instruction per entry is
+// the addition.
 static __global__ void k_ir_update(const int* __restrict__ out_perm, int n, int ld, int S,
                             const float* __restrict__ dx, double* __restrict__ x,
                             const int* __restrict__ done,
@@ -281,16 +325,17 @@ static __global__ void k_ir_update(const int* __restrict__ out_perm, int n, int 
                             unsigned long long* __restrict__ max_x) {
   // block = (32 scenarios) x (8 rows); grid-stride over row tiles.
   const int s = blockIdx.y * 32 + threadIdx.x;
-  __shared__ double sdx[8][33], sx[8][33];
-  double mdx = 0.0, mx = 0.0;
+  __shared__ unsigned int sdx[8][33], sx[8][33];
+  unsigned int mdx = 0u, mx = 0u;
   if (s < S && !done[s]) {
     for (int c = blockIdx.x * 8 + threadIdx.y; c < n; c += gridDim.x * 8) {
-      const double d = (double)dx[(int64_t)c * ld + s];
+      const float df = dx[(int64_t)c * ld + s];
       double* xp = x + (int64_t)out_perm[c] * ld + s;
-      const double nx = *xp + d;
+      const double nx = *xp + f2d_bits(df);
       *xp = nx;
-      mdx = fmax(mdx, fabs(d));
-      mx = fmax(mx, fabs(nx));
+      mdx = max(mdx, __float_as_uint(df) & 0x7fffffffu);
+      mx = max(mx, (unsigned int)((unsigned long long)__double_as_longlong(nx) >> 32) &
+                       0x7fffffffu);
     }
   }
   sdx[threadIdx.y][threadIdx.x] = mdx;
@@ -298,11 +343,12 @@ static __global__ void k_ir_update(const int* __restrict__ out_perm, int n, int 
   __syncthreads();
   if (threadIdx.y == 0 && s < S) {
     for (int k = 1; k < 8; k++) {
-      mdx = fmax(mdx, sdx[k][threadIdx.x]);
-      mx = fmax(mx, sx[k][threadIdx.x]);
+      mdx = max(mdx, sdx[k][threadIdx.x]);
+      mx = max(mx, sx[k][threadIdx.x]);
     }
-    atomicMax(max_dx + s, (unsigned long long)__double_as_longlong(mdx));
-    atomicMax(max_x + s, (unsigned long long)__double_as_longlong(mx));
+    if (mdx) atomicMax(max_dx + s, (unsigned long long)__double_as_longlong(
+                                       f2d_bits(__uint_as_float(mdx))));
+    if (mx) atomicMax(max_x + s, (unsigned long long)mx << 32);
   }
 }
 

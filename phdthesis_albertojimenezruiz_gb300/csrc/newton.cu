@@ -35,7 +35,7 @@ struct NtDev {
   const int* inc_elem;
   const int* inc_sign;    // +1: + terminal, -1: - terminal
   const double* b_lin;    // [n]
-  pvglu_panel_params panel;
+  pvglu_panel_const panel;  // constants of the element law
   double* iph;            // [n_elems x ld] photocurrent
   double* v;              // voltage iterate
   double* g;              // companion conductance G
@@ -53,7 +53,7 @@ struct NtDev {
 };
 
 constexpr int kUpdRows = 8;            // update block: 32 scenarios x 8 element rows
-constexpr int kUpdChunk = 1024;        // elements per partial sum
+constexpr int kUpdChunk = 64;          // elements per partial sum (>= 4 blocks per SM at 35k)
 
 __device__ __forceinline__ bool all_stopped(const NtDev& D) {
   return __ldcg(D.done + D.ld) >= D.S;
@@ -72,8 +72,8 @@ __global__ void k_nt_companion(NtDev D) {
     }
     const int64_t e = (int64_t)k * D.ld + s;
     const double v = D.v[e];
-    double cur, didv;
-    pvglu_panel_iv(&D.panel, D.iph[e], v, &cur, &didv);
+    double cur, didv, didiph;
+    pvglu_panel_eval(&D.panel, D.iph[e], v, &cur, &didv, &didiph);
     const double G = -didv;
     D.g[e] = G;
     D.ieq[e] = __dsub_rn(-cur, __dmul_rn(G, v));
@@ -100,15 +100,35 @@ __global__ void k_nt_rhs(NtDev D, double* __restrict__ out, const int* __restric
 // step factor m starts at 1 and halves while the candidate moves the voltage
 // by more than 1 V or is NaN; below 1e-13 the element keeps its voltage and
 // the scenario is flagged.
-__device__ __forceinline__ double damped_step(double old, double nv, bool* bad) {
+__device__ __forceinline__ bool finite_bits(double x) {
+  return ((unsigned long long)__double_as_longlong(x) & 0x7ff0000000000000ull) !=
+         0x7ff0000000000000ull;
+}
+
+// *change = |new - old| (|x - y| = |y - x| exactly in IEEE arithmetic).
+__device__ __forceinline__ double damped_step(double old, double nv, bool* bad,
+                                              double* change) {
+  // m = 1: old * 0 + nv * 1 is nv itself for finite old and nonzero nv
+  // (the zero case keeps the general form for the sign of zero).
+  if (nv != 0.0 && finite_bits(old) && finite_bits(nv)) {
+    const double d = fabs(__dsub_rn(old, nv));
+    if (!(d > 1.0)) {
+      *change = d;
+      return nv;
+    }
+  }
   double m = 1.0;
   for (;;) {
     const double t = __dadd_rn(__dmul_rn(old, __dsub_rn(1.0, m)), __dmul_rn(nv, m));
     if (m < 1e-13) {
       *bad = true;
+      *change = 0.0;
       return old;
     }
-    if (!isnan(old) && !isnan(t) && !(fabs(__dsub_rn(old, t)) > 1.0)) return t;
+    if (!isnan(old) && !isnan(t) && !(fabs(__dsub_rn(old, t)) > 1.0)) {
+      *change = fabs(__dsub_rn(t, old));
+      return t;
+    }
     m *= 0.5;
   }
 }
@@ -136,9 +156,9 @@ __global__ void __launch_bounds__(256) k_nt_update(NtDev D, const double* __rest
       const double xh = h >= 0 ? X[(int64_t)(xpos ? xpos[h] : h) * D.ld + s] : 0.0;
       const double xl = l >= 0 ? X[(int64_t)(xpos ? xpos[l] : l) * D.ld + s] : 0.0;
       const double old = D.v[e];
-      const double t = damped_step(old, __dsub_rn(xh, xl), &bad);
-      D.v[e] = t;
-      sum = __dadd_rn(sum, fabs(__dsub_rn(t, old)));
+      double change;
+      D.v[e] = damped_step(old, __dsub_rn(xh, xl), &bad, &change);
+      sum = __dadd_rn(sum, change);
     }
   }
   if (bad) D.damp_fail[s] = 1;
@@ -225,7 +245,7 @@ __global__ void k_nt_adjoint_companion(NtDev D) {
     if (s >= D.S) return;
     const int64_t e = (int64_t)k * D.ld + s;
     double cur, didv, didiph;
-    pvglu_panel_iv3(&D.panel, D.iph[e], D.v[e], &cur, &didv, &didiph);
+    pvglu_panel_eval(&D.panel, D.iph[e], D.v[e], &cur, &didv, &didiph);
     D.g[e] = -didv;
     D.ieq[e] = didiph;
   });
@@ -264,7 +284,7 @@ struct pvglu_newton {
                                 // FP64: saved when a scenario stops)
   double* lam = nullptr;        // adjoint vector
   int* pinned_ndone = nullptr;  // host-pinned copy of the stopped count
-  double ir_tol = 1e-12;
+  double ir_tol = 1e-10;
   int ir_sweeps = 8;
   // Captured iteration body and what it was captured with.
   cudaStream_t cap_stream = nullptr;
@@ -450,7 +470,8 @@ int pvglu_newton_create(pvglu_numeric* num, const pvglu_circuit* c, pvglu_newton
   D.n_elems = ne;
   D.ld = num->ld;
   D.S = num->S;
-  D.panel = pvglu_panel_params{c->i0, c->a, c->rs, c->rsh};
+  const pvglu_panel_params pp{c->i0, c->a, c->rs, c->rsh};
+  pvglu_panel_prepare(&pp, &D.panel);
   const size_t ev = (size_t)std::max(ne, 1) * D.ld, nv = (size_t)n * D.ld;
   std::vector<int> hi(c->elem_hi, c->elem_hi + ne), lo(c->elem_lo, c->elem_lo + ne);
   std::vector<double> bl(c->b_lin, c->b_lin + n);

@@ -14,8 +14,8 @@
 //     I = (Rsh*(Iph + I0) - V) / (Rs + Rsh) - (a / Rs) * W(theta),
 //     theta = Rs*Rsh*I0 / (a*(Rs + Rsh)) * exp(Rsh*(Rs*(Iph + I0) + V) / (a*(Rs + Rsh))).
 //
-// W is evaluated with Halley's iteration, in log form for large arguments so
-// that no exponential overflows for any terminal voltage.
+// W is evaluated in log form, w + log(w) = log(theta), so that no
+// exponential overflows for any terminal voltage.
 //
 // Every operation here is a correctly rounded IEEE add, multiply or divide,
 // and the exponential and logarithm are this file's own (pvglu_exp,
@@ -136,57 +136,140 @@ PVGLU_HD double pvglu_log(double x) {
   return e * ln2_hi + ((2.0 * s) * p + e * ln2_lo);
 }
 
-// Principal branch W0(theta) for theta = exp(log_theta) >= 0.  Halley's
-// iteration converges cubically; it stops once a step is below 1e-15
-// relative (the next one would be at the rounding level).
-PVGLU_HD double pvglu_lambert_w0_exp(double log_theta) {
-  double w;
-  if (log_theta < 1.0) {
-    // Solve w * exp(w) = theta directly.
-    const double theta = pvglu_exp(log_theta);
-    w = theta < 0.1 ? theta * (1.0 - theta)
-                    : 0.5 * pvglu_log(1.0 + theta) + 0.25 * theta / (1.0 + theta);
-    for (int it = 0; it < 16; it++) {
-      const double ew = pvglu_exp(w);
-      const double f = w * ew - theta;
-      const double wp1 = w + 1.0;
-      const double denom = ew * wp1 - (w + 2.0) * f / (2.0 * wp1);
-      const double dw = f / denom;
-      w -= dw;
-      if (fabs(dw) <= 1e-15 * fabs(w)) break;
-    }
-  } else {
-    // Solve h(w) = w + log(w) - log_theta = 0 (Halley on h).
-    w = log_theta - pvglu_log(log_theta);
-    if (w < 0.5) w = 0.5;
-    for (int it = 0; it < 16; it++) {
-      const double h = w + pvglu_log(w) - log_theta;
-      const double h1 = 1.0 + 1.0 / w;
-      const double h2 = -1.0 / (w * w);
-      const double dw = h / (h1 - 0.5 * h * h2 / h1);
-      w -= dw;
-      if (fabs(dw) <= 1e-15 * w) break;
-    }
-  }
-  return w;
+// FP32 counterparts of pvglu_exp / pvglu_log (same methods, fewer terms:
+// degree-7 Taylor polynomial, atanh series to s^11/11), for the starting
+// guess of the Lambert-W iteration.  Arguments within the normal float range.
+PVGLU_HD float pvglu_expf(float x) {
+  if (x > 88.0f) return INFINITY;
+  if (x < -80.0f) return 0.0f;
+  const float ln2_hi = 0.693115234375f;       // ln 2 to 12 bits (0x3F317000)
+  const float ln2_lo = 3.194618329871446e-05f;
+  const int k = (int)floorf(x * 1.4426950216293335f + 0.5f);
+  const float r = (x - k * ln2_hi) - k * ln2_lo;
+  float p = 0.00019841270113829523f;  // 1/7!
+  p = p * r + 0.0013888889225199819f;
+  p = p * r + 0.008333333767950535f;
+  p = p * r + 0.0416666679084301f;
+  p = p * r + 0.1666666716337204f;
+  p = p * r + 0.5f;
+  p = p * r + 1.0f;
+  p = p * r + 1.0f;
+  unsigned int u;
+  const unsigned int e = (unsigned int)(k + 127) << 23;
+  memcpy(&u, &p, sizeof u);
+  u += e - (127u << 23);
+  float out;
+  memcpy(&out, &u, sizeof out);
+  return out;
 }
 
-// Terminal current I(V) (out of the + terminal), dI/dV and dI/dIph.
+PVGLU_HD float pvglu_logf(float x) {
+  unsigned int b;
+  memcpy(&b, &x, sizeof b);
+  int e = (int)((b >> 23) & 0xff) - 127;
+  const unsigned int mb = (b & 0x7fffffu) | 0x3f800000u;
+  float m;
+  memcpy(&m, &mb, sizeof m);
+  if (m > 1.4142135381698608f) {
+    m *= 0.5f;
+    e += 1;
+  }
+  const float s = (m - 1.0f) / (m + 1.0f);
+  const float z = s * s;
+  float p = 0.09090909361839294f;  // 1/11
+  p = p * z + 0.1111111119389534f;
+  p = p * z + 0.1428571492433548f;
+  p = p * z + 0.20000000298023224f;
+  p = p * z + 0.3333333432674408f;
+  p = p * z + 1.0f;
+  return e * 0.693115234375f + ((2.0f * s) * p + e * 3.194618329871446e-05f);
+}
+
+// Principal branch W0(theta) for theta = exp(L).  W solves w + log(w) = L.
+// Below L = -40, W(theta) = theta (1 - theta + ...) equals theta to double
+// precision.  Otherwise an FP32 estimate (Winitzki's approximation or the
+// asymptotic series, then three Halley steps on h(w) = w + log(w) - L) is
+// finished by one FP64 Halley step, which takes the FP32 error (~1e-7)
+// below the FP64 rounding (cubic convergence).  On GB300 the FP64 work is
+// one logarithm and one division.
+PVGLU_HD double pvglu_lambert_w0_exp(double L) {
+  if (L < -40.0) return pvglu_exp(L);
+  const float lf = (float)L;
+  float w;
+  if (lf < 1.0f) {
+    const float theta = pvglu_expf(lf);
+    if (theta < 1e-3f) {
+      w = theta * (1.0f - theta);
+    } else {
+      const float l1 = pvglu_logf(1.0f + theta);  // log(1 + theta)
+      w = l1 * (1.0f - pvglu_logf(1.0f + l1) / (2.0f + l1));
+    }
+  } else {
+    const float ll = pvglu_logf(lf);
+    w = lf - ll + ll / lf;
+  }
+  for (int it = 0; it < 3; it++) {
+    const float h = w + pvglu_logf(w) - lf;
+    const float wp1 = w + 1.0f;
+    w = w - 2.0f * h * w * wp1 / (2.0f * wp1 * wp1 + h);
+  }
+  const double wd = (double)w;
+  const double h = wd + pvglu_log(wd) - L;
+  const double wp1 = wd + 1.0;
+  return wd - 2.0 * h * wd * wp1 / (2.0 * wp1 * wp1 + h);
+}
+
+// Constants of the panel law, computed once per parameter set.
+typedef struct {
+  double log_c;      // log(Rs Rsh I0 / (a (Rs + Rsh)))
+  double k_l0;       // Rsh / (a (Rs + Rsh))
+  double rs_iph;     // Rs (multiplies Iph + I0 in the exponent)
+  double i0;
+  double rsh_rsum;   // Rsh / (Rs + Rsh)
+  double inv_rsum;   // 1 / (Rs + Rsh)
+  double a_over_rs;
+  double k_gd;       // (Rs + Rsh) / (Rs Rsh)
+  double inv_rsh;
+  double rs;
+} pvglu_panel_const;
+
+PVGLU_HD void pvglu_panel_prepare(const pvglu_panel_params* p, pvglu_panel_const* c) {
+  const double rsum = p->rs + p->rsh;
+  c->log_c = pvglu_log(p->rs * p->rsh * p->i0 / (p->a * rsum));
+  c->k_l0 = p->rsh / (p->a * rsum);
+  c->rs_iph = p->rs;
+  c->i0 = p->i0;
+  c->rsh_rsum = p->rsh / rsum;
+  c->inv_rsum = 1.0 / rsum;
+  c->a_over_rs = p->a / p->rs;
+  c->k_gd = rsum / (p->rs * p->rsh);
+  c->inv_rsh = 1.0 / p->rsh;
+  c->rs = p->rs;
+}
+
+// Terminal current I(V) (out of the + terminal), dI/dV and dI/dIph.  With
+// w = W(theta) = Rs Rsh I0 / (a (Rs + Rsh)) * exp(Vd / a), Vd = V + I Rs:
+//   I = Rsh (Iph + I0) / (Rs + Rsh) - V / (Rs + Rsh) - (a / Rs) w,
+//   gd = dIdiode/dVd + 1/Rsh = w (Rs + Rsh) / (Rs Rsh) + 1/Rsh,
+//   dI/dV = -gd / (1 + Rs gd),  dI/dIph = 1 / (1 + Rs gd).
+PVGLU_HD void pvglu_panel_eval(const pvglu_panel_const* c, double iph, double v,
+                               double* current, double* didv, double* didiph) {
+  const double ip = iph + c->i0;
+  const double log_theta = c->log_c + c->k_l0 * (c->rs_iph * ip + v);
+  const double w = pvglu_lambert_w0_exp(log_theta);
+  const double i = c->rsh_rsum * ip - v * c->inv_rsum - c->a_over_rs * w;
+  const double gd = w * c->k_gd + c->inv_rsh;
+  const double q = 1.0 / (1.0 + c->rs * gd);
+  *current = i;
+  *didv = -gd * q;
+  *didiph = q;
+}
+
 PVGLU_HD void pvglu_panel_iv3(const pvglu_panel_params* p, double iph, double v,
                               double* current, double* didv, double* didiph) {
-  const double rs = p->rs, rsh = p->rsh, a = p->a, i0 = p->i0;
-  const double rsum = rs + rsh;
-  const double log_theta = pvglu_log(rs * rsh * i0 / (a * rsum)) +
-                           rsh * (rs * (iph + i0) + v) / (a * rsum);
-  const double w = pvglu_lambert_w0_exp(log_theta);
-  const double i = (rsh * (iph + i0) - v) / rsum - (a / rs) * w;
-  // Implicit derivatives: with gd = dIdiode/dVd + 1/Rsh at Vd = V + I*Rs,
-  // dI/dV = -gd / (1 + Rs*gd) and dI/dIph = 1 / (1 + Rs*gd).
-  const double vd = v + i * rs;
-  const double gd = i0 / a * pvglu_exp(vd / a) + 1.0 / rsh;
-  *current = i;
-  *didv = -gd / (1.0 + rs * gd);
-  *didiph = 1.0 / (1.0 + rs * gd);
+  pvglu_panel_const c;
+  pvglu_panel_prepare(p, &c);
+  pvglu_panel_eval(&c, iph, v, current, didv, didiph);
 }
 
 // Terminal current I(V) (out of the + terminal) and dI/dV.

@@ -173,6 +173,30 @@ def test_batched_plant_fp64(cuda, dims, S, schedule):
         assert norm_err(x[:, k], x_ref) <= TOL64, k
 
 
+@pytest.mark.parametrize("ld_scenarios", [1, 40])
+def test_fp32_scatter_rounds_like_numpy(cuda, ld_scenarios):
+    """The FP32 scatter converts FP64 values on the integer pipes: round to
+    nearest even for normal floats, signed zero below 2^-126, +-inf past the
+    float range; numpy's float32 cast is the reference for everything else."""
+    p = Plant(2, 4, 10)
+    s = Symbolic(p.rowptr, p.colidx)
+    num = Numeric(s, ld_scenarios, FP32, SCHED_LEVELS)
+    rng = np.random.default_rng(4)
+    a = rng.standard_normal((int(s.nnz_a), ld_scenarios)) * 10.0 ** rng.integers(-45, 45, (
+        int(s.nnz_a), ld_scenarios))
+    a[:8, 0] = [0.0, -0.0, 1.0 + 2.0 ** -24, 1.0 + 3 * 2.0 ** -24, 3.5e38, -1e39, 1e-40, np.nan]
+    num.scatter(dev(pad_cols(a, num.ld)))
+    got = values_of(num, int(s.nnz_lu))[:, :ld_scenarios]
+    src = s.array("slot_src")
+    want = np.zeros_like(got)
+    with np.errstate(over="ignore"):
+        cast = a.astype(np.float32).astype(np.float64)
+    cast[np.abs(a) < 2.0 ** -126] = 0.0
+    want[src >= 0] = cast[src[src >= 0]]
+    same = (got == want) | (np.isnan(got) & np.isnan(want))
+    assert same.all(), np.argwhere(~same)[:5]
+
+
 @pytest.mark.parametrize("schedule", SCHEDULES)
 def test_plant_35k_fp64(cuda, schedule):
     """The ~35k-unknown plant (50 x 24 x 28): single instance and a batch."""
