@@ -163,7 +163,8 @@ def cpu_baseline(a: np.ndarray, b: np.ndarray, p, sym_perm, budget_s: float, thr
                       f"one scenario per thread"}
 
 
-def newton_section(p, sym, stream, S: int, seed0: int, fd_check: bool = True) -> dict:
+def newton_section(p, sym, stream, S: int, seed0: int, fd_check: bool = True,
+                   precision: str = "fp32") -> dict:
     """Device Newton driver over the reference's gmin stages (tolerance
     1e-6 * n, the reference's) for S scenarios with FP32 factors + FP64
     refinement, then the adjoint dP/dG of the plant power for every panel;
@@ -171,13 +172,15 @@ def newton_section(p, sym, stream, S: int, seed0: int, fd_check: bool = True) ->
     solves (3-scenario handle, tolerance 1e-7 on the summed voltage change)."""
     import torch
 
-    from phdthesis_albertojimenezruiz_gb300 import FP32, SCHED_PERSISTENT, Newton, Numeric
+    from phdthesis_albertojimenezruiz_gb300 import (FP32, FP64, SCHED_PERSISTENT, Newton,
+                                                    Numeric)
 
     dev = torch.device("cuda", torch.cuda.current_device())
     g_to_iph = p.info["iph_stc"] / 1000.0
+    prec = FP64 if precision == "fp64" else FP32
 
-    def setup(g_cols, tol_ir=1e-10):
-        num = Numeric(sym, g_cols.shape[1], FP32, SCHED_PERSISTENT)
+    def setup(g_cols, tol_ir=1e-12):
+        num = Numeric(sym, g_cols.shape[1], prec, SCHED_PERSISTENT)
         nw = Newton.for_plant(num, p)
         ld = num.ld
         iph = np.zeros((p.n_panels, ld))
@@ -187,7 +190,8 @@ def newton_section(p, sym, stream, S: int, seed0: int, fd_check: bool = True) ->
         iph_d = torch.from_numpy(iph).to(dev)
         v0_d = torch.from_numpy(v0).to(dev)
         nw.set_iph(iph_d, stream=stream)
-        nw.set_refinement(tol_ir, IR_MAX_SWEEPS)
+        if prec == FP32:
+            nw.set_refinement(tol_ir, IR_MAX_SWEEPS)
         return num, nw, v0_d, iph_d
 
     g = np.stack([p.irradiance(seed=seed0 + s, preset="c2") for s in range(S)], axis=1)
@@ -214,8 +218,9 @@ def newton_section(p, sym, stream, S: int, seed0: int, fd_check: bool = True) ->
     it, out, _ = nw.results()
     bodies, graph = nw.last_run()
     newton_ms = e0.elapsed_time(e1)
-    res = {"workload": f"plant_{DIMS[0]}x{DIMS[1]}x{DIMS[2]}, {S} scenarios, FP32 LU + FP64 "
-                       "refinement, gmin stages 100..0.05,off, tol 1e-6*n",
+    lu = "FP64 LU" if prec == FP64 else "FP32 LU + FP64 refinement"
+    res = {"workload": f"plant_{DIMS[0]}x{DIMS[1]}x{DIMS[2]}, {S} scenarios, {lu}, "
+                       "gmin stages 100..0.05,off, tol 1e-6*n",
            "scenarios": S, "iterations_min": int(it.min()), "iterations_max": int(it.max()),
            "converged": int((out == 0).sum()), "bodies_launched": bodies, "cuda_graph": graph,
            "newton_ms": newton_ms,
@@ -302,6 +307,8 @@ def main() -> None:
                     help="scenarios of the device Newton + adjoint section (0: skip)")
     ap.add_argument("--only-newton", action="store_true",
                     help="run the Newton + adjoint section alone (profiling runs)")
+    ap.add_argument("--newton-precision", default="fp64", choices=["fp64", "fp32"],
+                    help="factor precision of the Newton section")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     IR_TOL, IR_MAX_SWEEPS = args.ir_tol, args.ir_sweeps
@@ -330,7 +337,7 @@ def main() -> None:
         p = Plant(*DIMS)
         sym = Symbolic(p.rowptr, p.colidx)
         res = newton_section(p, sym, torch.cuda.current_stream(), args.newton_scenarios, 5000,
-                             fd_check=False)
+                             fd_check=False, precision=args.newton_precision)
         if rank == 0:
             print(json.dumps(res))
         return
@@ -480,7 +487,8 @@ def main() -> None:
         if dist:
             dist.destroy_process_group()
         return
-    newton = (newton_section(p, sym, stream, args.newton_scenarios, 5000)
+    newton = (newton_section(p, sym, stream, args.newton_scenarios, 5000,
+                             precision=args.newton_precision)
               if args.newton_scenarios > 0 else None)
     cpu = cpu_baseline(a[:, :S], b[:, :S], p, sym.array("perm_amd"), args.cpu_budget,
                        os.cpu_count() or 1, prefer_ref=True)

@@ -194,7 +194,9 @@ int pvglu_scatter_refactor_solve_host(pvglu_numeric* h, const double* a_values_h
  * h (pvglu_scatter + pvglu_refactor done on an FP32 handle), refining in FP64:
  * r = b - J x with J from a_values (FP64, [nnz_a * ld]), correction solved in
  * FP32, accumulated in FP64.  Stops per scenario when
- * max|dx| <= tol * max|x|, after at most max_sweeps sweeps.  b, x: FP64
+ * max|dx| <= tol * max|x|, or when the error left after the sweep,
+ * estimated as max|dx| rho / (1 - rho) with rho = max|dx_k| / max|dx_k-1|
+ * <= 1/2, is <= tol * max|x|; after at most max_sweeps sweeps.  b, x: FP64
  * device [n * ld].  sweeps_out (device int[ld], may be NULL) receives the
  * sweeps per scenario; -1 marks a scenario that did not converge. */
 int pvglu_solve_refined(pvglu_numeric* h, const double* a_values, const double* b,

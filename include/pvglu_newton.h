@@ -71,8 +71,9 @@ int pvglu_newton_set_iph(pvglu_newton* nw, const double* iph, void* stream);
 int pvglu_newton_set_voltages(pvglu_newton* nw, const double* v, void* stream);
 
 /* Iteration of FP32 handles: refinement tolerance and sweep limit of each
- * linear solve (defaults 1e-10, 8; the Newton iteration itself removes what
- * a looser linear solve leaves). */
+ * linear solve (defaults 1e-12, 8).  Each Newton step solves for the node
+ * voltages themselves, not for a correction, so this tolerance bounds the
+ * accuracy of the converged operating point. */
 int pvglu_newton_set_refinement(pvglu_newton* nw, double tol, int max_sweeps);
 
 /* Runs the damped Newton iteration from the current voltage iterate over the

@@ -247,14 +247,14 @@ int run_refine(pvglu_numeric* h, const AValues& A, const double* b, double* x, b
   for (int sweep = 1; sweep <= max_sweeps; sweep++) {
     int rc = solve_permuted<float>(h, w, transpose, st, skip);  // dx of this sweep
     if (rc) return rc;
-    k_ir_update<<<grd, blk, 0, st>>>(out_perm, h->n, h->ld, h->S, w, x, h->ir_done,
+    k_ir_update<<<grd, blk, 0, st>>>(out_perm, h->n, h->ld, h->S, w, x, h->ir_done, ndone,
                                      h->ir_max_dx, h->ir_max_x);
     k_ir_check<<<(h->S + 127) / 128, 128, 0, st>>>(h->S, sweep, max_sweeps, tol, h->ir_done,
                                                    ndone, sweeps_out, h->ir_max_dx,
-                                                   h->ir_max_x);
+                                                   h->ir_max_x, h->ir_prev_dx);
     if (sweep < max_sweeps)  // residual of the scenarios still refining
       k_residual<<<rows_grid(h->n, h->ld, 256), 256, 0, st>>>(
-          r_ptr, r_idx, r_ent, h->n, h->ld, h->S, A, b, x, h->ir_done, w, r_pos);
+          r_ptr, r_idx, r_ent, h->n, h->ld, h->S, A, b, x, h->ir_done, ndone, w, r_pos);
   }
   PVGLU_CUDA(cudaGetLastError());
   return PVGLU_OK;
@@ -436,6 +436,7 @@ int pvglu_numeric_create(const pvglu_symbolic* sym, int n_scenarios, int precisi
   rc |= h->alloc((size_t)h->ld + 1, &h->ir_done);  // [ld] flags + converged count
   rc |= h->alloc((size_t)h->ld, &h->ir_max_dx);
   rc |= h->alloc((size_t)h->ld, &h->ir_max_x);
+  rc |= h->alloc((size_t)h->ld, &h->ir_prev_dx);
   rc |= h->alloc(4, &h->barrier);
   if (rc) {
     const std::string e = g_err;

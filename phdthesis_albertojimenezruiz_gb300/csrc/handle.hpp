@@ -61,6 +61,7 @@ struct pvglu_numeric {
   int* ir_done = nullptr;
   unsigned long long* ir_max_dx = nullptr;
   unsigned long long* ir_max_x = nullptr;
+  double* ir_prev_dx = nullptr;  // max|dx| of the previous sweep
   // Host copies of the level starts (launch ranges).
   std::vector<int> lu_sl, l_sl, u_sl, lt_sl;
   // Chain programs: refactor, L, U, U^T, L^T (programs.hpp).

@@ -301,8 +301,9 @@ __global__ void k_permute(const int* __restrict__ perm, int n, int ld, int S,
 static __global__ void k_residual(const int* __restrict__ ptr, const int* __restrict__ idx,
                            const int* __restrict__ ent, int n, int ld, int S, AValues A,
                            const double* __restrict__ b, const double* __restrict__ x,
-                           const int* __restrict__ done, float* __restrict__ r_perm,
-                           const int* __restrict__ pos) {
+                           const int* __restrict__ done, const int* __restrict__ ndone,
+                           float* __restrict__ r_perm, const int* __restrict__ pos) {
+  if (__ldcg(ndone) >= S) return;
   for_rows(n, ld, [&](int i, int s) {
     if (s >= S || done[s]) return;
     double acc = b[(int64_t)i * ld + s];
@@ -320,9 +321,10 @@ static __global__ void k_residual(const int* __restrict__ ptr, const int* __rest
 // the addition.
 static __global__ void k_ir_update(const int* __restrict__ out_perm, int n, int ld, int S,
                             const float* __restrict__ dx, double* __restrict__ x,
-                            const int* __restrict__ done,
+                            const int* __restrict__ done, const int* __restrict__ ndone,
                             unsigned long long* __restrict__ max_dx,
                             unsigned long long* __restrict__ max_x) {
+  if (__ldcg(ndone) >= S) return;
   // block = (32 scenarios) x (8 rows); grid-stride over row tiles.
   const int s = blockIdx.y * 32 + threadIdx.x;
   __shared__ unsigned int sdx[8][33], sx[8][33];
@@ -367,17 +369,30 @@ static __global__ void k_ir_init(int n, int ld, int S, const int* __restrict__ s
   });
 }
 
-// Convergence bookkeeping after sweep `sweep` (1-based).
+// Convergence bookkeeping after sweep `sweep` (1-based).  A scenario stops
+// when its correction is small, max|dx_k| <= tol max|x|, or when the error
+// left after it is: with rho = max|dx_k| / max|dx_k-1| <= 1/2 the corrections
+// shrink geometrically and the remaining error is about
+// max|dx_k| rho / (1 - rho) (the stopping estimate of iterative-refinement
+// analyses), so the sweep that would only confirm it is skipped.
 static __global__ void k_ir_check(int S, int sweep, int last_sweep, double tol, int* done,
-                           int* ndone, int* sweeps_out, unsigned long long* max_dx,
-                           unsigned long long* max_x) {
+                                  int* ndone, int* sweeps_out, unsigned long long* max_dx,
+                                  unsigned long long* max_x, double* prev_dx) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= S || done[s]) return;
   const double mdx = __longlong_as_double((long long)max_dx[s]);
   const double mx = __longlong_as_double((long long)max_x[s]);
   max_dx[s] = 0ull;
   max_x[s] = 0ull;
-  const bool ok = mdx <= tol * mx;
+  bool ok = mdx <= tol * mx;
+  if (!ok && sweep > 1) {
+    const double prev = prev_dx[s];
+    if (prev > 0.0 && mdx <= 0.5 * prev) {
+      const double rho = mdx / prev;
+      ok = mdx * rho <= tol * mx * (1.0 - rho);
+    }
+  }
+  prev_dx[s] = mdx;
   if (ok) {
     done[s] = 1;
     atomicAdd(ndone, 1);

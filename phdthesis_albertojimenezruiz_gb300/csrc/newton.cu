@@ -117,7 +117,17 @@ __device__ __forceinline__ double damped_step(double old, double nv, bool* bad,
       return nv;
     }
   }
+  // Every step factor m = 2^-j with m |nv - old| >= 4 fails the 1 V test
+  // whatever the rounding, so the halving starts at 2^-(e-1), e the binary
+  // exponent of |nv - old|; the first factor that passes is the one the
+  // full halving from m = 1 would reach.  Non-finite values take the full
+  // loop.
   double m = 1.0;
+  if (finite_bits(old) && finite_bits(nv)) {
+    const long long db = __double_as_longlong(__dsub_rn(old, nv)) & 0x7fffffffffffffffLL;
+    const int e = (int)(db >> 52) - 1023;
+    if (e > 1) m = __longlong_as_double((long long)(1023 - (e - 1)) << 52);
+  }
   for (;;) {
     const double t = __dadd_rn(__dmul_rn(old, __dsub_rn(1.0, m)), __dmul_rn(nv, m));
     if (m < 1e-13) {
@@ -185,15 +195,21 @@ __global__ void __launch_bounds__(256) k_nt_update(NtDev D, const double* __rest
 
 // End of an iteration for every running scenario: diff, stage advance
 // (000_PVPP_simulator.cpp:172-176: a stage ends once diff < tol), outcome.
+// One warp per scenario: lane l adds the chunk sums l, l + 32, ... in order,
+// then the 32 lane sums are added in a fixed tree order (deterministic).
 __global__ void k_nt_check(NtDev D, int n_chunks) {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
   if (s >= D.S) return;
   if (D.done[s]) {
-    D.just_done[s] = 0;
+    if (lane == 0) D.just_done[s] = 0;
     return;
   }
-  double diff = 0.0;
-  for (int c = 0; c < n_chunks; c++) diff += D.partial[(int64_t)c * D.ld + s];
+  double part = 0.0;
+  for (int c = lane; c < n_chunks; c += 32) part += D.partial[(int64_t)c * D.ld + s];
+  for (int off = 16; off > 0; off >>= 1) part += __shfl_down_sync(0xffffffffu, part, off);
+  if (lane != 0) return;
+  const double diff = part;
   D.diff[s] = diff;
   const int it = ++D.iters[s];
   int out = PVGLU_NEWTON_RUNNING;
@@ -284,7 +300,7 @@ struct pvglu_newton {
                                 // FP64: saved when a scenario stops)
   double* lam = nullptr;        // adjoint vector
   int* pinned_ndone = nullptr;  // host-pinned copy of the stopped count
-  double ir_tol = 1e-10;
+  double ir_tol = 1e-12;
   int ir_sweeps = 8;
   // Captured iteration body and what it was captured with.
   cudaStream_t cap_stream = nullptr;
@@ -349,7 +365,7 @@ int newton_body(pvglu_newton* nw, cudaStream_t st) {
   const dim3 ublk(32, pvglu::kUpdRows);
   const dim3 ugrd((unsigned)nw->n_chunks, D.ld == 1 ? 1u : (unsigned)(D.ld / 32));
   pvglu::k_nt_update<<<ugrd, ublk, 0, st>>>(D, X, xpos);
-  pvglu::k_nt_check<<<(D.S + 127) / 128, 128, 0, st>>>(D, nw->n_chunks);
+  pvglu::k_nt_check<<<(D.S + 3) / 4, 128, 0, st>>>(D, nw->n_chunks);
   if (fp64)
     pvglu::k_nt_keep<<<pvglu::rows_grid(D.n, D.ld, 256), 256, 0, st>>>(D, nw->w64, h->col_pos,
                                                                          nw->x64);

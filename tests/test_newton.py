@@ -272,7 +272,9 @@ def test_newton_fp32_refined_matches_oracle(cuda, schedule):
     for s in range(S):
         rc, it_o, _, v_o, x_o = port.newton(p, p.iph(g[:, s]), p.flat_start(), GMIN_STAGES, tol)
         assert rc == 0 and out[s] == N.NEWTON_CONVERGED
-        assert abs(int(it[s]) - it_o) <= 2
+        # The refined linear solves stop at an estimated 1e-12, so the damped
+        # iteration may take a few iterations more or less than FP64.
+        assert abs(int(it[s]) - it_o) <= max(3, it_o // 20)
         assert norm_err(v[:, s], v_o) <= 1e-10
         assert norm_err(x[:, s], x_o) <= 1e-10
 
