@@ -240,6 +240,9 @@ int run_refine(pvglu_numeric* h, const AValues& A, const double* b, double* x, b
   const int* r_idx = transpose ? h->at_row : h->d.a_colidx;
   const int* r_ent = transpose ? h->at_entry : nullptr;
   const int* r_pos = transpose ? h->col_pos : h->row_pos;
+  // 16-byte vector loads in the batched residual.
+  const bool vec16 = !((reinterpret_cast<uintptr_t>(A.a) | reinterpret_cast<uintptr_t>(b) |
+                        reinterpret_cast<uintptr_t>(x)) & 15);
   // x = 0: the first residual is b itself.
   permute<double, float>(h, in_perm, b, w, true, st);
   const dim3 blk(32, 8);
@@ -252,9 +255,14 @@ int run_refine(pvglu_numeric* h, const AValues& A, const double* b, double* x, b
     k_ir_check<<<(h->S + 127) / 128, 128, 0, st>>>(h->S, sweep, max_sweeps, tol, h->ir_done,
                                                    ndone, sweeps_out, h->ir_max_dx,
                                                    h->ir_max_x, h->ir_prev_dx);
-    if (sweep < max_sweeps)  // residual of the scenarios still refining
-      k_residual<<<rows_grid(h->n, h->ld, 256), 256, 0, st>>>(
-          r_ptr, r_idx, r_ent, h->n, h->ld, h->S, A, b, x, h->ir_done, ndone, w, r_pos);
+    if (sweep < max_sweeps) {  // residual of the scenarios still refining
+      if (A.a && h->ld % 64 == 0 && vec16)
+        k_residual_rows<<<rows_grid(h->n, h->ld, 256), 256, 0, st>>>(
+            r_ptr, r_idx, r_ent, h->n, h->ld, h->S, A.a, b, x, h->ir_done, ndone, w, r_pos);
+      else
+        k_residual<<<rows_grid(h->n, h->ld, 256), 256, 0, st>>>(
+            r_ptr, r_idx, r_ent, h->n, h->ld, h->S, A, b, x, h->ir_done, ndone, w, r_pos);
+    }
   }
   PVGLU_CUDA(cudaGetLastError());
   return PVGLU_OK;

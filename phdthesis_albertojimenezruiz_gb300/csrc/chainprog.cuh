@@ -14,6 +14,7 @@
 // lanes split the loads and stores of each segment (ld.global.cg), lane 0
 // executes the operations out of shared memory.
 #pragma once
+#include <type_traits>
 #include <cuda_runtime.h>
 
 #include "kernels.cuh"
@@ -136,7 +137,7 @@ __device__ __forceinline__ void decode_op(uint32_t op, int& code, int& a, int& b
 template <typename T>
 __device__ __forceinline__ void exec_op2(uint32_t op, int op_index, const int* op_col,
                                          typename Vec2<T>::type* t, int s0, int S,
-                                         double pivot_tol, DevStatus* st) {
+                                         T pivot_tol, DevStatus* st) {
   int code, a, b, c;
   decode_op(op, code, a, b, c);
   if (code == OP_FNMA) {
@@ -147,14 +148,26 @@ __device__ __forceinline__ void exec_op2(uint32_t op, int op_index, const int* o
     t[a << 5] = r;
   } else if (code == OP_SCALE) {
     const auto p = t[a << 5];
-    if (!(fabs((double)p.x) >= pivot_tol) && s0 < S) report_error(st, 3, op_col[op_index], s0);
-    if (!(fabs((double)p.y) >= pivot_tol) && s0 + 1 < S)
+    if (!(fabs(p.x) >= pivot_tol) && s0 < S) report_error(st, 3, op_col[op_index], s0);
+    if (!(fabs(p.y) >= pivot_tol) && s0 + 1 < S)
       report_error(st, 3, op_col[op_index], s0 + 1);
-    for (int i = 0; i < c; i++) {
-      auto q = t[(b + i) << 5];
-      q.x = q.x / p.x;
-      q.y = q.y / p.y;
-      t[(b + i) << 5] = q;
+    if constexpr (std::is_same<T, float>::value) {
+      // FP32 factors are refined afterwards: one reciprocal per pivot.
+      const float ix = __frcp_rn(p.x), iy = __frcp_rn(p.y);
+      for (int i = 0; i < c; i++) {
+        auto q = t[(b + i) << 5];
+        q.x *= ix;
+        q.y *= iy;
+        t[(b + i) << 5] = q;
+      }
+    } else {
+      // FP64 divides like the reference (GLU_CSC_CPU_levels_strings.cpp:60).
+      for (int i = 0; i < c; i++) {
+        auto q = t[(b + i) << 5];
+        q.x = q.x / p.x;
+        q.y = q.y / p.y;
+        t[(b + i) << 5] = q;
+      }
     }
   } else if (code == OP_DIV) {
     auto q = t[a << 5];
@@ -167,14 +180,14 @@ __device__ __forceinline__ void exec_op2(uint32_t op, int op_index, const int* o
 
 template <typename T>
 __device__ __forceinline__ void exec_op1(uint32_t op, int op_index, const int* op_col, T* t,
-                                         int S, double pivot_tol, DevStatus* st) {
+                                         int S, T pivot_tol, DevStatus* st) {
   int code, a, b, c;
   decode_op(op, code, a, b, c);
   if (code == OP_FNMA) {
     t[a] = fnms(t[a], t[b], t[c]);
   } else if (code == OP_SCALE) {
     const T p = t[a];
-    if (!(fabs((double)p) >= pivot_tol) && 0 < S) report_error(st, 3, op_col[op_index], 0);
+    if (!(fabs(p) >= pivot_tol) && 0 < S) report_error(st, 3, op_col[op_index], 0);
     for (int i = 0; i < c; i++) t[b + i] = t[b + i] / p;
   } else if (code == OP_DIV) {
     t[a] = t[a] / t[b];
@@ -193,7 +206,7 @@ template <typename T, int KIND, bool BATCH>
 __device__ __forceinline__ void prog_run_chain(const ProgDev& P, const DevStruct& d, int chain,
                                                T* __restrict__ v, T* __restrict__ x, int ld,
                                                int s0, int S, T* sm, WarpTma& tma,
-                                               double pivot_tol, DevStatus* st) {
+                                               T pivot_tol, DevStatus* st) {
   const int lane = threadIdx.x & 31;
   const int g_end = __ldg(P.chain_seg + chain + 1);
   for (int g = __ldg(P.chain_seg + chain); g < g_end; g++) {
@@ -287,7 +300,7 @@ template <typename T, int KIND, bool BATCH>
 __device__ __forceinline__ void prog_run_level(const ProgDev& P, const DevStruct& d, int cb,
                                                int ce, T* __restrict__ v, T* __restrict__ x,
                                                int ld, int S, T* sm_warp, WarpTma& tma,
-                                               double pivot_tol, DevStatus* st,
+                                               T pivot_tol, DevStatus* st,
                                                const int* done, int warp_id, int n_warps) {
   const int groups = BATCH ? ld / kGroup : 1;
   const int items = (ce - cb) * groups;
@@ -338,7 +351,7 @@ size_t prog_smem_bytes(int max_locals, int warps_per_block) {
 // ndone (or NULL): the launch does nothing once every scenario is done.
 template <typename T, int KIND, bool BATCH>
 __global__ void k_prog_level(ProgDev P, DevStruct d, int cb, int ce, T* __restrict__ v,
-                             T* __restrict__ x, int ld, int S, double pivot_tol, DevStatus* st,
+                             T* __restrict__ x, int ld, int S, T pivot_tol, DevStatus* st,
                              const int* done, const int* ndone) {
   if (ndone && __ldcg(ndone) >= S) return;
   extern __shared__ __align__(128) unsigned char smem_raw[];

@@ -88,7 +88,7 @@ constexpr int kProgWarps = kProgBlock / 32;
 template <typename T, int KIND, bool BATCH>
 __device__ __forceinline__ bool prog_phase(const ProgDev& P, const DevStruct& d, T* v, T* x,
                                            int ld, int S, T* sm, WarpTma& tma,
-                                           double pivot_tol, DevStatus* st, unsigned int* bar,
+                                           T pivot_tol, DevStatus* st, unsigned int* bar,
                                            const int* done, bool* need_sync) {
   const int warp_id = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int n_warps = (gridDim.x * blockDim.x) >> 5;
@@ -109,7 +109,7 @@ __device__ __forceinline__ bool prog_phase(const ProgDev& P, const DevStruct& d,
 template <typename T, bool BATCH>
 __global__ void __launch_bounds__(kProgBlock)
 k_prog_persistent(ProgSetDev PS, DevStruct d, T* __restrict__ v, T* __restrict__ x, int ld,
-                  int S, double pivot_tol, DevStatus* st, unsigned int* bar, int phases,
+                  int S, T pivot_tol, DevStatus* st, unsigned int* bar, int phases,
                   SkipDone skip) {
   if (skip.ndone && __ldcg(skip.ndone) >= S) return;
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -158,7 +158,7 @@ int prog_persistent_grid(int max_locals) {
 
 template <typename T, bool BATCH>
 int launch_prog_persistent(const ProgSetDev& PS, int max_chains, const DevStruct& d, T* v,
-                           T* x, int ld, int S, double pivot_tol, DevStatus* st,
+                           T* x, int ld, int S, T pivot_tol, DevStatus* st,
                            unsigned int* bar, int max_grid, int phases, cudaStream_t stream,
                            SkipDone skip) {
   if (max_grid <= 0) return 1;
