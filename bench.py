@@ -38,7 +38,7 @@ DIMS = (50, 24, 28)
 METRIC = "refactor+solve/s, 35k-unknown PV Jacobian: batched+FP32-IR vs plain FP64 GPU"
 UNIT = "refactor+solve/s"
 IR_TOL = 1e-12
-IR_MAX_SWEEPS = 8
+IR_MAX_SWEEPS = 6
 
 
 def _peaks() -> dict:
@@ -179,8 +179,16 @@ def newton_section(p, sym, stream, S: int, seed0: int, fd_check: bool = True,
     g_to_iph = p.info["iph_stc"] / 1000.0
     prec = FP64 if precision == "fp64" else FP32
 
+    from phdthesis_albertojimenezruiz_gb300.glu import autotune
+
+    tuned = {}
+
     def setup(g_cols, tol_ir=1e-12):
-        num = Numeric(sym, g_cols.shape[1], prec, SCHED_PERSISTENT)
+        count = g_cols.shape[1]
+        if count not in tuned:
+            tuned[count] = autotune(sym, count, prec)[:2]
+        ml, sc = tuned[count]
+        num = Numeric(sym, count, prec, sc, max_locals=ml)
         nw = Newton.for_plant(num, p)
         ld = num.ld
         iph = np.zeros((p.n_panels, ld))
@@ -221,7 +229,8 @@ def newton_section(p, sym, stream, S: int, seed0: int, fd_check: bool = True,
     lu = "FP64 LU" if prec == FP64 else "FP32 LU + FP64 refinement"
     res = {"workload": f"plant_{DIMS[0]}x{DIMS[1]}x{DIMS[2]}, {S} scenarios, {lu}, "
                        "gmin stages 100..0.05,off, tol 1e-6*n",
-           "scenarios": S, "iterations_min": int(it.min()), "iterations_max": int(it.max()),
+           "scenarios": S, "tuning": {"max_locals": tuned[S][0], "schedule": tuned[S][1]},
+           "iterations_min": int(it.min()), "iterations_max": int(it.max()),
            "converged": int((out == 0).sum()), "bodies_launched": bodies, "cuda_graph": graph,
            "newton_ms": newton_ms,
            "scenario_iterations_per_s": float(it.sum()) / (newton_ms / 1000.0),
@@ -309,6 +318,8 @@ def main() -> None:
                     help="run the Newton + adjoint section alone (profiling runs)")
     ap.add_argument("--newton-precision", default="fp64", choices=["fp64", "fp32"],
                     help="factor precision of the Newton section")
+    ap.add_argument("--max-locals", type=int, default=0,
+                    help="chain-program table size of the batched handle (0: default)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     IR_TOL, IR_MAX_SWEEPS = args.ir_tol, args.ir_sweeps
@@ -352,7 +363,16 @@ def main() -> None:
     b_d = torch.from_numpy(b).to(dev)
     x_d = torch.zeros_like(b_d)
     sweeps = torch.zeros(ld, dtype=torch.int32, device=dev)
-    num = Numeric(sym, S, FP32, SCHED_PERSISTENT)
+    from phdthesis_albertojimenezruiz_gb300.glu import autotune
+
+    if args.max_locals > 0:
+        tuned = {"max_locals": args.max_locals, "schedule": SCHED_PERSISTENT, "source": "flag"}
+    else:
+        ml, sc, tms = autotune(sym, S, FP32)
+        tuned = {"max_locals": ml, "schedule": sc, "ms_scatter_refactor_solve": tms,
+                 "source": "pvglu_autotune"}
+    num = Numeric(sym, S, FP32, tuned["schedule"], max_locals=tuned["max_locals"])
+    persistent = tuned["schedule"] == SCHED_PERSISTENT
     assert num.ld == ld
 
     def step():
@@ -402,7 +422,8 @@ def main() -> None:
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT,
                               "ms_per_step": ms / args.steps, "refactor_ms": refactor_ms,
-                              "scenarios": S, "sweeps_max": int(sw.max())}))
+                              "scenarios": S, "sweeps_max": int(sw.max()),
+                              "tuning": tuned}))
         if dist:
             dist.destroy_process_group()
         return
@@ -478,7 +499,9 @@ def main() -> None:
     peaks = _peaks()
     peak = peaks.get("hbm_gbs")
     achieved = bm["refactor"] * S / (refactor_ms / 1000.0) / 1e9
-    roofline = {"kernel": "k_persistent<float> (refactor phase)", "bound": "hbm",
+    roofline = {"kernel": ("k_prog_persistent<float,batched>" if persistent else
+                           "k_prog_level<float,refactor,batched>") + " (refactor phase)",
+                "bound": "hbm",
                 "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak if peak else None, "traffic": None,
                 "peak_source": "measured" if peak else "fallback",
@@ -492,8 +515,12 @@ def main() -> None:
               if args.newton_scenarios > 0 else None)
     cpu = cpu_baseline(a[:, :S], b[:, :S], p, sym.array("perm_amd"), args.cpu_budget,
                        os.cpu_count() or 1, prefer_ref=True)
-    # per step: scatter, refactor, permute b, then per sweep solve + step + check
-    launches = args.steps * (3 + 3 * IR_MAX_SWEEPS)
+    # per step: scatter, permute b, refactor, then per sweep (all launched;
+    # converged work exits at once) solve, update, check and residual.
+    refactor_launches = 1 if persistent else sym.info["lu_levels"]
+    solve_launches = 1 if persistent else sym.info["l_levels"] + sym.info["u_levels"]
+    launches = args.steps * (2 + refactor_launches +
+                             IR_MAX_SWEEPS * (solve_launches + 2) + IR_MAX_SWEEPS - 1)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
@@ -505,7 +532,7 @@ def main() -> None:
                    "scenarios_per_step": S, "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2 (FP64 Jacobian values "
                          f"{8 * nnz_a * ld / 1e6:.0f} MB per batch)",
-                   "ir_tol": IR_TOL, "ir_max_sweeps": IR_MAX_SWEEPS},
+                   "ir_tol": IR_TOL, "ir_max_sweeps": IR_MAX_SWEEPS, "tuning": tuned},
         "ir": {"sweeps_min": int(sw.min()), "sweeps_max": int(sw.max()),
                "not_converged": int((sw <= 0).sum()), "max_rel_err_vs_fp64": max_rel},
         "plain_fp64": {"value": plain, "unit": UNIT, "schedule": plain_name,

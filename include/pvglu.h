@@ -117,6 +117,16 @@ int pvglu_symbolic_get_array(const pvglu_symbolic* s, const char* name,
  * Replaces struct_CPU_CUDA_arrays::create_CUDA (factorize_electrical_system.h:63-98). */
 int pvglu_numeric_create(const pvglu_symbolic* s, int n_scenarios, int precision,
                          pvglu_numeric** out);
+/* As pvglu_numeric_create with the table size of the chain programs:
+ * max_locals values staged in shared memory per warp and segment (0: the
+ * default, 64 for batched FP32, 40 for batched FP64, 1023 for one scenario).
+ * Smaller tables give more resident warps and more segments per chain.
+ * PVGLU_ERR_BAD_ARG if the table does not fit in shared memory.  No
+ * counterpart in the reference (its kernels read every value from global
+ * memory). */
+int pvglu_numeric_create_ex(const pvglu_symbolic* s, int n_scenarios, int precision,
+                            int max_locals, pvglu_numeric** out);
+int pvglu_numeric_max_locals(const pvglu_numeric* h);
 int pvglu_numeric_destroy(pvglu_numeric* h);
 int pvglu_numeric_ld(const pvglu_numeric* h);
 /* Device pointer to the LU values (double* for FP64, float* for FP32). */
@@ -239,6 +249,18 @@ int pvglu_refine_system_host(pvglu_numeric* h, const double* a_values_host,
  * on the GPU (other streams, other threads) race on the array.
  * No counterpart in the reference. */
 int pvglu_solve_noalloc(pvglu_numeric* h, double* x, int flags, void* stream);
+
+/* ---------------- autotuner ---------------------------------------------- */
+
+/* Times scatter + refactor + solve for n_scenarios on this device over the
+ * chain-program table sizes and the schedules, with diagonally dominant
+ * stand-in values on s's pattern, and returns the fastest combination (for
+ * pvglu_numeric_create_ex and pvglu_numeric_set_schedule) and its time per
+ * call in ms.  Synchronous; allocates and frees temporary handles.  No
+ * counterpart in the reference (its launch shape is fixed by the >64-entry
+ * rule of 009_get_max_numbers_per_column.cpp). */
+int pvglu_autotune(const pvglu_symbolic* s, int n_scenarios, int precision,
+                   int* best_max_locals, int* best_schedule, double* best_ms);
 
 /* ---------------- failure-path self-test --------------------------------- */
 

@@ -69,6 +69,8 @@ _SIGS = {
     "pvglu_symbolic_get_info": ([_P, C.POINTER(SymbolicInfo)], _I),
     "pvglu_symbolic_get_array": ([_P, C.c_char_p, C.POINTER(_IP), C.POINTER(C.c_int64)], _I),
     "pvglu_numeric_create": ([_P, _I, _I, C.POINTER(_P)], _I),
+    "pvglu_numeric_create_ex": ([_P, _I, _I, _I, C.POINTER(_P)], _I),
+    "pvglu_numeric_max_locals": ([_P], _I),
     "pvglu_numeric_destroy": ([_P], _I),
     "pvglu_numeric_ld": ([_P], _I),
     "pvglu_numeric_values": ([_P], _P),
@@ -84,6 +86,7 @@ _SIGS = {
     "pvglu_scatter_refactor_solve_host": ([_P, _P, _P, _P, _P], _I),
     "pvglu_solve_refined": ([_P, _P, _P, _P, C.c_double, _I, _P, _P], _I),
     "pvglu_selftest_barrier_timeout": ([_I, C.c_longlong, _IP, _IP], _I),
+    "pvglu_autotune": ([_P, _I, _I, _IP, _IP, _DP], _I),
     "pvglu_refine_system_host": ([_P, _P, _P, _P, C.c_double, _I, _P, _P], _I),
     "pvglu_solve_noalloc": ([_P, _P, _I, _P], _I),
     "pvglu_numeric_set_stamps": ([_P, _I, _P, _P, _P, _P], _I),

@@ -246,7 +246,13 @@ int run_refine(pvglu_numeric* h, const AValues& A, const double* b, double* x, b
   // x = 0: the first residual is b itself.
   permute<double, float>(h, in_perm, b, w, true, st);
   const dim3 blk(32, 8);
-  const dim3 grd((unsigned)std::min(1024, (h->n + 7) / 8), (unsigned)(h->ld + 31) / 32);
+  // About one full SM of threads per SM: the launches after every scenario
+  // has converged (ndone == S) then cost little.
+  const int gy = (h->ld + 31) / 32;
+  const int fill = std::max(1, h->sm_count * 8);
+  const dim3 grd((unsigned)std::max(1, std::min((h->n + 7) / 8, (fill + gy - 1) / gy)),
+                 (unsigned)gy);
+  const int rgrid = std::min(rows_grid(h->n, h->ld, 256), fill);
   for (int sweep = 1; sweep <= max_sweeps; sweep++) {
     int rc = solve_permuted<float>(h, w, transpose, st, skip);  // dx of this sweep
     if (rc) return rc;
@@ -257,7 +263,7 @@ int run_refine(pvglu_numeric* h, const AValues& A, const double* b, double* x, b
                                                    h->ir_max_x, h->ir_prev_dx);
     if (sweep < max_sweeps) {  // residual of the scenarios still refining
       if (A.a && h->ld % 64 == 0 && vec16)
-        k_residual_rows<<<rows_grid(h->n, h->ld, 256), 256, 0, st>>>(
+        k_residual_rows<<<rgrid, 256, 0, st>>>(
             r_ptr, r_idx, r_ent, h->n, h->ld, h->S, A.a, b, x, h->ir_done, ndone, w, r_pos);
       else
         k_residual<<<rows_grid(h->n, h->ld, 256), 256, 0, st>>>(
@@ -345,9 +351,17 @@ int pvglu_symbolic_get_array(const pvglu_symbolic* h, const char* name, const in
 
 int pvglu_numeric_create(const pvglu_symbolic* sym, int n_scenarios, int precision,
                          pvglu_numeric** out) {
+  return pvglu_numeric_create_ex(sym, n_scenarios, precision, 0, out);
+}
+
+int pvglu_numeric_create_ex(const pvglu_symbolic* sym, int n_scenarios, int precision,
+                            int max_locals, pvglu_numeric** out) {
   if (!sym || !out || n_scenarios <= 0 ||
-      (precision != PVGLU_FP64 && precision != PVGLU_FP32))
+      (precision != PVGLU_FP64 && precision != PVGLU_FP32) || max_locals < 0 ||
+      max_locals > pvglu::kMaxLocals)
     return fail(PVGLU_ERR_BAD_ARG, "bad numeric_create arguments");
+  if (max_locals > 0 && max_locals < 8)
+    return fail(PVGLU_ERR_BAD_ARG, "max_locals must be 0 (default) or >= 8");
   *out = nullptr;
   const auto& s = sym->s;
   if (s.update_count > 0x7fffffffLL) return fail(PVGLU_ERR_TOO_LARGE, "update list > 2^31");
@@ -460,7 +474,30 @@ int pvglu_numeric_create(const pvglu_symbolic* sym, int n_scenarios, int precisi
   // Chain programs for the shared-memory schedules.  Table budget: a warp's
   // tile is max_locals x 32 scenarios (batched) or max_locals (single).
   h->batch = h->ld > 1;
-  h->max_locals = h->batch ? (precision == PVGLU_FP32 ? 64 : 40) : pvglu::kMaxLocals;
+  {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      h->sm_count = 1;
+  }
+  h->max_locals = max_locals > 0 ? max_locals
+                                 : (h->batch ? (precision == PVGLU_FP32 ? 64 : 40)
+                                             : pvglu::kMaxLocals);
+  {
+    const size_t smem = precision == PVGLU_FP64
+                            ? (h->batch ? pvglu::prog_smem_bytes<double, true>(h->max_locals,
+                                                                               pvglu::kProgWarps)
+                                        : pvglu::prog_smem_bytes<double, false>(
+                                              h->max_locals, pvglu::kProgWarps))
+                            : (h->batch ? pvglu::prog_smem_bytes<float, true>(h->max_locals,
+                                                                              pvglu::kProgWarps)
+                                        : pvglu::prog_smem_bytes<float, false>(
+                                              h->max_locals, pvglu::kProgWarps));
+    if (smem > 227 * 1024) {
+      delete h;
+      return fail(PVGLU_ERR_BAD_ARG, "max_locals too large for shared memory");
+    }
+  }
   for (int ph = 0; ph < 5; ph++) {
     pvglu::ChainProgram prog;
     pvglu::build_chain_program(s, ph - 1, h->max_locals, prog);
@@ -511,6 +548,7 @@ int pvglu_numeric_destroy(pvglu_numeric* h) {
 }
 
 int pvglu_numeric_ld(const pvglu_numeric* h) { return h ? h->ld : 0; }
+int pvglu_numeric_max_locals(const pvglu_numeric* h) { return h ? h->max_locals : 0; }
 void* pvglu_numeric_values(pvglu_numeric* h) { return h ? h->values : nullptr; }
 
 int pvglu_numeric_set_schedule(pvglu_numeric* h, int schedule) {
@@ -756,6 +794,78 @@ int pvglu_solve_noalloc(pvglu_numeric* h, double* x, int flags, void* stream) {
   if (rc) return rc;
   permute<double, double>(h, out_perm, w, x, false, st);
   PVGLU_CUDA(cudaGetLastError());
+  return PVGLU_OK;
+}
+
+int pvglu_autotune(const pvglu_symbolic* sym, int n_scenarios, int precision,
+                   int* best_max_locals, int* best_schedule, double* best_ms) {
+  if (!sym || n_scenarios <= 0 || !best_max_locals || !best_schedule ||
+      (precision != PVGLU_FP64 && precision != PVGLU_FP32))
+    return fail(PVGLU_ERR_BAD_ARG, "bad autotune arguments");
+  const auto& s = sym->s;
+  const int ld = n_scenarios == 1 ? 1 : ((n_scenarios + 63) / 64) * 64;
+  // Row-diagonally-dominant values (diagonal n + 1, every other entry -1):
+  // the factorization without pivoting is stable and the timing is that of
+  // any Jacobian with this pattern.
+  std::vector<double> a1(s.nnz_a);
+  for (int i = 0; i < s.n; i++)
+    for (int p = s.a_rowptr[i]; p < s.a_rowptr[i + 1]; p++)
+      a1[p] = s.a_colidx[p] == i ? (double)s.n + 1.0 : -1.0;
+  std::vector<double> ah((size_t)s.nnz_a * ld);
+  for (int64_t p = 0; p < s.nnz_a; p++)
+    for (int k = 0; k < ld; k++) ah[(size_t)p * ld + k] = a1[p];
+  double* ad = nullptr;
+  if (upload(ah, &ad)) return fail(PVGLU_ERR_NO_MEMORY, "autotune buffers");
+  std::vector<int> cands;
+  if (ld == 1) cands = {0, 256, 64};
+  else if (precision == PVGLU_FP32) cands = {16, 24, 32, 48, 64};
+  else cands = {16, 24, 32, 40, 56};
+  const int scheds[2] = {PVGLU_SCHED_LEVELS, PVGLU_SCHED_PERSISTENT};
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  double best = 1e300;
+  int bml = 0, bs = PVGLU_SCHED_LEVELS;
+  const size_t xbytes = (size_t)s.n * ld * (precision == PVGLU_FP64 ? 8 : 4);
+  void* xw = nullptr;
+  int rc = cudaMalloc(&xw, xbytes) == cudaSuccess ? PVGLU_OK : PVGLU_ERR_NO_MEMORY;
+  for (size_t ci = 0; !rc && ci < cands.size(); ci++) {
+    pvglu_numeric* h = nullptr;
+    if (pvglu_numeric_create_ex(sym, n_scenarios, precision, cands[ci], &h)) continue;
+    for (int sc : scheds) {
+      if (pvglu_numeric_set_schedule(h, sc)) continue;
+      float total = 0.f;
+      bool ok = true;
+      for (int rep = 0; rep < 4 && ok; rep++) {
+        cudaMemsetAsync(xw, 0, xbytes, nullptr);
+        cudaEventRecord(e0, nullptr);
+        ok = pvglu_scatter(h, ad, nullptr) == PVGLU_OK &&
+             pvglu_refactor_solve(h, xw, 0, nullptr) == PVGLU_OK;
+        cudaEventRecord(e1, nullptr);
+        if (cudaEventSynchronize(e1) != cudaSuccess) ok = false;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep > 0) total += ms;  // the first repetition warms up
+      }
+      if (ok && total / 3 < best) {
+        best = total / 3;
+        bml = h->max_locals;
+        bs = sc;
+      }
+    }
+    int code = 0, col = 0, scn = 0;
+    pvglu_numeric_check(h, nullptr, &code, &col, &scn);
+    pvglu_numeric_destroy(h);
+  }
+  cudaFree(xw);
+  cudaFree(ad);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) return fail(rc, "autotune allocation failed");
+  if (best >= 1e300) return fail(PVGLU_ERR_CUDA, "no autotune candidate ran");
+  *best_max_locals = bml;
+  *best_schedule = bs;
+  if (best_ms) *best_ms = best;
   return PVGLU_OK;
 }
 

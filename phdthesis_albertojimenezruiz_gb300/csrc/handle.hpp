@@ -66,6 +66,7 @@ struct pvglu_numeric {
   std::vector<int> lu_sl, l_sl, u_sl, lt_sl;
   // Chain programs: refactor, L, U, U^T, L^T (programs.hpp).
   bool batch = false;              // ld > 1: lane = scenario
+  int sm_count = 1;
   int max_locals = 0;
   pvglu::ProgSetDev progs{};
   std::vector<int> prog_level_chain[5];

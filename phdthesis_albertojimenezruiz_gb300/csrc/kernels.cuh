@@ -379,6 +379,7 @@ static __global__ void k_ir_update(const int* __restrict__ out_perm, int n, int 
   __shared__ unsigned int sdx[8][33], sx[8][33];
   unsigned int mdx = 0u, mx = 0u;
   if (s < S && !done[s]) {
+#pragma unroll 4
     for (int c = blockIdx.x * 8 + threadIdx.y; c < n; c += gridDim.x * 8) {
       const float df = dx[(int64_t)c * ld + s];
       double* xp = x + (int64_t)out_perm[c] * ld + s;

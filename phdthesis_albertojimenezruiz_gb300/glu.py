@@ -89,11 +89,13 @@ class Numeric:
     """Device LU state for `n_scenarios` Jacobians sharing one `Symbolic`."""
 
     def __init__(self, sym: Symbolic, n_scenarios: int = 1, precision: int = N.FP64,
-                 schedule: int = N.SCHED_LEVELS):
+                 schedule: int = N.SCHED_LEVELS, max_locals: int = 0):
         self.sym = sym
         h = C.c_void_p()
-        N.check(N.lib().pvglu_numeric_create(sym.handle, n_scenarios, precision, C.byref(h)),
-                "pvglu_numeric_create")
+        N.check(N.lib().pvglu_numeric_create_ex(sym.handle, n_scenarios, precision,
+                                                int(max_locals), C.byref(h)),
+                "pvglu_numeric_create_ex")
+        self.max_locals = N.lib().pvglu_numeric_max_locals(h)
         self.handle = h
         self.S = n_scenarios
         self.ld = N.lib().pvglu_numeric_ld(h)
@@ -186,6 +188,14 @@ class Numeric:
         if h and N._lib is not None:
             N.lib().pvglu_numeric_destroy(h)
             self.handle = None
+
+
+def autotune(sym: Symbolic, n_scenarios: int, precision: int) -> tuple[int, int, float]:
+    """pvglu_autotune: (max_locals, schedule, ms per scatter+refactor+solve)."""
+    ml, sc, ms = C.c_int(), C.c_int(), C.c_double()
+    N.check(N.lib().pvglu_autotune(sym.handle, int(n_scenarios), int(precision), C.byref(ml),
+                                   C.byref(sc), C.byref(ms)), "pvglu_autotune")
+    return ml.value, sc.value, ms.value
 
 
 # Names of the reference's entry points, for callers porting a driver.

@@ -248,6 +248,27 @@ def test_fp32_refinement_35k(cuda, schedule):
         assert err <= 1e-10, (k, err, sw[k])
 
 
+@pytest.mark.parametrize("S,precision", [(1, FP64), (96, FP32), (64, FP64)])
+def test_autotune_picks_a_working_configuration(cuda, S, precision):
+    from phdthesis_albertojimenezruiz_gb300.glu import autotune
+
+    p = Plant(4, 8, 20)
+    s = Symbolic(p.rowptr, p.colidx)
+    ml, sc, ms = autotune(s, S, precision)
+    assert sc in (SCHED_LEVELS, SCHED_PERSISTENT) and ms > 0
+    num = Numeric(s, S, precision, sc, max_locals=ml)
+    assert num.max_locals == ml
+    o = O.Port(p.rowptr, p.colidx, s.array("perm_amd"))
+    a, b = M.plant_batch(p, S, seed0=7, preset="c1")
+    num.scatter(dev(pad_cols(a, num.ld)))
+    num.refactor()
+    x = dev(pad_cols(b, num.ld), np.float64 if precision == FP64 else np.float32)
+    num.solve(x, original=True)
+    x = x.cpu().numpy().reshape(s.n, num.ld)
+    _, x_ref = o.scatter_refactor_solve(a[:, 0], b[:, 0])
+    assert norm_err(x[:, 0], x_ref) <= (TOL64 if precision == FP64 else 1e-4)
+
+
 def test_zero_pivot_reported_per_scenario(cuda):
     p = Plant(4, 8, 20)
     s = Symbolic(p.rowptr, p.colidx)
