@@ -319,7 +319,9 @@ def main() -> None:
     ap.add_argument("--newton-precision", default="fp64", choices=["fp64", "fp32"],
                     help="factor precision of the Newton section")
     ap.add_argument("--max-locals", type=int, default=0,
-                    help="chain-program table size of the batched handle (0: default)")
+                    help="chain-program table size of the batched handle (0: autotune)")
+    ap.add_argument("--schedule", default="persistent", choices=["levels", "persistent"],
+                    help="schedule used with --max-locals (autotuned otherwise)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     IR_TOL, IR_MAX_SWEEPS = args.ir_tol, args.ir_sweeps
@@ -366,7 +368,9 @@ def main() -> None:
     from phdthesis_albertojimenezruiz_gb300.glu import autotune
 
     if args.max_locals > 0:
-        tuned = {"max_locals": args.max_locals, "schedule": SCHED_PERSISTENT, "source": "flag"}
+        tuned = {"max_locals": args.max_locals,
+                 "schedule": SCHED_LEVELS if args.schedule == "levels" else SCHED_PERSISTENT,
+                 "source": "flags"}
     else:
         ml, sc, tms = autotune(sym, S, FP32)
         tuned = {"max_locals": ml, "schedule": sc, "ms_scatter_refactor_solve": tms,
@@ -472,20 +476,32 @@ def main() -> None:
     plain_name = max(single, key=single.get)
     plain = single[plain_name]
 
-    # End to end through the host-buffer C ABI call.
+    # End to end through the host-buffer C ABI call: every step copies its
+    # inputs from pinned host memory and its solutions back.  Two handles on
+    # two streams alternate, so one batch's copies overlap the other's
+    # kernels (the C2C link and the SMs work at the same time).
     a_h = torch.from_numpy(a).pin_memory()
     b_h = torch.from_numpy(b).pin_memory()
-    x_h = torch.empty_like(b_h).pin_memory()
-    for _ in range(2):
-        num.refine_system_host(a_h, b_h, x_h, IR_TOL, IR_MAX_SWEEPS, sweeps, stream=stream)
+    x_hs = [torch.empty_like(b_h).pin_memory() for _ in range(2)]
+    num2 = Numeric(sym, S, FP32, tuned["schedule"], max_locals=tuned["max_locals"])
+    stream2 = torch.cuda.Stream()
+    sweeps2 = torch.zeros(ld, dtype=torch.int32, device=dev)
+    lanes = [(num, stream, sweeps), (num2, stream2, sweeps2)]
+    for k in range(4):
+        h_, st_, sw_ = lanes[k % 2]
+        h_.refine_system_host(a_h, b_h, x_hs[k % 2], IR_TOL, IR_MAX_SWEEPS, sw_, stream=st_)
     torch.cuda.synchronize()
-    e2e_steps = max(3, args.steps // 2)
+    e2e_steps = max(4, args.steps)
     if dist:
         dist.barrier()
-    t0 = time.perf_counter()
+    e2 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    for _ in range(e2e_steps):
-        num.refine_system_host(a_h, b_h, x_h, IR_TOL, IR_MAX_SWEEPS, sweeps, stream=stream)
+    stream2.wait_event(e0)
+    for k in range(e2e_steps):
+        h_, st_, sw_ = lanes[k % 2]
+        h_.refine_system_host(a_h, b_h, x_hs[k % 2], IR_TOL, IR_MAX_SWEEPS, sw_, stream=st_)
+    e2.record(stream2)
+    stream.wait_event(e2)
     e1.record(stream)
     torch.cuda.synchronize()
     e2e_ms = e0.elapsed_time(e1)
@@ -494,6 +510,10 @@ def main() -> None:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_ms = float(t.item())
     e2e = S * world * e2e_steps / (e2e_ms / 1000.0)
+    e2e_sw = np.concatenate([sweeps.cpu().numpy()[:S], sweeps2.cpu().numpy()[:S]])
+    e2e_err = float(np.max(np.abs(x_hs[0].numpy()[:, :S] - xb).max(axis=0) /
+                           np.abs(xb).max(axis=0)))
+    del num2
 
     bm = bytes_model(nnz_a, nnz_lu, n, 4)
     peaks = _peaks()
@@ -539,7 +559,10 @@ def main() -> None:
                        "all_schedules": single,
                        "ratio_batched_fp32ir_over_plain": value / world / plain},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(8 * (nnz_a + n) * ld),
-                "d2h_bytes_per_step": int(8 * n * ld)},
+                "d2h_bytes_per_step": int(8 * n * ld),
+                "call": "pvglu_refine_system_host, two handles on two streams alternating",
+                "sweeps_max": int(e2e_sw.max()), "not_converged": int((e2e_sw <= 0).sum()),
+                "max_rel_err_vs_fp64": e2e_err},
         "roofline": roofline,
         "cpu_baseline": cpu,
         "newton_adjoint": newton,

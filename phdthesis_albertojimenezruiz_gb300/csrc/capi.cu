@@ -61,7 +61,7 @@ void solve_phase(pvglu_numeric* h, const std::vector<int>& sl, T* x, const int* 
 // grid size of the chain-program kernels of one handle.
 template <typename T, bool B>
 int prog_prepare(pvglu_numeric* h) {
-  const int smem = (int)pvglu::prog_smem_bytes<T, B>(h->max_locals, pvglu::kProgWarps);
+  const int smem = (int)pvglu::prog_smem_bytes<T, B>(h->table_max, pvglu::kProgWarps);
   const void* fns[] = {(const void*)pvglu::k_prog_level<T, -1, B>,
                        (const void*)pvglu::k_prog_level<T, 0, B>,
                        (const void*)pvglu::k_prog_level<T, 1, B>,
@@ -70,7 +70,7 @@ int prog_prepare(pvglu_numeric* h) {
   for (const void* f : fns)
     if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
       return 1;
-  h->prog_grid = pvglu::prog_persistent_grid<T, B>(h->max_locals);
+  h->prog_grid = pvglu::prog_persistent_grid<T, B>(h->table_max);
   return 0;
 }
 
@@ -79,14 +79,15 @@ template <typename T, bool B, int KIND>
 void prog_levels(pvglu_numeric* h, T* x, const int* done, const int* ndone, cudaStream_t st) {
   const int ph = KIND + 1;
   const auto& lc = h->prog_level_chain[ph];
-  const size_t smem = pvglu::prog_smem_bytes<T, B>(h->max_locals, pvglu::kProgWarps);
   const int groups = B ? h->ld / pvglu::kGroup : 1;
   for (size_t lv = 0; lv + 1 < lc.size(); lv++) {
     const int cb = lc[lv], ce = lc[lv + 1];
     const int64_t items = (int64_t)(ce - cb) * groups;
+    const int table = h->prog_level_ml[ph][lv];
+    const size_t smem = pvglu::prog_smem_bytes<T, B>(table, pvglu::kProgWarps);
     pvglu::k_prog_level<T, KIND, B>
         <<<launch_blocks(items, pvglu::kProgWarps), pvglu::kProgBlock, smem, st>>>(
-            h->progs.p[ph], h->d, cb, ce, static_cast<T*>(h->values), x, h->ld, h->S,
+            h->progs.p[ph], table, h->d, cb, ce, static_cast<T*>(h->values), x, h->ld, h->S,
             h->pivot_tol, h->status, done, ndone);
   }
 }
@@ -145,8 +146,12 @@ int solve_permuted(pvglu_numeric* h, T* x, bool transpose, cudaStream_t st,
 template <typename TI, typename TO>
 void permute(pvglu_numeric* h, const int* perm, const TI* x, TO* y, bool gather,
              cudaStream_t st) {
-  const int64_t total = (int64_t)h->n * h->ld;
-  (void)total;
+  if (gather && h->ld % 64 == 0 &&
+      !((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(y)) & 15)) {
+    const int vb = std::min(pvglu::rows_grid(h->n, h->ld, 256), h->sm_count * 8);
+    pvglu::k_rows_vec<TI, TO><<<vb, 256, 0, st>>>(perm, h->n, h->ld, h->S, x, y, nullptr);
+    return;
+  }
   pvglu::k_permute<TI, TO><<<pvglu::rows_grid(h->n, h->ld, 256), 256, 0, st>>>(
       perm, h->n, h->ld, h->S, x, y, gather ? 1 : 0);
 }
@@ -173,6 +178,17 @@ int solve_any(pvglu_numeric* h, T* x, int flags, cudaStream_t st) {
 namespace pvglu {
 
 int run_scatter(pvglu_numeric* h, const AValues& A, const int* ndone, cudaStream_t st) {
+  if (A.a && h->ld % 64 == 0 && !(reinterpret_cast<uintptr_t>(A.a) & 15)) {
+    const int vb = std::min(rows_grid(h->nnz, h->ld, 256), h->sm_count * 8);
+    if (h->precision == PVGLU_FP64)
+      k_rows_vec<double, double><<<vb, 256, 0, st>>>(h->d.slot_src, h->nnz, h->ld, h->S, A.a,
+                                                     (double*)h->values, ndone);
+    else
+      k_rows_vec<double, float><<<vb, 256, 0, st>>>(h->d.slot_src, h->nnz, h->ld, h->S, A.a,
+                                                    (float*)h->values, ndone);
+    PVGLU_CUDA(cudaGetLastError());
+    return PVGLU_OK;
+  }
   const int blocks = rows_grid(h->nnz, h->ld, 256);
   if (h->precision == PVGLU_FP64)
     k_scatter<double><<<blocks, 256, 0, st>>>(h->d.slot_src, h->nnz, h->ld, h->S, A,
@@ -252,7 +268,7 @@ int run_refine(pvglu_numeric* h, const AValues& A, const double* b, double* x, b
   const int fill = std::max(1, h->sm_count * 8);
   const dim3 grd((unsigned)std::max(1, std::min((h->n + 7) / 8, (fill + gy - 1) / gy)),
                  (unsigned)gy);
-  const int rgrid = std::min(rows_grid(h->n, h->ld, 256), fill);
+  const int rgrid = std::min(rows_grid(h->n, h->ld, 256), h->resid_blocks);
   for (int sweep = 1; sweep <= max_sweeps; sweep++) {
     int rc = solve_permuted<float>(h, w, transpose, st, skip);  // dx of this sweep
     if (rc) return rc;
@@ -479,6 +495,14 @@ int pvglu_numeric_create_ex(const pvglu_symbolic* sym, int n_scenarios, int prec
     if (cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
       h->sm_count = 1;
+    // One resident wave of the batched residual (its grid-stride loop covers
+    // the rows): no tail wave, and cheap launches after convergence.
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pvglu::k_residual_rows, 256, 0) !=
+            cudaSuccess ||
+        per_sm <= 0)
+      per_sm = 4;
+    h->resid_blocks = per_sm * h->sm_count;
   }
   h->max_locals = max_locals > 0 ? max_locals
                                  : (h->batch ? (precision == PVGLU_FP32 ? 64 : 40)
@@ -498,9 +522,29 @@ int pvglu_numeric_create_ex(const pvglu_symbolic* sym, int n_scenarios, int prec
       return fail(PVGLU_ERR_BAD_ARG, "max_locals too large for shared memory");
     }
   }
+  // Levels with at most one warp item per resident warp slot of a one-block-
+  // per-SM launch get the widest table that fits: their chains then run in
+  // fewer segments, and the occupancy a wide table costs is not used anyway.
+  const size_t elem = precision == PVGLU_FP64 ? sizeof(double) : sizeof(float);
+  const int group = h->batch ? pvglu::kGroup : 1;
+  const int wide = std::min<int>(
+      pvglu::kMaxLocals,
+      (int)((227 * 1024 - pvglu::kProgWarps * sizeof(unsigned long long)) /
+            ((size_t)pvglu::kProgWarps * group * elem)));
+  const int groups = h->batch ? h->ld / pvglu::kGroup : 1;
+  h->table_max = 0;
   for (int ph = 0; ph < 5; ph++) {
     pvglu::ChainProgram prog;
-    pvglu::build_chain_program(s, ph - 1, h->max_locals, prog);
+    const pvglu::LevelSet& ls = pvglu::program_levels(s, ph - 1);
+    std::vector<int> budget(ls.num_levels(), h->max_locals);
+    for (int lv = 0; lv < ls.num_levels(); lv++) {
+      const int64_t items = (int64_t)(ls.start_levels[lv + 1] - ls.start_levels[lv]) * groups;
+      if (items <= (int64_t)h->sm_count * pvglu::kProgWarps)
+        budget[lv] = std::max(h->max_locals, wide);
+    }
+    pvglu::build_chain_program(s, ph - 1, budget, prog);
+    h->prog_level_ml[ph] = prog.level_max_locals;
+    h->table_max = std::max(h->table_max, prog.max_locals);
     std::vector<int4> seg(prog.seg.size()), ops(prog.ops.size() / 4);
     for (size_t i = 0; i < seg.size(); i++) {
       const auto& g = prog.seg[i];
@@ -518,7 +562,6 @@ int pvglu_numeric_create_ex(const pvglu_symbolic* sym, int n_scenarios, int prec
     rc |= h->put(ops, &P.ops);
     rc |= h->put(prog.op_col, &P.op_col);
     P.n_levels = (int)prog.level_chain.size() - 1;
-    P.max_locals = h->max_locals;
     h->prog_level_chain[ph] = prog.level_chain;
     for (int lv = 0; lv < P.n_levels; lv++)
       h->prog_max_chains = std::max(h->prog_max_chains,
@@ -531,6 +574,8 @@ int pvglu_numeric_create_ex(const pvglu_symbolic* sym, int n_scenarios, int prec
     delete h;
     return fail(PVGLU_ERR_NO_MEMORY, "chain program upload failed");
   }
+  // The persistent kernel lays out one table size for every phase and level.
+  for (int ph = 0; ph < 5; ph++) h->progs.p[ph].max_locals = h->table_max;
   const int smem_rc = precision == PVGLU_FP64
                           ? (h->batch ? prog_prepare<double, true>(h) : prog_prepare<double, false>(h))
                           : (h->batch ? prog_prepare<float, true>(h) : prog_prepare<float, false>(h));

@@ -349,14 +349,15 @@ size_t prog_smem_bytes(int max_locals, int warps_per_block) {
 
 // done: per-scenario skip of the solves (NULL for the refactorization);
 // ndone (or NULL): the launch does nothing once every scenario is done.
+// `table`: the level's table budget (its programs were built for it).
 template <typename T, int KIND, bool BATCH>
-__global__ void k_prog_level(ProgDev P, DevStruct d, int cb, int ce, T* __restrict__ v,
-                             T* __restrict__ x, int ld, int S, T pivot_tol, DevStatus* st,
-                             const int* done, const int* ndone) {
+__global__ void k_prog_level(ProgDev P, int table, DevStruct d, int cb, int ce,
+                             T* __restrict__ v, T* __restrict__ x, int ld, int S, T pivot_tol,
+                             DevStatus* st, const int* done, const int* ndone) {
   if (ndone && __ldcg(ndone) >= S) return;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   WarpTma tma;
-  T* sm = prog_setup_warp<T, BATCH>(smem_raw, P.max_locals, tma);
+  T* sm = prog_setup_warp<T, BATCH>(smem_raw, table, tma);
   const int warp_id = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int n_warps = (gridDim.x * blockDim.x) >> 5;
   prog_run_level<T, KIND, BATCH>(P, d, cb, ce, v, x, ld, S, sm, tma, pivot_tol, st, done,

@@ -67,7 +67,10 @@ struct pvglu_numeric {
   // Chain programs: refactor, L, U, U^T, L^T (programs.hpp).
   bool batch = false;              // ld > 1: lane = scenario
   int sm_count = 1;
-  int max_locals = 0;
+  int resid_blocks = 1;             // resident blocks of k_residual_rows
+  int max_locals = 0;               // table budget of levels with many chains
+  int table_max = 0;                // widest table of any level (shared memory size)
+  std::vector<int> prog_level_ml[5];  // table budget per phase and level
   pvglu::ProgSetDev progs{};
   std::vector<int> prog_level_chain[5];
   int prog_max_chains = 1;

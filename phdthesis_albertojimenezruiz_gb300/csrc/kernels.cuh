@@ -16,6 +16,7 @@
 // uses atomicAdd, factorize_matrix_GLU_CUDA.cuh:99) and makes every result
 // independent of thread scheduling.
 #pragma once
+#include <type_traits>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -181,6 +182,44 @@ __global__ void k_scatter(const int* __restrict__ slot_src, int nnz, int ld, int
     if (src >= 0 && s < S) val = convert<T>(A(src, ld, s));
     v[(int64_t)q * ld + s] = val;
   });
+}
+
+// Batched row copy with conversion (ld a multiple of 64): destination row q
+// takes source row map[q] (zeros for map[q] < 0, and in the padding columns
+// s >= S).  One warp per row, each lane two adjacent columns per vector
+// access, two column pairs in flight.  Serves the explicit-value scatter
+// (map = slot_src) and the gather permutations (map = row_orig / col_orig).
+template <typename TI, typename TO>
+__global__ void __launch_bounds__(256)
+k_rows_vec(const int* __restrict__ map, int rows, int ld, int S, const TI* __restrict__ src,
+           TO* __restrict__ dst, const int* __restrict__ ndone) {
+  using VI = typename std::conditional<sizeof(TI) == 8, double2, float2>::type;
+  using VO = typename std::conditional<sizeof(TO) == 8, double2, float2>::type;
+  if (ndone && __ldcg(ndone) >= S) return;
+  const int lane = threadIdx.x & 31;
+  const int warps = (gridDim.x * blockDim.x) >> 5;
+  for (int q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < rows; q += warps) {
+    const int m = map[q];
+    TO* drow = dst + (int64_t)q * ld;
+    const TI* srow = src + (int64_t)(m < 0 ? 0 : m) * ld;
+    for (int s = 2 * lane; s < ld; s += 128) {
+      const bool has2 = s + 64 < ld;
+      VI a = {}, b = {};
+      if (m >= 0) {
+        a = *reinterpret_cast<const VI*>(srow + s);
+        if (has2) b = *reinterpret_cast<const VI*>(srow + s + 64);
+      }
+      VO oa, ob;
+      oa.x = s < S ? convert<TO>(a.x) : TO(0);
+      oa.y = s + 1 < S ? convert<TO>(a.y) : TO(0);
+      *reinterpret_cast<VO*>(drow + s) = oa;
+      if (has2) {
+        ob.x = s + 64 < S ? convert<TO>(b.x) : TO(0);
+        ob.y = s + 65 < S ? convert<TO>(b.y) : TO(0);
+        *reinterpret_cast<VO*>(drow + s + 64) = ob;
+      }
+    }
+  }
 }
 
 // A's entry values (caller order) from any AValues source.

@@ -168,13 +168,25 @@ void emit_unit(const Symbolic& s, int kind, int u, Table& t) {
 
 }  // namespace
 
+const LevelSet& program_levels(const Symbolic& s, int kind) { return level_set(s, kind); }
+
 void build_chain_program(const Symbolic& s, int kind, int max_locals, ChainProgram& out) {
-  max_locals = std::min(max_locals, kMaxLocals);
+  build_chain_program(s, kind, std::vector<int>(level_set(s, kind).num_levels(), max_locals),
+                      out);
+}
+
+void build_chain_program(const Symbolic& s, int kind, const std::vector<int>& level_max_locals,
+                         ChainProgram& out) {
   out = ChainProgram();
   out.kind = kind;
-  out.max_locals = max_locals;
   const LevelSet& ls = level_set(s, kind);
   out.level_chain = ls.start_levels;
+  out.level_max_locals.resize(ls.num_levels());
+  for (int lv = 0; lv < ls.num_levels(); lv++) {
+    out.level_max_locals[lv] = std::min(level_max_locals[lv], kMaxLocals);
+    out.max_locals = std::max(out.max_locals, out.level_max_locals[lv]);
+  }
+  int level = 0, max_locals = ls.num_levels() ? out.level_max_locals[0] : kMaxLocals;
   Table t;
   t.init(s.n, s.nnz_lu);
   std::vector<int> remap;
@@ -229,6 +241,8 @@ void build_chain_program(const Symbolic& s, int kind, int max_locals, ChainProgr
     t.reset();
   };
   for (int c = 0; c < ls.num_chains(); c++) {
+    while (level + 1 < ls.num_levels() && c >= ls.start_levels[level + 1]) level++;
+    max_locals = out.level_max_locals.empty() ? kMaxLocals : out.level_max_locals[level];
     for (int r : written_list) written(r) = 0;
     written_list.clear();
     out.chain_seg.push_back((int)out.seg.size());

@@ -48,7 +48,8 @@ struct Segment {
 
 struct ChainProgram {
   int kind = -1;                 // -1 refactor, 0 L, 1 U, 2 U^T, 3 L^T
-  int max_locals = 0;            // local table budget the program was built for
+  int max_locals = 0;            // largest local table budget of any level
+  std::vector<int> level_max_locals;  // [levels] table budget of each level
   std::vector<int> level_chain;  // [levels + 1] -> chain index
   std::vector<int> chain_seg;    // [chains + 1] -> segment index
   std::vector<Segment> seg;
@@ -61,5 +62,11 @@ struct ChainProgram {
 
 // kind -1 uses s.lu; 0 s.l; 1 s.u; 2 s.lu; 3 s.lt.
 void build_chain_program(const Symbolic& s, int kind, int max_locals, ChainProgram& out);
+// As above with a table budget per level (levels with few chains can afford a
+// wide table: fewer segments, and the warps they leave idle cost nothing).
+void build_chain_program(const Symbolic& s, int kind, const std::vector<int>& level_max_locals,
+                         ChainProgram& out);
+// The level set a program kind walks.
+const LevelSet& program_levels(const Symbolic& s, int kind);
 
 }  // namespace pvglu
