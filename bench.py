@@ -164,7 +164,7 @@ def cpu_baseline(a: np.ndarray, b: np.ndarray, p, sym_perm, budget_s: float, thr
 
 
 def newton_section(p, sym, stream, S: int, seed0: int, fd_check: bool = True,
-                   precision: str = "fp32") -> dict:
+                   precision: str = "fp32", fixed_tuning=None) -> dict:
     """Device Newton driver over the reference's gmin stages (tolerance
     1e-6 * n, the reference's) for S scenarios with FP32 factors + FP64
     refinement, then the adjoint dP/dG of the plant power for every panel;
@@ -186,7 +186,7 @@ def newton_section(p, sym, stream, S: int, seed0: int, fd_check: bool = True,
     def setup(g_cols, tol_ir=1e-12):
         count = g_cols.shape[1]
         if count not in tuned:
-            tuned[count] = autotune(sym, count, prec)[:2]
+            tuned[count] = fixed_tuning or autotune(sym, count, prec)[:2]
         ml, sc = tuned[count]
         num = Numeric(sym, count, prec, sc, max_locals=ml)
         nw = Newton.for_plant(num, p)
@@ -322,6 +322,8 @@ def main() -> None:
                     help="chain-program table size of the batched handle (0: autotune)")
     ap.add_argument("--schedule", default="persistent", choices=["levels", "persistent"],
                     help="schedule used with --max-locals (autotuned otherwise)")
+    ap.add_argument("--newton-max-locals", type=int, default=0,
+                    help="table size of the Newton handles, with --schedule (0: autotune)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     IR_TOL, IR_MAX_SWEEPS = args.ir_tol, args.ir_sweeps
@@ -349,8 +351,13 @@ def main() -> None:
 
         p = Plant(*DIMS)
         sym = Symbolic(p.rowptr, p.colidx)
+        fixed = None
+        if args.newton_max_locals > 0:
+            fixed = (args.newton_max_locals, SCHED_LEVELS if args.schedule == "levels"
+                     else SCHED_PERSISTENT)
         res = newton_section(p, sym, torch.cuda.current_stream(), args.newton_scenarios, 5000,
-                             fd_check=False, precision=args.newton_precision)
+                             fd_check=False, precision=args.newton_precision,
+                             fixed_tuning=fixed)
         if rank == 0:
             print(json.dumps(res))
         return
