@@ -38,6 +38,7 @@ DIMS = (50, 24, 28)
 METRIC = "refactor+solve/s, 35k-unknown PV Jacobian: batched+FP32-IR vs plain FP64 GPU"
 UNIT = "refactor+solve/s"
 IR_TOL = 1e-12
+REFACTOR_TRAFFIC_512 = 353.7e6  # bytes, ncu dram__bytes_read.sum + dram__bytes_write.sum
 IR_MAX_SWEEPS = 6
 
 
@@ -530,7 +531,11 @@ def main() -> None:
                            "k_prog_level<float,refactor,batched>") + " (refactor phase)",
                 "bound": "hbm",
                 "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak if peak else None, "traffic": None,
+                "frac": achieved / peak if peak else None,
+                # DRAM read + write bytes of one refactorization (its two level
+                # launches) from the ncu capture summarised in
+                # profiles/kernels_fp32ir_plant35k_512scen.md (512 scenarios).
+                "traffic": REFACTOR_TRAFFIC_512 if S == 512 else None,
                 "peak_source": "measured" if peak else "fallback",
                 "bytes_per_launch": bm["refactor"] * S, "avg_launch_ms": refactor_ms}
     if rank != 0:
