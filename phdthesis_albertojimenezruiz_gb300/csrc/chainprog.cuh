@@ -161,7 +161,7 @@ __device__ __forceinline__ void exec_op2(uint32_t op, int op_index, const int* o
         t[(b + i) << 5] = q;
       }
     } else {
-      // FP64 divides like the reference (GLU_CSC_CPU_levels_strings.cpp:60).
+      // FP64 divides like the reference (GLU_CSC_CPU_levels_strings.cpp:34).
       for (int i = 0; i < c; i++) {
         auto q = t[(b + i) << 5];
         q.x = q.x / p.x;

@@ -69,8 +69,8 @@ template <typename T>
 __device__ __forceinline__ T ldv(const T* p) { return __ldcg(p); }
 
 // a - b * c.  FP64 rounds the product and the difference separately, as the
-// reference's CPU code does (GLU_CSC_CPU_levels_strings.cpp:56,
-// GLU_CSC_CPU_Triangular.cpp:8,21); with the same update order per entry the
+// reference's CPU code does (GLU_CSC_CPU_levels_strings.cpp:57,
+// GLU_CSC_CPU_Triangular.cpp:10,24); with the same update order per entry the
 // FP64 factors and solutions are then bit-identical to the reference's
 // sequential path.  FP32 (refined afterwards in FP64) keeps the fused form.
 __device__ __forceinline__ double fnms(double a, double b, double c) {
