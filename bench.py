@@ -267,6 +267,144 @@ def newton_section(p, sym, stream, S: int, seed0: int, fd_check: bool = True,
     return res
 
 
+def _plant_batch(dims, S: int, ld: int, seed0: int, preset: str):
+    from phdthesis_albertojimenezruiz_gb300 import Plant
+
+    p = Plant(*dims)
+    g = np.stack([p.irradiance(seed=seed0 + s, preset=preset) for s in range(S)], axis=1)
+    v = np.repeat(p.flat_start()[:, None], S, axis=1)
+    a, b = p.companion_batch(g, v, ld=ld)
+    return p, a, b
+
+
+def _time_ms(fn, stream, reps: int) -> float:
+    import torch
+
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def config3_section(stream, steps: int) -> dict:
+    """512 scenarios over three plant sizes, FP64: scatter of each size class,
+    then one refactor + solve of all classes with one launch per level
+    (pvglu_group), replayed from a CUDA graph; beside it the same work as one
+    sequence per class."""
+    import torch
+
+    from phdthesis_albertojimenezruiz_gb300 import FP64, Numeric, Symbolic
+    from phdthesis_albertojimenezruiz_gb300.glu import Group, autotune
+
+    dims = [(10, 16, 20), (50, 24, 28), (120, 24, 28)]
+    counts = [171, 171, 170]
+    dev = torch.device("cuda", torch.cuda.current_device())
+    members, a_d, b_d, x_d, sizes = [], [], [], [], []
+    ml = None
+    for k, (d, S) in reversed(list(enumerate(zip(dims, counts)))):
+        ld = ((S + 63) // 64) * 64
+        p, a, b = _plant_batch(d, S, ld, 7000 + 1000 * k, "c3")
+        sym = Symbolic(p.rowptr, p.colidx)
+        # A group launch lays out the widest table of its members: one table
+        # budget for all, tuned on the largest class.
+        if ml is None:
+            ml = autotune(sym, S, FP64)[0]
+        num = Numeric(sym, S, FP64, 0, max_locals=ml)
+        members.append(num)
+        a_d.append(torch.from_numpy(a).to(dev))
+        b_d.append(torch.from_numpy(b).to(dev))
+        x_d.append(torch.zeros_like(b_d[-1]))
+        sizes.append({"plant": "x".join(map(str, d)), "unknowns": p.n, "scenarios": S,
+                      "max_locals": ml})
+    group = Group(members)
+
+    def grouped():
+        for num, a, b, x in zip(members, a_d, b_d, x_d):
+            num.scatter(a, stream=stream)
+            x.copy_(b)
+        group.refactor_solve(x_d, original=True, stream=stream)
+
+    def separate():
+        for num, a, b, x in zip(members, a_d, b_d, x_d):
+            num.scatter(a, stream=stream)
+            x.copy_(b)
+            num.refactor(stream=stream)
+            num.solve(x, original=True, stream=stream)
+
+    for _ in range(3):
+        grouped()
+        separate()
+    ms_group = _time_ms(grouped, stream, steps)
+    ms_sep = _time_ms(separate, stream, steps)
+    graph = torch.cuda.CUDAGraph()
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        with torch.cuda.graph(graph, stream=side):
+            for num, a, b, x in zip(members, a_d, b_d, x_d):
+                num.scatter(a, stream=side)
+                x.copy_(b)
+            group.refactor_solve(x_d, original=True, stream=side)
+    torch.cuda.synchronize()
+    ms_graph = _time_ms(graph.replay, torch.cuda.current_stream(), steps)
+    codes = [m.check()[0] for m in members]
+    total = sum(counts)
+    return {"workload": "512 scenarios over plants 10x16x20, 50x24x28, 120x24x28; FP64 scatter + "
+                        "refactor + solve per step", "classes": sizes,
+            "value": total / (ms_graph / 1000.0), "unit": UNIT,
+            "ms_per_step_graph": ms_graph, "ms_per_step_group": ms_group,
+            "ms_per_step_one_sequence_per_class": ms_sep, "status_codes": codes}
+
+
+def config4_section(stream, steps: int) -> dict:
+    """The largest plant (200x24x28, 135k unknowns), 64 scenarios, FP32
+    factors + FP64 refinement, with its error against the FP64 factors."""
+    import torch
+
+    from phdthesis_albertojimenezruiz_gb300 import FP32, FP64, Numeric, Symbolic
+    from phdthesis_albertojimenezruiz_gb300.glu import autotune
+
+    S, ld = 64, 64
+    p, a, b = _plant_batch((200, 24, 28), S, ld, 9000, "c4")
+    sym = Symbolic(p.rowptr, p.colidx)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    a_d = torch.from_numpy(a).to(dev)
+    b_d = torch.from_numpy(b).to(dev)
+    x_d = torch.zeros_like(b_d)
+    ml, sc, _ = autotune(sym, S, FP32)
+    num = Numeric(sym, S, FP32, sc, max_locals=ml)
+    sweeps = torch.zeros(ld, dtype=torch.int32, device=dev)
+
+    def step():
+        num.scatter(a_d, stream=stream)
+        num.refactor(stream=stream)
+        num.solve_refined(a_d, b_d, x_d, tol=IR_TOL, max_sweeps=IR_MAX_SWEEPS, sweeps=sweeps,
+                          stream=stream)
+
+    for _ in range(3):
+        step()
+    ms = _time_ms(step, stream, steps)
+    sw = sweeps.cpu().numpy()[:S]
+    num64 = Numeric(sym, S, FP64, 0)
+    num64.scatter(a_d, stream=stream)
+    num64.refactor(stream=stream)
+    x64 = b_d.clone()
+    num64.solve(x64, original=True, stream=stream)
+    torch.cuda.synchronize()
+    xa, xb = x_d.cpu().numpy()[:, :S], x64.cpu().numpy()[:, :S]
+    err = float(np.max(np.abs(xa - xb).max(axis=0) / np.abs(xb).max(axis=0)))
+    return {"workload": f"plant_200x24x28 ({sym.n} unknowns, nnz_lu {int(sym.nnz_lu)}), 64 "
+                        "scenarios, scatter + FP32 refactor + FP64-refined solve",
+            "value": S / (ms / 1000.0), "unit": UNIT, "ms_per_step": ms,
+            "tuning": {"max_locals": ml, "schedule": sc}, "sweeps_max": int(sw.max()),
+            "not_converged": int((sw <= 0).sum()), "max_rel_err_vs_fp64": err}
+
+
 def run_reference(args) -> None:
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -323,6 +461,11 @@ def main() -> None:
                     help="chain-program table size of the batched handle (0: autotune)")
     ap.add_argument("--schedule", default="persistent", choices=["levels", "persistent"],
                     help="schedule used with --max-locals (autotuned otherwise)")
+    ap.add_argument("--configs", default="3,4",
+                    help="extra workloads reported beside the headline (3: three plant sizes in "
+                         "one launch per level, 4: the 135k plant; empty: none)")
+    ap.add_argument("--only-configs", action="store_true",
+                    help="run the --configs workloads alone (profiling runs)")
     ap.add_argument("--newton-max-locals", type=int, default=0,
                     help="table size of the Newton handles, with --schedule (0: autotune)")
     args = ap.parse_args()
@@ -347,6 +490,16 @@ def main() -> None:
     from phdthesis_albertojimenezruiz_gb300 import (FP32, FP64, SCHED_LEVELS, SCHED_PERSISTENT,
                                                     SCHED_THREAD_CHAIN, Numeric, Symbolic)
 
+    if args.only_configs:
+        wanted = {c.strip() for c in args.configs.split(",") if c.strip()}
+        out = {}
+        if "3" in wanted:
+            out["config3"] = config3_section(torch.cuda.current_stream(), max(5, args.steps))
+        if "4" in wanted:
+            out["config4"] = config4_section(torch.cuda.current_stream(), max(5, args.steps))
+        if rank == 0:
+            print(json.dumps(out))
+        return
     if args.only_newton:
         from phdthesis_albertojimenezruiz_gb300 import Plant
 
@@ -542,6 +695,12 @@ def main() -> None:
         if dist:
             dist.destroy_process_group()
         return
+    extra = {}
+    wanted = {c.strip() for c in args.configs.split(",") if c.strip()}
+    if "3" in wanted:
+        extra["config3"] = config3_section(stream, max(5, args.steps))
+    if "4" in wanted:
+        extra["config4"] = config4_section(stream, max(5, args.steps))
     newton = (newton_section(p, sym, stream, args.newton_scenarios, 5000,
                              precision=args.newton_precision)
               if args.newton_scenarios > 0 else None)
@@ -578,6 +737,7 @@ def main() -> None:
         "roofline": roofline,
         "cpu_baseline": cpu,
         "newton_adjoint": newton,
+        **extra,
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }

@@ -250,6 +250,23 @@ int pvglu_refine_system_host(pvglu_numeric* h, const double* a_values_host,
  * No counterpart in the reference. */
 int pvglu_solve_noalloc(pvglu_numeric* h, double* x, int flags, void* stream);
 
+/* ---------------- size-class groups -------------------------------------- */
+
+/* Up to 4 numeric handles over different symbolic analyses (plants of
+ * different sizes) that share precision and batching.  A group refactor +
+ * solve issues one launch per level over the work items of every member
+ * (level l of all members together), instead of one sequence per member.
+ * Each member keeps its values (scatter them with pvglu_scatter first), its
+ * status and its pivot threshold.  No counterpart in the reference (one
+ * circuit per run). */
+typedef struct pvglu_group pvglu_group;
+int pvglu_group_create(pvglu_numeric* const* members, int count, pvglu_group** out);
+int pvglu_group_destroy(pvglu_group* g);
+/* Refactor every member, then solve member i's vector x[i] ([n_i * ld_i], the
+ * member's precision; pivot order, or caller order with PVGLU_SOLVE_ORIGINAL).
+ * x == NULL: refactor only. */
+int pvglu_group_refactor_solve(pvglu_group* g, void* const* x, int flags, void* stream);
+
 /* ---------------- autotuner ---------------------------------------------- */
 
 /* Times scatter + refactor + solve for n_scenarios on this device over the

@@ -87,6 +87,9 @@ _SIGS = {
     "pvglu_solve_refined": ([_P, _P, _P, _P, C.c_double, _I, _P, _P], _I),
     "pvglu_selftest_barrier_timeout": ([_I, C.c_longlong, _IP, _IP], _I),
     "pvglu_autotune": ([_P, _I, _I, _IP, _IP, _DP], _I),
+    "pvglu_group_create": ([_P, _I, C.POINTER(_P)], _I),
+    "pvglu_group_destroy": ([_P], _I),
+    "pvglu_group_refactor_solve": ([_P, _P, _I, _P], _I),
     "pvglu_refine_system_host": ([_P, _P, _P, _P, C.c_double, _I, _P, _P], _I),
     "pvglu_solve_noalloc": ([_P, _P, _I, _P], _I),
     "pvglu_numeric_set_stamps": ([_P, _I, _P, _P, _P, _P], _I),

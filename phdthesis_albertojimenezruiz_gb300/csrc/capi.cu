@@ -842,6 +842,156 @@ int pvglu_solve_noalloc(pvglu_numeric* h, double* x, int flags, void* stream) {
   return PVGLU_OK;
 }
 
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Size-class groups: handles with different symbolic analyses refactored and
+// solved together, one launch per level over the items of every class.
+struct pvglu_group {
+  std::vector<pvglu_numeric*> m;
+  int precision = PVGLU_FP64;
+  bool batch = false;
+};
+
+namespace {
+
+template <typename T, bool B, int KIND>
+int group_phase(pvglu_group* g, T* const* xs, cudaStream_t st) {
+  const int ph = KIND + 1;
+  int nlev = 0;
+  for (auto* h : g->m) nlev = std::max(nlev, (int)h->prog_level_chain[ph].size() - 1);
+  // Members whose level lv uses the same table size share a launch (a
+  // launch lays out its widest table, which would cost the others occupancy).
+  std::vector<int> tables;
+  for (int lv = 0; lv < nlev; lv++) {
+    tables.clear();
+    for (auto* h : g->m)
+      if (lv + 1 < (int)h->prog_level_chain[ph].size() &&
+          std::find(tables.begin(), tables.end(), h->prog_level_ml[ph][lv]) == tables.end())
+        tables.push_back(h->prog_level_ml[ph][lv]);
+    for (const int tb : tables) {
+    pvglu::MultiLaunch<T> M{};
+    int table = 0, items = 0;
+    for (size_t i = 0; i < g->m.size(); i++) {
+      pvglu_numeric* h = g->m[i];
+      const auto& lc = h->prog_level_chain[ph];
+      if (lv + 1 >= (int)lc.size() || h->prog_level_ml[ph][lv] != tb) continue;
+      auto& C = M.c[M.n++];
+      C.P = h->progs.p[ph];
+      C.d = h->d;
+      C.v = static_cast<T*>(h->values);
+      C.x = xs ? xs[i] : nullptr;
+      C.ld = h->ld;
+      C.S = h->S;
+      C.cb = lc[lv];
+      C.ce = lc[lv + 1];
+      C.groups = B ? h->ld / pvglu::kGroup : 1;
+      C.item_begin = items;
+      C.st = h->status;
+      C.pivot_tol = (T)h->pivot_tol;
+      items += (C.ce - C.cb) * C.groups;
+      table = std::max(table, h->prog_level_ml[ph][lv]);
+    }
+    if (!items) continue;
+    M.items = items;
+    const size_t smem = pvglu::prog_smem_bytes<T, B>(table, pvglu::kProgWarps);
+    pvglu::k_prog_level_multi<T, KIND, B>
+        <<<launch_blocks(items, pvglu::kProgWarps), pvglu::kProgBlock, smem, st>>>(M, table);
+    }
+  }
+  PVGLU_CUDA(cudaGetLastError());
+  return PVGLU_OK;
+}
+
+template <typename T, bool B>
+int group_prepare() {
+  const int smem = 227 * 1024;
+  const void* fns[] = {(const void*)pvglu::k_prog_level_multi<T, -1, B>,
+                       (const void*)pvglu::k_prog_level_multi<T, 0, B>,
+                       (const void*)pvglu::k_prog_level_multi<T, 1, B>};
+  for (const void* f : fns)
+    if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+      return 1;
+  return 0;
+}
+
+template <typename T, bool B>
+int group_run(pvglu_group* g, void* const* x, int flags, cudaStream_t st) {
+  std::vector<T*> xs(g->m.size(), nullptr);
+  const bool orig = (flags & PVGLU_SOLVE_ORIGINAL) != 0;
+  for (size_t i = 0; i < g->m.size(); i++) {
+    pvglu_numeric* h = g->m[i];
+    if (!x) break;
+    if (orig) {
+      xs[i] = static_cast<T*>(h->work);
+      permute<T, T>(h, h->d.row_orig, static_cast<const T*>(x[i]), xs[i], true, st);
+    } else {
+      xs[i] = static_cast<T*>(x[i]);
+    }
+  }
+  int rc = group_phase<T, B, -1>(g, nullptr, st);
+  if (!rc && x) rc = group_phase<T, B, 0>(g, xs.data(), st);
+  if (!rc && x) rc = group_phase<T, B, 1>(g, xs.data(), st);
+  if (rc) return rc;
+  if (x && orig)
+    for (size_t i = 0; i < g->m.size(); i++)
+      permute<T, T>(g->m[i], g->m[i]->d.col_orig, xs[i], static_cast<T*>(x[i]), false, st);
+  PVGLU_CUDA(cudaGetLastError());
+  return PVGLU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pvglu_group_create(pvglu_numeric* const* members, int count, pvglu_group** out) {
+  if (!members || !out || count <= 0 || count > pvglu::kMaxClasses)
+    return fail(PVGLU_ERR_BAD_ARG, "a group holds 1 to 4 handles");
+  *out = nullptr;
+  auto* g = new pvglu_group();
+  for (int i = 0; i < count; i++) {
+    pvglu_numeric* h = members[i];
+    if (!h || (i > 0 && (h->precision != g->precision || h->batch != g->batch))) {
+      delete g;
+      return fail(PVGLU_ERR_BAD_ARG, "group members must share precision and batching");
+    }
+    if (i == 0) {
+      g->precision = h->precision;
+      g->batch = h->batch;
+    }
+    g->m.push_back(h);
+  }
+  const int prc = g->precision == PVGLU_FP64
+                      ? (g->batch ? group_prepare<double, true>() : group_prepare<double, false>())
+                      : (g->batch ? group_prepare<float, true>() : group_prepare<float, false>());
+  if (prc) {
+    delete g;
+    return fail(PVGLU_ERR_CUDA, "cannot configure the group kernels");
+  }
+  *out = g;
+  return PVGLU_OK;
+}
+
+int pvglu_group_destroy(pvglu_group* g) {
+  delete g;
+  return PVGLU_OK;
+}
+
+int pvglu_group_refactor_solve(pvglu_group* g, void* const* x, int flags, void* stream) {
+  if (!g) return fail(PVGLU_ERR_BAD_ARG, "NULL group");
+  if (flags & PVGLU_SOLVE_TRANSPOSE) return fail(PVGLU_ERR_BAD_ARG, "transposed group solve");
+  if (x)
+    for (size_t i = 0; i < g->m.size(); i++)
+      if (!x[i] || (g->batch && (reinterpret_cast<uintptr_t>(x[i]) & 15)))
+        return fail(PVGLU_ERR_BAD_ARG, "each member needs a 16-byte aligned vector");
+  cudaStream_t st = as_stream(stream);
+  return g->precision == PVGLU_FP64
+             ? (g->batch ? group_run<double, true>(g, x, flags, st)
+                         : group_run<double, false>(g, x, flags, st))
+             : (g->batch ? group_run<float, true>(g, x, flags, st)
+                         : group_run<float, false>(g, x, flags, st));
+}
+
 int pvglu_autotune(const pvglu_symbolic* sym, int n_scenarios, int precision,
                    int* best_max_locals, int* best_schedule, double* best_ms) {
   if (!sym || n_scenarios <= 0 || !best_max_locals || !best_schedule ||

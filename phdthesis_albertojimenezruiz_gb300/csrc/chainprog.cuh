@@ -364,4 +364,59 @@ __global__ void k_prog_level(ProgDev P, int table, DevStruct d, int cb, int ce,
                                  warp_id, n_warps);
 }
 
+// ---------------------------------------------------------------------------
+// Several size classes (numeric handles with different symbolic analyses) in
+// one launch per level: the work items of level `lv` of every class are
+// numbered consecutively and each warp finds its class by the item ranges.
+// Classes share T, the phase and the batched layout; each keeps its own
+// programs, structure, values, vector and status.
+constexpr int kMaxClasses = 4;
+
+template <typename T>
+struct ClassLaunch {
+  ProgDev P;
+  DevStruct d;
+  T* v;
+  T* x;
+  int ld, S, cb, ce, groups;
+  int item_begin;  // first global item of this class
+  DevStatus* st;
+  T pivot_tol;
+};
+
+template <typename T>
+struct MultiLaunch {
+  ClassLaunch<T> c[kMaxClasses];
+  int n;       // classes in this launch
+  int items;   // total work items
+};
+
+template <typename T, int KIND, bool BATCH>
+__global__ void k_prog_level_multi(MultiLaunch<T> M, int table) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  WarpTma tma;
+  T* sm = prog_setup_warp<T, BATCH>(smem_raw, table, tma);
+  const int warp_id = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int n_warps = (gridDim.x * blockDim.x) >> 5;
+  // Constant class indices keep every field a direct kernel-parameter read
+  // (a runtime index would copy the descriptors to local memory).
+  auto run = [&](const ClassLaunch<T>& C, int it) {
+    const int local = it - C.item_begin;
+    const int ci = BATCH ? local / C.groups : local;
+    const int s0 = BATCH ? (local - ci * C.groups) * kGroup : 0;
+    prog_run_chain<T, KIND, BATCH>(C.P, C.d, C.cb + ci, C.v, C.x, C.ld, s0, C.S, sm, tma,
+                                   C.pivot_tol, C.st);
+  };
+  for (int it = warp_id; it < M.items; it += n_warps) {
+    if (M.n > 3 && it >= M.c[3].item_begin) run(M.c[3], it);
+    else if (M.n > 2 && it >= M.c[2].item_begin) run(M.c[2], it);
+    else if (M.n > 1 && it >= M.c[1].item_begin) run(M.c[1], it);
+    else run(M.c[0], it);
+  }
+  if (BATCH) {
+    bulk_wait_all();
+    fence_proxy_async();
+  }
+}
+
 }  // namespace pvglu

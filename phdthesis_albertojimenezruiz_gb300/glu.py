@@ -190,6 +190,32 @@ class Numeric:
             self.handle = None
 
 
+class Group:
+    """Numeric handles of different size classes refactored and solved
+    together, one launch per level (pvglu_group_*)."""
+
+    def __init__(self, members: list[Numeric]):
+        self.members = list(members)
+        arr = (C.c_void_p * len(members))(*[m.handle.value for m in members])
+        h = C.c_void_p()
+        N.check(N.lib().pvglu_group_create(arr, len(members), C.byref(h)), "pvglu_group_create")
+        self.handle = h
+
+    def refactor_solve(self, xs=None, original: bool = False, stream=None) -> None:
+        arr = None
+        if xs is not None:
+            arr = (C.c_void_p * len(xs))(*[_ptr(x).value for x in xs])
+        flags = N.SOLVE_ORIGINAL if original else 0
+        N.check(N.lib().pvglu_group_refactor_solve(self.handle, arr, flags, _stream_ptr(stream)),
+                "pvglu_group_refactor_solve")
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h and N._lib is not None:
+            N.lib().pvglu_group_destroy(h)
+            self.handle = None
+
+
 def autotune(sym: Symbolic, n_scenarios: int, precision: int) -> tuple[int, int, float]:
     """pvglu_autotune: (max_locals, schedule, ms per scatter+refactor+solve)."""
     ml, sc, ms = C.c_int(), C.c_int(), C.c_double()

@@ -269,6 +269,44 @@ def test_autotune_picks_a_working_configuration(cuda, S, precision):
     assert norm_err(x[:, 0], x_ref) <= (TOL64 if precision == FP64 else 1e-4)
 
 
+@pytest.mark.parametrize("precision", [FP64, FP32])
+@pytest.mark.parametrize("counts", [(1, 1, 1), (37, 64, 5)])
+def test_group_of_size_classes_matches_members(cuda, precision, counts):
+    """Three plant sizes refactored + solved by one launch per level give the
+    same values as each handle alone (bit-identical: same arithmetic)."""
+    import torch
+
+    from phdthesis_albertojimenezruiz_gb300.glu import Group
+
+    dims = [(2, 4, 10), (4, 8, 20), (3, 6, 12)]
+    tdt = np.float64 if precision == FP64 else np.float32
+    members, refs, xs = [], [], []
+    for k, (d, S) in enumerate(zip(dims, counts)):
+        p = Plant(*d)
+        s = Symbolic(p.rowptr, p.colidx)
+        a, b = M.plant_batch(p, S, seed0=50 + k, preset="c1")
+        alone = Numeric(s, S, precision, SCHED_LEVELS)
+        grouped = Numeric(s, S, precision, SCHED_LEVELS)
+        for h in (alone, grouped):
+            h.scatter(dev(pad_cols(a, h.ld)))
+        xa = dev(pad_cols(b, alone.ld), tdt)
+        alone.refactor()
+        alone.solve(xa, original=True)
+        torch.cuda.synchronize()
+        refs.append((values_of(alone, int(s.nnz_lu)), xa.cpu().numpy(), int(s.nnz_lu)))
+        members.append(grouped)
+        xs.append(dev(pad_cols(b, grouped.ld), tdt))
+    g = Group(members)
+    g.refactor_solve(xs, original=True)
+    torch.cuda.synchronize()
+    for h, x, (lu_ref, x_ref, nnz), S in zip(members, xs, refs, counts):
+        assert h.check()[0] == 0
+        # padding columns (s >= S) hold no scenario
+        assert np.array_equal(values_of(h, nnz)[:, :S], lu_ref[:, :S])
+        assert np.array_equal(x.cpu().numpy().reshape(-1, h.ld)[:, :S],
+                              x_ref.reshape(-1, h.ld)[:, :S])
+
+
 def test_zero_pivot_reported_per_scenario(cuda):
     p = Plant(4, 8, 20)
     s = Symbolic(p.rowptr, p.colidx)
