@@ -81,6 +81,15 @@ int pvglu_symbolic_create(int n, const int* rowptr, const int* colidx,
                           const int* perm, pvglu_symbolic** out);
 int pvglu_symbolic_destroy(pvglu_symbolic* s);
 
+/* Dump of a complete analysis to a file and back: every array of
+ * pvglu_symbolic_get_array plus the execution structures, with a hash that
+ * rejects a damaged file (PVGLU_ERR_BAD_ARG).  Lets a run restart without
+ * re-analysis; the reference rebuilds struct_CPU_CUDA_arrays
+ * (factorize_electrical_system.h:3-61) in prepare_matrices (000:10-93) at
+ * every start. */
+int pvglu_symbolic_save(const pvglu_symbolic* s, const char* path);
+int pvglu_symbolic_load(const char* path, pvglu_symbolic** out);
+
 typedef struct {
   int n;
   int64_t nnz_a, nnz_lu, update_count;

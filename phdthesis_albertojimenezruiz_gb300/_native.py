@@ -66,6 +66,8 @@ _SIGS = {
     "pvglu_version": ([], C.c_char_p),
     "pvglu_symbolic_create": ([_I, _P, _P, _P, C.POINTER(_P)], _I),
     "pvglu_symbolic_destroy": ([_P], _I),
+    "pvglu_symbolic_save": ([_P, C.c_char_p], _I),
+    "pvglu_symbolic_load": ([C.c_char_p, C.POINTER(_P)], _I),
     "pvglu_symbolic_get_info": ([_P, C.POINTER(SymbolicInfo)], _I),
     "pvglu_symbolic_get_array": ([_P, C.c_char_p, C.POINTER(_IP), C.POINTER(C.c_int64)], _I),
     "pvglu_numeric_create": ([_P, _I, _I, C.POINTER(_P)], _I),

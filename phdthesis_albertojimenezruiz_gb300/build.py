@@ -27,7 +27,7 @@ NVCCFLAGS = ["-std=c++17", "-O3", "-lineinfo", "--expt-relaxed-constexpr",
              "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
              "-Xptxas", "-warn-spills"] + ARCH
 
-HOST_SOURCES = ["symbolic.cpp", "programs.cpp", "plant.cpp", "plant_capi.cpp"]
+HOST_SOURCES = ["symbolic.cpp", "symbolic_io.cpp", "programs.cpp", "plant.cpp", "plant_capi.cpp"]
 CUDA_SOURCES = ["capi.cu", "newton.cu"]
 # newton.cu evaluates the panel model (panel_model.h) on the device; without
 # multiply-add contraction it rounds exactly like the host code.

@@ -313,6 +313,27 @@ int pvglu_symbolic_create(int n, const int* rowptr, const int* colidx, const int
   return PVGLU_OK;
 }
 
+int pvglu_symbolic_save(const pvglu_symbolic* h, const char* path) {
+  if (!h || !path) return fail(PVGLU_ERR_BAD_ARG, "NULL argument");
+  std::string err;
+  const int st = pvglu::save_symbolic(h->s, path, err);
+  return st ? fail(st, err) : PVGLU_OK;
+}
+
+int pvglu_symbolic_load(const char* path, pvglu_symbolic** out) {
+  if (!path || !out) return fail(PVGLU_ERR_BAD_ARG, "NULL argument");
+  *out = nullptr;
+  auto* h = new pvglu_symbolic();
+  std::string err;
+  const int st = pvglu::load_symbolic(path, h->s, err);
+  if (st) {
+    delete h;
+    return fail(st, err);
+  }
+  *out = h;
+  return PVGLU_OK;
+}
+
 int pvglu_symbolic_destroy(pvglu_symbolic* s) {
   delete s;
   return PVGLU_OK;

@@ -110,6 +110,10 @@ enum Status : int {
 int build_symbolic(int n, const int* rowptr, const int* colidx, const int* perm,
                    const SymbolicOptions& opt, Symbolic& out, std::string& err);
 
+// Dump format of a complete analysis (symbolic_io.cpp).
+int save_symbolic(const Symbolic& s, const char* path, std::string& err);
+int load_symbolic(const char* path, Symbolic& s, std::string& err);
+
 // Minimum-degree ordering of the pattern of A + A^T (exact degrees on the
 // explicit elimination graph; ties broken by the smallest index).
 void minimum_degree_order(int n, const std::vector<int>& rowptr,

@@ -46,18 +46,21 @@ def _ptr(t) -> C.c_void_p:
 class Symbolic:
     """Host symbolic analysis of one Jacobian pattern (caller's unknown order)."""
 
-    def __init__(self, rowptr, colidx, perm=None):
-        rowptr = np.ascontiguousarray(rowptr, dtype=np.int32)
-        colidx = np.ascontiguousarray(colidx, dtype=np.int32)
-        n = len(rowptr) - 1
-        self._keep = [rowptr, colidx]
-        p = None
-        if perm is not None:
-            p = np.ascontiguousarray(perm, dtype=np.int32)
-            self._keep.append(p)
-        h = C.c_void_p()
-        N.check(N.lib().pvglu_symbolic_create(n, _ptr(rowptr), _ptr(colidx), _ptr(p),
-                                              C.byref(h)), "pvglu_symbolic_create")
+    def __init__(self, rowptr, colidx, perm=None, _handle=None):
+        if _handle is None:
+            rowptr = np.ascontiguousarray(rowptr, dtype=np.int32)
+            colidx = np.ascontiguousarray(colidx, dtype=np.int32)
+            n = len(rowptr) - 1
+            self._keep = [rowptr, colidx]
+            p = None
+            if perm is not None:
+                p = np.ascontiguousarray(perm, dtype=np.int32)
+                self._keep.append(p)
+            h = C.c_void_p()
+            N.check(N.lib().pvglu_symbolic_create(n, _ptr(rowptr), _ptr(colidx), _ptr(p),
+                                                  C.byref(h)), "pvglu_symbolic_create")
+        else:
+            h = _handle
         self.handle = h
         info = N.SymbolicInfo()
         N.check(N.lib().pvglu_symbolic_get_info(h, C.byref(info)), "pvglu_symbolic_get_info")
@@ -77,6 +80,17 @@ class Symbolic:
 
     def arrays(self) -> dict[str, np.ndarray]:
         return {k: self.array(k) for k in SYMBOLIC_ARRAYS}
+
+    def save(self, path) -> None:
+        N.check(N.lib().pvglu_symbolic_save(self.handle, str(path).encode()),
+                "pvglu_symbolic_save")
+
+    @classmethod
+    def load(cls, path) -> "Symbolic":
+        h = C.c_void_p()
+        N.check(N.lib().pvglu_symbolic_load(str(path).encode(), C.byref(h)),
+                "pvglu_symbolic_load")
+        return cls(None, None, _handle=h)
 
     def __del__(self):
         h = getattr(self, "handle", None)

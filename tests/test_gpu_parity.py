@@ -375,3 +375,22 @@ def test_barrier_timeout_is_reported_not_hung(cuda):
     assert ret.value == 4   # every block returned
     # the context is still usable afterwards
     test_host_dropin_entry_points(cuda)
+
+
+def test_loaded_symbolic_factors_bit_identical(cuda, tmp_path):
+    """A handle built on a reloaded analysis computes the same FP64 factors
+    and solutions as one built on the original."""
+    p = Plant(4, 8, 20)
+    s = Symbolic(p.rowptr, p.colidx)
+    s.save(tmp_path / "s.pvs")
+    t = Symbolic.load(tmp_path / "s.pvs")
+    a, b = M.plant_batch(p, 40, seed0=3, preset="c1")
+    out = []
+    for sym in (s, t):
+        num = Numeric(sym, 40, FP64, SCHED_LEVELS)
+        num.scatter(dev(pad_cols(a, num.ld)))
+        num.refactor()
+        x = dev(pad_cols(b, num.ld))
+        num.solve(x, original=True)
+        out.append((values_of(num, int(sym.nnz_lu))[:, :40], x.cpu().numpy()[:, :40]))
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
