@@ -70,6 +70,22 @@ int pvglu_newton_set_iph(pvglu_newton* nw, const double* iph, void* stream);
  * (the flat start, or a previous solution). */
 int pvglu_newton_set_voltages(pvglu_newton* nw, const double* v, void* stream);
 
+/* Irradiance field on the device (the per-time-step input of the simulator:
+ * the reference paints moving cloud canvases, 001_clouds.cu:55-62, :96-137,
+ * and reads one value per panel, 003_create_electric_system.cpp:162-201).
+ * Host arrays, copied: panel positions elem_x, elem_y [n_elems] (m), and per
+ * scenario counts[s] <= max_shadows Gaussian shadows, shadows[(s *
+ * max_shadows + k) * 6 + j] = centre x, y, velocity x, y, depth, sigma
+ * (pvglu_plant_shadows gives them for the synthetic plant). */
+int pvglu_newton_set_field(pvglu_newton* nw, const double* elem_x, const double* elem_y,
+                           int max_shadows, const int* counts, const double* shadows,
+                           double g_clear, double iph_per_g);
+/* Photocurrents of every element and scenario at time t from the field,
+ * iph = iph_per_g * G (pvglu_shadow_irradiance), straight into the driver's
+ * photocurrent buffer: no host traffic per time step.  g_out (device
+ * [n_elems * ld]) receives G, or NULL. */
+int pvglu_newton_field_iph(pvglu_newton* nw, double t, double* g_out, void* stream);
+
 /* Iteration of FP32 handles: refinement tolerance and sweep limit of each
  * linear solve (defaults 1e-12, 8).  Each Newton step solves for the node
  * voltages themselves, not for a correction, so this tolerance bounds the

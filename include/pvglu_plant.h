@@ -55,6 +55,14 @@ int pvglu_plant_irradiance(const pvglu_plant* p, int min_shadows, int max_shadow
                            double min_depth, double max_depth, uint64_t seed, double t,
                            double* g_out);
 
+/* The seeded shadows behind pvglu_plant_irradiance for one scenario:
+ * *count shadows (at most max_shadows), params[6k .. 6k+5] = centre x, y
+ * [m] at t = 0, velocity x, y [m/s], depth [W/m^2], sigma [m].  For the
+ * device field of pvglu_newton_set_field. */
+int pvglu_plant_shadows(const pvglu_plant* p, int min_shadows, int max_shadows,
+                        double min_depth, double max_depth, uint64_t seed, int* count,
+                        double* params);
+
 /* Host evaluation of the panel model: current out of the + terminal and its
  * derivative for `count` (photocurrent, terminal voltage) pairs. */
 int pvglu_plant_panel_iv(const pvglu_plant* p, int count, const double* iph,

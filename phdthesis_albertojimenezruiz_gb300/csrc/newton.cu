@@ -254,6 +254,29 @@ __global__ void k_nt_reset(NtDev D) {
   D.gmin_s[s] = 0.0;
 }
 
+// Irradiance field of every scenario at time t (pvglu_shadow_irradiance),
+// written as photocurrent iph = iph_per_g * G (and G itself if asked).
+struct FieldDev {
+  const double* x;       // [n_elems] panel positions
+  const double* y;
+  const double* shadow;  // [ld][max_shadows][6]
+  const int* count;      // [ld]
+  int max_shadows;
+  double g_clear, iph_per_g;
+};
+
+__global__ void k_nt_field(NtDev D, FieldDev F, double t, double* __restrict__ g_out) {
+  for_rows(D.n_elems, D.ld, [&](int k, int s) {
+    const int64_t e = (int64_t)k * D.ld + s;
+    double g = 0.0;
+    if (s < D.S)
+      g = pvglu_shadow_irradiance(F.x[k], F.y[k], F.shadow + (int64_t)s * F.max_shadows * 6,
+                                  F.count[s], t, F.g_clear);
+    D.iph[e] = F.iph_per_g * g;
+    if (g_out) g_out[e] = g;
+  });
+}
+
 // Adjoint: companion conductance at the iterate without gmin, and
 // dI/dIph (kept in ieq) for the sensitivity.
 __global__ void k_nt_adjoint_companion(NtDev D) {
@@ -301,6 +324,9 @@ struct pvglu_newton {
   double* lam = nullptr;        // adjoint vector
   int* pinned_ndone = nullptr;  // host-pinned copy of the stopped count
   double ir_tol = 1e-12;
+  pvglu::FieldDev field{};
+  bool has_field = false;
+  std::vector<void*> field_allocs;
   int ir_sweeps = 8;
   // Captured iteration body and what it was captured with.
   cudaStream_t cap_stream = nullptr;
@@ -310,6 +336,7 @@ struct pvglu_newton {
   bool graph_failed = false;
   int last_bodies = 0, last_graph = 0;
   ~pvglu_newton() {
+    for (void* p : field_allocs) cudaFree(p);
     if (graph) cudaGraphExecDestroy(graph);
     if (cap_stream) cudaStreamDestroy(cap_stream);
     if (pinned_ndone) cudaFreeHost(pinned_ndone);
@@ -571,6 +598,51 @@ int pvglu_newton_set_voltages(pvglu_newton* nw, const double* v, void* stream) {
   if (!nw || !v) return fail(PVGLU_ERR_BAD_ARG, "NULL argument");
   PVGLU_CUDA(cudaMemcpyAsync(nw->D.v, v, (size_t)nw->n_elems * nw->D.ld * sizeof(double),
                              cudaMemcpyDeviceToDevice, as_stream(stream)));
+  return PVGLU_OK;
+}
+
+int pvglu_newton_set_field(pvglu_newton* nw, const double* elem_x, const double* elem_y,
+                           int max_shadows, const int* counts, const double* shadows,
+                           double g_clear, double iph_per_g) {
+  if (!nw || !elem_x || !elem_y || !counts || max_shadows < 0 || max_shadows > 4096 ||
+      (max_shadows > 0 && !shadows))
+    return fail(PVGLU_ERR_BAD_ARG, "bad set_field arguments");
+  const int S = nw->D.S, ld = nw->D.ld, ne = nw->n_elems;
+  for (int s = 0; s < S; s++)
+    if (counts[s] < 0 || counts[s] > max_shadows)
+      return fail(PVGLU_ERR_BAD_ARG, "shadow count out of range");
+  std::vector<double> xs(elem_x, elem_x + ne), ys(elem_y, elem_y + ne);
+  std::vector<double> sh((size_t)ld * std::max(max_shadows, 1) * 6, 0.0);
+  std::copy(shadows, shadows + (size_t)S * max_shadows * 6, sh.begin());
+  std::vector<int> cnt(ld, 0);
+  std::copy(counts, counts + S, cnt.begin());
+  for (void* p : nw->field_allocs) cudaFree(p);
+  nw->field_allocs.clear();
+  nw->has_field = false;
+  double *dx = nullptr, *dy = nullptr, *ds = nullptr;
+  int* dc = nullptr;
+  int rc = 0;
+  rc |= upload(xs, &dx);
+  nw->field_allocs.push_back(dx);
+  rc |= upload(ys, &dy);
+  nw->field_allocs.push_back(dy);
+  rc |= upload(sh, &ds);
+  nw->field_allocs.push_back(ds);
+  rc |= upload(cnt, &dc);
+  nw->field_allocs.push_back(dc);
+  if (rc) return fail(PVGLU_ERR_NO_MEMORY, "field upload failed");
+  nw->field = pvglu::FieldDev{dx, dy, ds, dc, max_shadows, g_clear, iph_per_g};
+  nw->has_field = true;
+  return PVGLU_OK;
+}
+
+int pvglu_newton_field_iph(pvglu_newton* nw, double t, double* g_out, void* stream) {
+  if (!nw) return fail(PVGLU_ERR_BAD_ARG, "NULL handle");
+  if (!nw->has_field) return fail(PVGLU_ERR_BAD_ARG, "no field set on this handle");
+  const pvglu::NtDev& D = nw->D;
+  pvglu::k_nt_field<<<pvglu::rows_grid(D.n_elems, D.ld, 256), 256, 0, as_stream(stream)>>>(
+      D, nw->field, t, g_out);
+  PVGLU_CUDA(cudaGetLastError());
   return PVGLU_OK;
 }
 

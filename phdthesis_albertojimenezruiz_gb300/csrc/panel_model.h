@@ -278,3 +278,22 @@ PVGLU_HD void pvglu_panel_iv(const pvglu_panel_params* p, double iph, double v,
   double didiph;
   pvglu_panel_iv3(p, iph, v, current, didv, &didiph);
 }
+
+// Irradiance [W/m^2] at panel position (x, y) [m] and time t [s] under
+// `count` Gaussian shadows drifting with constant velocity, clamped at 0:
+//   G = g_clear - sum_k depth_k exp(-((x - cx_k - vx_k t)^2 + (y - cy_k - vy_k t)^2) / (2 sigma_k^2)).
+// Shadow k is sh[6k .. 6k+5] = cx, cy, vx, vy, depth, sigma.  The clouds of
+// the reference are painted as opacity canvases moving at constant speed
+// (001_clouds.cu:55-62, :96-137); this is the synthetic field of the
+// benchmark configurations, shared by the host generator and the device.
+PVGLU_HD double pvglu_shadow_irradiance(double x, double y, const double* sh, int count, double t,
+                                        double g_clear) {
+  double g = g_clear;
+  for (int k = 0; k < count; k++) {
+    const double* c = sh + 6 * k;
+    const double dx = x - (c[0] + c[2] * t);
+    const double dy = y - (c[1] + c[3] * t);
+    g -= c[4] * pvglu_exp(-(dx * dx + dy * dy) / (2.0 * c[5] * c[5]));
+  }
+  return g > 0.0 ? g : 0.0;
+}

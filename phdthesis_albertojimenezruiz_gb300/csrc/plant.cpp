@@ -162,31 +162,32 @@ int build_plant(const PlantConfig& cfg, Plant& P) {
   return OK;
 }
 
-void plant_irradiance(const Plant& P, const ShadowConfig& sc, uint64_t seed,
-                      double t, double* g_out) {
+void plant_shadows(const Plant& P, const ShadowConfig& sc, uint64_t seed,
+                   std::vector<double>& params) {
   SplitMix64 rng(seed * 0x2545F4914F6CDD1Dull + 0x1234567ull);
   const int ns = sc.min_shadows +
                  (int)(rng.next() % (uint64_t)(sc.max_shadows - sc.min_shadows + 1));
-  std::vector<double> cx(ns), cy(ns), vx(ns), vy(ns), depth(ns), sigma(ns);
+  params.assign(6 * (size_t)ns, 0.0);
   for (int k = 0; k < ns; k++) {
-    cx[k] = rng.uniform(0.0, P.extent_x);
-    cy[k] = rng.uniform(0.0, P.extent_y);
-    depth[k] = rng.uniform(sc.min_depth, sc.max_depth);
-    sigma[k] = rng.uniform(sc.min_sigma, sc.max_sigma);
+    double* c = &params[6 * (size_t)k];
+    c[0] = rng.uniform(0.0, P.extent_x);
+    c[1] = rng.uniform(0.0, P.extent_y);
+    c[4] = rng.uniform(sc.min_depth, sc.max_depth);
+    c[5] = rng.uniform(sc.min_sigma, sc.max_sigma);
     const double speed = rng.uniform(sc.min_speed, sc.max_speed);
     const double ang = rng.uniform(0.0, 6.283185307179586);
-    vx[k] = speed * std::cos(ang);
-    vy[k] = speed * std::sin(ang);
+    c[2] = speed * std::cos(ang);
+    c[3] = speed * std::sin(ang);
   }
-  for (int i = 0; i < P.n_panels; i++) {
-    double g = sc.g_clear;
-    for (int k = 0; k < ns; k++) {
-      const double dx = P.pan_x[i] - (cx[k] + vx[k] * t);
-      const double dy = P.pan_y[i] - (cy[k] + vy[k] * t);
-      g -= depth[k] * std::exp(-(dx * dx + dy * dy) / (2.0 * sigma[k] * sigma[k]));
-    }
-    g_out[i] = g > 0.0 ? g : 0.0;
-  }
+}
+
+void plant_irradiance(const Plant& P, const ShadowConfig& sc, uint64_t seed,
+                      double t, double* g_out) {
+  std::vector<double> sh;
+  plant_shadows(P, sc, seed, sh);
+  const int ns = (int)(sh.size() / 6);
+  for (int i = 0; i < P.n_panels; i++)
+    g_out[i] = pvglu_shadow_irradiance(P.pan_x[i], P.pan_y[i], sh.data(), ns, t, sc.g_clear);
 }
 
 }  // namespace pvglu

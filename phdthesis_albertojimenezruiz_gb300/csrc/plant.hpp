@@ -66,6 +66,11 @@ struct Plant {
 
 int build_plant(const PlantConfig& cfg, Plant& out);
 
+// The seeded Gaussian shadows of one scenario: 6 values per shadow (cx, cy,
+// vx, vy, depth, sigma; see pvglu_shadow_irradiance).
+void plant_shadows(const Plant& p, const ShadowConfig& sc, uint64_t seed,
+                   std::vector<double>& params);
+
 // Per-panel irradiance G for one scenario at time t (seeded Gaussian shadows
 // drifting with constant velocity; G clamped at 0).
 void plant_irradiance(const Plant& p, const ShadowConfig& sc, uint64_t seed,

@@ -1,4 +1,5 @@
 // C ABI of the plant generator (include/pvglu_plant.h), host part.
+#include <algorithm>
 #include <string>
 #include <vector>
 
@@ -104,6 +105,23 @@ int pvglu_plant_irradiance(const pvglu_plant* h, int min_shadows, int max_shadow
   sc.min_depth = min_depth;
   sc.max_depth = max_depth;
   pvglu::plant_irradiance(h->p, sc, seed, t, g_out);
+  return PVGLU_OK;
+}
+
+int pvglu_plant_shadows(const pvglu_plant* h, int min_shadows, int max_shadows,
+                        double min_depth, double max_depth, uint64_t seed, int* count,
+                        double* params) {
+  if (!h || !count || !params || min_shadows < 0 || max_shadows < min_shadows)
+    return PVGLU_ERR_BAD_ARG;
+  pvglu::ShadowConfig sc;
+  sc.min_shadows = min_shadows;
+  sc.max_shadows = max_shadows;
+  sc.min_depth = min_depth;
+  sc.max_depth = max_depth;
+  std::vector<double> sh;
+  pvglu::plant_shadows(h->p, sc, seed, sh);
+  *count = (int)(sh.size() / 6);
+  std::copy(sh.begin(), sh.end(), params);
   return PVGLU_OK;
 }
 

@@ -51,6 +51,26 @@ class Newton:
         N.check(N.lib().pvglu_newton_set_voltages(self.handle, _ptr(v), _stream_ptr(stream)),
                 "pvglu_newton_set_voltages")
 
+    def set_field(self, elem_x, elem_y, shadows_per_scenario, g_clear: float = 1000.0,
+                  iph_per_g: float = 8.5 / 1000.0) -> None:
+        """Device irradiance field: one [count, 6] shadow array per scenario."""
+        mx = max([len(sh) for sh in shadows_per_scenario] + [1])
+        S = len(shadows_per_scenario)
+        counts = np.array([len(sh) for sh in shadows_per_scenario], dtype=np.int32)
+        params = np.zeros((S, mx, 6))
+        for s, sh in enumerate(shadows_per_scenario):
+            params[s, : len(sh)] = sh
+        self._field = [np.ascontiguousarray(elem_x, dtype=np.float64),
+                       np.ascontiguousarray(elem_y, dtype=np.float64), counts, params]
+        N.check(N.lib().pvglu_newton_set_field(self.handle, _ptr(self._field[0]),
+                                               _ptr(self._field[1]), int(mx), _ptr(counts),
+                                               _ptr(params), float(g_clear), float(iph_per_g)),
+                "pvglu_newton_set_field")
+
+    def field_iph(self, t: float, g_out=None, stream=None) -> None:
+        N.check(N.lib().pvglu_newton_field_iph(self.handle, float(t), _ptr(g_out),
+                                               _stream_ptr(stream)), "pvglu_newton_field_iph")
+
     def set_refinement(self, tol: float, max_sweeps: int) -> None:
         N.check(N.lib().pvglu_newton_set_refinement(self.handle, float(tol), int(max_sweeps)),
                 "pvglu_newton_set_refinement")

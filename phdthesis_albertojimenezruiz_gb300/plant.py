@@ -68,6 +68,17 @@ class Plant:
                                                float(t), _ptr(g)), "pvglu_plant_irradiance")
         return g
 
+    def shadows(self, seed: int, preset: str = "c1") -> np.ndarray:
+        """The seeded shadows of `irradiance(seed, t, preset)`: [count, 6] rows of
+        (centre x, centre y, velocity x, velocity y, depth, sigma)."""
+        sh = SHADOWS[preset]
+        out = np.zeros((sh["max_shadows"], 6))
+        cnt = C.c_int(0)
+        N.check(N.lib().pvglu_plant_shadows(self.handle, sh["min_shadows"], sh["max_shadows"],
+                                            sh["min_depth"], sh["max_depth"], int(seed),
+                                            C.byref(cnt), _ptr(out)), "pvglu_plant_shadows")
+        return out[: cnt.value].copy()
+
     def panel_iv(self, iph: np.ndarray, v: np.ndarray):
         iph = np.ascontiguousarray(iph, dtype=np.float64)
         v = np.ascontiguousarray(v, dtype=np.float64)

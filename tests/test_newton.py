@@ -354,3 +354,41 @@ def test_refine_transposed_and_stamped(cuda):
         np.add.at(A, (rows, p.colidx), a)
         ref = np.linalg.solve(A.T, b[:, s])
         assert norm_err(xt[:, s], ref) <= 1e-10
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("preset", ["c1", "c4"])
+def test_device_irradiance_field_matches_host(cuda, preset):
+    """The device field gives the host generator's irradiance bit for bit at
+    every time step, and a Newton solve fed from it matches one fed with the
+    host photocurrents."""
+    import torch
+
+    p, sym, port = setup((2, 4, 10))
+    S = 3
+    seeds = [11, 12, 13]
+    num = Numeric(sym, S, FP64, SCHED_LEVELS)
+    nw = Newton.for_plant(num, p)
+    ld = num.ld
+    nw.set_field(p.pan_x, p.pan_y, [p.shadows(sd, preset) for sd in seeds],
+                 iph_per_g=p.info["iph_stc"] / 1000.0)
+    g_dev = torch.zeros(p.n_panels * ld, dtype=torch.float64, device="cuda")
+    for t in (0.0, 1.0, 7.5):
+        nw.field_iph(t, g_dev)
+        torch.cuda.synchronize()
+        got = g_dev.cpu().numpy().reshape(p.n_panels, ld)[:, :S]
+        want = np.stack([p.irradiance(sd, t, preset) for sd in seeds], 1)
+        assert np.array_equal(got, want), t
+    # Newton from the field at t = 7.5 vs from host photocurrents.
+    v0 = dev(cols(np.repeat(p.flat_start()[:, None], S, 1), ld))
+    nw.set_voltages(v0)
+    nw.run(1e-6 * p.n)
+    x1 = torch.zeros(p.n * ld, dtype=torch.float64, device="cuda")
+    nw.solution(x1)
+    nw.set_iph(dev(cols((p.info["iph_stc"] / 1000.0) * want, ld)))  # the field's product order
+    nw.set_voltages(v0)
+    nw.run(1e-6 * p.n)
+    x2 = torch.zeros(p.n * ld, dtype=torch.float64, device="cuda")
+    nw.solution(x2)
+    torch.cuda.synchronize()
+    assert np.array_equal(x1.cpu().numpy(), x2.cpu().numpy())
