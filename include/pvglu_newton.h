@@ -113,6 +113,13 @@ const double* pvglu_newton_voltages(const pvglu_newton* nw);
 /* Node solution of each scenario's last linear solve, caller order, into
  * device x [n * ld]. */
 int pvglu_newton_solution(pvglu_newton* nw, double* x, void* stream);
+/* Kirchhoff current mismatch of each scenario at its node solution x:
+ * max_i |(A_lin x)_i + sum of the element currents at V = x[hi] - x[lo]
+ * leaving node i - b_lin_i| [A], the convergence measure of the synthetic
+ * configurations (||mismatch||_inf < 1e-9 A).  Host out [S].  Synchronous;
+ * uses the driver's companion buffer as scratch (the next iteration rebuilds
+ * it). */
+int pvglu_newton_mismatch(pvglu_newton* nw, double* out);
 /* Number of iteration bodies launched by the last pvglu_newton_run and
  * whether they ran as a graph (1) or as direct launches (0). */
 int pvglu_newton_last_run(const pvglu_newton* nw, int* bodies, int* graph);

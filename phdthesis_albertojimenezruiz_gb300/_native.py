@@ -110,6 +110,7 @@ _SIGS = {
     "pvglu_newton_solution": ([_P, _P, _P], _I),
     "pvglu_newton_last_run": ([_P, _IP, _IP], _I),
     "pvglu_newton_adjoint": ([_P, _P, _P, _P], _I),
+    "pvglu_newton_mismatch": ([_P, _P], _I),
     "pvglu_plant_create": ([_I, _I, _I, C.POINTER(_P)], _I),
     "pvglu_plant_destroy": ([_P], _I),
     "pvglu_plant_get_info": ([_P, C.POINTER(PlantInfo)], _I),

@@ -7,6 +7,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <string>
 #include <vector>
 
@@ -274,6 +275,41 @@ __global__ void k_nt_field(NtDev D, FieldDev F, double t, double* __restrict__ g
                                   F.count[s], t, F.g_clear);
     D.iph[e] = F.iph_per_g * g;
     if (g_out) g_out[e] = g;
+  });
+}
+
+// Kirchhoff mismatch at the node solution x (caller order): element currents
+// f = -I(V) with V = x[hi] - x[lo] (kept in `cur`), then per unknown
+// F = A_lin x + incidence * f - b_lin and max_i |F_i| per scenario (bits of
+// a non-negative double, atomicMax).
+__global__ void k_nt_elem_current(NtDev D, const double* __restrict__ x,
+                                  double* __restrict__ cur) {
+  for_rows(D.n_elems, D.ld, [&](int k, int s) {
+    if (s >= D.S) return;
+    const int64_t e = (int64_t)k * D.ld + s;
+    const int h = D.hi[k], l = D.lo[k];
+    const double v = (h >= 0 ? x[(int64_t)h * D.ld + s] : 0.0) -
+                     (l >= 0 ? x[(int64_t)l * D.ld + s] : 0.0);
+    double c, didv, didiph;
+    pvglu_panel_eval(&D.panel, D.iph[e], v, &c, &didv, &didiph);
+    cur[e] = -c;
+  });
+}
+
+__global__ void k_nt_mismatch(NtDev D, const int* __restrict__ a_rowptr,
+                              const int* __restrict__ a_colidx, const double* __restrict__ a_lin,
+                              const double* __restrict__ x, const double* __restrict__ cur,
+                              unsigned long long* __restrict__ out) {
+  for_rows(D.n, D.ld, [&](int i, int s) {
+    if (s >= D.S) return;
+    double f = -D.b_lin[i];
+    for (int p = a_rowptr[i]; p < a_rowptr[i + 1]; p++)
+      f += a_lin[p] * x[(int64_t)a_colidx[p] * D.ld + s];
+    for (int c = D.inc_ptr[i]; c < D.inc_ptr[i + 1]; c++) {
+      const double q = cur[(int64_t)D.inc_elem[c] * D.ld + s];
+      f = D.inc_sign[c] > 0 ? f + q : f - q;
+    }
+    atomicMax(out + s, (unsigned long long)__double_as_longlong(fabs(f)));
   });
 }
 
@@ -721,6 +757,29 @@ int pvglu_newton_solution(pvglu_newton* nw, double* x, void* stream) {
   const size_t nv = (size_t)h->n * h->ld;
   PVGLU_CUDA(cudaMemcpyAsync(x, nw->x64, nv * sizeof(double), cudaMemcpyDeviceToDevice,
                              as_stream(stream)));
+  return PVGLU_OK;
+}
+
+int pvglu_newton_mismatch(pvglu_newton* nw, double* out) {
+  if (!nw || !out) return fail(PVGLU_ERR_BAD_ARG, "NULL argument");
+  pvglu_numeric* h = nw->num;
+  const pvglu::NtDev& D = nw->D;
+  unsigned long long* mm = nullptr;
+  PVGLU_CUDA(cudaMalloc((void**)&mm, D.ld * sizeof(unsigned long long)));
+  cudaError_t e = cudaMemset(mm, 0, D.ld * sizeof(unsigned long long));
+  if (e == cudaSuccess) {
+    pvglu::k_nt_elem_current<<<pvglu::rows_grid(D.n_elems, D.ld, 256), 256>>>(D, nw->x64, D.ieq);
+    pvglu::k_nt_mismatch<<<pvglu::rows_grid(D.n, D.ld, 256), 256>>>(
+        D, h->d.a_rowptr, h->d.a_colidx, h->st_base, nw->x64, D.ieq, mm);
+    e = cudaGetLastError();
+  }
+  std::vector<unsigned long long> hb(D.ld);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e == cudaSuccess)
+    e = cudaMemcpy(hb.data(), mm, D.ld * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+  cudaFree(mm);
+  if (e != cudaSuccess) return fail(PVGLU_ERR_CUDA, cudaGetErrorString(e));
+  for (int s = 0; s < D.S; s++) std::memcpy(&out[s], &hb[s], sizeof(double));
   return PVGLU_OK;
 }
 

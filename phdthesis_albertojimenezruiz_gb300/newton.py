@@ -104,6 +104,12 @@ class Newton:
         N.check(N.lib().pvglu_newton_solution(self.handle, _ptr(x), _stream_ptr(stream)),
                 "pvglu_newton_solution")
 
+    def mismatch(self) -> np.ndarray:
+        """max_i |KCL mismatch| [A] per scenario at the node solution."""
+        out = np.zeros(self.num.S)
+        N.check(N.lib().pvglu_newton_mismatch(self.handle, _ptr(out)), "pvglu_newton_mismatch")
+        return out
+
     def adjoint(self, dpdx, dpdiph, stream=None) -> None:
         N.check(N.lib().pvglu_newton_adjoint(self.handle, _ptr(dpdx), _ptr(dpdiph),
                                              _stream_ptr(stream)), "pvglu_newton_adjoint")

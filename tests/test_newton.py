@@ -392,3 +392,20 @@ def test_device_irradiance_field_matches_host(cuda, preset):
     nw.solution(x2)
     torch.cuda.synchronize()
     assert np.array_equal(x1.cpu().numpy(), x2.cpu().numpy())
+
+
+@pytest.mark.gpu
+def test_kirchhoff_mismatch_after_convergence(cuda):
+    """The device mismatch agrees with a host evaluation of Kirchhoff's law
+    on the same node solution, and is below 1e-9 A once the iteration has
+    converged to a tight tolerance (the convergence test of the synthetic
+    configurations)."""
+    p, sym, port = setup((4, 8, 20))
+    S = 2
+    g = np.stack([bright(p, 30 + s) for s in range(S)], 1)
+    num, nw, it, out, diff, v, x = run_device(p, sym, g, FP64, SCHED_LEVELS, 1e-10)
+    mm = nw.mismatch()
+    for s in range(S):
+        host = kcl_residual(p, p.iph(g[:, s]), x[:, s])
+        assert abs(mm[s] - host) <= 1e-12 + 1e-6 * host
+        assert mm[s] < 1e-9
