@@ -405,6 +405,191 @@ def config4_section(stream, steps: int) -> dict:
             "not_converged": int((sw <= 0).sum()), "max_rel_err_vs_fp64": err}
 
 
+def _newton_handle(p, sym, S: int, precision, tol_ir: float = 1e-12):
+    from phdthesis_albertojimenezruiz_gb300 import FP32, Newton, Numeric
+    from phdthesis_albertojimenezruiz_gb300.glu import autotune
+
+    ml, sc, _ = autotune(sym, S, precision)
+    num = Numeric(sym, S, precision, sc, max_locals=ml)
+    nw = Newton.for_plant(num, p)
+    if precision == FP32:
+        nw.set_refinement(tol_ir, IR_MAX_SWEEPS)
+    return num, nw
+
+
+def _pad(a: np.ndarray, ld: int) -> np.ndarray:
+    out = np.zeros((a.shape[0], ld))
+    out[:, : a.shape[1]] = a
+    return out
+
+
+def config1_section() -> dict:
+    """4x8x20 plant (652 unknowns), FP64 Newton on the device to a Kirchhoff
+    mismatch below 1e-9 A, against the CPU oracle's Newton loop on the same
+    input (bit-identical expected) with both timed."""
+    import torch
+
+    from oracle import oracle as O
+    from phdthesis_albertojimenezruiz_gb300 import FP64, GMIN_STAGES, Plant, Symbolic
+
+    p = Plant(4, 8, 20)
+    sym = Symbolic(p.rowptr, p.colidx)
+    g = p.irradiance(seed=1, preset="c1")
+    num, nw = _newton_handle(p, sym, 1, FP64)
+    tol = 1e-9
+    iph = p.iph(g)
+    nw.set_iph(torch.from_numpy(iph).cuda())
+    nw.set_voltages(torch.from_numpy(p.flat_start()).cuda())
+    nw.run(tol)  # warm-up (graph capture)
+    torch.cuda.synchronize()
+    nw.set_voltages(torch.from_numpy(p.flat_start()).cuda())
+    t0 = time.perf_counter()
+    nw.run(tol)
+    gpu_s = time.perf_counter() - t0
+    it, out, _ = nw.results()
+    x = torch.zeros(p.n, dtype=torch.float64, device="cuda")
+    nw.solution(x)
+    mm = float(nw.mismatch()[0])
+    port = O.Port(p.rowptr, p.colidx, sym.array("perm_amd"))
+    t0 = time.perf_counter()
+    rc, it_o, _, _, x_o = port.newton(p, iph, p.flat_start(), GMIN_STAGES, tol)
+    cpu_s = time.perf_counter() - t0
+    return {"workload": f"plant_4x8x20 ({p.n} unknowns), FP64 Newton, gmin stages, "
+                        f"tol {tol} on sum |dV|", "iterations": int(it[0]),
+            "oracle_iterations": it_o, "converged": bool(out[0] == 0 and rc == 0),
+            "kcl_mismatch_a": mm, "bit_identical_to_oracle": bool(np.array_equal(x.cpu().numpy(), x_o)),
+            "gpu_newton_s": gpu_s, "cpu_oracle_newton_s": cpu_s}
+
+
+def config2_section() -> dict:
+    """The 35k plant over 300 time steps (t = 0..299 s, 5 shadows drifting at
+    5-15 m/s): the photocurrents of every step come from the device
+    irradiance field and all steps are solved as one batch, FP64."""
+    import torch
+
+    from phdthesis_albertojimenezruiz_gb300 import FP64, Plant, Symbolic
+
+    p = Plant(*DIMS)
+    sym = Symbolic(p.rowptr, p.colidx)
+    T = 300
+    num, nw = _newton_handle(p, sym, T, FP64)
+    ld = num.ld
+    sh = p.shadows(2024, "c2")
+    # scenario t sees the field at time t (dt = 1 s); photocurrents straight
+    # into the driver from the device field
+    nw.set_field(p.pan_x, p.pan_y, [sh] * T, iph_per_g=p.info["iph_stc"] / 1000.0,
+                 t_offset=np.arange(T, dtype=np.float64))
+    nw.field_iph(0.0)
+    v0 = torch.from_numpy(_pad(np.repeat(p.flat_start()[:, None], T, 1), ld)).cuda()
+    tol = 1e-6 * p.n
+    nw.set_voltages(v0)
+    nw.run(tol)
+    torch.cuda.synchronize()
+    nw.set_voltages(v0)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    nw.run(tol)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    it, out, _ = nw.results()
+    return {"workload": "plant_50x24x28, 300 time steps of one 5-shadow field as one FP64 "
+                        "batch, gmin stages, tol 1e-6*n", "time_steps": T,
+            "newton_ms": ms, "time_steps_per_s": T / (ms / 1000.0),
+            "iterations_min": int(it.min()), "iterations_max": int(it.max()),
+            "converged": int((out == 0).sum()),
+            "refactor_solves_per_s": float(it.sum()) / (ms / 1000.0)}
+
+
+def config5_fd_section(precision_name: str) -> dict:
+    """Per-panel adjoint gradients of the 35k plant against central
+    differences on 200 random panels, all 401 perturbed solves in one batch."""
+    import torch
+
+    from phdthesis_albertojimenezruiz_gb300 import FP32, FP64, Plant, Symbolic
+
+    prec = FP64 if precision_name == "fp64" else FP32
+    p = Plant(*DIMS)
+    sym = Symbolic(p.rowptr, p.colidx)
+    rng = np.random.default_rng(77)
+    panels = rng.choice(p.n_panels, 200, replace=False)
+    g0 = p.irradiance(seed=5000, preset="c2")
+    h = 1e-2
+    cols = [g0]
+    for k in panels:
+        for sign in (1.0, -1.0):
+            gk = g0.copy()
+            gk[k] += sign * h
+            cols.append(gk)
+    G = np.stack(cols, 1)
+    S = G.shape[1]
+    num, nw = _newton_handle(p, sym, S, prec)
+    ld = num.ld
+    nw.set_iph(torch.from_numpy(_pad(p.iph(G), ld)).cuda())
+    nw.set_voltages(torch.from_numpy(_pad(np.repeat(p.flat_start()[:, None], S, 1), ld)).cuda())
+    nw.run(1e-7)
+    x = torch.zeros(p.n * ld, dtype=torch.float64, device="cuda")
+    nw.solution(x)
+    dpdx = np.zeros((p.n, ld))
+    dpdx[p.inv_current, :S] = -p.v_mppt
+    grad = torch.zeros(p.n_panels * ld, dtype=torch.float64, device="cuda")
+    nw.adjoint(torch.from_numpy(dpdx).cuda(), grad)
+    torch.cuda.synchronize()
+    it, out, _ = nw.results()
+    x = x.cpu().numpy().reshape(p.n, ld)
+    P = -p.v_mppt * x[p.inv_current, :S].sum(axis=0)
+    adj = grad.cpu().numpy().reshape(p.n_panels, ld)[panels, 0] * (p.info["iph_stc"] / 1000.0)
+    fd = (P[1::2] - P[2::2]) / (2 * h)
+    err = np.abs(adj - fd)
+    scale = np.abs(adj).max()
+    # The FP64 CPU adjoint of the oracle (factors bit-identical to the
+    # reference's) at the same operating point, every panel.
+    from oracle import oracle as O
+
+    port = O.Port(p.rowptr, p.colidx, sym.array("perm_amd"))
+    v = torch.as_tensor(_VoltView(nw.voltages_ptr(), p.n_panels * ld),
+                        device="cuda").cpu().numpy().reshape(p.n_panels, ld)[:, 0]
+    dpdx1 = np.zeros(p.n)
+    dpdx1[p.inv_current] = -p.v_mppt
+    ref = port.adjoint(p, p.iph(g0), v, dpdx1) * (p.info["iph_stc"] / 1000.0)
+    full = grad.cpu().numpy().reshape(p.n_panels, ld)[:, 0] * (p.info["iph_stc"] / 1000.0)
+    return {"workload": f"plant_50x24x28, dP/dG of 200 random panels, central differences "
+                        f"(h = {h} W/m^2) as 400 extra scenarios in the same batch, "
+                        f"{precision_name} forward", "scenarios": S,
+            "converged": int((out == 0).sum()),
+            "fd_max_abs_err_over_max_grad": float(err.max() / scale),
+            "fd_median_rel_err": float(np.median(err / np.maximum(np.abs(fd), 1e-12))),
+            "fd_note": "per-panel differences of a 6.6 MW plant power are at the FP64 "
+                       "rounding floor of P; the all-panel directional check is in "
+                       "newton_adjoint.fd_check",
+            "vs_cpu_fp64_adjoint_all_panels_max_rel": float(
+                np.abs(full - ref).max() / np.abs(ref).max()),
+            "max_grad_w_per_w_m2": float(scale)}
+
+
+class _VoltView:
+    def __init__(self, ptr, count):
+        self.__cuda_array_interface__ = {"shape": (count,), "typestr": "<f8",
+                                         "data": (ptr, False), "version": 3}
+
+
+def run_configs(args, stream) -> dict:
+    wanted = {c.strip() for c in args.configs.split(",") if c.strip()}
+    out = {}
+    if "1" in wanted:
+        out["config1"] = config1_section()
+    if "2" in wanted:
+        out["config2"] = config2_section()
+    if "3" in wanted:
+        out["config3"] = config3_section(stream, max(5, args.steps))
+    if "4" in wanted:
+        out["config4"] = config4_section(stream, max(5, args.steps))
+    if "5" in wanted:
+        out["config5_fd"] = {m: config5_fd_section(m) for m in ("fp64", "fp32")}
+    return out
+
+
 def run_reference(args) -> None:
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -461,9 +646,11 @@ def main() -> None:
                     help="chain-program table size of the batched handle (0: autotune)")
     ap.add_argument("--schedule", default="persistent", choices=["levels", "persistent"],
                     help="schedule used with --max-locals (autotuned otherwise)")
-    ap.add_argument("--configs", default="3,4",
-                    help="extra workloads reported beside the headline (3: three plant sizes in "
-                         "one launch per level, 4: the 135k plant; empty: none)")
+    ap.add_argument("--configs", default="1,2,3,4,5",
+                    help="extra workloads reported beside the headline (1: 4x8x20 Newton vs the "
+                         "oracle, 2: 300 time steps, 3: three plant sizes per level launch, "
+                         "4: the 135k plant, 5: per-panel adjoint vs central differences; "
+                         "empty: none)")
     ap.add_argument("--only-configs", action="store_true",
                     help="run the --configs workloads alone (profiling runs)")
     ap.add_argument("--newton-max-locals", type=int, default=0,
@@ -491,12 +678,7 @@ def main() -> None:
                                                     SCHED_THREAD_CHAIN, Numeric, Symbolic)
 
     if args.only_configs:
-        wanted = {c.strip() for c in args.configs.split(",") if c.strip()}
-        out = {}
-        if "3" in wanted:
-            out["config3"] = config3_section(torch.cuda.current_stream(), max(5, args.steps))
-        if "4" in wanted:
-            out["config4"] = config4_section(torch.cuda.current_stream(), max(5, args.steps))
+        out = run_configs(args, torch.cuda.current_stream())
         if rank == 0:
             print(json.dumps(out))
         return
@@ -695,12 +877,7 @@ def main() -> None:
         if dist:
             dist.destroy_process_group()
         return
-    extra = {}
-    wanted = {c.strip() for c in args.configs.split(",") if c.strip()}
-    if "3" in wanted:
-        extra["config3"] = config3_section(stream, max(5, args.steps))
-    if "4" in wanted:
-        extra["config4"] = config4_section(stream, max(5, args.steps))
+    extra = run_configs(args, stream)
     newton = (newton_section(p, sym, stream, args.newton_scenarios, 5000,
                              precision=args.newton_precision)
               if args.newton_scenarios > 0 else None)

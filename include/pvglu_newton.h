@@ -79,8 +79,10 @@ int pvglu_newton_set_voltages(pvglu_newton* nw, const double* v, void* stream);
  * (pvglu_plant_shadows gives them for the synthetic plant). */
 int pvglu_newton_set_field(pvglu_newton* nw, const double* elem_x, const double* elem_y,
                            int max_shadows, const int* counts, const double* shadows,
-                           double g_clear, double iph_per_g);
-/* Photocurrents of every element and scenario at time t from the field,
+                           const double* t_offset, double g_clear, double iph_per_g);
+/* t_offset (host [S] or NULL): scenario s sees the field at time t +
+ * t_offset[s] (time steps of one field solved as one batch).
+ * Photocurrents of every element and scenario at time t from the field,
  * iph = iph_per_g * G (pvglu_shadow_irradiance), straight into the driver's
  * photocurrent buffer: no host traffic per time step.  g_out (device
  * [n_elems * ld]) receives G, or NULL. */

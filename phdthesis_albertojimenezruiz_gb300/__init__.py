@@ -9,10 +9,11 @@ from . import _native
 from ._native import (FP32, FP64, SCHED_LEVELS, SCHED_PERSISTENT, SCHED_THREAD_CHAIN,
                       PvgluError)
 from .glu import Numeric, Symbolic
-from .newton import GMIN_STAGES, Newton
+from .newton import GMIN_STAGES, Newton, plant_power
 from .plant import Plant
 
 _native.lib()  # fail loudly at import when the native library is absent
 
 __all__ = ["FP32", "FP64", "GMIN_STAGES", "SCHED_LEVELS", "SCHED_PERSISTENT",
-           "SCHED_THREAD_CHAIN", "Newton", "Numeric", "PvgluError", "Plant", "Symbolic"]
+           "SCHED_THREAD_CHAIN", "Newton", "Numeric", "PvgluError", "Plant", "Symbolic",
+           "plant_power"]

@@ -262,6 +262,7 @@ struct FieldDev {
   const double* y;
   const double* shadow;  // [ld][max_shadows][6]
   const int* count;      // [ld]
+  const double* toff;    // [ld] time offset of each scenario
   int max_shadows;
   double g_clear, iph_per_g;
 };
@@ -272,7 +273,7 @@ __global__ void k_nt_field(NtDev D, FieldDev F, double t, double* __restrict__ g
     double g = 0.0;
     if (s < D.S)
       g = pvglu_shadow_irradiance(F.x[k], F.y[k], F.shadow + (int64_t)s * F.max_shadows * 6,
-                                  F.count[s], t, F.g_clear);
+                                  F.count[s], t + F.toff[s], F.g_clear);
     D.iph[e] = F.iph_per_g * g;
     if (g_out) g_out[e] = g;
   });
@@ -639,7 +640,7 @@ int pvglu_newton_set_voltages(pvglu_newton* nw, const double* v, void* stream) {
 
 int pvglu_newton_set_field(pvglu_newton* nw, const double* elem_x, const double* elem_y,
                            int max_shadows, const int* counts, const double* shadows,
-                           double g_clear, double iph_per_g) {
+                           const double* t_offset, double g_clear, double iph_per_g) {
   if (!nw || !elem_x || !elem_y || !counts || max_shadows < 0 || max_shadows > 4096 ||
       (max_shadows > 0 && !shadows))
     return fail(PVGLU_ERR_BAD_ARG, "bad set_field arguments");
@@ -652,6 +653,8 @@ int pvglu_newton_set_field(pvglu_newton* nw, const double* elem_x, const double*
   std::copy(shadows, shadows + (size_t)S * max_shadows * 6, sh.begin());
   std::vector<int> cnt(ld, 0);
   std::copy(counts, counts + S, cnt.begin());
+  std::vector<double> toff(ld, 0.0);
+  if (t_offset) std::copy(t_offset, t_offset + S, toff.begin());
   for (void* p : nw->field_allocs) cudaFree(p);
   nw->field_allocs.clear();
   nw->has_field = false;
@@ -666,8 +669,11 @@ int pvglu_newton_set_field(pvglu_newton* nw, const double* elem_x, const double*
   nw->field_allocs.push_back(ds);
   rc |= upload(cnt, &dc);
   nw->field_allocs.push_back(dc);
+  double* dt = nullptr;
+  rc |= upload(toff, &dt);
+  nw->field_allocs.push_back(dt);
   if (rc) return fail(PVGLU_ERR_NO_MEMORY, "field upload failed");
-  nw->field = pvglu::FieldDev{dx, dy, ds, dc, max_shadows, g_clear, iph_per_g};
+  nw->field = pvglu::FieldDev{dx, dy, ds, dc, dt, max_shadows, g_clear, iph_per_g};
   nw->has_field = true;
   return PVGLU_OK;
 }

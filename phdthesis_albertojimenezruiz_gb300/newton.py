@@ -52,19 +52,22 @@ class Newton:
                 "pvglu_newton_set_voltages")
 
     def set_field(self, elem_x, elem_y, shadows_per_scenario, g_clear: float = 1000.0,
-                  iph_per_g: float = 8.5 / 1000.0) -> None:
-        """Device irradiance field: one [count, 6] shadow array per scenario."""
+                  iph_per_g: float = 8.5 / 1000.0, t_offset=None) -> None:
+        """Device irradiance field: one [count, 6] shadow array per scenario;
+        t_offset [S]: scenario s sees the field at t + t_offset[s]."""
         mx = max([len(sh) for sh in shadows_per_scenario] + [1])
         S = len(shadows_per_scenario)
         counts = np.array([len(sh) for sh in shadows_per_scenario], dtype=np.int32)
         params = np.zeros((S, mx, 6))
         for s, sh in enumerate(shadows_per_scenario):
             params[s, : len(sh)] = sh
+        toff = None if t_offset is None else np.ascontiguousarray(t_offset, dtype=np.float64)
         self._field = [np.ascontiguousarray(elem_x, dtype=np.float64),
-                       np.ascontiguousarray(elem_y, dtype=np.float64), counts, params]
+                       np.ascontiguousarray(elem_y, dtype=np.float64), counts, params, toff]
         N.check(N.lib().pvglu_newton_set_field(self.handle, _ptr(self._field[0]),
                                                _ptr(self._field[1]), int(mx), _ptr(counts),
-                                               _ptr(params), float(g_clear), float(iph_per_g)),
+                                               _ptr(params), _ptr(toff), float(g_clear),
+                                               float(iph_per_g)),
                 "pvglu_newton_set_field")
 
     def field_iph(self, t: float, g_out=None, stream=None) -> None:
@@ -119,3 +122,46 @@ class Newton:
         if h and N._lib is not None:
             N.lib().pvglu_newton_destroy(h)
             self.handle = None
+
+
+def plant_power(newton: Newton, plant, g, tol: float = 1e-9, gmin=GMIN_STAGES):
+    """Total MPPT power [W] of every scenario of `plant` at per-panel irradiance
+    g (torch CUDA float64 [n_panels, S]), differentiable in g.
+
+    Forward: the device Newton driver from the flat start (its factors and
+    pattern stay in `newton`); backward: the adjoint (pvglu_newton_adjoint) at
+    the converged operating point.  torch.autograd.Function semantics: the
+    returned tensor has a grad_fn whose backward gives dP/dG."""
+    import torch
+
+    class _PlantPower(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, gg):
+            num = newton.num
+            ld, S = num.ld, num.S
+            iph_per_g = plant.info["iph_stc"] / 1000.0
+            iph = torch.zeros(plant.n_panels, ld, dtype=torch.float64, device=gg.device)
+            iph[:, :S] = iph_per_g * gg
+            v0 = torch.zeros_like(iph)
+            v0[:, :S] = torch.as_tensor(plant.flat_start(), device=gg.device)[:, None]
+            newton.set_iph(iph)
+            newton.set_voltages(v0)
+            newton.run(tol, gmin=gmin)
+            x = torch.zeros(plant.n, ld, dtype=torch.float64, device=gg.device)
+            newton.solution(x)
+            cur = torch.as_tensor(plant.inv_current, dtype=torch.long, device=gg.device)
+            ctx.iph_per_g = iph_per_g
+            return -plant.v_mppt * x[cur, :S].sum(dim=0)
+
+        @staticmethod
+        def backward(ctx, grad_p):
+            num = newton.num
+            ld, S = num.ld, num.S
+            dpdx = torch.zeros(plant.n, ld, dtype=torch.float64, device=grad_p.device)
+            cur = torch.as_tensor(plant.inv_current, dtype=torch.long, device=grad_p.device)
+            dpdx[cur, :S] = -plant.v_mppt * grad_p[None, :].to(torch.float64)
+            out = torch.zeros(plant.n_panels, ld, dtype=torch.float64, device=grad_p.device)
+            newton.adjoint(dpdx, out)
+            return ctx.iph_per_g * out[:, :S]
+
+    return _PlantPower.apply(g)
