@@ -233,7 +233,6 @@ int run_refine(pvglu_numeric* h, const AValues& A, const double* b, double* x, b
                double tol, int max_sweeps, int* sweeps_out, cudaStream_t st,
                const int* init_done) {
   if (h->precision != PVGLU_FP32) return fail(PVGLU_ERR_BAD_ARG, "needs an FP32 handle");
-  const int64_t nv = (int64_t)h->n * h->ld;
   float* w = static_cast<float*>(h->work);
   int* ndone = h->ir_done + h->ld;
   if (init_done) {
@@ -241,7 +240,7 @@ int run_refine(pvglu_numeric* h, const AValues& A, const double* b, double* x, b
     k_ir_init<<<rows_grid(h->n, h->ld, 256), 256, 0, st>>>(h->n, h->ld, h->S, init_done,
                                                            h->ir_done, ndone, x);
   } else {
-    PVGLU_CUDA(cudaMemsetAsync(x, 0, nv * sizeof(double), st));
+    // x needs no clearing: the first sweep assigns it (k_ir_update, first).
     PVGLU_CUDA(cudaMemsetAsync(h->ir_done, 0, (h->ld + 1) * sizeof(int), st));
   }
   PVGLU_CUDA(cudaMemsetAsync(h->ir_max_dx, 0, h->ld * sizeof(unsigned long long), st));
@@ -273,7 +272,7 @@ int run_refine(pvglu_numeric* h, const AValues& A, const double* b, double* x, b
     int rc = solve_permuted<float>(h, w, transpose, st, skip);  // dx of this sweep
     if (rc) return rc;
     k_ir_update<<<grd, blk, 0, st>>>(out_perm, h->n, h->ld, h->S, w, x, h->ir_done, ndone,
-                                     h->ir_max_dx, h->ir_max_x);
+                                     h->ir_max_dx, h->ir_max_x, sweep == 1 ? 1 : 0);
     k_ir_check<<<(h->S + 127) / 128, 128, 0, st>>>(h->S, sweep, max_sweeps, tol, h->ir_done,
                                                    ndone, sweeps_out, h->ir_max_dx,
                                                    h->ir_max_x, h->ir_prev_dx);
@@ -566,19 +565,22 @@ int pvglu_numeric_create_ex(const pvglu_symbolic* sym, int n_scenarios, int prec
     pvglu::build_chain_program(s, ph - 1, budget, prog);
     h->prog_level_ml[ph] = prog.level_max_locals;
     h->table_max = std::max(h->table_max, prog.max_locals);
-    std::vector<int4> seg(prog.seg.size()), ops(prog.ops.size() / 4);
+    std::vector<int4> seg(prog.seg.size()), ops(prog.ops.size() / 4), carry(prog.seg.size());
     for (size_t i = 0; i < seg.size(); i++) {
       const auto& g = prog.seg[i];
       seg[i] = make_int4(g.load_begin,
                          g.n_load < 0 ? -1
-                                      : (g.n_load | (g.n_own << 16) | (g.reads_own_chain << 30)),
+                                      : (g.n_load | (g.n_own << 16) | (g.n_carry << 26) |
+                                         (g.reads_own_chain << 30)),
                          g.op_begin, g.n_op);
+      carry[i] = make_int4(g.carry[0], g.carry[1], g.carry[2], g.carry[3]);
     }
     std::memcpy(ops.data(), prog.ops.data(), ops.size() * sizeof(int4));
     pvglu::ProgDev& P = h->progs.p[ph];
     rc |= h->put(prog.level_chain, &P.level_chain);
     rc |= h->put(prog.chain_seg, &P.chain_seg);
     rc |= h->put(seg, &P.seg);
+    rc |= h->put(carry, &P.carry);
     rc |= h->put(prog.loads, &P.loads);
     rc |= h->put(ops, &P.ops);
     rc |= h->put(prog.op_col, &P.op_col);

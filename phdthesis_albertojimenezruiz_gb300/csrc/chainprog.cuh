@@ -26,7 +26,9 @@ struct ProgDev {
   const int* level_chain;  // [levels + 1]
   int n_levels;
   const int* chain_seg;    // [chains + 1]
-  const int4* seg;         // {load_begin, n_load | n_own << 16 (or -1: DIRECT), op_begin, n_op}
+  const int4* seg;         // {load_begin, n_load | n_own << 16 | n_carry << 26 |
+                           //  reads_own_chain << 30 (or -1: DIRECT), op_begin, n_op}
+  const int4* carry;       // [segments] up to 4 moves (from << 16 | to) of table rows
   const int* loads;
   const int4* ops;         // packed operations, 4 per int4
   const int* op_col;       // column of each SCALE operation
@@ -233,20 +235,44 @@ __device__ __forceinline__ void prog_run_chain(const ProgDev& P, const DevStruct
       continue;
     }
     const int* lr = P.loads + sg.x;
-    const int nl = sg.y & 0xffff, n_own = (sg.y >> 16) & 0x3ff;
+    const int nl = sg.y & 0xffff, n_own = (sg.y >> 16) & 0x3ff, n_carry = (sg.y >> 26) & 7;
+    // Rows the previous segment of this chain left in the table: moved, not
+    // loaded (to-locals kept for the load loop).
+    int c_to[4] = {-1, -1, -1, -1};
+    int4 cv = make_int4(-1, -1, -1, -1);
+    if (n_carry) {
+      cv = __ldg(P.carry + g);
+      c_to[0] = cv.x & 0xffff;
+      if (n_carry > 1) c_to[1] = cv.y & 0xffff;
+      if (n_carry > 2) c_to[2] = cv.z & 0xffff;
+      if (n_carry > 3) c_to[3] = cv.w & 0xffff;
+    }
+    auto is_carried = [&](int l) {
+      return l == c_to[0] || l == c_to[1] || l == c_to[2] || l == c_to[3];
+    };
     if (BATCH) {
       using V2 = typename Vec2<T>::type;
       constexpr unsigned kRow = kGroup * sizeof(T);
       // The previous segment's bulk stores must have read the table; when
-      // this segment reads rows they wrote, they must also be complete.
+      // this segment loads rows they wrote, they must also be complete.
       if ((sg.y >> 30) & 1) bulk_wait_all();
       else bulk_wait_read();
       __syncwarp();
-      if (lane == 0) mbar_arrive_expect_tx(tma.mbar, (unsigned)nl * kRow);
+      if (n_carry) {
+        V2* t = reinterpret_cast<V2*>(sm) + lane;
+        const int from[4] = {cv.x >> 16, cv.y >> 16, cv.z >> 16, cv.w >> 16};
+        V2 hold[4];
+        for (int c = 0; c < n_carry; c++) hold[c] = t[from[c] << 5];
+        __syncwarp();
+        for (int c = 0; c < n_carry; c++) t[c_to[c] << 5] = hold[c];
+        __syncwarp();
+      }
+      if (lane == 0) mbar_arrive_expect_tx(tma.mbar, (unsigned)(nl - n_carry) * kRow);
       __syncwarp();
       for (int l = lane; l < nl; l += 32)
-        bulk_load(sm + l * kGroup, prog_row<T, KIND>(__ldg(lr + l), v, x, ld, s0), kRow,
-                  tma.mbar);
+        if (!is_carried(l))
+          bulk_load(sm + l * kGroup, prog_row<T, KIND>(__ldg(lr + l), v, x, ld, s0), kRow,
+                    tma.mbar);
       long long polls = 0;
       while (!mbar_try_wait(tma.mbar, tma.phase)) {
         if (++polls > kMbarMaxPolls) {
@@ -273,7 +299,16 @@ __device__ __forceinline__ void prog_run_chain(const ProgDev& P, const DevStruct
         bulk_store(prog_row<T, KIND>(__ldg(lr + l), v, x, ld, s0), sm + l * kGroup, kRow);
       bulk_commit();
     } else {
-      for (int l = lane; l < nl; l += 32) sm[l] = prog_fetch1<T, KIND>(__ldg(lr + l), v, x);
+      if (n_carry) {
+        const int from[4] = {cv.x >> 16, cv.y >> 16, cv.z >> 16, cv.w >> 16};
+        T hold[4];
+        for (int c = 0; c < n_carry; c++) hold[c] = sm[from[c]];
+        __syncwarp();
+        if (lane == 0)
+          for (int c = 0; c < n_carry; c++) sm[c_to[c]] = hold[c];
+      }
+      for (int l = lane; l < nl; l += 32)
+        if (!is_carried(l)) sm[l] = prog_fetch1<T, KIND>(__ldg(lr + l), v, x);
       __syncwarp();
       if (lane == 0) {
         const int4* o4 = P.ops + (sg.z >> 2);

@@ -407,22 +407,27 @@ k_residual_rows(const int* __restrict__ ptr, const int* __restrict__ idx,
 // maxima are taken on integer bits (|dx| exactly, |x| truncated to its upper
 // 32 bits, a lower bound within 2^-20): the one FP64 instruction per entry is
 // the addition.
+// first: x starts at 0, so x = dx without reading x (and padding columns
+// s >= S are set to 0).
 static __global__ void k_ir_update(const int* __restrict__ out_perm, int n, int ld, int S,
                             const float* __restrict__ dx, double* __restrict__ x,
                             const int* __restrict__ done, const int* __restrict__ ndone,
                             unsigned long long* __restrict__ max_dx,
-                            unsigned long long* __restrict__ max_x) {
+                            unsigned long long* __restrict__ max_x, int first) {
   if (__ldcg(ndone) >= S) return;
   // block = (32 scenarios) x (8 rows); grid-stride over row tiles.
   const int s = blockIdx.y * 32 + threadIdx.x;
   __shared__ unsigned int sdx[8][33], sx[8][33];
   unsigned int mdx = 0u, mx = 0u;
+  if (first && s >= S && s < ld)
+    for (int c = blockIdx.x * 8 + threadIdx.y; c < n; c += gridDim.x * 8)
+      x[(int64_t)out_perm[c] * ld + s] = 0.0;
   if (s < S && !done[s]) {
 #pragma unroll 4
     for (int c = blockIdx.x * 8 + threadIdx.y; c < n; c += gridDim.x * 8) {
       const float df = dx[(int64_t)c * ld + s];
       double* xp = x + (int64_t)out_perm[c] * ld + s;
-      const double nx = *xp + f2d_bits(df);
+      const double nx = first ? f2d_bits(df) : *xp + f2d_bits(df);
       *xp = nx;
       mdx = max(mdx, __float_as_uint(df) & 0x7fffffffu);
       mx = max(mx, (unsigned int)((unsigned long long)__double_as_longlong(nx) >> 32) &

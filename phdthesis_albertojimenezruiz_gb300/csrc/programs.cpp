@@ -196,6 +196,9 @@ void build_chain_program(const Symbolic& s, int kind, const std::vector<int>& le
   auto written = [&](int ref) -> char& {
     return (kind >= 0 && ref >= 0) ? written_x[ref] : written_v[kind < 0 ? ref : -ref - 1];
   };
+  // Final table layout of the previous segment of the current chain
+  // (ref -> local), for carries.  Empty at a chain start and after DIRECT.
+  std::vector<std::pair<int, int>> prev_layout;
   auto close = [&]() {
     if (t.units.empty()) return;
     // Own entries first (in load order), then the read-only ones.
@@ -207,13 +210,6 @@ void build_chain_program(const Symbolic& s, int kind, const std::vector<int>& le
     g.n_own = 0;
     g.reads_own_chain = 0;
     for (int l = 0; l < nl; l++)
-      if (!t.own[l] && written(t.refs[l])) g.reads_own_chain = 1;
-    for (int l = 0; l < nl; l++)
-      if (t.own[l] && !written(t.refs[l])) {
-        written(t.refs[l]) = 1;
-        written_list.push_back(t.refs[l]);
-      }
-    for (int l = 0; l < nl; l++)
       if (t.own[l]) {
         remap[l] = g.n_own++;
         out.loads.push_back(t.refs[l]);
@@ -224,6 +220,24 @@ void build_chain_program(const Symbolic& s, int kind, const std::vector<int>& le
         remap[l] = next++;
         out.loads.push_back(t.refs[l]);
       }
+    // Carries: entries the previous segment's table holds (its final values).
+    std::vector<char> carried(nl, 0);
+    for (int l = 0; l < nl && g.n_carry < kMaxCarry; l++)
+      for (const auto& pl : prev_layout)
+        if (pl.first == t.refs[l]) {
+          g.carry[g.n_carry++] = (pl.second << 16) | remap[l];
+          carried[l] = 1;
+          break;
+        }
+    for (int l = 0; l < nl; l++)
+      if (!t.own[l] && !carried[l] && written(t.refs[l])) g.reads_own_chain = 1;
+    for (int l = 0; l < nl; l++)
+      if (t.own[l] && !written(t.refs[l])) {
+        written(t.refs[l]) = 1;
+        written_list.push_back(t.refs[l]);
+      }
+    prev_layout.clear();
+    for (int l = 0; l < nl; l++) prev_layout.push_back({t.refs[l], remap[l]});
     g.op_begin = (int)out.ops.size();
     for (const RawOp& o : t.ops) {
       const int a = remap[o.a];
@@ -245,6 +259,7 @@ void build_chain_program(const Symbolic& s, int kind, const std::vector<int>& le
     max_locals = out.level_max_locals.empty() ? kMaxLocals : out.level_max_locals[level];
     for (int r : written_list) written(r) = 0;
     written_list.clear();
+    prev_layout.clear();
     out.chain_seg.push_back((int)out.seg.size());
     const int first_seg = (int)out.seg.size();
     for (int k = ls.start_chains[c]; k < ls.start_chains[c + 1]; k++) {
@@ -259,6 +274,7 @@ void build_chain_program(const Symbolic& s, int kind, const std::vector<int>& le
         // the segment collected so far (chain order is execution order).
         close();
         out.seg.push_back(Segment{0, -1, 0, u, 0, 1});
+        prev_layout.clear();  // the DIRECT unit updates rows in global memory
         // A DIRECT unit writes its own entries through global memory.
         const int own_ref = kind < 0 ? -1 : u;
         if (own_ref >= 0 && !written(own_ref)) {

@@ -41,9 +41,16 @@ inline uint32_t pack_op(int code, int a, int b, int c) {
 // segment's own entries, written back after the operations.
 // A segment with n_load < 0 is DIRECT: unit `op_begin` (a column or row
 // too wide for the table) is executed straight from global memory.
+// Up to kMaxCarry entries a segment needs that the previous segment of the
+// same chain already holds in its table are moved inside shared memory
+// instead of being loaded (carry[k] = from << 16 | to, -1 unused).
+constexpr int kMaxCarry = 4;
+
 struct Segment {
   int load_begin, n_load, n_own, op_begin, n_op;
-  int reads_own_chain = 0;  // reads entries written by an earlier segment of the chain
+  int reads_own_chain = 0;  // loads entries written by an earlier segment of the chain
+  int n_carry = 0;
+  int carry[kMaxCarry] = {-1, -1, -1, -1};
 };
 
 struct ChainProgram {
