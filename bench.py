@@ -676,6 +676,7 @@ def main() -> None:
 
     from phdthesis_albertojimenezruiz_gb300 import (FP32, FP64, SCHED_LEVELS, SCHED_PERSISTENT,
                                                     SCHED_THREAD_CHAIN, Numeric, Symbolic)
+    from phdthesis_albertojimenezruiz_gb300.replicas import max_over_ranks
 
     if args.only_configs:
         out = run_configs(args, torch.cuda.current_stream())
@@ -757,11 +758,7 @@ def main() -> None:
         torch.cuda.synchronize()
     if dist:
         dist.barrier()
-    ms = ev0.elapsed_time(ev1)
-    if dist:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ev0.elapsed_time(ev1), dist, dev)
     refactor_ms = float(np.mean([s.elapsed_time(e) for s, e in rf]))
     sw = sweeps.cpu().numpy()[:S]
     value = S * world * args.steps / (ms / 1000.0)
@@ -847,11 +844,7 @@ def main() -> None:
     stream.wait_event(e2)
     e1.record(stream)
     torch.cuda.synchronize()
-    e2e_ms = e0.elapsed_time(e1)
-    if dist:
-        t = torch.tensor([e2e_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = max_over_ranks(e0.elapsed_time(e1), dist, dev)
     e2e = S * world * e2e_steps / (e2e_ms / 1000.0)
     e2e_sw = np.concatenate([sweeps.cpu().numpy()[:S], sweeps2.cpu().numpy()[:S]])
     e2e_err = float(np.max(np.abs(x_hs[0].numpy()[:, :S] - xb).max(axis=0) /
@@ -868,8 +861,7 @@ def main() -> None:
                 "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak if peak else None,
                 # DRAM read + write bytes of one refactorization (its two level
-                # launches) from the ncu capture summarised in
-                # profiles/kernels_fp32ir_plant35k_512scen.md (512 scenarios).
+                # launches) from an ncu capture of this workload (512 scenarios).
                 "traffic": REFACTOR_TRAFFIC_512 if S == 512 else None,
                 "peak_source": "measured" if peak else "fallback",
                 "bytes_per_launch": bm["refactor"] * S, "avg_launch_ms": refactor_ms}
