@@ -88,6 +88,15 @@ int pvglu_newton_set_field(pvglu_newton* nw, const double* elem_x, const double*
  * [n_elems * ld]) receives G, or NULL. */
 int pvglu_newton_field_iph(pvglu_newton* nw, double t, double* g_out, void* stream);
 
+/* Broken panels.  The reference replaces a broken panel by a wire of
+ * resistance 1e-5 ohm between the same nodes (003_create_electric_system.cpp:
+ * 248-260, main.h:76): the Jacobian pattern does not change, so no new
+ * analysis is needed -- the flagged elements (host [n_elems], nonzero =
+ * broken; NULL clears) switch to that linear law on the device (conductance
+ * 1/r_wire, no current source, no damping, not part of the Newton diff, no
+ * irradiance sensitivity). */
+int pvglu_newton_set_broken(pvglu_newton* nw, const int* broken, double r_wire);
+
 /* Iteration of FP32 handles: refinement tolerance and sweep limit of each
  * linear solve (defaults 1e-12, 8).  Each Newton step solves for the node
  * voltages themselves, not for a correction, so this tolerance bounds the

@@ -107,10 +107,12 @@ class Port(_Base):
             lib.oracle_scatter_refactor_solve.argtypes = [C.c_void_p] * 4 + [C.c_int]
             D = C.c_double
             lib.oracle_newton.argtypes = ([C.c_void_p, C.c_int] + [C.c_void_p] * 4 + [C.c_int] +
-                                          [C.c_void_p] * 2 + [D] * 4 + [C.c_void_p] * 3 +
-                                          [C.c_int, D, C.c_int] + [C.c_void_p] * 3)
+                                          [C.c_void_p] * 2 + [D] * 4 + [C.c_void_p, D] +
+                                          [C.c_void_p] * 3 + [C.c_int, D, C.c_int] +
+                                          [C.c_void_p] * 3)
             lib.oracle_adjoint.argtypes = ([C.c_void_p, C.c_int] + [C.c_void_p] * 4 + [C.c_int] +
-                                           [C.c_void_p] * 2 + [D] * 4 + [C.c_void_p] * 4)
+                                           [C.c_void_p] * 2 + [D] * 4 + [C.c_void_p, D] +
+                                           [C.c_void_p] * 4)
             lib.oracle_free.argtypes = [C.c_void_p]
             cls._lib = lib
         return cls._lib
@@ -156,7 +158,7 @@ class Port(_Base):
 
 
     # ---- Newton loop and adjoint (oracle_newton.cpp) -------------------------
-    def _circuit(self, plant):
+    def _circuit(self, plant, broken=None, r_wire=1e-5):
         i = plant.info
         keep = [np.ascontiguousarray(plant.rowptr, dtype=np.int32),
                 np.ascontiguousarray(plant.colidx, dtype=np.int32),
@@ -164,15 +166,18 @@ class Port(_Base):
                 np.ascontiguousarray(plant.b_lin, dtype=np.float64),
                 np.ascontiguousarray(plant.pan_hi, dtype=np.int32),
                 np.ascontiguousarray(plant.pan_lo, dtype=np.int32)]
+        br = None if broken is None else np.ascontiguousarray(broken, dtype=np.int32)
+        keep.append(br)
         args = [self.h, plant.n, _p(keep[0]), _p(keep[1]), _p(keep[2]), _p(keep[3]),
                 plant.n_panels, _p(keep[4]), _p(keep[5]), i["panel_i0"], i["panel_a"],
-                i["panel_rs"], i["panel_rsh"]]
+                i["panel_rs"], i["panel_rsh"], _p(br), float(r_wire)]
         return keep, args
 
-    def newton(self, plant, iph, v0, gmin, tol, max_iterations=5000):
-        """One scenario of the simulator's Newton loop.  Returns
-        (outcome, iterations, last diff, element voltages, node solution)."""
-        keep, args = self._circuit(plant)
+    def newton(self, plant, iph, v0, gmin, tol, max_iterations=5000, broken=None, r_wire=1e-5):
+        """One scenario of the simulator's Newton loop (broken: panels
+        replaced by a wire).  Returns (outcome, iterations, last diff, element
+        voltages, node solution)."""
+        keep, args = self._circuit(plant, broken, r_wire)
         iph = np.ascontiguousarray(iph, dtype=np.float64)
         v = np.array(v0, dtype=np.float64, copy=True)
         g = np.ascontiguousarray(gmin, dtype=np.float64)
@@ -184,9 +189,9 @@ class Port(_Base):
         del keep
         return rc, it.value, diff.value, v, x
 
-    def adjoint(self, plant, iph, v, dpdx):
+    def adjoint(self, plant, iph, v, dpdx, broken=None, r_wire=1e-5):
         """dP/dIph per element at the iterate v for P = dpdx . x."""
-        keep, args = self._circuit(plant)
+        keep, args = self._circuit(plant, broken, r_wire)
         iph = np.ascontiguousarray(iph, dtype=np.float64)
         v = np.ascontiguousarray(v, dtype=np.float64)
         dpdx = np.ascontiguousarray(dpdx, dtype=np.float64)

@@ -38,7 +38,11 @@ struct Circuit {
   const int *rowptr, *colidx, *hi, *lo;
   const double *a_lin, *b_lin;
   pvglu_panel_params panel;
+  const int* broken;  // [n_elems] or NULL: panels replaced by a wire
+  double g_wire;
 };
+
+bool is_broken(const Circuit& c, int k) { return c.broken && c.broken[k]; }
 
 // 002b:5-38 (admittance between n1 and n2, ground = -1).
 void add_admittance(std::vector<Row>& A, int n1, int n2, double g) {
@@ -65,6 +69,11 @@ bool assemble(const Circuit& c, const double* iph, const double* v, double gmin,
     for (int p = c.rowptr[i]; p < c.rowptr[i + 1]; p++) A[i][c.colidx[p]] = c.a_lin[p];
   b.assign(c.b_lin, c.b_lin + c.n);
   for (int k = 0; k < c.n_elems; k++) {
+    if (is_broken(c, k)) {  // 003_create_electric_system.cpp:252-255: a linear wire
+      add_admittance(A, c.hi[k], c.lo[k], c.g_wire);
+      if (didiph) (*didiph)[k] = 0.0;
+      continue;
+    }
     double cur, didv, dphi;
     pvglu_panel_iv3(&c.panel, iph[k], v[k], &cur, &didv, &dphi);
     const double f = -cur, G = -didv;
@@ -92,10 +101,11 @@ extern "C" {
 // last linear solution (caller order); iterations and the last diff out.
 int oracle_newton(void* sym, int n, const int* rowptr, const int* colidx, const double* a_lin,
                   const double* b_lin, int n_elems, const int* hi, const int* lo, double i0,
-                  double a, double rs, double rsh, const double* iph, double* v,
-                  const double* gmin, int n_stages, double tol, int max_iterations, double* x,
-                  int* iterations, double* last_diff) {
-  const Circuit c{n, n_elems, rowptr, colidx, hi, lo, a_lin, b_lin, {i0, a, rs, rsh}};
+                  double a, double rs, double rsh, const int* broken, double r_wire,
+                  const double* iph, double* v, const double* gmin, int n_stages, double tol,
+                  int max_iterations, double* x, int* iterations, double* last_diff) {
+  const Circuit c{n,     n_elems, rowptr, colidx, hi, lo, a_lin, b_lin, {i0, a, rs, rsh},
+                  broken, 1.0 / r_wire};
   const int* csc_row = nullptr;
   long long nnz_lu = 0;
   oracle_get(sym, "csc_row", &csc_row, &nnz_lu);
@@ -122,19 +132,23 @@ int oracle_newton(void* sym, int n, const int* rowptr, const int* colidx, const 
         newv[k] = (hi[k] >= 0 ? sol[hi[k]] : 0.0) - (lo[k] >= 0 ? sol[lo[k]] : 0.0);
         movement[k] = 1.0;
       }
+      // A wire is not a nonlinear element: it takes its new voltage drop and
+      // is not part of the damping or of diff (011:37-90 only walks the
+      // nonlinear sources).
+      auto nonlinear = [&](int k) { return !is_broken(c, k); };
       for (;;) {
         for (int k = 0; k < n_elems; k++)
-          cand[k] = v[k] * (1.0 - movement[k]) + newv[k] * movement[k];
+          cand[k] = nonlinear(k) ? v[k] * (1.0 - movement[k]) + newv[k] * movement[k] : newv[k];
         for (int k = 0; k < n_elems; k++)
-          if (movement[k] < 1e-13) {
+          if (nonlinear(k) && movement[k] < 1e-13) {
             *iterations = it;
             for (int i = 0; i < n; i++) x[i] = sol[i];
             return 3;
           }
         bool reduce = false;
         for (int k = 0; k < n_elems; k++) {
-          const bool ok = !std::isnan(v[k]) && !std::isnan(cand[k]) &&
-                          !(std::fabs(v[k] - cand[k]) > 1.0);
+          const bool ok = !nonlinear(k) || (!std::isnan(v[k]) && !std::isnan(cand[k]) &&
+                                            !(std::fabs(v[k] - cand[k]) > 1.0));
           if (ok) continue;
           movement[k] /= 2.0;
           reduce = true;
@@ -143,7 +157,7 @@ int oracle_newton(void* sym, int n, const int* rowptr, const int* colidx, const 
       }
       diff = 0;
       for (int k = 0; k < n_elems; k++) {
-        diff += std::fabs(cand[k] - v[k]);
+        if (nonlinear(k)) diff += std::fabs(cand[k] - v[k]);
         v[k] = cand[k];
       }
     }
@@ -159,9 +173,10 @@ int oracle_newton(void* sym, int n, const int* rowptr, const int* colidx, const 
 // dP/dIph[k] = dI/dIph * (lambda[hi] - lambda[lo]).  Returns 0, 4 (pivot) or 5.
 int oracle_adjoint(void* sym, int n, const int* rowptr, const int* colidx, const double* a_lin,
                    const double* b_lin, int n_elems, const int* hi, const int* lo, double i0,
-                   double a, double rs, double rsh, const double* iph, const double* v,
-                   const double* dpdx, double* dpdiph) {
-  const Circuit c{n, n_elems, rowptr, colidx, hi, lo, a_lin, b_lin, {i0, a, rs, rsh}};
+                   double a, double rs, double rsh, const int* broken, double r_wire,
+                   const double* iph, const double* v, const double* dpdx, double* dpdiph) {
+  const Circuit c{n,     n_elems, rowptr, colidx, hi, lo, a_lin, b_lin, {i0, a, rs, rsh},
+                  broken, 1.0 / r_wire};
   const int *csc_row = nullptr, *perm_amd = nullptr, *perm_rows = nullptr;
   long long nnz_lu = 0, len = 0;
   oracle_get(sym, "csc_row", &csc_row, &nnz_lu);

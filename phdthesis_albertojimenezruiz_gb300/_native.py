@@ -102,6 +102,7 @@ _SIGS = {
     "pvglu_newton_set_iph": ([_P, _P, _P], _I),
     "pvglu_newton_set_voltages": ([_P, _P, _P], _I),
     "pvglu_newton_set_refinement": ([_P, C.c_double, _I], _I),
+    "pvglu_newton_set_broken": ([_P, _P, C.c_double], _I),
     "pvglu_newton_set_field": ([_P, _P, _P, _I, _P, _P, _P, C.c_double, C.c_double], _I),
     "pvglu_newton_field_iph": ([_P, C.c_double, _P, _P], _I),
     "pvglu_newton_run": ([_P, _P, _I, C.c_double, _I, _I, _P], _I),

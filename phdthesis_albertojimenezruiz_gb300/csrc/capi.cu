@@ -637,7 +637,7 @@ int pvglu_numeric_set_pivot_tol(pvglu_numeric* h, double tol) {
 
 int pvglu_scatter(pvglu_numeric* h, const double* a_values, void* stream) {
   if (!h || !a_values) return fail(PVGLU_ERR_BAD_ARG, "NULL argument");
-  const pvglu::AValues A{a_values, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  const pvglu::AValues A{a_values, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   return pvglu::run_scatter(h, A, nullptr, as_stream(stream));
 }
 
@@ -696,7 +696,7 @@ int pvglu_refine(pvglu_numeric* h, const double* a_values, const double* g, cons
     return fail(PVGLU_ERR_BAD_ARG, "bad refine arguments");
   if (g && !h->st_ptr) return fail(PVGLU_ERR_BAD_ARG, "no stamps set on this handle");
   const pvglu::AValues A = a_values ? pvglu::AValues{a_values, nullptr, nullptr, nullptr,
-                                                     nullptr, nullptr, nullptr}
+                                                     nullptr, nullptr, nullptr, nullptr}
                                     : h->stamps(g, gmin);
   return pvglu::run_refine(h, A, b, x, (flags & PVGLU_SOLVE_TRANSPOSE) != 0, tol, max_sweeps,
                            sweeps_out, as_stream(stream));

@@ -89,8 +89,9 @@ struct pvglu_numeric {
   int* st_ptr = nullptr;
   int* st_elem = nullptr;
   int* st_sign = nullptr;
-  pvglu::AValues stamps(const double* g, const double* gmin) const {
-    return pvglu::AValues{nullptr, st_base, st_ptr, st_elem, st_sign, g, gmin};
+  pvglu::AValues stamps(const double* g, const double* gmin,
+                        const int* linear = nullptr) const {
+    return pvglu::AValues{nullptr, st_base, st_ptr, st_elem, st_sign, g, gmin, linear};
   }
   ~pvglu_numeric() {
     for (void* p : allocs) cudaFree(p);

@@ -157,6 +157,7 @@ struct AValues {
   const int* sign;      // +1 / -1
   const double* g;      // [n_elems x ld] element conductances
   const double* gmin;   // [ld] per-scenario convergence conductance, or NULL
+  const int* linear;    // [n_elems] elements that take no gmin (wires), or NULL
   __device__ __forceinline__ double operator()(int e, int ld, int s) const {
     if (a) return a[(int64_t)e * ld + s];
     double val = base[e];
@@ -164,7 +165,7 @@ struct AValues {
     for (int c = ptr[e]; c < ptr[e + 1]; c++) {
       const double sg = (double)sign[c];
       val += sg * g[(int64_t)elem[c] * ld + s];
-      if (gm > 0.0) val += sg * gm;
+      if (gm > 0.0 && !(linear && linear[elem[c]])) val += sg * gm;
     }
     return val;
   }

@@ -37,6 +37,8 @@ struct NtDev {
   const int* inc_sign;    // +1: + terminal, -1: - terminal
   const double* b_lin;    // [n]
   pvglu_panel_const panel;  // constants of the element law
+  const int* broken;        // [n_elems] 1: replaced by a wire (or NULL: none)
+  double g_wire;            // conductance of that wire
   double* iph;            // [n_elems x ld] photocurrent
   double* v;              // voltage iterate
   double* g;              // companion conductance G
@@ -72,6 +74,11 @@ __global__ void k_nt_companion(NtDev D) {
       D.gmin_s[s] = gm > 0.0 ? gm : 0.0;
     }
     const int64_t e = (int64_t)k * D.ld + s;
+    if (D.broken && D.broken[k]) {  // linear wire: exact companion, no source
+      D.g[e] = D.g_wire;
+      D.ieq[e] = 0.0;
+      return;
+    }
     const double v = D.v[e];
     double cur, didv, didiph;
     pvglu_panel_eval(&D.panel, D.iph[e], v, &cur, &didv, &didiph);
@@ -167,6 +174,10 @@ __global__ void __launch_bounds__(256) k_nt_update(NtDev D, const double* __rest
       const double xh = h >= 0 ? X[(int64_t)(xpos ? xpos[h] : h) * D.ld + s] : 0.0;
       const double xl = l >= 0 ? X[(int64_t)(xpos ? xpos[l] : l) * D.ld + s] : 0.0;
       const double old = D.v[e];
+      if (D.broken && D.broken[k]) {  // a wire is a linear element: no damping, no diff
+        D.v[e] = __dsub_rn(xh, xl);
+        continue;
+      }
       double change;
       D.v[e] = damped_step(old, __dsub_rn(xh, xl), &bad, &change);
       sum = __dadd_rn(sum, change);
@@ -291,6 +302,10 @@ __global__ void k_nt_elem_current(NtDev D, const double* __restrict__ x,
     const int h = D.hi[k], l = D.lo[k];
     const double v = (h >= 0 ? x[(int64_t)h * D.ld + s] : 0.0) -
                      (l >= 0 ? x[(int64_t)l * D.ld + s] : 0.0);
+    if (D.broken && D.broken[k]) {
+      cur[e] = D.g_wire * v;
+      return;
+    }
     double c, didv, didiph;
     pvglu_panel_eval(&D.panel, D.iph[e], v, &c, &didv, &didiph);
     cur[e] = -c;
@@ -320,6 +335,11 @@ __global__ void k_nt_adjoint_companion(NtDev D) {
   for_rows(D.n_elems, D.ld, [&](int k, int s) {
     if (s >= D.S) return;
     const int64_t e = (int64_t)k * D.ld + s;
+    if (D.broken && D.broken[k]) {
+      D.g[e] = D.g_wire;
+      D.ieq[e] = 0.0;  // a wire does not depend on the irradiance
+      return;
+    }
     double cur, didv, didiph;
     pvglu_panel_eval(&D.panel, D.iph[e], D.v[e], &cur, &didv, &didiph);
     D.g[e] = -didv;
@@ -363,6 +383,7 @@ struct pvglu_newton {
   double ir_tol = 1e-12;
   pvglu::FieldDev field{};
   bool has_field = false;
+  int* broken_dev = nullptr;
   std::vector<void*> field_allocs;
   int ir_sweeps = 8;
   // Captured iteration body and what it was captured with.
@@ -374,6 +395,7 @@ struct pvglu_newton {
   int last_bodies = 0, last_graph = 0;
   ~pvglu_newton() {
     for (void* p : field_allocs) cudaFree(p);
+    if (broken_dev) cudaFree(broken_dev);
     if (graph) cudaGraphExecDestroy(graph);
     if (cap_stream) cudaStreamDestroy(cap_stream);
     if (pinned_ndone) cudaFreeHost(pinned_ndone);
@@ -408,7 +430,7 @@ int newton_body(pvglu_newton* nw, cudaStream_t st) {
   pvglu::k_nt_companion<<<pvglu::rows_grid(D.n_elems, D.ld, 256), 256, 0, st>>>(D);
   pvglu::k_nt_rhs<<<pvglu::rows_grid(D.n, D.ld, 256), 256, 0, st>>>(
       D, fp64 ? nw->w64 : nw->rhs64, fp64 ? h->row_pos : nullptr);
-  const pvglu::AValues A = h->stamps(D.g, D.gmin_s);
+  const pvglu::AValues A = h->stamps(D.g, D.gmin_s, D.broken);
   int rc = pvglu::run_scatter(h, A, ndone, st);
   if (rc) return rc;
   const double* X;
@@ -685,6 +707,29 @@ int pvglu_newton_field_iph(pvglu_newton* nw, double t, double* g_out, void* stre
   pvglu::k_nt_field<<<pvglu::rows_grid(D.n_elems, D.ld, 256), 256, 0, as_stream(stream)>>>(
       D, nw->field, t, g_out);
   PVGLU_CUDA(cudaGetLastError());
+  return PVGLU_OK;
+}
+
+int pvglu_newton_set_broken(pvglu_newton* nw, const int* broken, double r_wire) {
+  if (!nw || (broken && !(r_wire > 0.0))) return fail(PVGLU_ERR_BAD_ARG, "bad set_broken arguments");
+  if (nw->broken_dev) {
+    cudaFree(nw->broken_dev);
+    nw->broken_dev = nullptr;
+  }
+  nw->D.broken = nullptr;
+  if (!broken) return PVGLU_OK;
+  std::vector<int> flags(broken, broken + nw->n_elems);
+  for (int& f : flags) f = f ? 1 : 0;
+  int* d = nullptr;
+  if (upload(flags, &d)) return fail(PVGLU_ERR_NO_MEMORY, "broken flags upload");
+  nw->broken_dev = d;
+  nw->D.broken = d;
+  nw->D.g_wire = 1.0 / r_wire;
+  // The captured body holds the old device view: capture it again.
+  if (nw->graph) {
+    cudaGraphExecDestroy(nw->graph);
+    nw->graph = nullptr;
+  }
   return PVGLU_OK;
 }
 

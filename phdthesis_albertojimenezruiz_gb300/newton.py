@@ -74,6 +74,12 @@ class Newton:
         N.check(N.lib().pvglu_newton_field_iph(self.handle, float(t), _ptr(g_out),
                                                _stream_ptr(stream)), "pvglu_newton_field_iph")
 
+    def set_broken(self, broken=None, r_wire: float = 1e-5) -> None:
+        """Flags [n_elems] of panels replaced by a wire (None clears)."""
+        self._broken = None if broken is None else np.ascontiguousarray(broken, dtype=np.int32)
+        N.check(N.lib().pvglu_newton_set_broken(self.handle, _ptr(self._broken), float(r_wire)),
+                "pvglu_newton_set_broken")
+
     def set_refinement(self, tol: float, max_sweeps: int) -> None:
         N.check(N.lib().pvglu_newton_set_refinement(self.handle, float(tol), int(max_sweeps)),
                 "pvglu_newton_set_refinement")

@@ -442,3 +442,44 @@ def test_plant_power_autograd(cuda):
         dn = plant_power(nw, p, torch.tensor(g0 - h * d[:, None], device="cuda"))
     fd = ((up - dn) / (2 * h)).cpu().numpy()
     assert np.all(np.abs(grad.T @ d - fd) <= 1e-6 * np.abs(fd))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("schedule", [SCHED_LEVELS, SCHED_PERSISTENT])
+def test_broken_panels_match_oracle(cuda, schedule):
+    """Broken panels become 1e-5 ohm wires on the same pattern (no new
+    analysis): the device Newton and adjoint equal the oracle's."""
+    import torch
+
+    p, sym, port = setup((2, 4, 10))
+    S = 2
+    g = np.stack([bright(p, 50 + s) for s in range(S)], 1)
+    broken = np.zeros(p.n_panels, np.int32)
+    broken[[3, 17, 41]] = 1
+    num = Numeric(sym, S, FP64, schedule)
+    nw = Newton.for_plant(num, p)
+    nw.set_broken(broken)
+    ld = num.ld
+    nw.set_iph(dev(cols(p.iph(g), ld)))
+    nw.set_voltages(dev(cols(np.repeat(p.flat_start()[:, None], S, 1), ld)))
+    tol = 1e-6 * p.n
+    nw.run(tol)
+    it, out, _ = nw.results()
+    x = torch.zeros(p.n * ld, dtype=torch.float64, device="cuda")
+    nw.solution(x)
+    dpdx = objective(p)
+    grad = torch.zeros(p.n_panels * ld, dtype=torch.float64, device="cuda")
+    v = torch.as_tensor(_DevView(nw.voltages_ptr(), (p.n_panels * ld,)),
+                        device="cuda").cpu().numpy().reshape(p.n_panels, ld)
+    nw.adjoint(dev(cols(np.repeat(dpdx[:, None], S, 1), ld)), grad)
+    torch.cuda.synchronize()
+    x = x.cpu().numpy().reshape(p.n, ld)
+    grad = grad.cpu().numpy().reshape(p.n_panels, ld)
+    for s in range(S):
+        rc, it_o, _, v_o, x_o = port.newton(p, p.iph(g[:, s]), p.flat_start(), GMIN_STAGES, tol,
+                                            broken=broken)
+        assert rc == 0 and out[s] == N.NEWTON_CONVERGED and it[s] == it_o
+        assert np.array_equal(x[:, s], x_o)
+        ref = port.adjoint(p, p.iph(g[:, s]), v[:, s], dpdx, broken=broken)
+        assert norm_err(grad[:, s], ref) <= 1e-10
+        assert np.all(grad[broken == 1, s] == 0.0)
