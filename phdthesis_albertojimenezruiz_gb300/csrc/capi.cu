@@ -225,66 +225,208 @@ int run_refactor_solve_perm(pvglu_numeric* h, void* x, bool transpose, SkipDone 
                                     : run_phases<float>(h, phases, (float*)x, st, skip);
 }
 
+namespace {
+
+// One refinement's arguments and the launch pieces it is made of.
+struct Refine {
+  pvglu_numeric* h;
+  AValues A;
+  const double* b;
+  double* x;
+  bool transpose;
+  double tol;
+  int max_sweeps;
+  int* sweeps_out;
+  const int* init_done;
+  float* w;
+  int* ndone;
+  // J x = b:   w = b[row_orig], M y = w, x[col_orig] = y, residual rows by A.
+  // J^T x = b: w = b[col_orig], M^T z = w, x[row_orig] = z, rows by A^T.
+  const int *in_perm, *out_perm, *r_ptr, *r_idx, *r_ent, *r_pos;
+  bool vec16;  // 16-byte vector loads in the batched residual
+  dim3 grd, blk;
+  int rgrid;
+
+  Refine(pvglu_numeric* h_, const AValues& A_, const double* b_, double* x_, bool tr, double tol_,
+         int ms, int* so, const int* init)
+      : h(h_), A(A_), b(b_), x(x_), transpose(tr), tol(tol_), max_sweeps(ms), sweeps_out(so),
+        init_done(init) {
+    w = static_cast<float*>(h->work);
+    ndone = h->ir_done + h->ld;
+    in_perm = tr ? h->d.col_orig : h->d.row_orig;
+    out_perm = tr ? h->d.row_orig : h->d.col_orig;
+    r_ptr = tr ? h->at_ptr : h->d.a_rowptr;
+    r_idx = tr ? h->at_row : h->d.a_colidx;
+    r_ent = tr ? h->at_entry : nullptr;
+    r_pos = tr ? h->col_pos : h->row_pos;
+    vec16 = !((reinterpret_cast<uintptr_t>(A.a) | reinterpret_cast<uintptr_t>(b) |
+               reinterpret_cast<uintptr_t>(x)) & 15);
+    // About one full SM of threads per SM: the launches after every scenario
+    // has converged (ndone == S) then cost little.
+    blk = dim3(32, 8);
+    const int gy = (h->ld + 31) / 32;
+    const int fill = std::max(1, h->sm_count * 8);
+    grd = dim3((unsigned)std::max(1, std::min((h->n + 7) / 8, (fill + gy - 1) / gy)),
+               (unsigned)gy);
+    rgrid = std::min(rows_grid(h->n, h->ld, 256), h->resid_blocks);
+  }
+
+  // Bookkeeping reset, and w = b in pivot order (x = 0: the first residual is b).
+  int start(cudaStream_t st) const {
+    if (init_done) {
+      PVGLU_CUDA(cudaMemsetAsync(ndone, 0, sizeof(int), st));
+      k_ir_init<<<rows_grid(h->n, h->ld, 256), 256, 0, st>>>(h->n, h->ld, h->S, init_done,
+                                                             h->ir_done, ndone, x);
+    } else {
+      // x needs no clearing: the first sweep assigns it (k_ir_update, first).
+      PVGLU_CUDA(cudaMemsetAsync(h->ir_done, 0, (h->ld + 1) * sizeof(int), st));
+    }
+    PVGLU_CUDA(cudaMemsetAsync(h->ir_max_dx, 0, h->ld * sizeof(unsigned long long), st));
+    PVGLU_CUDA(cudaMemsetAsync(h->ir_max_x, 0, h->ld * sizeof(unsigned long long), st));
+    if (sweeps_out) PVGLU_CUDA(cudaMemsetAsync(sweeps_out, 0, h->ld * sizeof(int), st));
+    permute<double, float>(h, in_perm, b, w, true, st);
+    PVGLU_CUDA(cudaGetLastError());
+    return PVGLU_OK;
+  }
+
+  // dx = M^-1 w (FP32) and x += dx (FP64) for the scenarios still refining.
+  int correct(bool first, cudaStream_t st) const {
+    const int rc = solve_permuted<float>(h, w, transpose, st, SkipDone{h->ir_done, ndone});
+    if (rc) return rc;
+    k_ir_update<<<grd, blk, 0, st>>>(out_perm, h->n, h->ld, h->S, w, x, h->ir_done, ndone,
+                                     h->ir_max_dx, h->ir_max_x, first ? 1 : 0);
+    PVGLU_CUDA(cudaGetLastError());
+    return PVGLU_OK;
+  }
+
+  // w = b - A x (FP64, rounded to FP32) in pivot order for the scenarios
+  // still refining.
+  int residual(cudaStream_t st) const {
+    if (A.a && h->ld % 64 == 0 && vec16)
+      k_residual_rows<<<rgrid, 256, 0, st>>>(r_ptr, r_idx, r_ent, h->n, h->ld, h->S, A.a, b, x,
+                                             h->ir_done, ndone, w, r_pos);
+    else
+      k_residual<<<rows_grid(h->n, h->ld, 256), 256, 0, st>>>(
+          r_ptr, r_idx, r_ent, h->n, h->ld, h->S, A, b, x, h->ir_done, ndone, w, r_pos);
+    PVGLU_CUDA(cudaGetLastError());
+    return PVGLU_OK;
+  }
+
+  int check_loop(cudaGraphConditionalHandle loop, cudaStream_t st) const {
+    const int threads = std::min(1024, (h->S + 31) / 32 * 32);
+    k_ir_check_loop<<<1, threads, 0, st>>>(h->S, max_sweeps, tol, h->ir_done, ndone, sweeps_out,
+                                           h->ir_max_dx, h->ir_max_x, h->ir_prev_dx,
+                                           h->ir_sweeps_done, loop);
+    PVGLU_CUDA(cudaGetLastError());
+    return PVGLU_OK;
+  }
+};
+
+// Builds (or finds) the graph of a refinement: the first sweep, then a
+// conditional while node whose body is residual, correction and check; the
+// check's block decides whether the body runs again, so no launch is spent
+// on sweeps after convergence.  Returns false when the graph cannot be built
+// (the refinement then stays on direct launches for this handle).
+bool refine_graph(const Refine& R) {
+  pvglu_numeric* h = R.h;
+  const pvglu_numeric::RefineKey key{R.A,    R.b,         R.x,          R.sweeps_out,
+                                     R.init_done, R.tol, R.transpose ? 1 : 0, R.max_sweeps,
+                                     h->schedule};
+  if (h->ir_graph && h->ir_key == key) return true;
+  if (h->ir_graph) {
+    cudaGraphExecDestroy(h->ir_graph);
+    h->ir_graph = nullptr;
+  }
+  if (h->ir_graph_failed) return false;
+  for (cudaStream_t& c : h->ir_cap)
+    if (!c && cudaStreamCreateWithFlags(&c, cudaStreamNonBlocking) != cudaSuccess) {
+      cudaGetLastError();
+      h->ir_graph_failed = true;
+      return false;
+    }
+  cudaStream_t outer = h->ir_cap[0], inner = h->ir_cap[1];
+  cudaGraph_t g = nullptr, cg = nullptr, tmp = nullptr;
+  cudaGraphExec_t ex = nullptr;
+  bool ok = cudaStreamBeginCapture(outer, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+  const bool outer_open = ok;
+  bool inner_open = false;
+  cudaGraphConditionalHandle loop = 0;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t n_deps = 0;
+  cudaGraphNode_t node = nullptr;
+  cudaGraph_t body = nullptr;
+  ok = ok && cudaMemsetAsync(h->ir_sweeps_done, 0, sizeof(int), outer) == cudaSuccess;
+  ok = ok && R.start(outer) == PVGLU_OK && R.correct(true, outer) == PVGLU_OK;
+  ok = ok && cudaStreamGetCaptureInfo(outer, &cs, nullptr, &cg) == cudaSuccess && cg &&
+       cudaGraphConditionalHandleCreate(&loop, cg, 0, cudaGraphCondAssignDefault) == cudaSuccess;
+  ok = ok && R.check_loop(loop, outer) == PVGLU_OK;
+  ok = ok && cudaStreamGetCaptureInfo(outer, &cs, nullptr, &cg, &deps, nullptr, &n_deps) ==
+                 cudaSuccess;
+  if (ok) {
+    cudaGraphNodeParams np{};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = loop;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    ok = cudaGraphAddNode(&node, cg, deps, nullptr, n_deps, &np) == cudaSuccess;
+    if (ok) body = np.conditional.phGraph_out[0];
+    ok = ok && cudaStreamUpdateCaptureDependencies(outer, &node, nullptr, 1,
+                                                   cudaStreamSetCaptureDependencies) ==
+                   cudaSuccess;
+  }
+  if (ok) {
+    inner_open = cudaStreamBeginCaptureToGraph(inner, body, nullptr, nullptr, 0,
+                                               cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    ok = inner_open && R.residual(inner) == PVGLU_OK && R.correct(false, inner) == PVGLU_OK &&
+         R.check_loop(loop, inner) == PVGLU_OK;
+  }
+  if (inner_open) ok = (cudaStreamEndCapture(inner, &tmp) == cudaSuccess) && ok;
+  if (outer_open) ok = (cudaStreamEndCapture(outer, &g) == cudaSuccess) && ok && g;
+  ok = ok && cudaGraphInstantiate(&ex, g, 0) == cudaSuccess;
+  if (g) cudaGraphDestroy(g);
+  if (!ok) {
+    cudaGetLastError();
+    h->ir_graph_failed = true;
+    return false;
+  }
+  h->ir_graph = ex;
+  h->ir_key = key;
+  return true;
+}
+
+}  // namespace
+
 // Mixed-precision refinement on factors already in the handle: x0 = 0, then
 // per sweep dx = M^-1 r (FP32), x += dx (FP64), r = b - A x (FP64), until
 // max|dx| <= tol * max|x| per scenario or max_sweeps.  Converged scenarios
 // drop out of every later kernel (done flags; the whole launch once all are).
+// Replayed from a graph with a conditional loop when the stream is not being
+// captured and the schedule launches no cooperative kernel, otherwise
+// launched sweep by sweep.
 int run_refine(pvglu_numeric* h, const AValues& A, const double* b, double* x, bool transpose,
                double tol, int max_sweeps, int* sweeps_out, cudaStream_t st,
                const int* init_done) {
   if (h->precision != PVGLU_FP32) return fail(PVGLU_ERR_BAD_ARG, "needs an FP32 handle");
-  float* w = static_cast<float*>(h->work);
-  int* ndone = h->ir_done + h->ld;
-  if (init_done) {
-    PVGLU_CUDA(cudaMemsetAsync(ndone, 0, sizeof(int), st));
-    k_ir_init<<<rows_grid(h->n, h->ld, 256), 256, 0, st>>>(h->n, h->ld, h->S, init_done,
-                                                           h->ir_done, ndone, x);
-  } else {
-    // x needs no clearing: the first sweep assigns it (k_ir_update, first).
-    PVGLU_CUDA(cudaMemsetAsync(h->ir_done, 0, (h->ld + 1) * sizeof(int), st));
-  }
-  PVGLU_CUDA(cudaMemsetAsync(h->ir_max_dx, 0, h->ld * sizeof(unsigned long long), st));
-  PVGLU_CUDA(cudaMemsetAsync(h->ir_max_x, 0, h->ld * sizeof(unsigned long long), st));
-  if (sweeps_out) PVGLU_CUDA(cudaMemsetAsync(sweeps_out, 0, h->ld * sizeof(int), st));
-  const SkipDone skip{h->ir_done, ndone};
-  // J x = b:   w = b[row_orig], M y = w, x[col_orig] = y, residual rows by A.
-  // J^T x = b: w = b[col_orig], M^T z = w, x[row_orig] = z, rows by A^T.
-  const int* in_perm = transpose ? h->d.col_orig : h->d.row_orig;
-  const int* out_perm = transpose ? h->d.row_orig : h->d.col_orig;
-  const int* r_ptr = transpose ? h->at_ptr : h->d.a_rowptr;
-  const int* r_idx = transpose ? h->at_row : h->d.a_colidx;
-  const int* r_ent = transpose ? h->at_entry : nullptr;
-  const int* r_pos = transpose ? h->col_pos : h->row_pos;
-  // 16-byte vector loads in the batched residual.
-  const bool vec16 = !((reinterpret_cast<uintptr_t>(A.a) | reinterpret_cast<uintptr_t>(b) |
-                        reinterpret_cast<uintptr_t>(x)) & 15);
-  // x = 0: the first residual is b itself.
-  permute<double, float>(h, in_perm, b, w, true, st);
-  const dim3 blk(32, 8);
-  // About one full SM of threads per SM: the launches after every scenario
-  // has converged (ndone == S) then cost little.
-  const int gy = (h->ld + 31) / 32;
-  const int fill = std::max(1, h->sm_count * 8);
-  const dim3 grd((unsigned)std::max(1, std::min((h->n + 7) / 8, (fill + gy - 1) / gy)),
-                 (unsigned)gy);
-  const int rgrid = std::min(rows_grid(h->n, h->ld, 256), h->resid_blocks);
-  for (int sweep = 1; sweep <= max_sweeps; sweep++) {
-    int rc = solve_permuted<float>(h, w, transpose, st, skip);  // dx of this sweep
-    if (rc) return rc;
-    k_ir_update<<<grd, blk, 0, st>>>(out_perm, h->n, h->ld, h->S, w, x, h->ir_done, ndone,
-                                     h->ir_max_dx, h->ir_max_x, sweep == 1 ? 1 : 0);
-    k_ir_check<<<(h->S + 127) / 128, 128, 0, st>>>(h->S, sweep, max_sweeps, tol, h->ir_done,
-                                                   ndone, sweeps_out, h->ir_max_dx,
-                                                   h->ir_max_x, h->ir_prev_dx);
-    if (sweep < max_sweeps) {  // residual of the scenarios still refining
-      if (A.a && h->ld % 64 == 0 && vec16)
-        k_residual_rows<<<rgrid, 256, 0, st>>>(
-            r_ptr, r_idx, r_ent, h->n, h->ld, h->S, A.a, b, x, h->ir_done, ndone, w, r_pos);
-      else
-        k_residual<<<rows_grid(h->n, h->ld, 256), 256, 0, st>>>(
-            r_ptr, r_idx, r_ent, h->n, h->ld, h->S, A, b, x, h->ir_done, ndone, w, r_pos);
+  const Refine R(h, A, b, x, transpose, tol, max_sweeps, sweeps_out, init_done);
+  if (max_sweeps > 1 && h->schedule != PVGLU_SCHED_PERSISTENT) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    PVGLU_CUDA(cudaStreamIsCapturing(st, &cs));
+    if (cs == cudaStreamCaptureStatusNone && refine_graph(R)) {
+      PVGLU_CUDA(cudaGraphLaunch(h->ir_graph, st));
+      return PVGLU_OK;
     }
   }
+  int rc = R.start(st);
+  for (int sweep = 1; !rc && sweep <= max_sweeps; sweep++) {
+    rc = R.correct(sweep == 1, st);
+    if (rc) break;
+    k_ir_check<<<(h->S + 127) / 128, 128, 0, st>>>(h->S, sweep, max_sweeps, tol, h->ir_done,
+                                                   R.ndone, sweeps_out, h->ir_max_dx,
+                                                   h->ir_max_x, h->ir_prev_dx);
+    if (sweep < max_sweeps) rc = R.residual(st);
+  }
+  if (rc) return rc;
   PVGLU_CUDA(cudaGetLastError());
   return PVGLU_OK;
 }
@@ -495,6 +637,7 @@ int pvglu_numeric_create_ex(const pvglu_symbolic* sym, int n_scenarios, int prec
   rc |= h->alloc((size_t)h->ld, &h->ir_max_dx);
   rc |= h->alloc((size_t)h->ld, &h->ir_max_x);
   rc |= h->alloc((size_t)h->ld, &h->ir_prev_dx);
+  rc |= h->alloc((size_t)1, &h->ir_sweeps_done);
   rc |= h->alloc(4, &h->barrier);
   if (rc) {
     const std::string e = g_err;

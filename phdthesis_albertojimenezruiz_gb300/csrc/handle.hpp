@@ -62,6 +62,29 @@ struct pvglu_numeric {
   unsigned long long* ir_max_dx = nullptr;
   unsigned long long* ir_max_x = nullptr;
   double* ir_prev_dx = nullptr;  // max|dx| of the previous sweep
+  int* ir_sweeps_done = nullptr;  // sweep counter of the graph-replayed refinement
+  // Refinement replayed from a graph whose sweeps run under a conditional
+  // while node (run_refine); rebuilt when its launch arguments change.
+  struct RefineKey {
+    pvglu::AValues A;
+    const double* b;
+    double* x;
+    int* sweeps_out;
+    const int* init_done;
+    double tol;
+    int transpose, max_sweeps, schedule;
+    bool operator==(const RefineKey& o) const {
+      return A.a == o.A.a && A.base == o.A.base && A.ptr == o.A.ptr && A.elem == o.A.elem &&
+             A.sign == o.A.sign && A.g == o.A.g && A.gmin == o.A.gmin && A.linear == o.A.linear &&
+             b == o.b && x == o.x && sweeps_out == o.sweeps_out && init_done == o.init_done &&
+             tol == o.tol && transpose == o.transpose && max_sweeps == o.max_sweeps &&
+             schedule == o.schedule;
+    }
+  };
+  RefineKey ir_key{};
+  cudaGraphExec_t ir_graph = nullptr;
+  cudaStream_t ir_cap[2] = {nullptr, nullptr};  // capture streams: outer, loop body
+  bool ir_graph_failed = false;
   // Host copies of the level starts (launch ranges).
   std::vector<int> lu_sl, l_sl, u_sl, lt_sl;
   // Chain programs: refactor, L, U, U^T, L^T (programs.hpp).
@@ -94,6 +117,9 @@ struct pvglu_numeric {
     return pvglu::AValues{nullptr, st_base, st_ptr, st_elem, st_sign, g, gmin, linear};
   }
   ~pvglu_numeric() {
+    if (ir_graph) cudaGraphExecDestroy(ir_graph);
+    for (cudaStream_t c : ir_cap)
+      if (c) cudaStreamDestroy(c);
     for (void* p : allocs) cudaFree(p);
     for (void* p : stamp_allocs) cudaFree(p);
   }

@@ -470,11 +470,10 @@ static __global__ void k_ir_init(int n, int ld, int S, const int* __restrict__ s
 // shrink geometrically and the remaining error is about
 // max|dx_k| rho / (1 - rho) (the stopping estimate of iterative-refinement
 // analyses), so the sweep that would only confirm it is skipped.
-static __global__ void k_ir_check(int S, int sweep, int last_sweep, double tol, int* done,
-                                  int* ndone, int* sweeps_out, unsigned long long* max_dx,
-                                  unsigned long long* max_x, double* prev_dx) {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= S || done[s]) return;
+__device__ __forceinline__ bool ir_check_one(int s, int sweep, int last_sweep, double tol,
+                                             int* done, int* sweeps_out,
+                                             unsigned long long* max_dx,
+                                             unsigned long long* max_x, double* prev_dx) {
   const double mdx = __longlong_as_double((long long)max_dx[s]);
   const double mx = __longlong_as_double((long long)max_x[s]);
   max_dx[s] = 0ull;
@@ -490,10 +489,45 @@ static __global__ void k_ir_check(int S, int sweep, int last_sweep, double tol, 
   prev_dx[s] = mdx;
   if (ok) {
     done[s] = 1;
-    atomicAdd(ndone, 1);
     if (sweeps_out) sweeps_out[s] = sweep;
   } else if (sweep == last_sweep) {
     if (sweeps_out) sweeps_out[s] = -1;
+  }
+  return ok;
+}
+
+static __global__ void k_ir_check(int S, int sweep, int last_sweep, double tol, int* done,
+                                  int* ndone, int* sweeps_out, unsigned long long* max_dx,
+                                  unsigned long long* max_x, double* prev_dx) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= S || done[s]) return;
+  if (ir_check_one(s, sweep, last_sweep, tol, done, sweeps_out, max_dx, max_x, prev_dx))
+    atomicAdd(ndone, 1);
+}
+
+// The same check in one block for the refinement replayed from a graph: the
+// sweep number lives on the device (*sweeps_done, sweeps finished before this
+// one), and the block sets the graph's loop condition: another sweep while a
+// scenario is still refining and sweeps remain.
+static __global__ void k_ir_check_loop(int S, int last_sweep, double tol, int* done, int* ndone,
+                                       int* sweeps_out, unsigned long long* max_dx,
+                                       unsigned long long* max_x, double* prev_dx,
+                                       int* sweeps_done, cudaGraphConditionalHandle loop) {
+  __shared__ int newly;
+  const int sweep = *sweeps_done + 1;
+  if (threadIdx.x == 0) newly = 0;
+  __syncthreads();
+  int mine = 0;
+  for (int s = threadIdx.x; s < S; s += blockDim.x)
+    if (!done[s] && ir_check_one(s, sweep, last_sweep, tol, done, sweeps_out, max_dx, max_x,
+                                 prev_dx))
+      mine++;
+  if (mine) atomicAdd(&newly, mine);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int total = atomicAdd(ndone, newly) + newly;
+    *sweeps_done = sweep;
+    cudaGraphSetConditional(loop, (total < S && sweep < last_sweep) ? 1u : 0u);
   }
 }
 

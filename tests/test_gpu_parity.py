@@ -394,3 +394,39 @@ def test_loaded_symbolic_factors_bit_identical(cuda, tmp_path):
         num.solve(x, original=True)
         out.append((values_of(num, int(sym.nnz_lu))[:, :40], x.cpu().numpy()[:, :40]))
     assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+
+
+def test_refinement_graph_matches_direct_launches(cuda):
+    """The levels schedule replays the refinement from a graph with a
+    conditional sweep loop, the persistent schedule launches it sweep by
+    sweep: same solutions bit for bit, same sweep counts, also after the
+    graph is rebuilt for new arguments and when the sweep cap stops it."""
+    import torch
+
+    p = Plant(10, 16, 20)
+    s = Symbolic(p.rowptr, p.colidx)
+    S = 96
+    a, b = M.plant_batch(p, S, seed0=500, preset="c3")
+    out = {}
+    for sched in (SCHED_LEVELS, SCHED_PERSISTENT):
+        num = Numeric(s, S, FP32, sched)
+        a_dev = dev(pad_cols(a, num.ld))
+        b_dev = dev(pad_cols(b, num.ld))
+        num.scatter(a_dev)
+        num.refactor()
+        runs = []
+        for tol, ms in ((1e-12, 8), (1e-12, 8), (1e-6, 8), (1e-300, 2), (1e-12, 1)):
+            x = torch.full_like(b_dev, float("nan"))
+            sweeps = torch.zeros(num.ld, dtype=torch.int32, device="cuda")
+            num.solve_refined(a_dev, b_dev, x, tol=tol, max_sweeps=ms, sweeps=sweeps)
+            torch.cuda.synchronize()
+            runs.append((x.cpu().numpy()[:, :S], sweeps.cpu().numpy()[:S]))
+        out[sched] = runs
+    for (xg, sg), (xd, sd) in zip(out[SCHED_LEVELS], out[SCHED_PERSISTENT]):
+        assert np.array_equal(sg, sd)
+        assert np.array_equal(xg, xd)
+    sw = [r[1] for r in out[SCHED_LEVELS]]
+    assert (sw[0] > 1).all() and np.array_equal(sw[0], sw[1])
+    assert (sw[2] <= sw[0]).all() and (sw[2] >= 1).all()
+    assert (sw[3] == -1).all()
+    assert (sw[4] == -1).all() or (sw[4] == 1).all()
