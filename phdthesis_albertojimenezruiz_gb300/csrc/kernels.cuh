@@ -353,52 +353,52 @@ static __global__ void k_residual(const int* __restrict__ ptr, const int* __rest
   });
 }
 
-// Batched residual with explicit values (ld a multiple of 64): one warp per
-// row, each lane two adjacent scenarios per 16-byte load, two scenario pairs
-// in flight per iteration.  The row's pattern is loaded once by the warp.
-// Same arithmetic per scenario as k_residual (one FP64 FMA per entry, in the
-// row's entry order).
-static __global__ void __launch_bounds__(256)
+// Batched residual with explicit values (ld a multiple of 64).  A warp item
+// is one row and one chunk of 64 scenarios (two adjacent scenarios per lane
+// and 16-byte load); the loads of up to three entries are issued together,
+// so a row of the plant (three entries, mostly) costs one round of memory
+// latency after its pattern.  A and b are read once (streaming loads); x rows
+// are shared by neighbouring rows and stay cached.  Same arithmetic per
+// scenario as k_residual (one FP64 FMA per entry, in the row's entry order).
+static __global__ void __launch_bounds__(256, 6)
 k_residual_rows(const int* __restrict__ ptr, const int* __restrict__ idx,
                 const int* __restrict__ ent, int n, int ld, int S,
                 const double* __restrict__ a, const double* __restrict__ b,
                 const double* __restrict__ x, const int* __restrict__ done,
                 const int* __restrict__ ndone, float* __restrict__ r_perm,
                 const int* __restrict__ pos) {
+  constexpr int kU = 3;  // entries in flight per warp
   if (__ldcg(ndone) >= S) return;
   const int lane = threadIdx.x & 31;
+  const int chunks = ld >> 6;
+  const int items = n * chunks;
   const int warps = (gridDim.x * blockDim.x) >> 5;
-  for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
-    const int p0 = ptr[i], p1 = ptr[i + 1];
-    const int64_t ro = (int64_t)pos[i] * ld;
-    for (int s = 2 * lane; s < ld; s += 128) {
-      // scenario pairs s and s + 64 of this lane
-      const bool has2 = s + 64 < ld;
-      const double2 b0 = *reinterpret_cast<const double2*>(b + (int64_t)i * ld + s);
-      double2 b1 = make_double2(0.0, 0.0);
-      if (has2) b1 = *reinterpret_cast<const double2*>(b + (int64_t)i * ld + s + 64);
-      double r0x = b0.x, r0y = b0.y, r1x = b1.x, r1y = b1.y;
-      for (int p = p0; p < p1; p++) {
-        const int e = ent ? ent[p] : p;
-        const int64_t ao = (int64_t)e * ld + s, xo = (int64_t)idx[p] * ld + s;
-        const double2 a0 = *reinterpret_cast<const double2*>(a + ao);
-        const double2 x0 = *reinterpret_cast<const double2*>(x + xo);
-        r0x -= a0.x * x0.x;
-        r0y -= a0.y * x0.y;
-        if (has2) {
-          const double2 a1 = *reinterpret_cast<const double2*>(a + ao + 64);
-          const double2 x1 = *reinterpret_cast<const double2*>(x + xo + 64);
-          r1x -= a1.x * x1.x;
-          r1y -= a1.y * x1.y;
+  for (int it = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; it < items; it += warps) {
+    const int i = it / chunks;
+    const int s = (it - i * chunks) * 64 + 2 * lane;
+    const int p0 = __ldg(ptr + i), p1 = __ldg(ptr + i + 1);
+    const double2 bb = __ldcs(reinterpret_cast<const double2*>(b + (int64_t)i * ld + s));
+    double rx = bb.x, ry = bb.y;
+    for (int p = p0; p < p1; p += kU) {
+      double2 av[kU], xv[kU];
+#pragma unroll
+      for (int u = 0; u < kU; u++)
+        if (p + u < p1) {
+          const int e = ent ? __ldg(ent + p + u) : p + u;
+          const int j = __ldg(idx + p + u);
+          av[u] = __ldcs(reinterpret_cast<const double2*>(a + (int64_t)e * ld + s));
+          xv[u] = *reinterpret_cast<const double2*>(x + (int64_t)j * ld + s);
         }
-      }
-      if (s < S && !done[s]) r_perm[ro + s] = d2f_bits(r0x);
-      if (s + 1 < S && !done[s + 1]) r_perm[ro + s + 1] = d2f_bits(r0y);
-      if (has2) {
-        if (s + 64 < S && !done[s + 64]) r_perm[ro + s + 64] = d2f_bits(r1x);
-        if (s + 65 < S && !done[s + 65]) r_perm[ro + s + 65] = d2f_bits(r1y);
-      }
+#pragma unroll
+      for (int u = 0; u < kU; u++)
+        if (p + u < p1) {
+          rx -= av[u].x * xv[u].x;
+          ry -= av[u].y * xv[u].y;
+        }
     }
+    const int64_t ro = (int64_t)__ldg(pos + i) * ld;
+    if (s < S && !done[s]) r_perm[ro + s] = d2f_bits(rx);
+    if (s + 1 < S && !done[s + 1]) r_perm[ro + s + 1] = d2f_bits(ry);
   }
 }
 
