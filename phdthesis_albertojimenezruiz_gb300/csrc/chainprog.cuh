@@ -36,6 +36,8 @@ struct ProgDev {
 };
 
 constexpr int kGroup = 64;                       // scenarios per warp item
+constexpr int kProgBlock = 128;                  // threads per block of the executors
+constexpr int kProgWarps = kProgBlock / 32;
 constexpr long long kMbarMaxPolls = 1LL << 20;   // bounded mbarrier waits
 
 // ---------------------------------------------------------------------------
@@ -253,6 +255,13 @@ __device__ __forceinline__ void prog_run_chain(const ProgDev& P, const DevStruct
     if (BATCH) {
       using V2 = typename Vec2<T>::type;
       constexpr unsigned kRow = kGroup * sizeof(T);
+      // The segment's operation words, one int4 (four operations) per lane,
+      // fetched before the waits below and broadcast by shuffles: the
+      // operations then wait on no memory but the table.
+      const int4* o4 = P.ops + (sg.z >> 2);
+      const int n_w = sg.w >> 2;
+      int4 ow = make_int4(0, 0, 0, 0);
+      if (lane < n_w) ow = __ldg(o4 + lane);
       // The previous segment's bulk stores must have read the table; when
       // this segment loads rows they wrote, they must also be complete.
       if ((sg.y >> 30) & 1) bulk_wait_all();
@@ -282,14 +291,20 @@ __device__ __forceinline__ void prog_run_chain(const ProgDev& P, const DevStruct
       }
       tma.phase ^= 1u;
       V2* t = reinterpret_cast<V2*>(sm) + lane;
-      const int4* o4 = P.ops + (sg.z >> 2);
-      for (int k = 0; k < (sg.w >> 2); k++) {
-        const int4 w = __ldg(o4 + k);
-        const int base = sg.z + 4 * k;
-        exec_op2<T>((uint32_t)w.x, base, P.op_col, t, s0 + 2 * lane, S, pivot_tol, st);
-        exec_op2<T>((uint32_t)w.y, base + 1, P.op_col, t, s0 + 2 * lane, S, pivot_tol, st);
-        exec_op2<T>((uint32_t)w.z, base + 2, P.op_col, t, s0 + 2 * lane, S, pivot_tol, st);
-        exec_op2<T>((uint32_t)w.w, base + 3, P.op_col, t, s0 + 2 * lane, S, pivot_tol, st);
+      for (int k0 = 0; k0 < n_w; k0 += 32) {
+        if (k0 > 0) ow = lane + k0 < n_w ? __ldg(o4 + k0 + lane) : make_int4(0, 0, 0, 0);
+        const int kn = min(32, n_w - k0);
+        for (int k = 0; k < kn; k++) {
+          const uint32_t wx = (uint32_t)__shfl_sync(0xffffffffu, ow.x, k);
+          const uint32_t wy = (uint32_t)__shfl_sync(0xffffffffu, ow.y, k);
+          const uint32_t wz = (uint32_t)__shfl_sync(0xffffffffu, ow.z, k);
+          const uint32_t ww = (uint32_t)__shfl_sync(0xffffffffu, ow.w, k);
+          const int base = sg.z + 4 * (k0 + k);
+          exec_op2<T>(wx, base, P.op_col, t, s0 + 2 * lane, S, pivot_tol, st);
+          exec_op2<T>(wy, base + 1, P.op_col, t, s0 + 2 * lane, S, pivot_tol, st);
+          exec_op2<T>(wz, base + 2, P.op_col, t, s0 + 2 * lane, S, pivot_tol, st);
+          exec_op2<T>(ww, base + 3, P.op_col, t, s0 + 2 * lane, S, pivot_tol, st);
+        }
       }
       // Make this lane's table writes visible to the async proxy, then let
       // lanes write back the own rows with bulk stores.

@@ -82,9 +82,6 @@ struct ProgSetDev {
   ProgDev p[5];  // refactor, L, U, U^T, L^T
 };
 
-constexpr int kProgBlock = 128;
-constexpr int kProgWarps = kProgBlock / 32;
-
 template <typename T, int KIND, bool BATCH>
 __device__ __forceinline__ bool prog_phase(const ProgDev& P, const DevStruct& d, T* v, T* x,
                                            int ld, int S, T* sm, WarpTma& tma,
