@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -409,7 +410,13 @@ int run_refine(pvglu_numeric* h, const AValues& A, const double* b, double* x, b
                const int* init_done) {
   if (h->precision != PVGLU_FP32) return fail(PVGLU_ERR_BAD_ARG, "needs an FP32 handle");
   const Refine R(h, A, b, x, transpose, tol, max_sweeps, sweeps_out, init_done);
-  if (max_sweeps > 1 && h->schedule != PVGLU_SCHED_PERSISTENT) {
+  // PVGLU_REFINE_GRAPH=0: the same kernels launched one by one, for
+  // profilers that do not list the kernels of conditional graph bodies.
+  static const bool graph_on = [] {
+    const char* e = std::getenv("PVGLU_REFINE_GRAPH");
+    return !(e && e[0] == '0');
+  }();
+  if (graph_on && max_sweeps > 1 && h->schedule != PVGLU_SCHED_PERSISTENT) {
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     PVGLU_CUDA(cudaStreamIsCapturing(st, &cs));
     if (cs == cudaStreamCaptureStatusNone && refine_graph(R)) {

@@ -38,6 +38,13 @@ struct ProgDev {
 constexpr int kGroup = 64;                       // scenarios per warp item
 constexpr int kProgBlock = 128;                  // threads per block of the executors
 constexpr int kProgWarps = kProgBlock / 32;
+// Resident blocks per SM the level executors are compiled for: FP32 tables
+// allow 9 blocks at the usual table sizes (at most 56 registers); FP64
+// executors are given up to 80 registers (6 blocks).
+template <typename T>
+constexpr int prog_min_blocks() {
+  return sizeof(T) == 4 ? 9 : 6;
+}
 constexpr long long kMbarMaxPolls = 1LL << 20;   // bounded mbarrier waits
 
 // ---------------------------------------------------------------------------
@@ -401,7 +408,8 @@ size_t prog_smem_bytes(int max_locals, int warps_per_block) {
 // ndone (or NULL): the launch does nothing once every scenario is done.
 // `table`: the level's table budget (its programs were built for it).
 template <typename T, int KIND, bool BATCH>
-__global__ void k_prog_level(ProgDev P, int table, DevStruct d, int cb, int ce,
+__global__ void __launch_bounds__(kProgBlock, prog_min_blocks<T>())
+k_prog_level(ProgDev P, int table, DevStruct d, int cb, int ce,
                              T* __restrict__ v, T* __restrict__ x, int ld, int S, T pivot_tol,
                              DevStatus* st, const int* done, const int* ndone) {
   if (ndone && __ldcg(ndone) >= S) return;
@@ -442,7 +450,8 @@ struct MultiLaunch {
 };
 
 template <typename T, int KIND, bool BATCH>
-__global__ void k_prog_level_multi(MultiLaunch<T> M, int table) {
+__global__ void __launch_bounds__(kProgBlock, prog_min_blocks<T>())
+k_prog_level_multi(MultiLaunch<T> M, int table) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   WarpTma tma;
   T* sm = prog_setup_warp<T, BATCH>(smem_raw, table, tma);
