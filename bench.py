@@ -49,8 +49,45 @@ def _peaks() -> dict:
     return {}
 
 
+class _Nvml:
+    """Read-only NVML queries through the driver's libnvidia-ml (ctypes)."""
+
+    SM = 1  # NVML_CLOCK_SM
+    # Clock event reason bits of nvmlDeviceGetCurrentClocksEventReasons.
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+               0x40: "hw_thermal_slowdown"}
+
+    def __init__(self, torch_index: int):
+        import ctypes
+
+        self.C = ctypes
+        lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if lib.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        self.lib = lib
+        self.dev = ctypes.c_void_p()
+        import torch
+
+        uuid = str(torch.cuda.get_device_properties(torch_index).uuid)
+        uuid = uuid if uuid.startswith("GPU-") else "GPU-" + uuid
+        if lib.nvmlDeviceGetHandleByUUID(uuid.encode(), ctypes.byref(self.dev)) != 0:
+            raise OSError("no NVML handle for " + uuid)
+        self.reasons_fn = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            lib.nvmlDeviceGetCurrentClocksThrottleReasons
+
+    def sample(self):
+        C = self.C
+        mhz, mx, rs = C.c_uint(), C.c_uint(), C.c_ulonglong()
+        if (self.lib.nvmlDeviceGetClockInfo(self.dev, self.SM, C.byref(mhz)) or
+                self.lib.nvmlDeviceGetMaxClockInfo(self.dev, self.SM, C.byref(mx)) or
+                self.reasons_fn(self.dev, C.byref(rs))):
+            return None
+        return mhz.value, mx.value, [n for b, n in self.REASONS.items() if rs.value & b]
+
+
 class ClockSampler:
-    """nvidia-smi clock/throttle sampling during the timed region."""
+    """SM clock and clock-event reasons during the timed region: NVML polled
+    every millisecond from a thread, else nvidia-smi's 200 ms loop."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -60,8 +97,30 @@ class ClockSampler:
         self.index = index
         self.proc = None
         self.out = None
+        self.nvml = None
+        self.samples = []
+        self.thread = None
+        self.stop = False
+        try:
+            self.nvml = _Nvml(index)
+            self.nvml.sample()
+        except Exception:  # noqa: BLE001  (no NVML: fall back to nvidia-smi)
+            self.nvml = None
+
+    def _poll(self):
+        while not self.stop:
+            smp = self.nvml.sample()
+            if smp:
+                self.samples.append(smp)
+            time.sleep(0.001)
 
     def __enter__(self):
+        if self.nvml:
+            import threading
+
+            self.thread = threading.Thread(target=self._poll, daemon=True)
+            self.thread.start()
+            return self
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
@@ -72,6 +131,9 @@ class ClockSampler:
         return self
 
     def __exit__(self, *exc):
+        if self.thread:
+            self.stop = True
+            self.thread.join(timeout=5)
         if self.proc:
             self.proc.terminate()
             try:
@@ -81,6 +143,11 @@ class ClockSampler:
                 self.out = ""
 
     def summary(self) -> dict:
+        if self.samples:
+            sm = [x[0] for x in self.samples]
+            reasons = sorted({r for x in self.samples for r in x[2]})
+            return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": max(x[1] for x in self.samples),
+                    "reasons": reasons, "samples": len(sm), "source": "nvml, 1 ms"}
         if not self.out:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
         sm, mx, reasons = [], [], set()
@@ -99,7 +166,7 @@ class ClockSampler:
                     reasons.add(nm)
         return {"sm_mhz": float(np.median(sm)) if sm else None,
                 "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "source": "nvidia-smi, 200 ms"}
 
 
 def make_inputs(S: int, ld: int, seed0: int = 1000):
@@ -879,8 +946,12 @@ def main() -> None:
     # converged work exits at once) solve, update, check and residual.
     refactor_launches = 1 if persistent else sym.info["lu_levels"]
     solve_launches = 1 if persistent else sym.info["l_levels"] + sym.info["u_levels"]
-    launches = args.steps * (2 + refactor_launches +
-                             IR_MAX_SWEEPS * (solve_launches + 2) + IR_MAX_SWEEPS - 1)
+    sweeps_run = int(sw.max())
+    if persistent:  # sweep by sweep: every sweep up to the cap is launched
+        refine_launches = IR_MAX_SWEEPS * (solve_launches + 2) + IR_MAX_SWEEPS - 1
+    else:  # graph: permute, first sweep, then residual + solve + update + check per sweep
+        refine_launches = 1 + (solve_launches + 2) + (sweeps_run - 1) * (solve_launches + 3)
+    launches = args.steps * (1 + refactor_launches + refine_launches)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
@@ -892,7 +963,8 @@ def main() -> None:
                    "scenarios_per_step": S, "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2 (FP64 Jacobian values "
                          f"{8 * nnz_a * ld / 1e6:.0f} MB per batch)",
-                   "ir_tol": IR_TOL, "ir_max_sweeps": IR_MAX_SWEEPS, "tuning": tuned},
+                   "ir_tol": IR_TOL, "ir_max_sweeps": IR_MAX_SWEEPS, "tuning": tuned,
+                   "flops_per_refactor_solve": sym.info["flops_refactor"] + 2.0 * nnz_lu},
         "ir": {"sweeps_min": int(sw.min()), "sweeps_max": int(sw.max()),
                "not_converged": int((sw <= 0).sum()), "max_rel_err_vs_fp64": max_rel},
         "plain_fp64": {"value": plain, "unit": UNIT, "schedule": plain_name,

@@ -430,3 +430,47 @@ def test_refinement_graph_matches_direct_launches(cuda):
     assert (sw[2] <= sw[0]).all() and (sw[2] >= 1).all()
     assert (sw[3] == -1).all()
     assert (sw[4] == -1).all() or (sw[4] == 1).all()
+
+
+_REFINE_SCRIPT = r"""
+import sys
+import numpy as np, torch
+sys.path.insert(0, sys.argv[2])
+import matrices as M
+from phdthesis_albertojimenezruiz_gb300 import FP32, SCHED_LEVELS, Numeric, Plant, Symbolic
+p = Plant(10, 16, 20)
+s = Symbolic(p.rowptr, p.colidx)
+S = 64
+a, b = M.plant_batch(p, S, seed0=700, preset="c3")
+num = Numeric(s, S, FP32, SCHED_LEVELS)
+a_dev = torch.from_numpy(np.ascontiguousarray(a)).cuda()
+b_dev = torch.from_numpy(np.ascontiguousarray(b)).cuda()
+num.scatter(a_dev)
+num.refactor()
+x = torch.zeros_like(b_dev)
+sw = torch.zeros(num.ld, dtype=torch.int32, device="cuda")
+num.solve_refined(a_dev, b_dev, x, tol=1e-12, max_sweeps=8, sweeps=sw)
+torch.cuda.synchronize()
+np.save(sys.argv[1], np.concatenate([x.cpu().numpy().ravel(), sw.cpu().numpy().astype(np.float64)]))
+"""
+
+
+def test_refinement_profiling_switch_gives_the_same_bits(cuda, tmp_path):
+    """PVGLU_REFINE_GRAPH=0 launches the refinement kernel by kernel instead
+    of replaying the conditional graph: the results are bit-identical."""
+    import os
+    import subprocess
+    import sys
+
+    tests_dir = os.path.dirname(os.path.abspath(__file__))
+    root = os.path.dirname(tests_dir)
+    script = tmp_path / "refine.py"
+    script.write_text(_REFINE_SCRIPT)
+    outs = []
+    for flag in ("1", "0"):
+        out = tmp_path / f"x{flag}.npy"
+        env = dict(os.environ, PVGLU_REFINE_GRAPH=flag, PYTHONPATH=root)
+        subprocess.run([sys.executable, str(script), str(out), tests_dir], check=True, env=env,
+                       cwd=root, timeout=600)
+        outs.append(np.load(out))
+    assert np.array_equal(outs[0], outs[1])
