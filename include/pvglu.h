@@ -225,7 +225,15 @@ int pvglu_solve_refined(pvglu_numeric* h, const double* a_values, const double* 
 /* General form of pvglu_solve_refined: A's values either explicit
  * (a_values, g NULL) or from the registered stamps (g [n_elems * ld] and
  * optional gmin [ld], a_values NULL).  flags: PVGLU_SOLVE_TRANSPOSE refines
- * J^T x = b (the adjoint system) with an FP64 residual over J's columns. */
+ * J^T x = b (the adjoint system) with an FP64 residual over J's columns.
+ * Launches: on a stream that is not being captured, and for the per-level
+ * schedules, the sweeps run from a CUDA graph of the handle whose sweep loop
+ * is a conditional while node (built on the first call with these pointers,
+ * tolerance and sweep cap; replayed afterwards), so no sweep after
+ * convergence is launched.  Inside a capture, with the persistent schedule,
+ * or with PVGLU_REFINE_GRAPH=0 in the environment, the sweeps are launched
+ * one by one, max_sweeps of them, each exiting at once after convergence.
+ * The results are the same in both forms. */
 int pvglu_refine(pvglu_numeric* h, const double* a_values, const double* g, const double* gmin,
                  const double* b, double* x, int flags, double tol, int max_sweeps,
                  int* sweeps_out, void* stream);
