@@ -297,6 +297,19 @@ void build_chain_program(const Symbolic& s, int kind, const std::vector<int>& le
         std::max(out.longest_chain_segments, (int)out.seg.size() - first_seg);
   }
   out.chain_seg.push_back((int)out.seg.size());
+  // A level's table is as wide as its widest segment (the budget is only an
+  // upper bound): shared memory per block, and so the blocks an SM holds,
+  // follow what the level uses.  The narrow levels of a plant (one segment
+  // per inverter chain) need a small part of the wide budget they are given.
+  out.max_locals = 1;
+  for (int lv = 0; lv < ls.num_levels(); lv++) {
+    int used = 1;
+    for (int c = ls.start_levels[lv]; c < ls.start_levels[lv + 1]; c++)
+      for (int g = out.chain_seg[c]; g < out.chain_seg[c + 1]; g++)
+        used = std::max(used, out.seg[g].n_load);
+    out.level_max_locals[lv] = used;
+    out.max_locals = std::max(out.max_locals, used);
+  }
 }
 
 }  // namespace pvglu

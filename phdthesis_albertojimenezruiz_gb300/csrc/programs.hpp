@@ -55,8 +55,9 @@ struct Segment {
 
 struct ChainProgram {
   int kind = -1;                 // -1 refactor, 0 L, 1 U, 2 U^T, 3 L^T
-  int max_locals = 0;            // largest local table budget of any level
-  std::vector<int> level_max_locals;  // [levels] table budget of each level
+  int max_locals = 0;            // widest table of any level
+  std::vector<int> level_max_locals;  // [levels] table size of each level: its widest
+                                      // segment, at most the level's budget
   std::vector<int> level_chain;  // [levels + 1] -> chain index
   std::vector<int> chain_seg;    // [chains + 1] -> segment index
   std::vector<Segment> seg;
