@@ -17,11 +17,14 @@
 // W is evaluated in log form, w + log(w) = log(theta), so that no
 // exponential overflows for any terminal voltage.
 //
-// Every operation here is a correctly rounded IEEE add, multiply or divide,
-// and the exponential and logarithm are this file's own (pvglu_exp,
-// pvglu_log), so host code built without FMA contraction
-// (-ffp-contract=off) and device code built with --fmad=false produce
-// bit-identical results.
+// Every operation here is a correctly rounded IEEE add, multiply, divide or
+// explicit fused multiply-add (fma(), one rounding on every host and on the
+// device), and the exponential and logarithm are this file's own (pvglu_exp,
+// pvglu_log), so host code built without FMA contraction (-ffp-contract=off)
+// and device code built with --fmad=false produce bit-identical results.
+// FP64 is scarce on GB300, so the evaluation is written to few FP64
+// instructions: fma() in the polynomials, no special-case tests where the
+// argument is known to be positive and normal.
 #pragma once
 #include <math.h>
 #include <stdint.h>
@@ -66,7 +69,8 @@ PVGLU_HD double pvglu_pow2(int k) { return pvglu_from_bits((int64_t)(k + 1023) <
 // exp(x): Cody-Waite reduction x = k ln2 + r, |r| <= ln2/2, with ln2 split
 // into ln2_hi (21 significant bits, so k * ln2_hi is exact) and ln2_lo, then
 // the degree-13 Taylor polynomial of exp(r) (remainder < 5e-18 relative) in
-// Horner form, scaled by 2^k.  A few ulps from the correctly rounded value.
+// Horner form with fused multiply-adds, scaled by 2^k.  A few ulps from the
+// correctly rounded value.
 PVGLU_HD double pvglu_exp(double x) {
   if (x != x) return x;
   if (x > 709.782712893384) return INFINITY;
@@ -77,39 +81,32 @@ PVGLU_HD double pvglu_exp(double x) {
   const int k = (int)floor(x * inv_ln2 + 0.5);
   const double r = (x - k * ln2_hi) - k * ln2_lo;
   double p = 1.6059043836821613e-10;  // 1/13!
-  p = p * r + 2.08767569878681e-09;   // 1/12!
-  p = p * r + 2.505210838544172e-08;
-  p = p * r + 2.755731922398589e-07;
-  p = p * r + 2.7557319223985893e-06;
-  p = p * r + 2.48015873015873e-05;
-  p = p * r + 0.0001984126984126984;
-  p = p * r + 0.001388888888888889;
-  p = p * r + 0.008333333333333333;
-  p = p * r + 0.041666666666666664;
-  p = p * r + 0.16666666666666666;
-  p = p * r + 0.5;
-  p = p * r + 1.0;
-  p = p * r + 1.0;
+  p = fma(p, r, 2.08767569878681e-09);   // 1/12!
+  p = fma(p, r, 2.505210838544172e-08);
+  p = fma(p, r, 2.755731922398589e-07);
+  p = fma(p, r, 2.7557319223985893e-06);
+  p = fma(p, r, 2.48015873015873e-05);
+  p = fma(p, r, 0.0001984126984126984);
+  p = fma(p, r, 0.001388888888888889);
+  p = fma(p, r, 0.008333333333333333);
+  p = fma(p, r, 0.041666666666666664);
+  p = fma(p, r, 0.16666666666666666);
+  p = fma(p, r, 0.5);
+  p = fma(p, r, 1.0);
+  p = fma(p, r, 1.0);
   if (k > 1023) return (p * 2.0) * pvglu_pow2(k - 1);
   if (k < -1021) return (p * pvglu_pow2(k + 1000)) * pvglu_pow2(-1000);
   return p * pvglu_pow2(k);
 }
 
-// log(x): x = 2^e m with m in [sqrt(1/2), sqrt(2)), then
-// log(m) = 2 atanh(s) = 2 (s + s^3/3 + ... + s^27/27), s = (m - 1)/(m + 1),
-// |s| <= 0.1716 (remainder < 1e-19 relative); m - 1 is exact.  A few ulps
-// from the correctly rounded value.
-PVGLU_HD double pvglu_log(double x) {
-  if (x != x || x < 0.0) return NAN;
-  if (x == 0.0) return -INFINITY;
-  if (x == INFINITY) return x;
-  int e = 0;
-  if (x < 2.2250738585072014e-308) {  // subnormal: scale into the normal range
-    x *= 18014398509481984.0;         // 2^54
-    e = -54;
-  }
+// log(x) for positive, normal, finite x: x = 2^e m with m in
+// [sqrt(1/2), sqrt(2)), then log(m) = 2 atanh(s) = 2 (s + s^3/3 + ... +
+// s^21/21), s = (m - 1)/(m + 1), |s| <= 0.1716, so s^2 <= 0.0295 and the
+// first omitted term is below 7e-19 relative; m - 1 is exact.  Horner form
+// with fused multiply-adds.  A few ulps from the correctly rounded value.
+PVGLU_HD double pvglu_log_normal(double x) {
   const int64_t b = pvglu_bits(x);
-  e += (int)((b >> 52) & 0x7ff) - 1023;
+  int e = (int)((b >> 52) & 0x7ff) - 1023;
   double m = pvglu_from_bits((b & 0x000fffffffffffffLL) | 0x3ff0000000000000LL);
   if (m > 1.4142135623730951) {
     m *= 0.5;
@@ -117,23 +114,32 @@ PVGLU_HD double pvglu_log(double x) {
   }
   const double s = (m - 1.0) / (m + 1.0);
   const double z = s * s;
-  double p = 0.037037037037037035;  // 1/27
-  p = p * z + 0.04;
-  p = p * z + 0.043478260869565216;
-  p = p * z + 0.047619047619047616;
-  p = p * z + 0.05263157894736842;
-  p = p * z + 0.058823529411764705;
-  p = p * z + 0.06666666666666667;
-  p = p * z + 0.07692307692307693;
-  p = p * z + 0.09090909090909091;
-  p = p * z + 0.1111111111111111;
-  p = p * z + 0.14285714285714285;
-  p = p * z + 0.2;
-  p = p * z + 0.3333333333333333;
-  p = p * z + 1.0;
+  double p = 0.047619047619047616;  // 1/21
+  p = fma(p, z, 0.05263157894736842);
+  p = fma(p, z, 0.058823529411764705);
+  p = fma(p, z, 0.06666666666666667);
+  p = fma(p, z, 0.07692307692307693);
+  p = fma(p, z, 0.09090909090909091);
+  p = fma(p, z, 0.1111111111111111);
+  p = fma(p, z, 0.14285714285714285);
+  p = fma(p, z, 0.2);
+  p = fma(p, z, 0.3333333333333333);
+  p = fma(p, z, 1.0);
   const double ln2_hi = 0.6931471824645996;
   const double ln2_lo = -1.904654299957768e-09;
-  return e * ln2_hi + ((2.0 * s) * p + e * ln2_lo);
+  const double ed = (double)e;
+  return fma(ed, ln2_hi, fma(2.0 * s, p, ed * ln2_lo));
+}
+
+// log(x) for every double: NaN, negative, zero, infinity and subnormal
+// arguments handled, the rest by pvglu_log_normal.
+PVGLU_HD double pvglu_log(double x) {
+  if (x != x || x < 0.0) return NAN;
+  if (x == 0.0) return -INFINITY;
+  if (x == INFINITY) return x;
+  if (x < 2.2250738585072014e-308)  // subnormal: scale into the normal range
+    return pvglu_log_normal(x * 18014398509481984.0) - 54.0 * 0.6931471805599453;
+  return pvglu_log_normal(x);
 }
 
 // FP32 counterparts of pvglu_exp / pvglu_log (same methods, fewer terms:
@@ -190,8 +196,8 @@ PVGLU_HD float pvglu_logf(float x) {
 // precision.  Otherwise an FP32 estimate (Winitzki's approximation or the
 // asymptotic series, then three Halley steps on h(w) = w + log(w) - L) is
 // finished by one FP64 Halley step, which takes the FP32 error (~1e-7)
-// below the FP64 rounding (cubic convergence).  On GB300 the FP64 work is
-// one logarithm and one division.
+// below the FP64 rounding (cubic convergence).  The FP64 work is one
+// logarithm of a positive normal number and one division.
 PVGLU_HD double pvglu_lambert_w0_exp(double L) {
   if (L < -40.0) return pvglu_exp(L);
   const float lf = (float)L;
@@ -213,10 +219,12 @@ PVGLU_HD double pvglu_lambert_w0_exp(double L) {
     const float wp1 = w + 1.0f;
     w = w - 2.0f * h * w * wp1 / (2.0f * wp1 * wp1 + h);
   }
+  // w > 0 and normal here (W(e^-40) is about 4e-18), or NaN from a NaN L,
+  // which h carries on.
   const double wd = (double)w;
-  const double h = wd + pvglu_log(wd) - L;
+  const double h = (wd + pvglu_log_normal(wd)) - L;
   const double wp1 = wd + 1.0;
-  return wd - 2.0 * h * wd * wp1 / (2.0 * wp1 * wp1 + h);
+  return wd - (2.0 * h * wd * wp1) / fma(2.0 * wp1, wp1, h);
 }
 
 // Constants of the panel law, computed once per parameter set.
@@ -255,11 +263,11 @@ PVGLU_HD void pvglu_panel_prepare(const pvglu_panel_params* p, pvglu_panel_const
 PVGLU_HD void pvglu_panel_eval(const pvglu_panel_const* c, double iph, double v,
                                double* current, double* didv, double* didiph) {
   const double ip = iph + c->i0;
-  const double log_theta = c->log_c + c->k_l0 * (c->rs_iph * ip + v);
+  const double log_theta = fma(c->k_l0, fma(c->rs_iph, ip, v), c->log_c);
   const double w = pvglu_lambert_w0_exp(log_theta);
-  const double i = c->rsh_rsum * ip - v * c->inv_rsum - c->a_over_rs * w;
-  const double gd = w * c->k_gd + c->inv_rsh;
-  const double q = 1.0 / (1.0 + c->rs * gd);
+  const double i = fma(-c->a_over_rs, w, fma(c->rsh_rsum, ip, -v * c->inv_rsum));
+  const double gd = fma(w, c->k_gd, c->inv_rsh);
+  const double q = 1.0 / fma(c->rs, gd, 1.0);
   *current = i;
   *didv = -gd * q;
   *didiph = q;
