@@ -32,6 +32,7 @@ struct NtDev {
   int n, n_elems, ld, S;
   const int* hi;          // [n_elems]
   const int* lo;
+  const int2* xidx;       // [n_elems] rows of hi and lo in the linear solution (-1: ground)
   const int* inc_ptr;     // [n+1] elements incident to each unknown
   const int* inc_elem;
   const int* inc_sign;    // +1: + terminal, -1: - terminal
@@ -57,6 +58,7 @@ struct NtDev {
 
 constexpr int kUpdRows = 8;            // update block: 32 scenarios x 8 element rows
 constexpr int kUpdChunk = 64;          // elements per partial sum (>= 4 blocks per SM at 35k)
+constexpr int kUpdPer = kUpdChunk / kUpdRows;  // elements per thread (batched)
 
 __device__ __forceinline__ bool all_stopped(const NtDev& D) {
   return __ldcg(D.done + D.ld) >= D.S;
@@ -151,12 +153,13 @@ __device__ __forceinline__ double damped_step(double old, double nv, bool* bad,
   }
 }
 
-// New voltage drops from the solution X (pivot order through xpos, or caller
-// order when xpos is NULL), damped update, per-chunk sums of |change| in a
-// fixed order (deterministic).  Block: 32 scenarios x 8 element rows; grid:
-// (chunks, ld / 32).  With one scenario the 256 threads split the elements.
-__global__ void __launch_bounds__(256) k_nt_update(NtDev D, const double* __restrict__ X,
-                                                   const int* __restrict__ xpos) {
+// New voltage drops from the solution X (rows D.xidx: pivot order for FP64
+// factors, caller order after refinement), damped update, per-chunk sums of
+// |change| in a fixed order (deterministic).  Block: 32 scenarios x 8
+// element rows; grid: (chunks, ld / 32); a thread's elements have their
+// solution rows and voltages loaded together before the updates.  With one
+// scenario the 256 threads split the elements.
+__global__ void __launch_bounds__(256) k_nt_update(NtDev D, const double* __restrict__ X) {
   if (all_stopped(D)) return;
   __shared__ double red[kUpdRows][33];
   const bool single = D.ld == 1;
@@ -168,18 +171,30 @@ __global__ void __launch_bounds__(256) k_nt_update(NtDev D, const double* __rest
   if (s < D.S && !D.done[s]) {
     const int k0 = single ? kb + threadIdx.y * 32 + threadIdx.x : kb + threadIdx.y;
     const int dk = single ? 32 * kUpdRows : kUpdRows;
-    for (int k = k0; k < ke; k += dk) {
-      const int64_t e = (int64_t)k * D.ld + s;
-      const int h = D.hi[k], l = D.lo[k];
-      const double xh = h >= 0 ? X[(int64_t)(xpos ? xpos[h] : h) * D.ld + s] : 0.0;
-      const double xl = l >= 0 ? X[(int64_t)(xpos ? xpos[l] : l) * D.ld + s] : 0.0;
-      const double old = D.v[e];
+    double* __restrict__ v = D.v;
+    const int ld = D.ld;
+    double xh[kUpdPer], xl[kUpdPer], old[kUpdPer];
+#pragma unroll
+    for (int j = 0; j < kUpdPer; j++) {
+      const int k = k0 + j * dk;
+      if (k < ke) {
+        const int2 xi = __ldg(D.xidx + k);
+        xh[j] = xi.x >= 0 ? X[(int64_t)xi.x * ld + s] : 0.0;
+        xl[j] = xi.y >= 0 ? X[(int64_t)xi.y * ld + s] : 0.0;
+        old[j] = v[(int64_t)k * ld + s];
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < kUpdPer; j++) {
+      const int k = k0 + j * dk;
+      if (k >= ke) continue;
+      const int64_t e = (int64_t)k * ld + s;
       if (D.broken && D.broken[k]) {  // a wire is a linear element: no damping, no diff
-        D.v[e] = __dsub_rn(xh, xl);
+        v[e] = __dsub_rn(xh[j], xl[j]);
         continue;
       }
       double change;
-      D.v[e] = damped_step(old, __dsub_rn(xh, xl), &bad, &change);
+      v[e] = damped_step(old[j], __dsub_rn(xh[j], xl[j]), &bad, &change);
       sum = __dadd_rn(sum, change);
     }
   }
@@ -434,23 +449,20 @@ int newton_body(pvglu_newton* nw, cudaStream_t st) {
   int rc = pvglu::run_scatter(h, A, ndone, st);
   if (rc) return rc;
   const double* X;
-  const int* xpos;
-  if (fp64) {
+  if (fp64) {  // solution in pivot order (D.xidx)
     rc = pvglu::run_refactor_solve_perm(h, nw->w64, false, skip, st);
     X = nw->w64;
-    xpos = h->col_pos;
-  } else {
+  } else {  // refined solution in caller order
     rc = pvglu::run_refactor(h, st, skip);
     if (!rc)
       rc = pvglu::run_refine(h, A, nw->rhs64, nw->x64, false, nw->ir_tol, nw->ir_sweeps,
                              nullptr, st, D.done);
     X = nw->x64;
-    xpos = nullptr;
   }
   if (rc) return rc;
   const dim3 ublk(32, pvglu::kUpdRows);
   const dim3 ugrd((unsigned)nw->n_chunks, D.ld == 1 ? 1u : (unsigned)(D.ld / 32));
-  pvglu::k_nt_update<<<ugrd, ublk, 0, st>>>(D, X, xpos);
+  pvglu::k_nt_update<<<ugrd, ublk, 0, st>>>(D, X);
   pvglu::k_nt_check<<<(D.S + 3) / 4, 128, 0, st>>>(D, nw->n_chunks);
   if (fp64)
     pvglu::k_nt_keep<<<pvglu::rows_grid(D.n, D.ld, 256), 256, 0, st>>>(D, nw->w64, h->col_pos,
@@ -584,6 +596,22 @@ int pvglu_newton_create(pvglu_numeric* num, const pvglu_circuit* c, pvglu_newton
   D.hi = tmp;
   rc |= nw->put(lo, &tmp);
   D.lo = tmp;
+  {
+    // Solution rows of each element's terminals: FP64 factors leave the
+    // solution in pivot order (position col_pos[i] of unknown i), the
+    // refinement in caller order.
+    const pvglu::Symbolic& sy = num->sym->s;
+    std::vector<int> pos(n);
+    for (int i = 0; i < n; i++) pos[i] = i;
+    if (num->precision == PVGLU_FP64)
+      for (int c2 = 0; c2 < n; c2++) pos[sy.col_orig[c2]] = c2;
+    std::vector<int2> xi(std::max(ne, 1), make_int2(-1, -1));
+    for (int k = 0; k < ne; k++)
+      xi[k] = make_int2(hi[k] >= 0 ? pos[hi[k]] : -1, lo[k] >= 0 ? pos[lo[k]] : -1);
+    int2* xt = nullptr;
+    rc |= nw->put(xi, &xt);
+    D.xidx = xt;
+  }
   rc |= nw->put(iptr, &tmp);
   D.inc_ptr = tmp;
   rc |= nw->put(ielem, &tmp);
