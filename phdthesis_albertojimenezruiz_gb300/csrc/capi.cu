@@ -62,15 +62,13 @@ void solve_phase(pvglu_numeric* h, const std::vector<int>& sl, T* x, const int* 
 // grid size of the chain-program kernels of one handle.
 template <typename T, bool B>
 int prog_prepare(pvglu_numeric* h) {
-  const int smem = (int)pvglu::prog_smem_bytes<T, B>(h->table_max, pvglu::kProgWarps);
   const void* fns[] = {(const void*)pvglu::k_prog_level<T, -1, B>,
                        (const void*)pvglu::k_prog_level<T, 0, B>,
                        (const void*)pvglu::k_prog_level<T, 1, B>,
                        (const void*)pvglu::k_prog_level<T, 2, B>,
                        (const void*)pvglu::k_prog_level<T, 3, B>};
   for (const void* f : fns)
-    if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
-      return 1;
+    if (pvglu::allow_max_dynamic_smem(f) != cudaSuccess) return 1;
   h->prog_grid = pvglu::prog_persistent_grid<T, B>(h->table_max);
   return 0;
 }
@@ -1078,13 +1076,11 @@ int group_phase(pvglu_group* g, T* const* xs, cudaStream_t st) {
 
 template <typename T, bool B>
 int group_prepare() {
-  const int smem = 227 * 1024;
   const void* fns[] = {(const void*)pvglu::k_prog_level_multi<T, -1, B>,
                        (const void*)pvglu::k_prog_level_multi<T, 0, B>,
                        (const void*)pvglu::k_prog_level_multi<T, 1, B>};
   for (const void* f : fns)
-    if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
-      return 1;
+    if (pvglu::allow_max_dynamic_smem(f) != cudaSuccess) return 1;
   return 0;
 }
 

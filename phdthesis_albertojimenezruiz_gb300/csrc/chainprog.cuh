@@ -379,6 +379,25 @@ __device__ __forceinline__ void prog_run_level(const ProgDev& P, const DevStruct
   }
 }
 
+// Host: lets `kernel` request up to the device's opt-in shared memory per
+// block minus its own static shared memory.  The attribute is per kernel for
+// the whole process and handles differ in table size, so it is set to the
+// limit; a launch still requests only what its tables need.  Returns
+// cudaSuccess or the error (cleared).
+inline cudaError_t allow_max_dynamic_smem(const void* kernel) {
+  int dev = 0, optin = 0;
+  cudaFuncAttributes fa{};
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess)
+    e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, kernel);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             optin - (int)fa.sharedSizeBytes);
+  if (e != cudaSuccess) cudaGetLastError();
+  return e;
+}
+
 // Table layout of a block: warps_per_block tables, then one mbarrier per
 // warp.  Returns this warp's table and initialises its mbarrier.
 template <typename T, bool BATCH>

@@ -144,9 +144,7 @@ int prog_persistent_grid(int max_locals) {
     return 0;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
   const size_t smem = prog_smem_bytes<T, BATCH>(max_locals, kProgWarps);
-  if (cudaFuncSetAttribute(k_prog_persistent<T, BATCH>,
-                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-    return 0;
+  if (allow_max_dynamic_smem((const void*)k_prog_persistent<T, BATCH>) != cudaSuccess) return 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_prog_persistent<T, BATCH>,
                                                     kProgBlock, smem) != cudaSuccess)
     return 0;

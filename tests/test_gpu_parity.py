@@ -474,3 +474,32 @@ def test_refinement_profiling_switch_gives_the_same_bits(cuda, tmp_path):
                        cwd=root, timeout=600)
         outs.append(np.load(out))
     assert np.array_equal(outs[0], outs[1])
+
+
+@pytest.mark.parametrize("schedule", [SCHED_LEVELS, SCHED_PERSISTENT])
+def test_handles_with_different_table_sizes_coexist(cuda, schedule):
+    """A handle with wide tables still launches after a handle with narrow
+    tables was created (the kernels' shared-memory limit is process-wide),
+    and both give the FP64 oracle's solution after refinement."""
+    import torch
+
+    p = Plant(10, 16, 20)
+    s = Symbolic(p.rowptr, p.colidx)
+    o = O.Port(p.rowptr, p.colidx, s.array("perm_amd"))
+    S = 64
+    a, b = M.plant_batch(p, S, seed0=900, preset="c3")
+    wide = Numeric(s, S, FP32, schedule, max_locals=200)
+    narrow = Numeric(s, S, FP32, schedule, max_locals=8)
+    for num in (wide, narrow, wide):
+        a_dev = dev(pad_cols(a, num.ld))
+        b_dev = dev(pad_cols(b, num.ld))
+        num.scatter(a_dev)
+        num.refactor()
+        x = torch.zeros_like(b_dev)
+        num.solve_refined(a_dev, b_dev, x, tol=1e-12, max_sweeps=10)
+        torch.cuda.synchronize()
+        assert num.check()[0] == 0
+        x = x.cpu().numpy()
+        for k in (0, S - 1):
+            _, x_ref = o.scatter_refactor_solve(a[:, k], b[:, k])
+            assert np.abs(x[:, k] - x_ref).max() / np.abs(x_ref).max() <= 1e-10
