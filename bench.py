@@ -39,6 +39,7 @@ METRIC = "refactor+solve/s, 35k-unknown PV Jacobian: batched+FP32-IR vs plain FP
 UNIT = "refactor+solve/s"
 IR_TOL = 1e-12
 REFACTOR_TRAFFIC_512 = 362.0e6  # bytes, ncu dram__bytes_read.sum + dram__bytes_write.sum
+RESIDUAL_TRAFFIC_512 = 735.6e6  # bytes, the same for one k_residual_rows launch
 IR_MAX_SWEEPS = 6
 
 
@@ -827,6 +828,20 @@ def main() -> None:
         dist.barrier()
     ms = max_over_ranks(ev0.elapsed_time(ev1), dist, dev)
     refactor_ms = float(np.mean([s.elapsed_time(e) for s, e in rf]))
+    # The residual kernel alone (the largest share of a step: two launches per
+    # step), timed with CUDA events on the launching stream over 20 calls.
+    r_buf = torch.empty(n * ld, dtype=torch.float32, device=dev)
+    for _ in range(3):
+        num.refine_residual(a_d, b_d, x_d, r_buf, stream=stream)
+    er0 = torch.cuda.Event(enable_timing=True)
+    er1 = torch.cuda.Event(enable_timing=True)
+    er0.record(stream)
+    for _ in range(20):
+        num.refine_residual(a_d, b_d, x_d, r_buf, stream=stream)
+    er1.record(stream)
+    torch.cuda.synchronize()
+    resid_ms = er0.elapsed_time(er1) / 20
+    del r_buf
     sw = sweeps.cpu().numpy()[:S]
     value = S * world * args.steps / (ms / 1000.0)
     if args.only_batched:  # profiling runs: the batched path alone
@@ -922,16 +937,30 @@ def main() -> None:
     peaks = _peaks()
     peak = peaks.get("hbm_gbs")
     achieved = bm["refactor"] * S / (refactor_ms / 1000.0) / 1e9
-    roofline = {"kernel": ("k_prog_persistent<float,batched>" if persistent else
-                           "k_prog_level<float,refactor,batched>") + " (refactor phase)",
-                "bound": "hbm",
-                "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak if peak else None,
-                # DRAM read + write bytes of one refactorization (its two level
-                # launches) from an ncu capture of this workload (512 scenarios).
-                "traffic": REFACTOR_TRAFFIC_512 if S == 512 else None,
-                "peak_source": "measured" if peak else "fallback",
-                "bytes_per_launch": bm["refactor"] * S, "avg_launch_ms": refactor_ms}
+    roofline_refactor = {
+        "kernel": ("k_prog_persistent<float,batched>" if persistent else
+                   "k_prog_level<float,refactor,batched>") + " (refactor phase)",
+        "bound": "hbm",
+        "achieved": achieved, "peak": peak, "unit": "GB/s",
+        "frac": achieved / peak if peak else None,
+        # DRAM read + write bytes of one refactorization (its two level
+        # launches) from an ncu capture of this workload (512 scenarios).
+        "traffic": REFACTOR_TRAFFIC_512 if S == 512 else None,
+        "peak_source": "measured" if peak else "fallback",
+        "bytes_per_launch": bm["refactor"] * S, "avg_launch_ms": refactor_ms}
+    achieved_r = bm["residual"] * S / (resid_ms / 1000.0) / 1e9
+    roofline = {
+        "kernel": "k_residual_rows (FP64 residual of the refinement, the largest share of a "
+                  "step; one FP64 FMA per entry and scenario)",
+        "bound": "hbm",
+        "achieved": achieved_r, "peak": peak, "unit": "GB/s",
+        "frac": achieved_r / peak if peak else None,
+        # DRAM read + write bytes of one residual launch from an ncu capture
+        # of this workload (512 scenarios).
+        "traffic": RESIDUAL_TRAFFIC_512 if S == 512 else None,
+        "peak_source": "measured" if peak else "fallback",
+        "bytes_per_launch": bm["residual"] * S, "avg_launch_ms": resid_ms,
+        "timing": "pvglu_refine_residual x20 (each with a 2 KB flag reset), CUDA events"}
     if rank != 0:
         if dist:
             dist.destroy_process_group()
@@ -976,6 +1005,7 @@ def main() -> None:
                 "sweeps_max": int(e2e_sw.max()), "not_converged": int((e2e_sw <= 0).sum()),
                 "max_rel_err_vs_fp64": e2e_err},
         "roofline": roofline,
+        "roofline_refactor": roofline_refactor,
         "cpu_baseline": cpu,
         "newton_adjoint": newton,
         **extra,

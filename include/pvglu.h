@@ -238,6 +238,15 @@ int pvglu_refine(pvglu_numeric* h, const double* a_values, const double* g, cons
                  const double* b, double* x, int flags, double tol, int max_sweeps,
                  int* sweeps_out, void* stream);
 
+/* One residual of the refinement, for callers that run their own loop (and
+ * for timing the kernel): r = b - J x with FP64 arithmetic (J from a_values,
+ * [nnz_a * ld]), rounded to FP32 and stored in pivot order, the right-hand
+ * side of a correction solve with pvglu_solve on this FP32 handle.  b, x:
+ * FP64 device [n * ld], caller order; r: FP32 device [n * ld]; every
+ * scenario s < S is computed.  No counterpart in the reference. */
+int pvglu_refine_residual(pvglu_numeric* h, const double* a_values, const double* b,
+                          const double* x, float* r, void* stream);
+
 /* Host-buffer form of one refined linear step on an FP32 handle: H2D of A's
  * values ([nnz_a * ld], FP64) and b ([n * ld], FP64, original order),
  * scatter, FP32 refactor, pvglu_solve_refined, D2H of x ([n * ld], FP64).

@@ -934,6 +934,19 @@ int pvglu_scatter_refactor_solve_host(pvglu_numeric* h, const double* a_values_h
   return PVGLU_OK;
 }
 
+int pvglu_refine_residual(pvglu_numeric* h, const double* a_values, const double* b,
+                          const double* x, float* r, void* stream) {
+  if (!h || !a_values || !b || !x || !r) return fail(PVGLU_ERR_BAD_ARG, "NULL argument");
+  if (h->precision != PVGLU_FP32) return fail(PVGLU_ERR_BAD_ARG, "needs an FP32 handle");
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  // Every scenario is computed: no convergence flag is set.
+  PVGLU_CUDA(cudaMemsetAsync(h->ir_done, 0, (h->ld + 1) * sizeof(int), st));
+  const pvglu::AValues A{a_values, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  pvglu::Refine R(h, A, b, const_cast<double*>(x), false, 1.0, 1, nullptr, nullptr);
+  R.w = r;
+  return R.residual(st);
+}
+
 int pvglu_refine_system_host(pvglu_numeric* h, const double* a_values_host,
                              const double* b_host, double* x_host, double tol, int max_sweeps,
                              int* sweeps_out, void* stream) {

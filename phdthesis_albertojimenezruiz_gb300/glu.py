@@ -190,6 +190,13 @@ class Numeric:
                                                           _ptr(x), _stream_ptr(stream)),
                 "pvglu_scatter_refactor_solve_host")
 
+    def refine_residual(self, a_values, b, x, r, stream=None) -> None:
+        """r = b - J x (FP64 arithmetic) rounded to FP32, pivot order: one
+        residual of the refinement (FP32 handles)."""
+        N.check(N.lib().pvglu_refine_residual(self.handle, _ptr(a_values), _ptr(b), _ptr(x),
+                                              _ptr(r), _stream_ptr(stream)),
+                "pvglu_refine_residual")
+
     def refine_system_host(self, a_values, b, x, tol=1e-12, max_sweeps=10, sweeps=None,
                            stream=None) -> None:
         N.check(N.lib().pvglu_refine_system_host(self.handle, _ptr(a_values), _ptr(b), _ptr(x),

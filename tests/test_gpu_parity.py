@@ -503,3 +503,32 @@ def test_handles_with_different_table_sizes_coexist(cuda, schedule):
         for k in (0, S - 1):
             _, x_ref = o.scatter_refactor_solve(a[:, k], b[:, k])
             assert np.abs(x[:, k] - x_ref).max() / np.abs(x_ref).max() <= 1e-10
+
+
+def test_refine_residual_matches_numpy(cuda):
+    """pvglu_refine_residual: r = b - J x with FP64 arithmetic, rounded to FP32,
+    in pivot order (row p holds the residual of row row_orig[p])."""
+    import torch
+
+    p = Plant(4, 8, 20)
+    s = Symbolic(p.rowptr, p.colidx)
+    S = 64
+    a, b = M.plant_batch(p, S, seed0=40, preset="c1")
+    num = Numeric(s, S, FP32, SCHED_LEVELS)
+    rng = np.random.default_rng(5)
+    x = rng.uniform(-1.0, 1.0, (s.n, S)) * 30.0
+    r = torch.full((s.n * num.ld,), float("nan"), dtype=torch.float32, device="cuda")
+    num.refine_residual(dev(a), dev(b), dev(x), r)
+    torch.cuda.synchronize()
+    r = r.cpu().numpy().astype(np.float64).reshape(s.n, num.ld)[:, :S]
+    row_orig = s.array("row_orig")
+    got = np.empty_like(r)
+    got[row_orig] = r
+    rows = np.repeat(np.arange(s.n), np.diff(p.rowptr))
+    for k in range(S):
+        ax = np.zeros(s.n)
+        np.add.at(ax, rows, a[:, k] * x[p.colidx, k])
+        mag = np.zeros(s.n)
+        np.add.at(mag, rows, np.abs(a[:, k] * x[p.colidx, k]))
+        want = b[:, k] - ax
+        assert np.all(np.abs(got[:, k] - want) <= 2.0 ** -23 * np.abs(want) + 1e-13 * (mag + np.abs(b[:, k])))
