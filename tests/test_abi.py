@@ -41,3 +41,41 @@ def test_binding_matches_headers():
 def test_version_and_error_string():
     assert N.lib().pvglu_version().startswith(b"pvglu")
     assert N.lib().pvglu_last_error() is not None
+
+
+def test_headers_are_plain_c_and_link(tmp_path):
+    """Every header compiles as C99 with warnings as errors, and a C program
+    linked against libpvglu runs a host-only call through the ABI (symbolic
+    analysis of a 3x3 tridiagonal pattern)."""
+    import shutil
+    import subprocess
+
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        import pytest
+
+        pytest.skip("no C compiler")
+    lib = Path(N.load_library()._name)
+    src = tmp_path / "abi.c"
+    src.write_text(r"""
+#include <stdio.h>
+#include "pvglu.h"
+#include "pvglu_newton.h"
+#include "pvglu_plant.h"
+int main(void) {
+  const int rowptr[4] = {0, 2, 5, 7};
+  const int colidx[7] = {0, 1, 0, 1, 2, 1, 2};
+  pvglu_symbolic* s = NULL;
+  pvglu_symbolic_info info;
+  if (pvglu_symbolic_create(3, rowptr, colidx, NULL, &s) != PVGLU_OK) return 1;
+  if (pvglu_symbolic_get_info(s, &info) != PVGLU_OK) return 2;
+  printf("%s n=%d nnz_lu=%lld\n", pvglu_version(), info.n, (long long)info.nnz_lu);
+  return pvglu_symbolic_destroy(s) == PVGLU_OK && info.n == 3 && info.nnz_lu == 7 ? 0 : 3;
+}
+""")
+    exe = tmp_path / "abi"
+    subprocess.run([gcc, "-std=c99", "-Wall", "-Wextra", "-Werror", "-pedantic", "-I",
+                    str(INCLUDE), str(src), "-o", str(exe), "-L", str(lib.parent), "-lpvglu",
+                    f"-Wl,-rpath,{lib.parent}"], check=True, timeout=120)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True, timeout=120)
+    assert "n=3 nnz_lu=7" in out.stdout
