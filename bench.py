@@ -180,6 +180,18 @@ def make_inputs(S: int, ld: int, seed0: int = 1000):
     return p, a, b
 
 
+def make_conductances(p, S: int, ld: int, seed0: int = 1000) -> np.ndarray:
+    """Companion conductance of every panel for the scenarios of make_inputs
+    (same seeds, flat start): [n_panels, ld], columns past S zero.  With the
+    plant's stamps they give the same Jacobians as make_inputs' A values."""
+    g = np.stack([p.irradiance(seed=seed0 + s, preset="c2") for s in range(S)], axis=1)
+    v = np.repeat(p.flat_start()[:, None], S, axis=1)
+    _, didv = p.panel_iv(p.iph(g).ravel(), v.ravel())
+    out = np.zeros((p.n_panels, ld))
+    out[:, :S] = -didv.reshape(p.n_panels, S)
+    return out
+
+
 def bytes_model(nnz_a: int, nnz_lu: int, n: int, w: int) -> dict:
     """Algorithmic bytes per scenario for each kernel (values and vectors;
     structure is shared by the batch and amortised away)."""
@@ -931,6 +943,42 @@ def main() -> None:
     e2e_sw = np.concatenate([sweeps.cpu().numpy()[:S], sweeps2.cpu().numpy()[:S]])
     e2e_err = float(np.max(np.abs(x_hs[0].numpy()[:, :S] - xb).max(axis=0) /
                            np.abs(xb).max(axis=0)))
+
+    # The same end to end with the Jacobian as element conductances
+    # (pvglu_refine_stamps_host): n_panels values per scenario cross the host
+    # link instead of nnz_a.  Not the reference's interface (its hot path
+    # takes assembled values); reported beside `e2e`.
+    gpan = make_conductances(p, S, ld, seed0=1000 + rank * S)
+    g_h = torch.from_numpy(gpan).pin_memory()
+    for h_ in (num, num2):
+        h_.set_stamps(p.n_panels, p.a_lin, p.contrib_ptr, p.contrib_panel, p.contrib_sign)
+    for k in range(4):
+        h_, st_, sw_ = lanes[k % 2]
+        h_.refine_stamps_host(g_h, b_h, x_hs[k % 2], IR_TOL, IR_MAX_SWEEPS, sw_, stream=st_)
+    torch.cuda.synchronize()
+    es0 = torch.cuda.Event(enable_timing=True)
+    es1 = torch.cuda.Event(enable_timing=True)
+    es2 = torch.cuda.Event(enable_timing=True)
+    es0.record(stream)
+    stream2.wait_event(es0)
+    for k in range(e2e_steps):
+        h_, st_, sw_ = lanes[k % 2]
+        h_.refine_stamps_host(g_h, b_h, x_hs[k % 2], IR_TOL, IR_MAX_SWEEPS, sw_, stream=st_)
+    es2.record(stream2)
+    stream.wait_event(es2)
+    es1.record(stream)
+    torch.cuda.synchronize()
+    e2s_ms = max_over_ranks(es0.elapsed_time(es1), dist, dev)
+    e2s_sw = np.concatenate([sweeps.cpu().numpy()[:S], sweeps2.cpu().numpy()[:S]])
+    e2e_structured = {
+        "value": S * world * e2e_steps / (e2s_ms / 1000.0), "unit": UNIT,
+        "h2d_bytes_per_step": int(g_h.numel() * 8 + b_h.numel() * 8),
+        "d2h_bytes_per_step": int(x_hs[0].numel() * 8),
+        "call": "pvglu_refine_stamps_host (panel conductances in, x out), two handles on two "
+                "streams alternating",
+        "sweeps_max": int(e2s_sw.max()), "not_converged": int((e2s_sw <= 0).sum()),
+        "max_rel_err_vs_fp64": float(np.max(np.abs(x_hs[0].numpy()[:, :S] - xb).max(axis=0) /
+                                            np.abs(xb).max(axis=0)))}
     del num2
 
     bm = bytes_model(nnz_a, nnz_lu, n, 4)
@@ -1004,6 +1052,7 @@ def main() -> None:
                 "call": "pvglu_refine_system_host, two handles on two streams alternating",
                 "sweeps_max": int(e2e_sw.max()), "not_converged": int((e2e_sw <= 0).sum()),
                 "max_rel_err_vs_fp64": e2e_err},
+        "e2e_structured": e2e_structured,
         "roofline": roofline,
         "roofline_refactor": roofline_refactor,
         "cpu_baseline": cpu,

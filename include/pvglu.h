@@ -255,6 +255,17 @@ int pvglu_refine_system_host(pvglu_numeric* h, const double* a_values_host,
                              const double* b_host, double* x_host, double tol, int max_sweeps,
                              int* sweeps_out, void* stream);
 
+/* As pvglu_refine_system_host with the Jacobian given by the stamps of
+ * pvglu_numeric_set_stamps: H2D of the element conductances g ([n_elems *
+ * ld], FP64) instead of A's values, A's values assembled from the stamps
+ * on the device, then as pvglu_refine_system_host, D2H of x.  A Newton caller
+ * computes one conductance per element (002b:183-197) before it assembles
+ * A, so this moves n_elems values per scenario over the host link instead of
+ * nnz_a.  No counterpart in the reference. */
+int pvglu_refine_stamps_host(pvglu_numeric* h, const double* g_host, const double* b_host,
+                             double* x_host, double tol, int max_sweeps, int* sweeps_out,
+                             void* stream);
+
 /* ---------------- allocation-free solve ---------------------------------- */
 
 /* The original-order solve of pvglu_solve (flags: PVGLU_SOLVE_TRANSPOSE

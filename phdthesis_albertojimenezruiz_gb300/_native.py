@@ -94,6 +94,7 @@ _SIGS = {
     "pvglu_group_refactor_solve": ([_P, _P, _I, _P], _I),
     "pvglu_refine_system_host": ([_P, _P, _P, _P, C.c_double, _I, _P, _P], _I),
     "pvglu_refine_residual": ([_P, _P, _P, _P, _P, _P], _I),
+    "pvglu_refine_stamps_host": ([_P, _P, _P, _P, C.c_double, _I, _P, _P], _I),
     "pvglu_solve_noalloc": ([_P, _P, _I, _P], _I),
     "pvglu_numeric_set_stamps": ([_P, _I, _P, _P, _P, _P], _I),
     "pvglu_scatter_stamps": ([_P, _P, _P, _P], _I),

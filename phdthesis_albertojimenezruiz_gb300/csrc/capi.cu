@@ -967,6 +967,37 @@ int pvglu_refine_system_host(pvglu_numeric* h, const double* a_values_host,
   return PVGLU_OK;
 }
 
+int pvglu_refine_stamps_host(pvglu_numeric* h, const double* g_host, const double* b_host,
+                             double* x_host, double tol, int max_sweeps, int* sweeps_out,
+                             void* stream) {
+  if (!h || !g_host || !b_host || !x_host || h->precision != PVGLU_FP32)
+    return fail(PVGLU_ERR_BAD_ARG, "needs an FP32 handle and non-NULL buffers");
+  if (!h->st_ptr) return fail(PVGLU_ERR_BAD_ARG, "no stamps set on this handle");
+  cudaStream_t st = as_stream(stream);
+  const size_t g_count = (size_t)std::max(h->n_elems, 1) * h->ld;
+  if (h->g64_count < g_count) {  // first call, or stamps with more elements since
+    if (h->alloc(g_count, &h->g64)) return fail(PVGLU_ERR_NO_MEMORY, "conductance staging buffer");
+    h->g64_count = g_count;
+  }
+  PVGLU_CUDA(cudaMemcpyAsync(h->g64, g_host, (size_t)h->n_elems * h->ld * sizeof(double),
+                             cudaMemcpyHostToDevice, st));
+  PVGLU_CUDA(cudaMemcpyAsync(h->b64, b_host, (size_t)h->n * h->ld * sizeof(double),
+                             cudaMemcpyHostToDevice, st));
+  // A's values assembled once from the stamps (one pass), then the explicit-
+  // value path: its scatter and its residual stream A with vector loads.
+  double* a = h->work64;
+  pvglu::k_assemble<<<pvglu::rows_grid(h->nnz_a, h->ld, 256), 256, 0, st>>>(
+      h->nnz_a, h->ld, h->S, h->stamps(h->g64, nullptr), a);
+  PVGLU_CUDA(cudaGetLastError());
+  int rc = pvglu_scatter(h, a, stream);
+  if (!rc) rc = pvglu_refactor(h, stream);
+  if (!rc) rc = pvglu_solve_refined(h, a, h->b64, h->x64, tol, max_sweeps, sweeps_out, stream);
+  if (rc) return rc;
+  PVGLU_CUDA(cudaMemcpyAsync(x_host, h->x64, (size_t)h->n * h->ld * sizeof(double),
+                             cudaMemcpyDeviceToHost, st));
+  return PVGLU_OK;
+}
+
 }  // extern "C"
 
 // ---------------------------------------------------------------------------

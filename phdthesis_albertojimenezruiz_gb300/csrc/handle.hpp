@@ -55,6 +55,8 @@ struct pvglu_numeric {
   double* work64 = nullptr;     // [nnz_a * ld] staging / [n * ld] vectors
   double* b64 = nullptr;        // [n * ld]
   double* x64 = nullptr;        // [n * ld]
+  double* g64 = nullptr;        // [n_elems * ld] conductances of pvglu_refine_stamps_host
+  size_t g64_count = 0;
   int* col_pos = nullptr;       // inverse of col_orig
   int* row_pos = nullptr;       // inverse of row_orig
   pvglu::DevStatus* status = nullptr;

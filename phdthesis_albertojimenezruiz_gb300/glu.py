@@ -204,6 +204,15 @@ class Numeric:
                                                  _stream_ptr(stream)),
                 "pvglu_refine_system_host")
 
+    def refine_stamps_host(self, g, b, x, tol=1e-12, max_sweeps=10, sweeps=None,
+                           stream=None) -> None:
+        """Host-buffer refined step with the Jacobian from the registered
+        stamps: element conductances g [n_elems x ld] in, x out."""
+        N.check(N.lib().pvglu_refine_stamps_host(self.handle, _ptr(g), _ptr(b), _ptr(x),
+                                                 float(tol), int(max_sweeps), _ptr(sweeps),
+                                                 _stream_ptr(stream)),
+                "pvglu_refine_stamps_host")
+
     def __del__(self):
         h = getattr(self, "handle", None)
         if h and N._lib is not None:
