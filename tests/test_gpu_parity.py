@@ -488,7 +488,7 @@ def test_handles_with_different_table_sizes_coexist(cuda, schedule):
     o = O.Port(p.rowptr, p.colidx, s.array("perm_amd"))
     S = 64
     a, b = M.plant_batch(p, S, seed0=900, preset="c3")
-    wide = Numeric(s, S, FP32, schedule, max_locals=200)
+    wide = Numeric(s, S, FP32, schedule, max_locals=100)
     narrow = Numeric(s, S, FP32, schedule, max_locals=8)
     for num in (wide, narrow, wide):
         a_dev = dev(pad_cols(a, num.ld))
