@@ -1285,15 +1285,17 @@ int pvglu_selftest_barrier_timeout(int blocks, long long max_spins, int* status_
   unsigned int* bar = nullptr;
   pvglu::DevStatus* st = nullptr;
   int* passed = nullptr;
-  PVGLU_CUDA(cudaMalloc((void**)&bar, 4 * sizeof(unsigned int)));
-  PVGLU_CUDA(cudaMalloc((void**)&st, sizeof(pvglu::DevStatus)));
-  PVGLU_CUDA(cudaMalloc((void**)&passed, sizeof(int)));
-  PVGLU_CUDA(cudaMemset(bar, 0, 4 * sizeof(unsigned int)));
-  PVGLU_CUDA(cudaMemset(st, 0, sizeof(pvglu::DevStatus)));
-  PVGLU_CUDA(cudaMemset(passed, 0, sizeof(int)));
+  // Every buffer is freed on every path (cudaFree(NULL) is a no-op).
+  cudaError_t e = cudaMalloc((void**)&bar, 4 * sizeof(unsigned int));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&st, sizeof(pvglu::DevStatus));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&passed, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(bar, 0, 4 * sizeof(unsigned int));
+  if (e == cudaSuccess) e = cudaMemset(st, 0, sizeof(pvglu::DevStatus));
+  if (e == cudaSuccess) e = cudaMemset(passed, 0, sizeof(int));
   void* args[] = {(void*)&bar, (void*)&st, (void*)&max_spins, (void*)&passed};
-  cudaError_t e = cudaLaunchCooperativeKernel((const void*)pvglu::k_barrier_timeout_probe,
-                                              dim3(blocks), dim3(64), args, 0, nullptr);
+  if (e == cudaSuccess)
+    e = cudaLaunchCooperativeKernel((const void*)pvglu::k_barrier_timeout_probe, dim3(blocks),
+                                    dim3(64), args, 0, nullptr);
   if (e == cudaSuccess) e = cudaDeviceSynchronize();
   pvglu::DevStatus hs{};
   if (e == cudaSuccess) e = cudaMemcpy(&hs, st, sizeof(hs), cudaMemcpyDeviceToHost);
