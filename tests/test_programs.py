@@ -52,3 +52,11 @@ def test_plant_programs(checker, tmp_path, dims):
 def test_golden_programs(checker, tmp_path, name):
     g = load_golden(name)
     run(checker, tmp_path, g["rowptr"], g["colidx"])
+
+
+@pytest.mark.parametrize("n,deg,src,seed", [(40, 3.0, 3, 1), (150, 5.0, 6, 2), (300, 2.0, 0, 3)])
+def test_random_pattern_programs(checker, tmp_path, n, deg, src, seed):
+    import matrices as M
+
+    rp, ci, _, _ = M.random_mna(n, deg, src, seed)
+    run(checker, tmp_path, rp, ci)
