@@ -172,3 +172,44 @@ def test_product_vs_port_random_patterns():
             got, want = s.arrays(), o.arrays()
             for k in REF_ARRAYS:
                 assert np.array_equal(got[k], want[k]), (n, deg, src, seed, perm is None, k)
+
+
+def test_malformed_patterns_are_refused_not_crashed():
+    """Fuzz of the analysis entry point with malformed CSR (out-of-range and
+    duplicate columns, non-monotone row pointers, missing diagonals, bad
+    permutations) and with valid random patterns: every call returns an
+    analysis or raises PvgluError; accepted analyses have a permutation
+    ordering and schedule every column once."""
+    from phdthesis_albertojimenezruiz_gb300 import PvgluError
+
+    rng = np.random.default_rng(11)
+    accepted = refused = 0
+    for it in range(1200):
+        n = int(rng.integers(0, 12))
+        kind = it % 5
+        perm = None
+        if kind == 0:
+            counts = rng.integers(0, 5, n)
+            rp = np.concatenate([[0], np.cumsum(counts)]).astype(np.int32)
+            ci = rng.integers(-2, n + 2, int(rp[-1])).astype(np.int32)
+        elif kind == 1:
+            rp = rng.integers(-3, 10, n + 1).astype(np.int32)
+            ci = np.zeros(32, dtype=np.int32)
+        else:
+            rows = []
+            for i in range(n):
+                extra = rng.integers(0, n, int(rng.integers(0, 4))).tolist() if n else []
+                rows.append(sorted(set(([i] if kind != 3 else []) + extra)))
+            rp = np.concatenate([[0], np.cumsum([len(r) for r in rows])]).astype(np.int32)
+            ci = np.array([c for r in rows for c in r] + [0], dtype=np.int32)
+            if kind == 4 and n:
+                perm = rng.integers(-1, n + 1, n).astype(np.int32)
+        try:
+            s = Symbolic(rp, ci, perm)
+        except PvgluError:
+            refused += 1
+            continue
+        accepted += 1
+        assert np.array_equal(np.sort(s.array("perm_amd")), np.arange(s.n))
+        assert np.array_equal(np.sort(s.array("lu_cols")), np.arange(s.n))
+    assert accepted > 100 and refused > 100
