@@ -1,5 +1,7 @@
 // C ABI of the hot path (include/pvglu.h): handles, device structure upload,
-// scatter / refactor / solve launch sequences.
+// scatter / refactor / solve launch sequences, the mixed-precision refinement
+// (replayed from a CUDA graph whose sweep loop is a conditional while node),
+// the host-buffer steps, size-class groups and the autotuner.
 #include <cuda_runtime.h>
 
 #include <algorithm>

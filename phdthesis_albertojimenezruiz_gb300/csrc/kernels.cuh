@@ -3,9 +3,10 @@
 // permutations and the FP64 residual of iterative refinement.
 //
 // Layout: the value of LU slot q for scenario s lives at V[q * ld + s] (slot
-// major, scenario fastest).  A warp therefore walks one column for 32
-// scenarios and every value access is a coalesced 128/256-byte transaction,
-// while the structure indices it reads are warp-uniform broadcasts.  With a
+// major, scenario fastest).  A warp therefore handles one slot or row for 32
+// or 64 consecutive scenarios (two per lane with 8/16-byte accesses in the
+// batched kernels) and every value access is a coalesced 128-512-byte
+// transaction, while the structure indices it reads are warp-uniform.  With a
 // single scenario (ld = 1) the same code runs one thread per chain, which is
 // the reference's launch shape (factorize_electrical_system_CUDA.cu:72-98).
 //
