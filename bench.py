@@ -434,11 +434,70 @@ def config3_section(stream, steps: int) -> dict:
     ms_graph = _time_ms(graph.replay, torch.cuda.current_stream(), steps)
     codes = [m.check()[0] for m in members]
     total = sum(counts)
+    del group, members, a_d, b_d, x_d
+    newton = config3_newton(dims, counts)
     return {"workload": "512 scenarios over plants 10x16x20, 50x24x28, 120x24x28; FP64 scatter + "
                         "refactor + solve per step", "classes": sizes,
             "value": total / (ms_graph / 1000.0), "unit": UNIT,
             "ms_per_step_graph": ms_graph, "ms_per_step_group": ms_group,
-            "ms_per_step_one_sequence_per_class": ms_sep, "status_codes": codes}
+            "ms_per_step_one_sequence_per_class": ms_sep, "status_codes": codes,
+            "newton": newton}
+
+
+def config3_newton(dims, counts) -> dict:
+    """The three-size batch as Newton loops: each size class has its own
+    autotuned FP64 handle and device Newton driver (the iteration body
+    captured once as a CUDA graph and replayed), seeded cloud fields of 3-8
+    shadows per scenario, all three classes running at once on their own
+    streams from flat starts through the gmin stages to convergence."""
+    import torch
+
+    from phdthesis_albertojimenezruiz_gb300 import FP64, Newton, Numeric, Plant, Symbolic
+    from phdthesis_albertojimenezruiz_gb300.glu import autotune
+
+    dev = torch.device("cuda", torch.cuda.current_device())
+    lanes = []
+    for k, (d, S) in enumerate(zip(dims, counts)):
+        p = Plant(*d)
+        sym = Symbolic(p.rowptr, p.colidx)
+        ml, sc, _ = autotune(sym, S, FP64)
+        num = Numeric(sym, S, FP64, sc, max_locals=ml)
+        nw = Newton.for_plant(num, p)
+        ld = num.ld
+        g = np.stack([p.irradiance(seed=7000 + 1000 * k + s, preset="c3") for s in range(S)], 1)
+        st = torch.cuda.Stream()
+        iph = torch.from_numpy(_pad(p.iph(g), ld)).to(dev)
+        v0 = torch.from_numpy(_pad(np.repeat(p.flat_start()[:, None], S, 1), ld)).to(dev)
+        nw.set_iph(iph, stream=st)
+        lanes.append({"plant": "x".join(map(str, d)), "p": p, "num": num, "nw": nw, "st": st,
+                      "v0": v0, "tuning": {"max_locals": ml, "schedule": sc}})
+
+    def run(lane):
+        lane["nw"].set_voltages(lane["v0"], stream=lane["st"])
+        lane["nw"].run(1e-6 * lane["p"].n, check_every=8, stream=lane["st"])
+
+    for lane in lanes:  # warm-up: graph capture, first touch
+        run(lane)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=len(lanes)) as ex:
+        list(ex.map(run, lanes))
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    classes, iters, conv = [], 0, 0
+    for lane in lanes:
+        it, out, _ = lane["nw"].results()
+        bodies, graph = lane["nw"].last_run()
+        iters += int(it.sum())
+        conv += int((out == 0).sum())
+        classes.append({"plant": lane["plant"], "scenarios": int(len(it)),
+                        "iterations_min": int(it.min()), "iterations_max": int(it.max()),
+                        "converged": int((out == 0).sum()), "cuda_graph": graph,
+                        "tuning": lane["tuning"]})
+    return {"workload": "Newton to convergence (gmin stages, tol 1e-6*n) of all 512 scenarios, "
+                        "three size classes on three streams at once, FP64",
+            "wall_s": wall, "scenario_iterations_per_s": iters / wall,
+            "refactor_solves_per_s": iters / wall, "converged": conv, "classes": classes}
 
 
 def config4_section(stream, steps: int) -> dict:
@@ -478,11 +537,97 @@ def config4_section(stream, steps: int) -> dict:
     torch.cuda.synchronize()
     xa, xb = x_d.cpu().numpy()[:, :S], x64.cpu().numpy()[:, :S]
     err = float(np.max(np.abs(xa - xb).max(axis=0) / np.abs(xb).max(axis=0)))
+    # Every scenario against the oracle's FP64 path (sequential GLU + CSC
+    # substitution on the CPU, the reference's arithmetic).
+    from oracle import oracle as O
+
+    port = O.Port(p.rowptr, p.colidx, sym.array("perm_amd"))
+    errs = []
+    for k in range(S):
+        _, x_ref = port.scatter_refactor_solve(a[:, k], b[:, k])
+        errs.append(float(np.abs(xa[:, k] - x_ref).max() / np.abs(x_ref).max()))
     return {"workload": f"plant_200x24x28 ({sym.n} unknowns, nnz_lu {int(sym.nnz_lu)}), 64 "
                         "scenarios, scatter + FP32 refactor + FP64-refined solve",
             "value": S / (ms / 1000.0), "unit": UNIT, "ms_per_step": ms,
             "tuning": {"max_locals": ml, "schedule": sc}, "sweeps_max": int(sw.max()),
-            "not_converged": int((sw <= 0).sum()), "max_rel_err_vs_fp64": err}
+            "not_converged": int((sw <= 0).sum()), "max_rel_err_vs_gpu_fp64": err,
+            "per_scenario": {"sweeps": [int(v) for v in sw],
+                             "rel_err_vs_oracle_fp64": [float(f"{e:.2e}") for e in errs]},
+            "max_rel_err_vs_oracle_fp64": max(errs)}
+
+
+def newton_iterates_section(stream, S: int, steps: int) -> dict:
+    """FP32 + refinement against FP64 on Jacobians of real Newton iterates.
+
+    The headline times companion Jacobians at the flat start.  Here the FP64
+    device Newton of the 35k plant is run, for the headline's S scenarios,
+    through the gmin stages up to and including stage j; the Jacobian of each
+    scenario at its iterate there (with that stage's convergence conductance)
+    is then solved by scatter + FP32 refactor + FP64 refinement and by
+    scatter + FP64 refactor + solve, both timed, with the refinement's sweep
+    counts and its error against the FP64 solution."""
+    import torch
+
+    from phdthesis_albertojimenezruiz_gb300 import (FP32, FP64, GMIN_STAGES, Newton, Numeric,
+                                                    Plant, Symbolic)
+    from phdthesis_albertojimenezruiz_gb300.glu import autotune
+
+    p = Plant(*DIMS)
+    sym = Symbolic(p.rowptr, p.colidx)
+    ld = ((S + 63) // 64) * 64
+    dev = torch.device("cuda", torch.cuda.current_device())
+    g = np.stack([p.irradiance(seed=1000 + s, preset="c2") for s in range(S)], axis=1)
+    ml64, sc64, _ = autotune(sym, S, FP64)
+    ml32, sc32, _ = autotune(sym, S, FP32)
+    nt = Numeric(sym, S, FP64, sc64, max_locals=ml64)
+    nw = Newton.for_plant(nt, p)
+    nw.set_iph(torch.from_numpy(_pad(p.iph(g), ld)).to(dev))
+    v0 = torch.from_numpy(_pad(np.repeat(p.flat_start()[:, None], S, 1), ld)).to(dev)
+    n32 = Numeric(sym, S, FP32, sc32, max_locals=ml32)
+    n64 = Numeric(sym, S, FP64, sc64, max_locals=ml64)
+    sweeps = torch.zeros(ld, dtype=torch.int32, device=dev)
+    out = []
+    for j in (0, 2, 5, 8, 10, 11):
+        nw.set_voltages(v0)
+        nw.run(1e-6 * p.n, gmin=GMIN_STAGES[:j + 1])
+        v = torch.as_tensor(_VoltView(nw.voltages_ptr(), p.n_panels * ld),
+                            device=dev).cpu().numpy().reshape(p.n_panels, ld)[:, :S]
+        gm = GMIN_STAGES[j]
+        a, b = p.companion_batch(g, v, ld=ld, gmin=gm)
+        a_d = torch.from_numpy(a).to(dev)
+        b_d = torch.from_numpy(b).to(dev)
+        x32 = torch.zeros_like(b_d)
+        x64 = torch.empty_like(b_d)
+
+        def step32():
+            n32.scatter(a_d, stream=stream)
+            n32.refactor(stream=stream)
+            n32.solve_refined(a_d, b_d, x32, tol=IR_TOL, max_sweeps=40, sweeps=sweeps,
+                              stream=stream)
+
+        def step64():
+            n64.scatter(a_d, stream=stream)
+            x64.copy_(b_d)
+            n64.refactor_solve(x64, original=True, stream=stream)
+
+        for _ in range(3):
+            step32()
+            step64()
+        ms32 = _time_ms(step32, stream, steps)
+        ms64 = _time_ms(step64, stream, steps)
+        sw = sweeps.cpu().numpy()[:S]
+        xa, xb = x32.cpu().numpy()[:, :S], x64.cpu().numpy()[:, :S]
+        err = np.abs(xa - xb).max(axis=0) / np.abs(xb).max(axis=0)
+        out.append({"stage": j, "gmin": gm if gm > 0 else None,
+                    "fp32ir_per_s": S / (ms32 / 1000.0), "fp64_per_s": S / (ms64 / 1000.0),
+                    "fp32ir_over_fp64": ms64 / ms32,
+                    "sweeps_histogram": {str(int(k)): int((sw == k).sum()) for k in np.unique(sw)},
+                    "not_converged": int((sw <= 0).sum()),
+                    "max_rel_err_vs_fp64": float(err[sw > 0].max()) if (sw > 0).any() else None})
+        del a_d, b_d, x32, x64
+    return {"workload": f"plant_50x24x28, {S} scenarios, Jacobians at the FP64 Newton iterate "
+                        "at the end of gmin stage j (stage j's conductance included); "
+                        "refinement tolerance 1e-12, up to 40 sweeps", "stages": out}
 
 
 def _newton_handle(p, sym, S: int, precision, tol_ir: float = 1e-12):
@@ -574,30 +719,80 @@ def config2_section() -> dict:
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
     it, out, _ = nw.results()
+    del nw, num
+    seq = config2_sequential(p, sym, sh, T)
     return {"workload": "plant_50x24x28, 300 time steps of one 5-shadow field as one FP64 "
                         "batch, gmin stages, tol 1e-6*n", "time_steps": T,
             "newton_ms": ms, "time_steps_per_s": T / (ms / 1000.0),
             "iterations_min": int(it.min()), "iterations_max": int(it.max()),
             "converged": int((out == 0).sum()),
-            "refactor_solves_per_s": float(it.sum()) / (ms / 1000.0)}
+            "refactor_solves_per_s": float(it.sum()) / (ms / 1000.0),
+            "single_instance_sequential": seq,
+            "batch_over_sequential": seq["wall_s"] * 1000.0 / ms}
+
+
+def config2_sequential(p, sym, shadows, T: int) -> dict:
+    """The plain single-instance FP64 path over the same 300 snapshots, in
+    sequence, as the reference's simulator runs them
+    (000_PVPP_simulator.cpp:120-236: each snapshot from the flat start
+    through the gmin stages): one scenario handle with the fastest
+    single-instance schedule, the snapshot's photocurrents from the device
+    field at t, the Newton body replayed from its CUDA graph."""
+    import torch
+
+    num, nw = _newton_handle(p, sym, 1, 0)
+    nw.set_field(p.pan_x, p.pan_y, [shadows], iph_per_g=p.info["iph_stc"] / 1000.0)
+    v0 = torch.from_numpy(p.flat_start()).cuda()
+    tol = 1e-6 * p.n
+    nw.field_iph(0.0)
+    nw.set_voltages(v0)
+    nw.run(tol)  # warm-up: graph capture
+    torch.cuda.synchronize()
+    iters, conv = [], 0
+    t0 = time.perf_counter()
+    for t in range(T):
+        nw.field_iph(float(t))
+        nw.set_voltages(v0)
+        nw.run(tol, check_every=16)
+        it, out, _ = nw.results()
+        iters.append(int(it[0]))
+        conv += int(out[0] == 0)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    return {"time_steps": T, "wall_s": wall, "time_steps_per_s": T / wall,
+            "iterations_min": min(iters), "iterations_max": max(iters), "converged": conv,
+            "refactor_solves_per_s": sum(iters) / wall}
 
 
 def config5_fd_section(precision_name: str) -> dict:
-    """Per-panel adjoint gradients of the 35k plant against central
-    differences on 200 random panels, all 401 perturbed solves in one batch."""
+    """Per-panel dP/dG of the 35k plant, the 128-scenario batch of the
+    differentiation configuration, checked on scenario 0:
+    * against central differences at h = 1e-3 W/m^2 on 200 random panels,
+      each difference solved in extended precision by the oracle on the
+      panel's inverter block (the plant decomposes by inverter, so the plant
+      power moves only through that inverter's power);
+    * against the oracle's CPU FP64 adjoint (the reference's factors) on
+      every panel.
+    Beside them, the same differences taken from the GPU's own FP64 Newton
+    solves on 20 of those panels (40 extra scenarios in the batch), which
+    shows the FP64 floor of such differences."""
     import torch
 
+    from oracle import oracle as O
     from phdthesis_albertojimenezruiz_gb300 import FP32, FP64, Plant, Symbolic
 
     prec = FP64 if precision_name == "fp64" else FP32
     p = Plant(*DIMS)
     sym = Symbolic(p.rowptr, p.colidx)
+    g_to_iph = p.info["iph_stc"] / 1000.0
     rng = np.random.default_rng(77)
     panels = rng.choice(p.n_panels, 200, replace=False)
-    g0 = p.irradiance(seed=5000, preset="c2")
-    h = 1e-2
-    cols = [g0]
-    for k in panels:
+    h = 1e-3
+    base = [p.irradiance(seed=5000 + s, preset="c2") for s in range(128)]
+    g0 = base[0]
+    cols = list(base)
+    gpu_fd_panels = panels[:20]
+    for k in gpu_fd_panels:
         for sign in (1.0, -1.0):
             gk = g0.copy()
             gk[k] += sign * h
@@ -618,34 +813,63 @@ def config5_fd_section(precision_name: str) -> dict:
     torch.cuda.synchronize()
     it, out, _ = nw.results()
     x = x.cpu().numpy().reshape(p.n, ld)
-    P = -p.v_mppt * x[p.inv_current, :S].sum(axis=0)
-    adj = grad.cpu().numpy().reshape(p.n_panels, ld)[panels, 0] * (p.info["iph_stc"] / 1000.0)
-    fd = (P[1::2] - P[2::2]) / (2 * h)
-    err = np.abs(adj - fd)
-    scale = np.abs(adj).max()
-    # The FP64 CPU adjoint of the oracle (factors bit-identical to the
-    # reference's) at the same operating point, every panel.
-    from oracle import oracle as O
-
-    port = O.Port(p.rowptr, p.colidx, sym.array("perm_amd"))
     v = torch.as_tensor(_VoltView(nw.voltages_ptr(), p.n_panels * ld),
                         device="cuda").cpu().numpy().reshape(p.n_panels, ld)[:, 0]
+    full = grad.cpu().numpy().reshape(p.n_panels, ld)[:, 0] * g_to_iph
+    adj = full[panels]
+    # Extended-precision central differences on the inverter blocks.
+    per_inv = DIMS[1] * DIMS[2]
+    q = Plant(1, DIMS[1], DIMS[2])
+    qs = Symbolic(q.rowptr, q.colidx)
+    qport = O.Port(q.rowptr, q.colidx, qs.array("perm_amd"))
+    qdpdx = np.zeros(q.n)
+    qdpdx[q.inv_current] = -q.v_mppt
+    iph0 = p.iph(g0)
+
+    def ext(k):
+        _, pans = p.inverter_block(int(k) // per_inv)
+        fd, _, res = qport.fd_ext(q, iph0[pans], v[pans], qdpdx, int(k) - pans.start,
+                                  g_to_iph * h)
+        return g_to_iph * fd, res
+
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=os.cpu_count() or 1) as ex:
+        ext_out = list(ex.map(ext, panels))
+    ext_s = time.perf_counter() - t0
+    fd = np.array([e[0] for e in ext_out])
+    rel = np.abs(adj - fd) / np.abs(fd)
+    # The GPU's own FP64 differences, inverter power by inverter power.
+    xs = x[:, 128:S]
+    gpu_rel = []
+    for j, k in enumerate(gpu_fd_panels):
+        inv = int(k) // per_inv
+        pw = -p.v_mppt * xs[p.inv_current[inv], 2 * j:2 * j + 2]
+        fdk = (pw[0] - pw[1]) / (2 * h)
+        gpu_rel.append(abs(full[k] - fdk) / abs(fdk))
+    # The FP64 CPU adjoint of the oracle (factors bit-identical to the
+    # reference's) at the same operating point, every panel.
+    port = O.Port(p.rowptr, p.colidx, sym.array("perm_amd"))
     dpdx1 = np.zeros(p.n)
     dpdx1[p.inv_current] = -p.v_mppt
-    ref = port.adjoint(p, p.iph(g0), v, dpdx1) * (p.info["iph_stc"] / 1000.0)
-    full = grad.cpu().numpy().reshape(p.n_panels, ld)[:, 0] * (p.info["iph_stc"] / 1000.0)
-    return {"workload": f"plant_50x24x28, dP/dG of 200 random panels, central differences "
-                        f"(h = {h} W/m^2) as 400 extra scenarios in the same batch, "
-                        f"{precision_name} forward", "scenarios": S,
+    ref = port.adjoint(p, p.iph(g0), v, dpdx1) * g_to_iph
+    return {"workload": f"plant_50x24x28, 128 scenarios, {precision_name} forward; dP/dG of "
+                        "scenario 0 on 200 random panels against central differences "
+                        f"(h = {h} W/m^2)", "scenarios": S,
             "converged": int((out == 0).sum()),
-            "fd_max_abs_err_over_max_grad": float(err.max() / scale),
-            "fd_median_rel_err": float(np.median(err / np.maximum(np.abs(fd), 1e-12))),
-            "fd_note": "per-panel differences of a 6.6 MW plant power are at the FP64 "
-                       "rounding floor of P; the all-panel directional check is in "
-                       "newton_adjoint.fd_check",
+            "fd_max_rel_err": float(rel.max()), "fd_median_rel_err": float(np.median(rel)),
+            "fd_max_abs_err_over_max_grad": float(np.abs(adj - fd).max() / np.abs(adj).max()),
+            "fd_method": "each +-h pair solved in long double (Newton in correction form, "
+                         "residual in long double, FP64 Jacobian) on the panel's inverter block "
+                         "by the oracle, from the GPU's converged voltages",
+            "fd_seconds": ext_s,
+            "gpu_fp64_fd_20_panels": {
+                "max_rel_err": float(max(gpu_rel)), "median_rel_err": float(np.median(gpu_rel)),
+                "note": "differences of the GPU's FP64 Newton solves (inverter power): node "
+                        "voltages near 1 kV are quantised at 2.3e-13 V, about 1e-8 W of "
+                        "inverter power, against 1e-5 to 1e-2 W of difference"},
             "vs_cpu_fp64_adjoint_all_panels_max_rel": float(
                 np.abs(full - ref).max() / np.abs(ref).max()),
-            "max_grad_w_per_w_m2": float(scale)}
+            "max_grad_w_per_w_m2": float(np.abs(full).max())}
 
 
 class _VoltView:
@@ -667,6 +891,9 @@ def run_configs(args, stream) -> dict:
         out["config4"] = config4_section(stream, max(5, args.steps))
     if "5" in wanted:
         out["config5_fd"] = {m: config5_fd_section(m) for m in ("fp64", "fp32")}
+    if "i" in wanted:
+        out["fp32ir_on_newton_iterates"] = newton_iterates_section(stream, args.scenarios,
+                                                                   max(5, args.steps))
     return out
 
 
@@ -684,15 +911,19 @@ def run_reference(args) -> None:
     res = None
     for _ in range(args.warmup):
         cpu_baseline(a, b, p, perm, 1.0, threads)
-    vals = []
+    vals, walls = [], []
     for _ in range(args.steps):
+        t0 = time.perf_counter()
         res = cpu_baseline(a, b, p, perm, 3.0, threads)
+        walls.append(time.perf_counter() - t0)
         vals.append(res["value"])
     value = float(np.median(vals))
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1000.0 * threads / value, "higher_is_better": True,
+        # A step is one bounded sample (about 3 s of refactor+solves on all
+        # host threads), so its wall time is reported as the step time.
+        "ms_per_step": 1000.0 * float(np.median(walls)), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": "plant_50x24x28 (33,750 unknowns) refactor+solve, CPU GLU",
                    "scenarios_per_step": threads},
@@ -726,10 +957,11 @@ def main() -> None:
                     help="chain-program table size of the batched handle (0: autotune)")
     ap.add_argument("--schedule", default="persistent", choices=["levels", "persistent"],
                     help="schedule used with --max-locals (autotuned otherwise)")
-    ap.add_argument("--configs", default="1,2,3,4,5",
+    ap.add_argument("--configs", default="1,2,3,4,5,i",
                     help="extra workloads reported beside the headline (1: 4x8x20 Newton vs the "
                          "oracle, 2: 300 time steps, 3: three plant sizes per level launch, "
-                         "4: the 135k plant, 5: per-panel adjoint vs central differences; "
+                         "4: the 135k plant, 5: per-panel adjoint vs central differences, "
+                         "i: FP32 + refinement vs FP64 on Newton-iterate Jacobians; "
                          "empty: none)")
     ap.add_argument("--only-configs", action="store_true",
                     help="run the --configs workloads alone (profiling runs)")
@@ -910,6 +1142,28 @@ def main() -> None:
     plain_name = max(single, key=single.get)
     plain = single[plain_name]
 
+    # The same 512-scenario batch in FP64 (scatter + FP64 refactor + solve,
+    # autotuned), which splits the headline's gain over the plain path into
+    # the part that batching gives and the part that FP32 + refinement adds.
+    ml64, sc64, _ = autotune(sym, S, FP64)
+    num64b = Numeric(sym, S, FP64, sc64, max_locals=ml64)
+    x64b = torch.empty_like(b_d)
+
+    def fp64_step():
+        num64b.scatter(a_d, stream=stream)
+        x64b.copy_(b_d)
+        num64b.refactor_solve(x64b, original=True, stream=stream)
+
+    for _ in range(args.warmup):
+        fp64_step()
+    ms64 = _time_ms(fp64_step, stream, args.steps)
+    batched_fp64 = {"value": S / (ms64 / 1000.0), "unit": UNIT, "ms_per_step": ms64,
+                    "tuning": {"max_locals": ml64, "schedule": sc64},
+                    "max_rel_err_vs_fp32ir": float(np.max(
+                        np.abs(x64b.cpu().numpy()[:, :S] - xa).max(axis=0) /
+                        np.abs(xa).max(axis=0)))}
+    del num64b, x64b
+
     # End to end through the host-buffer C ABI call: every step copies its
     # inputs from pinned host memory and its solutions back.  Two handles on
     # two streams alternate, so one batch's copies overlap the other's
@@ -1044,9 +1298,6 @@ def main() -> None:
                    "flops_per_refactor_solve": sym.info["flops_refactor"] + 2.0 * nnz_lu},
         "ir": {"sweeps_min": int(sw.min()), "sweeps_max": int(sw.max()),
                "not_converged": int((sw <= 0).sum()), "max_rel_err_vs_fp64": max_rel},
-        "plain_fp64": {"value": plain, "unit": UNIT, "schedule": plain_name,
-                       "all_schedules": single,
-                       "ratio_batched_fp32ir_over_plain": value / world / plain},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(8 * (nnz_a + n) * ld),
                 "d2h_bytes_per_step": int(8 * n * ld),
                 "call": "pvglu_refine_system_host, two handles on two streams alternating",
@@ -1060,6 +1311,15 @@ def main() -> None:
         **extra,
         "gpu_launches": launches,
         "clocks": clk.summary(),
+        # Last on the line, so that a tail of the output keeps them: the
+        # target's denominator (the plain single-instance FP64 GPU path) and
+        # the split of the headline into batching and precision.
+        "batched_fp64": batched_fp64,
+        "plain_fp64": {"value": plain, "unit": UNIT, "schedule": plain_name,
+                       "all_schedules": single},
+        "ratios": {"batched_fp32ir_over_plain_fp64": value / world / plain,
+                   "batched_fp64_over_plain_fp64": batched_fp64["value"] / plain,
+                   "batched_fp32ir_over_batched_fp64": value / world / batched_fp64["value"]},
     }
     print(json.dumps(line))
     if dist:

@@ -279,11 +279,15 @@ int pvglu_refine_stamps_host(pvglu_numeric* h, const double* g_host, const doubl
  * itself is still created beforehand with pvglu_numeric_create.)
  * Limit: n * ld <= 1,048,576 FP64 entries (8 MiB, reserved on every GPU
  * that loads the library until the process exits); larger handles get
- * PVGLU_ERR_TOO_LARGE.  The first call on a device looks the array up with
- * cudaGetSymbolAddress for that device, so make that first call before any
- * stream capture.  All calls share the array and it keeps the last call's
- * contents; nothing in it needs to start at zero.  Calls whose work overlaps
- * on the GPU (other streams, other threads) race on the array.
+ * PVGLU_ERR_TOO_LARGE.  The handle's device must be the current device
+ * (PVGLU_ERR_BAD_ARG otherwise).  Set-up: the first call on a device looks
+ * the array's device address up with cudaGetSymbolAddress, with that device
+ * current, and caches it; a device reset ends the context, and the first
+ * call in the new context looks it up again.  Make the first call on each
+ * device (and after a reset) before any stream capture.  All calls share the
+ * array and it keeps the last call's contents; nothing in it needs to start
+ * at zero.  Calls whose work overlaps on the GPU (other streams, other
+ * threads) race on the array.
  * No counterpart in the reference. */
 int pvglu_solve_noalloc(pvglu_numeric* h, double* x, int flags, void* stream);
 

@@ -9,6 +9,7 @@ this module; the product never imports it.
 from __future__ import annotations
 
 import ctypes as C
+import os
 import subprocess
 from pathlib import Path
 
@@ -18,7 +19,10 @@ HERE = Path(__file__).resolve().parent
 ROOT = HERE.parent
 PORT_LIB = HERE / "liboracle.so"
 REF_LIB = HERE / "_ref" / "libpvref.so"
-REF_SRC = Path("/root/reference/PVPP_Plant_Simulator")
+# The reference checkout: $PVGLU_REFERENCE_DIR, by default a sibling
+# "reference" directory of this repository.
+REF_SRC = Path(os.environ.get("PVGLU_REFERENCE_DIR", str(ROOT.parent / "reference"))) / \
+    "PVPP_Plant_Simulator"
 
 ARRAYS = ("perm_amd", "perm_rows", "fill_rowptr", "fill_col", "lu_sl", "lu_sc", "lu_cols",
           "l_sl", "l_sc", "l_cols", "u_sl", "u_sc", "u_cols", "max_elements_per_column",
@@ -113,6 +117,9 @@ class Port(_Base):
             lib.oracle_adjoint.argtypes = ([C.c_void_p, C.c_int] + [C.c_void_p] * 4 + [C.c_int] +
                                            [C.c_void_p] * 2 + [D] * 4 + [C.c_void_p, D] +
                                            [C.c_void_p] * 4)
+            lib.oracle_fd_ext.argtypes = ([C.c_void_p, C.c_int] + [C.c_void_p] * 4 + [C.c_int] +
+                                          [C.c_void_p] * 2 + [D] * 4 + [C.c_void_p] * 3 +
+                                          [C.c_int, D, C.c_int] + [C.c_void_p] * 3)
             lib.oracle_free.argtypes = [C.c_void_p]
             cls._lib = lib
         return cls._lib
@@ -201,6 +208,25 @@ class Port(_Base):
         if rc:
             raise RuntimeError(f"oracle adjoint failed ({rc})")
         return out
+
+    def fd_ext(self, plant, iph, v0, dpdx, k, delta, max_iterations=40):
+        """Central difference (P(iph_k + delta) - P(iph_k - delta)) / (2 delta)
+        of P = dpdx . x, both operating points solved in long double from the
+        element voltages v0 (oracle_fd_ext).  Returns (difference quotient,
+        Newton iterations of the two sides, largest final residual [A])."""
+        keep, args = self._circuit(plant)
+        iph = np.ascontiguousarray(iph, dtype=np.float64)
+        v0 = np.ascontiguousarray(v0, dtype=np.float64)
+        dpdx = np.ascontiguousarray(dpdx, dtype=np.float64)
+        fd = C.c_double(0.0)
+        res = C.c_double(0.0)
+        its = np.zeros(2, np.int32)
+        rc = self.lib.oracle_fd_ext(*args[:13], _p(iph), _p(v0), _p(dpdx), int(k), float(delta),
+                                    int(max_iterations), C.byref(fd), _p(its), C.byref(res))
+        del keep
+        if rc:
+            raise RuntimeError(f"oracle extended-precision difference failed ({rc})")
+        return fd.value, (int(its[0]), int(its[1])), res.value
 
 
 class Ref(_Base):

@@ -14,7 +14,9 @@
 //   37-90) and a long double diff.
 // The element law is the plant's own definition (panel_model.h), an input of
 // the check like the plant's pattern and linear part.
+#include <algorithm>
 #include <cmath>
+#include <limits>
 #include <map>
 #include <vector>
 
@@ -167,6 +169,143 @@ int oracle_newton(void* sym, int n, const int* rowptr, const int* colidx, const 
   *last_diff = (double)diff;
   return 0;
 }
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Central difference of a linear objective P = dpdx . x with respect to the
+// photocurrent of element k, in extended precision (long double: a 64-bit
+// significand on x86-64, 113 bits on aarch64).
+//
+// FP64 cannot resolve such a difference to 1e-6 at small steps: node
+// voltages near 1 kV are quantised at 2.3e-13 V, which through a 0.02 ohm
+// cable is 1.1e-11 A of inverter current, 1.2e-8 W at the inverter voltage,
+// while one panel's 1e-3 W/m^2 step moves the plant power by about 5e-4 W.
+// So the two perturbed operating points are solved here with the node
+// voltages held in long double: Newton in correction form, the nonlinear
+// residual b_lin - A_lin x - incidence f(V) evaluated in long double with the
+// panel law solved in long double, the correction solved with the FP64
+// Jacobian through the oracle's GLU.  That converges to the long double
+// solution whenever FP64 factors of J give a contraction (cond(J) eps64 < 1).
+// Start: the FP64 element voltages v0 (e.g. a converged FP64 operating
+// point).  Outputs the difference quotient (P(+delta) - P(-delta)) / (2 delta),
+// the Newton iterations of each side and the largest final residual [A].
+// Returns 0, 4 (pivot failure), 5 (stamp outside the pattern) or 6 (no
+// convergence within max_iter).
+
+namespace {
+
+using ld_t = long double;
+
+// I(V) of the single-diode panel (panel_model.h) solved in long double by
+// Newton on g(I) = Iph - I0 (exp((V + I Rs) / a) - 1) - (V + I Rs) / Rsh - I,
+// from the start value *cur (the previous solution of this element, or the
+// FP64 law's value); also dI/dV.  Stops when a step is within a few ulps of
+// long double or stops shrinking.
+void panel_iv_ext(const pvglu_panel_params& p, ld_t iph, ld_t v, ld_t* cur, ld_t* didv) {
+  const ld_t eps = std::numeric_limits<ld_t>::epsilon();
+  const ld_t i0 = p.i0, a = p.a, rs = p.rs, rsh = p.rsh;
+  ld_t i = *cur, e = 0, last = 1e300L;
+  for (int it = 0; it < 60; it++) {
+    const ld_t vd = v + i * rs;
+    e = expl(vd / a);
+    const ld_t g = iph - i0 * (e - 1.0L) - vd / rsh - i;
+    const ld_t dg = -i0 * e * rs / a - rs / rsh - 1.0L;
+    const ld_t step = g / dg;
+    i -= step;
+    const ld_t mag = fabsl(step);
+    if (mag <= 4.0L * eps * (fabsl(i) + 1.0L) || mag >= last) break;
+    last = mag;
+  }
+  e = expl((v + i * rs) / a);
+  const ld_t gd = i0 * e / a + 1.0L / rsh;  // -dI/dVd
+  *cur = i;
+  *didv = -gd / (1.0L + rs * gd);
+}
+
+}  // namespace
+
+extern "C" int oracle_fd_ext(void* sym, int n, const int* rowptr, const int* colidx,
+                             const double* a_lin, const double* b_lin, int n_elems,
+                             const int* hi, const int* lo, double i0, double a, double rs,
+                             double rsh, const double* iph, const double* v0, const double* dpdx,
+                             int k, double delta, int max_iter, double* fd_out,
+                             int* iterations_out, double* resid_out) {
+  const Circuit c{n, n_elems, rowptr, colidx, hi, lo, a_lin, b_lin, {i0, a, rs, rsh}, nullptr, 0};
+  const int* csc_row = nullptr;
+  long long nnz_lu = 0;
+  oracle_get(sym, "csc_row", &csc_row, &nnz_lu);
+  std::vector<double> lu(nnz_lu), a_vals, b, vd(n_elems), iphd(iph, iph + n_elems);
+  std::vector<ld_t> x(n), r(n), icur(n_elems);
+  ld_t P[2] = {0, 0};
+  double worst = 0.0;
+  for (int side = 0; side < 2; side++) {
+    const ld_t sign = side == 0 ? 1.0L : -1.0L;
+    const ld_t iph_k = (ld_t)iph[k] + sign * (ld_t)delta;
+    // Start: one FP64 linear solve at v0.
+    for (int e = 0; e < n_elems; e++) vd[e] = v0[e];
+    if (!assemble(c, iphd.data(), vd.data(), -1.0, a_vals, b, nullptr)) return 5;
+    if (oracle_scatter_refactor_solve(sym, a_vals.data(), lu.data(), b.data(), 1)) return 4;
+    for (int i = 0; i < n; i++) x[i] = b[i];
+    for (int e = 0; e < n_elems; e++) {
+      double cur64, didv64, dphi64;
+      pvglu_panel_iv3(&c.panel, iph[e], v0[e], &cur64, &didv64, &dphi64);
+      icur[e] = cur64;
+    }
+    ld_t best = 1e300L;
+    int stall = 0, it = 0;
+    bool done = false;
+    for (it = 1; it <= max_iter && !done; it++) {
+      // Residual in long double, the linear part in branch form:
+      // sum_j a_ij x_j = (sum_j a_ij) x_i + sum_{j != i} a_ij (x_j - x_i).
+      // Node rows of pure conductances have a zero row sum, so no product
+      // of a large conductance sum with a 1 kV voltage is formed and the
+      // floor is that of the branch currents themselves.
+      for (int i = 0; i < n; i++) {
+        ld_t rowsum = 0, acc = 0;
+        for (int p = rowptr[i]; p < rowptr[i + 1]; p++) {
+          rowsum += (ld_t)a_lin[p];
+          if (colidx[p] != i) acc += (ld_t)a_lin[p] * (x[colidx[p]] - x[i]);
+        }
+        r[i] = ((ld_t)b_lin[i] - rowsum * x[i]) - acc;
+      }
+      for (int e = 0; e < n_elems; e++) {
+        const ld_t ve = (hi[e] >= 0 ? x[hi[e]] : 0.0L) - (lo[e] >= 0 ? x[lo[e]] : 0.0L);
+        ld_t didv;
+        panel_iv_ext(c.panel, e == k ? iph_k : (ld_t)iph[e], ve, &icur[e], &didv);
+        const ld_t f = -icur[e];  // element current hi -> lo
+        if (hi[e] >= 0) r[hi[e]] -= f;
+        if (lo[e] >= 0) r[lo[e]] += f;
+        vd[e] = (double)ve;
+      }
+      ld_t rmax = 0;
+      for (int i = 0; i < n; i++) rmax = fmaxl(rmax, fabsl(r[i]));
+      if (rmax < best * 0.5L) {
+        best = rmax;
+        stall = 0;
+      } else if (++stall >= 3) {
+        done = true;  // at the long double floor
+        break;
+      }
+      // Correction with the FP64 Jacobian at the current voltages.
+      if (!assemble(c, iphd.data(), vd.data(), -1.0, a_vals, b, nullptr)) return 5;
+      for (int i = 0; i < n; i++) b[i] = (double)r[i];
+      if (oracle_scatter_refactor_solve(sym, a_vals.data(), lu.data(), b.data(), 1)) return 4;
+      for (int i = 0; i < n; i++) x[i] += b[i];
+    }
+    if (!done) return 6;
+    worst = std::max(worst, (double)best);
+    iterations_out[side] = it;
+    ld_t pv = 0;
+    for (int i = 0; i < n; i++) pv += (ld_t)dpdx[i] * x[i];
+    P[side] = pv;
+  }
+  *fd_out = (double)((P[0] - P[1]) / (2.0L * (ld_t)delta));
+  *resid_out = worst;
+  return 0;
+}
+
+extern "C" {
 
 // Adjoint check: J at the iterate v without convergence conductance,
 // J^T lambda = dpdx through the oracle's factors and permutations, then

@@ -662,7 +662,9 @@ int pvglu_numeric_create_ex(const pvglu_symbolic* sym, int n_scenarios, int prec
   h->batch = h->ld > 1;
   {
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess ||
+    if (cudaGetDevice(&dev) != cudaSuccess) dev = 0;
+    h->device = dev;
+    if (
         cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
       h->sm_count = 1;
     // One resident wave of the batched residual (its grid-stride loop covers
@@ -869,6 +871,12 @@ int pvglu_refactor_solve(pvglu_numeric* h, void* x, int flags, void* stream) {
 
 int pvglu_solve(pvglu_numeric* h, void* x, int flags, void* stream) {
   if (!h || !x) return fail(PVGLU_ERR_BAD_ARG, "NULL argument");
+  int dev = 0;
+  PVGLU_CUDA(cudaGetDevice(&dev));
+  if (dev != h->device)
+    return fail(PVGLU_ERR_BAD_ARG, "the handle was created on device " +
+                                       std::to_string(h->device) + ", the current device is " +
+                                       std::to_string(dev));
   cudaStream_t st = as_stream(stream);
   return h->precision == PVGLU_FP64 ? solve_any<double>(h, (double*)x, flags, st)
                                     : solve_any<float>(h, (float*)x, flags, st);
@@ -1006,28 +1014,72 @@ int pvglu_refine_stamps_host(pvglu_numeric* h, const double* g_host, const doubl
 // Allocation-free solve.  Its permuted work vector lives in this file-scope
 // device array instead of the handle's work buffer.  Every GPU that loads
 // the library reserves the array until the process exits.  Host code must not
-// use the array's name as a device address: the address is obtained once per
-// device with cudaGetSymbolAddress.
+// use the array's name as a device address: the address is obtained with
+// cudaGetSymbolAddress, once per device and CUDA context, with that device
+// current.
 constexpr int64_t kNoAllocScratchElems = int64_t(1) << 20;  // 8 MiB of FP64
 static __device__ __align__(256) double g_noalloc_scratch[kNoAllocScratchElems];
 
 namespace {
 std::mutex g_noalloc_mu;
-double* g_noalloc_ptr[128] = {};  // per device ordinal
+struct NoAllocSlot {
+  double* ptr = nullptr;
+  unsigned long long ctx_id = 0;  // context the address belongs to
+};
+NoAllocSlot g_noalloc_slot[128];  // per device ordinal
 
-int noalloc_scratch(double** out) {
-  int dev = 0;
-  PVGLU_CUDA(cudaGetDevice(&dev));
+// Unique id of the calling thread's current CUDA context (driver entry points
+// looked up through the runtime, so the library links no driver library).  A
+// device reset ends the context; the next context gets a new id, and the
+// array's address is looked up again for it.
+int current_context_id(unsigned long long* id) {
+  using GetCurrent = int (*)(void**);
+  using GetId = int (*)(void*, unsigned long long*);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static bool looked_up = false;
+  if (!looked_up) {
+    void* f0 = nullptr;
+    void* f1 = nullptr;
+    cudaDriverEntryPointQueryResult q0{}, q1{};
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f0, 12000, cudaEnableDefault, &q0) ==
+            cudaSuccess &&
+        q0 == cudaDriverEntryPointSuccess &&
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &f1, 12000, cudaEnableDefault, &q1) ==
+            cudaSuccess &&
+        q1 == cudaDriverEntryPointSuccess) {
+      get_current = reinterpret_cast<GetCurrent>(f0);
+      get_id = reinterpret_cast<GetId>(f1);
+    }
+    cudaGetLastError();
+    looked_up = true;
+  }
+  if (!get_current || !get_id) return fail(PVGLU_ERR_CUDA, "driver context entry points unavailable");
+  void* ctx = nullptr;
+  if (get_current(&ctx) != 0 || !ctx) return fail(PVGLU_ERR_CUDA, "no current CUDA context");
+  if (get_id(ctx, id) != 0) return fail(PVGLU_ERR_CUDA, "cuCtxGetId failed");
+  return PVGLU_OK;
+}
+
+// Set-up of the allocation-free solve on the current device: the device
+// address of g_noalloc_scratch, looked up on the first call in each context
+// of each device and cached.  cudaGetSymbolAddress allocates nothing.
+int noalloc_scratch(int dev, double** out) {
   if (dev < 0 || dev >= 128) return fail(PVGLU_ERR_BAD_ARG, "device ordinal out of range");
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (!g_noalloc_ptr[dev]) {
+  unsigned long long ctx = 0;
+  int rc = current_context_id(&ctx);
+  if (rc) return rc;
+  NoAllocSlot& slot = g_noalloc_slot[dev];
+  if (!slot.ptr || slot.ctx_id != ctx) {
     void* p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess)
       return fail(PVGLU_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-    g_noalloc_ptr[dev] = static_cast<double*>(p);
+    slot.ptr = static_cast<double*>(p);
+    slot.ctx_id = ctx;
   }
-  *out = g_noalloc_ptr[dev];
+  *out = slot.ptr;
   return PVGLU_OK;
 }
 }  // namespace
@@ -1042,8 +1094,14 @@ int pvglu_solve_noalloc(pvglu_numeric* h, double* x, int flags, void* stream) {
     return fail(PVGLU_ERR_TOO_LARGE,
                 "n * ld = " + std::to_string(need) + " exceeds the static scratch of " +
                     std::to_string(kNoAllocScratchElems) + " FP64 entries");
+  int dev = 0;
+  PVGLU_CUDA(cudaGetDevice(&dev));
+  if (dev != h->device)
+    return fail(PVGLU_ERR_BAD_ARG, "the handle was created on device " +
+                                       std::to_string(h->device) + ", the current device is " +
+                                       std::to_string(dev));
   double* w = nullptr;
-  int rc = noalloc_scratch(&w);
+  int rc = noalloc_scratch(dev, &w);
   if (rc) return rc;
   cudaStream_t st = as_stream(stream);
   const bool tr = (flags & PVGLU_SOLVE_TRANSPOSE) != 0;

@@ -206,10 +206,26 @@ __device__ __forceinline__ void exec_op1(uint32_t op, int op_index, const int* o
 }
 
 // Per-warp state of the batched path: its table, its mbarrier and phase.
+// aborted: a table wait ran out (warp-uniform); the warp then runs no more
+// operations or stores and waits once more, bounded, for the loads it has in
+// flight before it returns (prog_drain).
 struct WarpTma {
   unsigned long long* mbar;
   unsigned phase;
+  bool aborted;
 };
+
+// After an aborted table wait: a second bounded wait for the bulk loads still
+// in flight into this warp's table (they must land before the block's shared
+// memory can be given to another block), then for this warp's bulk stores.
+__device__ __forceinline__ void prog_drain(WarpTma& tma) {
+  long long polls = 0;
+  while (!mbar_try_wait(tma.mbar, tma.phase) && ++polls <= kMbarMaxPolls) {
+  }
+  tma.phase ^= 1u;
+  bulk_wait_all();
+  __syncwarp();
+}
 
 // Runs every segment of `chain`, batched over the 64 scenarios starting at
 // s0 (BATCH) or for the single scenario.  sm: this warp's table.
@@ -290,11 +306,20 @@ __device__ __forceinline__ void prog_run_chain(const ProgDev& P, const DevStruct
           bulk_load(sm + l * kGroup, prog_row<T, KIND>(__ldg(lr + l), v, x, ld, s0), kRow,
                     tma.mbar);
       long long polls = 0;
+      bool late = false;
       while (!mbar_try_wait(tma.mbar, tma.phase)) {
         if (++polls > kMbarMaxPolls) {
-          report_error(st, 6, -2, s0);
+          late = true;
           break;
         }
+      }
+      // The table is either complete for every lane or the warp stops: no
+      // operation runs on a partly loaded table and nothing is stored.
+      if (__any_sync(0xffffffffu, late)) {
+        if (lane == 0) report_error(st, 6, -2, s0);
+        tma.aborted = true;
+        prog_drain(tma);
+        return;
       }
       tma.phase ^= 1u;
       V2* t = reinterpret_cast<V2*>(sm) + lane;
@@ -363,6 +388,7 @@ __device__ __forceinline__ void prog_run_level(const ProgDev& P, const DevStruct
   const int items = (ce - cb) * groups;
   const int lane = threadIdx.x & 31;
   for (int it = warp_id; it < items; it += n_warps) {
+    if (BATCH && tma.aborted) break;
     const int ci = BATCH ? it / groups : it;
     const int c = cb + ci;
     const int s0 = BATCH ? (it - ci * groups) * kGroup : 0;
@@ -409,6 +435,7 @@ __device__ __forceinline__ T* prog_setup_warp(unsigned char* smem_raw, int max_l
   T* sm = reinterpret_cast<T*>(smem_raw + (size_t)w * table);
   tma.mbar = reinterpret_cast<unsigned long long*>(smem_raw + (size_t)nw * table) + w;
   tma.phase = 0;
+  tma.aborted = false;
   if (BATCH) {
     if ((threadIdx.x & 31) == 0) mbar_init(tma.mbar, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -432,6 +459,8 @@ k_prog_level(ProgDev P, int table, DevStruct d, int cb, int ce,
                              T* __restrict__ v, T* __restrict__ x, int ld, int S, T pivot_tol,
                              DevStatus* st, const int* done, const int* ndone) {
   if (ndone && __ldcg(ndone) >= S) return;
+  // A table wait that ran out in an earlier level stops the later levels.
+  if (BATCH && __ldcg(&st->code) == 6) return;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   WarpTma tma;
   T* sm = prog_setup_warp<T, BATCH>(smem_raw, table, tma);
@@ -486,6 +515,7 @@ k_prog_level_multi(MultiLaunch<T> M, int table) {
                                    C.pivot_tol, C.st);
   };
   for (int it = warp_id; it < M.items; it += n_warps) {
+    if (BATCH && tma.aborted) break;
     if (M.n > 3 && it >= M.c[3].item_begin) run(M.c[3], it);
     else if (M.n > 2 && it >= M.c[2].item_begin) run(M.c[2], it);
     else if (M.n > 1 && it >= M.c[1].item_begin) run(M.c[1], it);

@@ -46,6 +46,7 @@ struct pvglu_numeric {
   const pvglu_symbolic* sym = nullptr;
   int n = 0, nnz = 0, nnz_a = 0;
   int S = 0, ld = 0, precision = PVGLU_FP64;
+  int device = 0;               // CUDA device the handle's memory lives on
   int schedule = PVGLU_SCHED_LEVELS;
   double pivot_tol = 1e-8;
   pvglu::DevStruct d{};

@@ -99,6 +99,9 @@ __device__ __forceinline__ bool prog_phase(const ProgDev& P, const DevStruct& d,
     *need_sync = true;
     prog_run_level<T, KIND, BATCH>(P, d, P.level_chain[lv], P.level_chain[lv + 1], v, x, ld,
                                    S, sm, tma, pivot_tol, st, done, warp_id, n_warps);
+    // A warp whose table wait ran out raises the abort word: every block
+    // leaves at the next barrier.
+    if (BATCH && tma.aborted && (threadIdx.x & 31) == 0) atomicExch(bar + 2, 1u);
   }
   return true;
 }

@@ -13,6 +13,7 @@
 //     u8 element size (4 or 8), u64 element count, the elements
 //   u64 FNV-1a hash of every byte before it
 #include <algorithm>
+#include <climits>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -278,6 +279,14 @@ int load_symbolic(const char* path, Symbolic& s, std::string& err) {
   r.get(s.update_count);
   r.get(s.right_looking_hazards);
   r.get(s.flops_refactor);
+  // The counts are stored as int64 and held as int: refuse what int cannot
+  // hold instead of truncating it (the hash is no defence against a crafted
+  // file).
+  if (!r.ok || n < 0 || n > INT_MAX || row_swaps < 0 || row_swaps > INT_MAX || invol < 0 ||
+      invol > 1 || s.nnz_a < 0 || s.nnz_lu < 0 || s.update_count < 0) {
+    err = "symbolic dump is malformed (counts out of range)";
+    return ERR_BAD_ARG;
+  }
   s.n = (int)n;
   s.row_swaps = (int)row_swaps;
   s.perm_rows_is_involution = (int)invol;

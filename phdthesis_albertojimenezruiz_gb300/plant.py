@@ -91,6 +91,19 @@ class Plant:
     def iph(self, g: np.ndarray) -> np.ndarray:
         return self.info["iph_stc"] * g / 1000.0
 
+    def inverter_block(self, v: int) -> tuple[slice, slice]:
+        """Unknowns and panels of inverter v: (node slice, panel slice).
+
+        The generator numbers the circuit inverter by inverter (the strings'
+        panel nodes, then the combiner bus, the inverter terminal and the
+        source current), and no element joins two inverters (each is a
+        fixed-voltage sink), so block v of every array is the circuit of
+        Plant(1, strings, series) shifted by v blocks."""
+        per_node = self.dims[1] * self.dims[2] + 3
+        per_pan = self.dims[1] * self.dims[2]
+        return (slice(v * per_node, (v + 1) * per_node),
+                slice(v * per_pan, (v + 1) * per_pan))
+
     def flat_start(self) -> np.ndarray:
         """Panel voltages of the flat start: every panel at V_mppt / n_series."""
         return np.full(self.n_panels, self.v_mppt / self.n_series)
@@ -117,8 +130,11 @@ class Plant:
                   -self.inc_sign * ieq[self.inc_panel])
         return gpan, ieq, a, b
 
-    def companion_batch(self, g_irr: np.ndarray, v_panel: np.ndarray, ld: int | None = None):
+    def companion_batch(self, g_irr: np.ndarray, v_panel: np.ndarray, ld: int | None = None,
+                        gmin: float = 0.0):
         """`companion` for S scenarios at once: g_irr, v_panel [n_panels, S].
+        gmin > 0 adds the convergence conductance of a Newton stage to every
+        panel's stamp (002b_sistema_electrico_base_matriz.cpp:198-202).
 
         Returns A values [nnz_a, ld] and b [n, ld] (columns past S zero)."""
         npan, S = g_irr.shape
@@ -130,7 +146,8 @@ class Plant:
         entry = np.repeat(np.arange(len(self.a_lin)), counts)
         a = np.zeros((len(self.a_lin), ld))
         a[:, :S] = self.a_lin[:, None]
-        np.add.at(a[:, :S], entry, self.contrib_sign[:, None] * gpan[self.contrib_panel])
+        gst = gpan + gmin if gmin > 0 else gpan
+        np.add.at(a[:, :S], entry, self.contrib_sign[:, None] * gst[self.contrib_panel])
         b = np.zeros((self.n, ld))
         b[:, :S] = self.b_lin[:, None]
         node = np.repeat(np.arange(self.n), np.diff(self.inc_ptr))

@@ -248,6 +248,63 @@ def test_fp32_refinement_35k(cuda, schedule):
         assert err <= 1e-10, (k, err, sw[k])
 
 
+@pytest.mark.parametrize("schedule", SCHEDULES)
+@pytest.mark.parametrize("dims,preset", [((120, 24, 28), "c3"), ((200, 24, 28), "c4")])
+def test_large_plants_fp64_vs_oracle(cuda, dims, preset, schedule):
+    """The 84k-unknown plant of the three-size batch (120 x 24 x 28) and the
+    135k-unknown plant of the precision configuration (200 x 24 x 28), FP64,
+    single instance and a batch of 3, against the oracle scenario by
+    scenario: factors 1e-12 componentwise, solutions 1e-12 normwise."""
+    p = Plant(*dims)
+    s = Symbolic(p.rowptr, p.colidx)
+    o = O.Port(p.rowptr, p.colidx, s.array("perm_amd"))
+    S = 3
+    a, b = M.plant_batch(p, S, seed0=4100 + dims[0], preset=preset)
+    refs = [o.scatter_refactor_solve(a[:, k], b[:, k]) for k in range(S)]
+    for count in (1, S):
+        num = Numeric(s, count, FP64, schedule)
+        num.scatter(dev(pad_cols(a[:, :count], num.ld)))
+        num.refactor()
+        assert num.check()[0] == 0
+        x = dev(pad_cols(b[:, :count], num.ld))
+        num.solve(x, original=True)
+        x = x.cpu().numpy().reshape(s.n, num.ld)
+        lu = values_of(num, int(s.nnz_lu))
+        for k in range(count):
+            assert rel_err(lu[:, k], refs[k][0]) <= TOL64, (count, k)
+            assert norm_err(x[:, k], refs[k][1]) <= TOL64, (count, k)
+
+
+@pytest.mark.parametrize("schedule", [SCHED_LEVELS, SCHED_PERSISTENT])
+@pytest.mark.parametrize("dims,preset", [((120, 24, 28), "c3"), ((200, 24, 28), "c4")])
+def test_large_plants_fp32_refinement_vs_oracle(cuda, dims, preset, schedule):
+    """FP32 factors + FP64 refinement on the 84k and 135k plants: every
+    scenario within 1e-10 of the oracle's FP64 solution (normwise)."""
+    import torch
+
+    p = Plant(*dims)
+    s = Symbolic(p.rowptr, p.colidx)
+    o = O.Port(p.rowptr, p.colidx, s.array("perm_amd"))
+    S = 4
+    a, b = M.plant_batch(p, S, seed0=4300 + dims[0], preset=preset)
+    num = Numeric(s, S, FP32, schedule)
+    a_dev = dev(pad_cols(a, num.ld))
+    b_dev = dev(pad_cols(b, num.ld))
+    num.scatter(a_dev)
+    num.refactor()
+    assert num.check()[0] == 0
+    x = torch.zeros_like(b_dev)
+    sweeps = torch.zeros(num.ld, dtype=torch.int32, device="cuda")
+    num.solve_refined(a_dev, b_dev, x, tol=1e-12, max_sweeps=10, sweeps=sweeps)
+    torch.cuda.synchronize()
+    x = x.cpu().numpy()
+    sw = sweeps.cpu().numpy()[:S]
+    assert (sw > 0).all(), sw
+    for k in range(S):
+        _, x_ref = o.scatter_refactor_solve(a[:, k], b[:, k])
+        assert norm_err(x[:, k], x_ref) <= 1e-10, (k, sw[k])
+
+
 @pytest.mark.parametrize("S,precision", [(1, FP64), (96, FP32), (64, FP64)])
 def test_autotune_picks_a_working_configuration(cuda, S, precision):
     from phdthesis_albertojimenezruiz_gb300.glu import autotune

@@ -129,3 +129,26 @@ def test_out_of_range_content_with_valid_checksum_is_refused(tmp_path):
                 Symbolic.load(f)
             checked += 1
     assert checked >= 20
+
+
+def test_counts_beyond_int_with_valid_checksum_are_refused(tmp_path):
+    """The dump stores n, the row-swap count and the involution flag as
+    int64; values that an int cannot hold (n = 2^32 + n would truncate to n
+    and pass every array check) are refused, not narrowed."""
+    import struct
+
+    p = Plant(1, 2, 5)
+    s = Symbolic(p.rowptr, p.colidx)
+    path = tmp_path / "s.pvs"
+    s.save(path)
+    raw = path.read_bytes()
+    head = 8 + 4 + 4  # magic, version, byte order; then n, nnz_a, nnz_lu, row_swaps, invol
+    (n,) = struct.unpack_from("<q", raw, head)
+    for slot, value in ((0, (1 << 32) + n), (0, -1), (3, (1 << 32)), (4, 2), (4, -1)):
+        bad = bytearray(raw)
+        struct.pack_into("<q", bad, head + 8 * slot, value)
+        struct.pack_into("<Q", bad, len(bad) - 8, _fnv1a(bytes(bad[:-8])))
+        f = tmp_path / f"count{slot}_{value}.pvs"
+        f.write_bytes(bytes(bad))
+        with pytest.raises(PvgluError):
+            Symbolic.load(f)

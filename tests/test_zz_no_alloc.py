@@ -1,8 +1,12 @@
 """pvglu_solve_noalloc: the solve whose work vector lives in the library's
 static device array, for callers whose solve path must not allocate device
-memory.  Checked through the C ABI against the ordinary pvglu_solve on two
-calls in a row (the array keeps the previous call's contents), and for its
-size limit.  Kept in a file of its own that pytest collects last.
+memory (an application that reserves the GPU's memory up front, or a loop
+that cannot take an allocation's implicit synchronisation).  Checked through
+the C ABI against the ordinary pvglu_solve on two calls in a row (the array
+keeps the previous call's contents) and against the CPU oracle, in every
+schedule, single and batched (the batched chain programs move the static
+array's rows with bulk copies), and for its size limit.  Kept in a file of
+its own that pytest collects last.
 """
 from __future__ import annotations
 
@@ -12,7 +16,9 @@ import numpy as np
 import pytest
 from conftest import norm_err
 
-from phdthesis_albertojimenezruiz_gb300 import FP64, SCHED_LEVELS, SCHED_PERSISTENT, Numeric, Plant, Symbolic
+from oracle import oracle as O
+from phdthesis_albertojimenezruiz_gb300 import (FP64, SCHED_LEVELS, SCHED_PERSISTENT,
+                                                SCHED_THREAD_CHAIN, Numeric, Plant, Symbolic)
 from phdthesis_albertojimenezruiz_gb300 import _native as N
 
 pytestmark = pytest.mark.gpu
@@ -24,8 +30,8 @@ def _noalloc(num: Numeric, x, flags: int) -> int:
                                        C.c_void_p(0))
 
 
-@pytest.mark.parametrize("schedule", [SCHED_LEVELS, SCHED_PERSISTENT])
-@pytest.mark.parametrize("S", [1, 8])
+@pytest.mark.parametrize("schedule", [SCHED_LEVELS, SCHED_PERSISTENT, SCHED_THREAD_CHAIN])
+@pytest.mark.parametrize("S", [1, 8, 64])
 def test_noalloc_matches_solve_twice(cuda, schedule, S):
     import torch
 
@@ -33,6 +39,7 @@ def test_noalloc_matches_solve_twice(cuda, schedule, S):
 
     p = Plant(10, 16, 20)
     s = Symbolic(p.rowptr, p.colidx)
+    o = O.Port(p.rowptr, p.colidx, s.array("perm_amd"))
     num = Numeric(s, S, FP64, schedule)
     a, _ = M.plant_batch(p, S, seed0=41)
     a_pad = np.zeros((a.shape[0], num.ld))
@@ -52,6 +59,10 @@ def test_noalloc_matches_solve_twice(cuda, schedule, S):
         w, g = want.cpu().numpy()[:, :S], got.cpu().numpy()[:, :S]
         for k in range(S):
             assert norm_err(g[:, k], w[:, k]) <= TOL64, (call, k)
+        if not flags & N.SOLVE_TRANSPOSE:
+            for k in sorted({0, S // 2, S - 1}):
+                _, x_ref = o.scatter_refactor_solve(a[:, k], b[:, k])
+                assert norm_err(g[:, k], x_ref) <= TOL64, (call, k)
 
 
 def test_noalloc_rejects_oversized_handle(cuda):
