@@ -630,6 +630,131 @@ def newton_iterates_section(stream, S: int, steps: int) -> dict:
                         "refinement tolerance 1e-12, up to 40 sweeps", "stages": out}
 
 
+def wide_section(stream, steps: int, S: int = 512) -> dict:
+    """Patterns whose factors have columns and rows too wide for a chain-
+    program table (run as WIDE program levels, a block per unit): the
+    reference's own plant topology with the reference's AMD ordering (7
+    blocks x 50 strings x 50 panels, 34,717 unknowns, bus columns and rows of
+    2,455 entries, 100 U levels), and two fill-heavy test patterns.  Per
+    pattern: the single-instance FP64 path in each schedule, the batched FP64
+    path (S scenarios, HBM fraction of scatter + refactor + solve), the
+    batched FP32 + refinement path, and the reference's CPU path (the
+    oracle's sequential GLU + substitution, one core) on the same matrix."""
+    import torch
+
+    sys.path.insert(0, str(ROOT / "tests"))
+    import matrices as M
+    from oracle import oracle as O
+    from phdthesis_albertojimenezruiz_gb300 import (FP32, FP64, SCHED_LEVELS, SCHED_PERSISTENT,
+                                                    SCHED_THREAD_CHAIN, Numeric, Symbolic)
+    from phdthesis_albertojimenezruiz_gb300.glu import autotune
+    from phdthesis_albertojimenezruiz_gb300.plant import block_plant
+
+    dev = torch.device("cuda", torch.cuda.current_device())
+    peak = _peaks().get("hbm_gbs")
+    with np.load(ROOT / "tests" / "golden" / "orderings" / "block_plant_amd.npz") as z:
+        perm7 = z["perm_7x50x50"]
+    cases = []
+    cols = [block_plant(7, 50, 50, seed=300 + k) for k in range(8)]
+    cases.append(("reference_topology_7x50x50 (reference AMD ordering)", cols[0][0], cols[0][1],
+                  perm7, np.stack([c[2] for c in cols], 1), np.stack([c[3] for c in cols], 1)))
+    for name in ("mesh_30x30", "random_1500"):
+        rp, ci, a, b = M.CASES[name]()
+        cases.append((name, rp, ci, None, a[:, None], b[:, None]))
+    out = []
+    for name, rp, ci, perm, a_few, b_few in cases:
+        sym = Symbolic(rp, ci, perm)
+        n, nnz_a, nnz_lu = sym.n, int(sym.nnz_a), int(sym.nnz_lu)
+        res = {"pattern": name, "n": n, "nnz_a": nnz_a, "nnz_lu": nnz_lu,
+               "lu_levels": sym.info["lu_levels"], "u_levels": sym.info["u_levels"]}
+        # Single instance, FP64, every schedule.
+        a1 = torch.from_numpy(np.ascontiguousarray(a_few[:, 0])).to(dev)
+        b1 = torch.from_numpy(np.ascontiguousarray(b_few[:, 0])).to(dev)
+        x1 = b1.clone()
+        single = {}
+        for sname, sched in (("thread_chain_levels", SCHED_THREAD_CHAIN),
+                             ("programs_levels", SCHED_LEVELS),
+                             ("programs_persistent", SCHED_PERSISTENT)):
+            one = Numeric(sym, 1, FP64, sched)
+
+            def plain_step():
+                one.scatter(a1, stream=stream)
+                x1.copy_(b1)
+                one.refactor_solve(x1, original=True, stream=stream)
+
+            for _ in range(3):
+                plain_step()
+            single[sname] = 1000.0 / _time_ms(plain_step, stream, max(10, steps))
+            if sched == SCHED_LEVELS:
+                res["single_program_info"] = one.info
+            del one
+        res["single_fp64_per_s"] = single
+        # Batched: S scenarios (the distinct Jacobians tiled).
+        ld = ((S + 63) // 64) * 64
+        reps = -(-S // a_few.shape[1])
+        a = np.zeros((nnz_a, ld))
+        b = np.zeros((n, ld))
+        a[:, :S] = np.tile(a_few, (1, reps))[:, :S]
+        b[:, :S] = np.tile(b_few, (1, reps))[:, :S]
+        a_d = torch.from_numpy(a).to(dev)
+        b_d = torch.from_numpy(b).to(dev)
+        ml64, sc64, _ = autotune(sym, S, FP64)
+        n64 = Numeric(sym, S, FP64, sc64, max_locals=ml64)
+        x64 = torch.empty_like(b_d)
+
+        def step64():
+            n64.scatter(a_d, stream=stream)
+            x64.copy_(b_d)
+            n64.refactor_solve(x64, original=True, stream=stream)
+
+        for _ in range(3):
+            step64()
+        ms64 = _time_ms(step64, stream, steps)
+        bm = bytes_model(nnz_a, nnz_lu, n, 8)
+        byt = (bm["scatter"] + bm["refactor"] + bm["solve"]) * S
+        res["batched_fp64"] = {
+            "value": S / (ms64 / 1000.0), "unit": UNIT, "ms_per_step": ms64,
+            "tuning": {"max_locals": ml64, "schedule": sc64}, "program_info": n64.info,
+            "hbm": {"bytes_per_step": byt, "achieved_gbs": byt / (ms64 / 1000.0) / 1e9,
+                    "frac": byt / (ms64 / 1000.0) / 1e9 / peak if peak else None}}
+        ml32, sc32, _ = autotune(sym, S, FP32)
+        n32 = Numeric(sym, S, FP32, sc32, max_locals=ml32)
+        x32 = torch.zeros_like(b_d)
+        sweeps = torch.zeros(ld, dtype=torch.int32, device=dev)
+
+        def step32():
+            n32.scatter(a_d, stream=stream)
+            n32.refactor(stream=stream)
+            n32.solve_refined(a_d, b_d, x32, tol=IR_TOL, max_sweeps=30, sweeps=sweeps,
+                              stream=stream)
+
+        for _ in range(3):
+            step32()
+        ms32 = _time_ms(step32, stream, steps)
+        sw = sweeps.cpu().numpy()[:S]
+        xa, xb = x32.cpu().numpy()[:, :S], x64.cpu().numpy()[:, :S]
+        res["batched_fp32ir"] = {
+            "value": S / (ms32 / 1000.0), "unit": UNIT, "ms_per_step": ms32,
+            "tuning": {"max_locals": ml32, "schedule": sc32},
+            "sweeps_max": int(sw.max()), "not_converged": int((sw <= 0).sum()),
+            "max_rel_err_vs_fp64": float(np.max(np.abs(xa - xb).max(axis=0) /
+                                                np.abs(xb).max(axis=0)))}
+        # The oracle (the reference's sequential arithmetic) on scenario 0,
+        # timed on one core, and checked against the batched FP64 factors.
+        port = O.Port(rp, ci, sym.array("perm_amd"))
+        t0 = time.perf_counter()
+        cnt = 0
+        while cnt < 3 or time.perf_counter() - t0 < 1.0:
+            lu_ref, x_ref = port.scatter_refactor_solve(a[:, 0], b[:, 0])
+            cnt += 1
+        res["cpu_oracle_1core_per_s"] = cnt / (time.perf_counter() - t0)
+        res["batched_fp64_bit_identical_to_oracle"] = bool(np.array_equal(xb[:, 0], x_ref))
+        out.append(res)
+        del n64, n32, a_d, b_d, x64, x32
+    return {"workload": f"WIDE program levels: single instance and {S} scenarios per step, "
+                        "scatter + refactor + solve", "patterns": out}
+
+
 def _newton_handle(p, sym, S: int, precision, tol_ir: float = 1e-12):
     from phdthesis_albertojimenezruiz_gb300 import FP32, Newton, Numeric
     from phdthesis_albertojimenezruiz_gb300.glu import autotune
@@ -894,6 +1019,8 @@ def run_configs(args, stream) -> dict:
     if "i" in wanted:
         out["fp32ir_on_newton_iterates"] = newton_iterates_section(stream, args.scenarios,
                                                                    max(5, args.steps))
+    if "w" in wanted:
+        out["wide_units"] = wide_section(stream, max(5, args.steps), args.scenarios)
     return out
 
 
@@ -957,12 +1084,13 @@ def main() -> None:
                     help="chain-program table size of the batched handle (0: autotune)")
     ap.add_argument("--schedule", default="persistent", choices=["levels", "persistent"],
                     help="schedule used with --max-locals (autotuned otherwise)")
-    ap.add_argument("--configs", default="1,2,3,4,5,i",
+    ap.add_argument("--configs", default="1,2,3,4,5,i,w",
                     help="extra workloads reported beside the headline (1: 4x8x20 Newton vs the "
                          "oracle, 2: 300 time steps, 3: three plant sizes per level launch, "
                          "4: the 135k plant, 5: per-panel adjoint vs central differences, "
-                         "i: FP32 + refinement vs FP64 on Newton-iterate Jacobians; "
-                         "empty: none)")
+                         "i: FP32 + refinement vs FP64 on Newton-iterate Jacobians, "
+                         "w: wide units on the reference's plant topology and fill-heavy "
+                         "patterns; empty: none)")
     ap.add_argument("--only-configs", action="store_true",
                     help="run the --configs workloads alone (profiling runs)")
     ap.add_argument("--newton-max-locals", type=int, default=0,

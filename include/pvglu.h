@@ -136,6 +136,17 @@ int pvglu_numeric_create(const pvglu_symbolic* s, int n_scenarios, int precision
 int pvglu_numeric_create_ex(const pvglu_symbolic* s, int n_scenarios, int precision,
                             int max_locals, pvglu_numeric** out);
 int pvglu_numeric_max_locals(const pvglu_numeric* h);
+/* How the handle executes its refactorization and solves: program levels
+ * over all five phases (refactor, L, U, U^T, L^T), how many of them are WIDE
+ * levels and how many wide units they hold (columns or rows too wide for
+ * the table, run by a whole block each), the widest table, and the
+ * operations and loads of the chain programs.  No counterpart in the
+ * reference. */
+typedef struct {
+  int program_levels, wide_levels, wide_units, table_max;
+  int64_t ops, loads;
+} pvglu_numeric_info;
+int pvglu_numeric_get_info(const pvglu_numeric* h, pvglu_numeric_info* info);
 int pvglu_numeric_destroy(pvglu_numeric* h);
 int pvglu_numeric_ld(const pvglu_numeric* h);
 /* Device pointer to the LU values (double* for FP64, float* for FP32). */

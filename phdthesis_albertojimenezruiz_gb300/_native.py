@@ -38,6 +38,13 @@ class SymbolicInfo(C.Structure):
     ]
 
 
+class NumericInfo(C.Structure):
+    _fields_ = [
+        ("program_levels", C.c_int), ("wide_levels", C.c_int), ("wide_units", C.c_int),
+        ("table_max", C.c_int), ("ops", C.c_int64), ("loads", C.c_int64),
+    ]
+
+
 class PlantInfo(C.Structure):
     _fields_ = [
         ("n", C.c_int), ("n_panels", C.c_int), ("nnz_a", C.c_int64),
@@ -73,6 +80,7 @@ _SIGS = {
     "pvglu_numeric_create": ([_P, _I, _I, C.POINTER(_P)], _I),
     "pvglu_numeric_create_ex": ([_P, _I, _I, _I, C.POINTER(_P)], _I),
     "pvglu_numeric_max_locals": ([_P], _I),
+    "pvglu_numeric_get_info": ([_P, _P], _I),
     "pvglu_numeric_destroy": ([_P], _I),
     "pvglu_numeric_ld": ([_P], _I),
     "pvglu_numeric_values": ([_P], _P),

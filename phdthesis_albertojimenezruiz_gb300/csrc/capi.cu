@@ -68,11 +68,26 @@ int prog_prepare(pvglu_numeric* h) {
                        (const void*)pvglu::k_prog_level<T, 0, B>,
                        (const void*)pvglu::k_prog_level<T, 1, B>,
                        (const void*)pvglu::k_prog_level<T, 2, B>,
-                       (const void*)pvglu::k_prog_level<T, 3, B>};
+                       (const void*)pvglu::k_prog_level<T, 3, B>,
+                       (const void*)pvglu::k_wide_level<T, -1, B>,
+                       (const void*)pvglu::k_wide_level<T, 0, B>,
+                       (const void*)pvglu::k_wide_level<T, 1, B>,
+                       (const void*)pvglu::k_wide_level<T, 2, B>,
+                       (const void*)pvglu::k_wide_level<T, 3, B>};
   for (const void* f : fns)
     if (pvglu::allow_max_dynamic_smem(f) != cudaSuccess) return 1;
   h->prog_grid = pvglu::prog_persistent_grid<T, B>(h->table_max);
   return 0;
+}
+
+// Shared memory of a WIDE level launch: the ordered-sum scratch, and in
+// single mode the level's widest column staged beside it when it fits.
+template <typename T, bool B>
+size_t wide_smem(const pvglu_numeric* h, int ph, int lv) {
+  const size_t scratch = pvglu::wide_scratch_bytes<T, B>(pvglu::kProgBlock);
+  if (B || ph != 0) return scratch;
+  const size_t want = scratch + (size_t)h->prog_level_wide_len[ph][lv] * sizeof(T);
+  return std::min(want, h->smem_optin);
 }
 
 // One phase of chain programs with one launch per level.
@@ -84,6 +99,14 @@ void prog_levels(pvglu_numeric* h, T* x, const int* done, const int* ndone, cuda
   for (size_t lv = 0; lv + 1 < lc.size(); lv++) {
     const int cb = lc[lv], ce = lc[lv + 1];
     const int64_t items = (int64_t)(ce - cb) * groups;
+    if (h->prog_level_wide_len[ph][lv] > 0) {  // a WIDE level: a block per unit and group
+      const size_t smem = wide_smem<T, B>(h, ph, (int)lv);
+      pvglu::k_wide_level<T, KIND, B>
+          <<<launch_blocks(items, 1), pvglu::kProgBlock, smem, st>>>(
+              h->progs.p[ph], h->d, cb, ce, static_cast<T*>(h->values), x, h->ld, h->S,
+              h->pivot_tol, h->status, done, ndone, (int)smem);
+      continue;
+    }
     const int table = h->prog_level_ml[ph][lv];
     const size_t smem = pvglu::prog_smem_bytes<T, B>(table, pvglu::kProgWarps);
     pvglu::k_prog_level<T, KIND, B>
@@ -736,14 +759,56 @@ int pvglu_numeric_create_ex(const pvglu_symbolic* sym, int n_scenarios, int prec
     rc |= h->put(prog.loads, &P.loads);
     rc |= h->put(ops, &P.ops);
     rc |= h->put(prog.op_col, &P.op_col);
+    std::vector<int> lwide(prog.level_wide.begin(), prog.level_wide.end());
+    rc |= h->put(lwide, &P.level_wide);
+    rc |= h->put(prog.wide.unit, &P.w_unit);
+    rc |= h->put(prog.wide.lvl, &P.w_lvl);
+    rc |= h->put(prog.wide.lv_tgt, &P.lv_tgt);
+    rc |= h->put(prog.wide.tg_slot, &P.tg_slot);
+    rc |= h->put(prog.wide.tg_pair, &P.tg_pair);
+    rc |= h->put(prog.wide.pr_q, &P.pr_q);
+    rc |= h->put(prog.wide.pr_p, &P.pr_p);
     P.n_levels = (int)prog.level_chain.size() - 1;
     h->prog_level_chain[ph] = prog.level_chain;
-    for (int lv = 0; lv < P.n_levels; lv++)
+    // Per program level: 0, or for a WIDE level its widest unit (column
+    // length for the refactorization, entries for a solve row), for the
+    // shared memory of its launch.
+    h->prog_level_wide_len[ph].assign(P.n_levels, 0);
+    for (int lv = 0; lv < P.n_levels; lv++) {
       h->prog_max_chains = std::max(h->prog_max_chains,
                                     prog.level_chain[lv + 1] - prog.level_chain[lv]);
+      if (!prog.level_wide[lv]) continue;
+      int widest = 1;
+      for (int c = prog.level_chain[lv]; c < prog.level_chain[lv + 1]; c++) {
+        const int u = prog.units[prog.chain_unit[c]];
+        widest = std::max(widest, s.csc_colptr[u + 1] - s.csc_colptr[u]);
+      }
+      h->prog_level_wide_len[ph][lv] = widest;
+    }
     h->prog_ops += (int64_t)prog.ops.size();
     h->prog_loads += (int64_t)prog.loads.size();
-    h->prog_direct += prog.direct_segments;
+    h->prog_wide_units += prog.wide_units;
+    h->prog_wide_levels += prog.wide_levels;
+  }
+  // Wide levels of the persistent kernel use the warps' tables as scratch:
+  // at least the ordered-sum buffer (wide.cuh) must fit.
+  {
+    const size_t need = precision == PVGLU_FP64
+                            ? (h->batch ? pvglu::wide_scratch_bytes<double, true>(pvglu::kProgBlock)
+                                        : pvglu::wide_scratch_bytes<double, false>(pvglu::kProgBlock))
+                            : (h->batch ? pvglu::wide_scratch_bytes<float, true>(pvglu::kProgBlock)
+                                        : pvglu::wide_scratch_bytes<float, false>(pvglu::kProgBlock));
+    const size_t per_row = (size_t)pvglu::kProgWarps * group * elem;
+    h->table_max = std::max<int>(h->table_max, (int)((need + per_row - 1) / per_row));
+  }
+  {
+    int dev = 0, optin = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) ==
+            cudaSuccess)
+      h->smem_optin = (size_t)optin - 1024;
+    else
+      cudaGetLastError();
   }
   if (rc) {
     delete h;
@@ -764,6 +829,19 @@ int pvglu_numeric_create_ex(const pvglu_symbolic* sym, int n_scenarios, int prec
 
 int pvglu_numeric_destroy(pvglu_numeric* h) {
   delete h;
+  return PVGLU_OK;
+}
+
+int pvglu_numeric_get_info(const pvglu_numeric* h, pvglu_numeric_info* info) {
+  if (!h || !info) return fail(PVGLU_ERR_BAD_ARG, "NULL argument");
+  info->program_levels = 0;
+  for (int ph = 0; ph < 5; ph++)
+    info->program_levels += std::max(0, (int)h->prog_level_chain[ph].size() - 1);
+  info->wide_levels = (int)h->prog_wide_levels;
+  info->wide_units = (int)h->prog_wide_units;
+  info->table_max = h->table_max;
+  info->ops = h->prog_ops;
+  info->loads = h->prog_loads;
   return PVGLU_OK;
 }
 
@@ -1140,17 +1218,32 @@ int group_phase(pvglu_group* g, T* const* xs, cudaStream_t st) {
   std::vector<int> tables;
   for (int lv = 0; lv < nlev; lv++) {
     tables.clear();
-    for (auto* h : g->m)
-      if (lv + 1 < (int)h->prog_level_chain[ph].size() &&
-          std::find(tables.begin(), tables.end(), h->prog_level_ml[ph][lv]) == tables.end())
+    for (size_t i = 0; i < g->m.size(); i++) {
+      pvglu_numeric* h = g->m[i];
+      if (lv + 1 >= (int)h->prog_level_chain[ph].size()) continue;
+      if (h->prog_level_wide_len[ph][lv] > 0) {
+        // A member's WIDE level: its own launch, a block per unit and group.
+        const auto& lc = h->prog_level_chain[ph];
+        const int64_t items = (int64_t)(lc[lv + 1] - lc[lv]) * (B ? h->ld / pvglu::kGroup : 1);
+        const size_t smem = wide_smem<T, B>(h, ph, lv);
+        pvglu::k_wide_level<T, KIND, B><<<launch_blocks(items, 1), pvglu::kProgBlock, smem, st>>>(
+            h->progs.p[ph], h->d, lc[lv], lc[lv + 1], static_cast<T*>(h->values),
+            xs ? xs[i] : nullptr, h->ld, h->S, (T)h->pivot_tol, h->status, nullptr, nullptr,
+            (int)smem);
+        continue;
+      }
+      if (std::find(tables.begin(), tables.end(), h->prog_level_ml[ph][lv]) == tables.end())
         tables.push_back(h->prog_level_ml[ph][lv]);
+    }
     for (const int tb : tables) {
     pvglu::MultiLaunch<T> M{};
     int table = 0, items = 0;
     for (size_t i = 0; i < g->m.size(); i++) {
       pvglu_numeric* h = g->m[i];
       const auto& lc = h->prog_level_chain[ph];
-      if (lv + 1 >= (int)lc.size() || h->prog_level_ml[ph][lv] != tb) continue;
+      if (lv + 1 >= (int)lc.size() || h->prog_level_ml[ph][lv] != tb ||
+          h->prog_level_wide_len[ph][lv] > 0)
+        continue;
       auto& C = M.c[M.n++];
       C.P = h->progs.p[ph];
       C.d = h->d;

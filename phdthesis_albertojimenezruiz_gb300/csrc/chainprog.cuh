@@ -13,6 +13,9 @@
 // Single mode (BATCH = false): a warp runs one chain of the one scenario; the
 // lanes split the loads and stores of each segment (ld.global.cg), lane 0
 // executes the operations out of shared memory.
+//
+// Units too wide for a table are not chain-program segments: they form WIDE
+// program levels of their own, executed by whole blocks (wide.cuh).
 #pragma once
 #include <type_traits>
 #include <cuda_runtime.h>
@@ -24,15 +27,24 @@ namespace pvglu {
 
 struct ProgDev {
   const int* level_chain;  // [levels + 1]
+  const int* level_wide;   // [levels] 1: a WIDE level (wide.cuh)
   int n_levels;
   const int* chain_seg;    // [chains + 1]
   const int4* seg;         // {load_begin, n_load | n_own << 16 | n_carry << 26 |
-                           //  reads_own_chain << 30 (or -1: DIRECT), op_begin, n_op}
+                           //  reads_own_chain << 30 (or -1: WIDE), op_begin, n_op}
   const int4* carry;       // [segments] up to 4 moves (from << 16 | to) of table rows
   const int* loads;
   const int4* ops;         // packed operations, 4 per int4
   const int* op_col;       // column of each SCALE operation
   int max_locals;
+  // Wide units (programs.hpp, WidePlan).
+  const int* w_unit;
+  const int* w_lvl;
+  const int* lv_tgt;
+  const int* tg_slot;
+  const int* tg_pair;
+  const int* pr_q;
+  const int* pr_p;
 };
 
 constexpr int kGroup = 64;                       // scenarios per warp item
@@ -238,27 +250,6 @@ __device__ __forceinline__ void prog_run_chain(const ProgDev& P, const DevStruct
   const int g_end = __ldg(P.chain_seg + chain + 1);
   for (int g = __ldg(P.chain_seg + chain); g < g_end; g++) {
     const int4 sg = __ldg(P.seg + g);
-    if (sg.y < 0) {  // DIRECT unit: straight from global memory (generic proxy)
-      if (BATCH) {
-        bulk_wait_all();
-        fence_proxy_async();
-        __syncwarp();
-        for (int k = 0; k < 2; k++) {
-          const int s = s0 + 2 * lane + k;
-          if (KIND < 0) refactor_column<T>(d, sg.z, s, ld, v, pivot_tol, st);
-          else solve_unknown<T, (KIND < 0 ? 0 : KIND)>(d, sg.z, s, ld, v, x);
-        }
-        fence_proxy_async();
-        __syncwarp();
-      } else {
-        if (lane == 0) {
-          if (KIND < 0) refactor_column<T>(d, sg.z, 0, 1, v, pivot_tol, st);
-          else solve_unknown<T, (KIND < 0 ? 0 : KIND)>(d, sg.z, 0, 1, v, x);
-        }
-        __syncwarp();
-      }
-      continue;
-    }
     const int* lr = P.loads + sg.x;
     const int nl = sg.y & 0xffff, n_own = (sg.y >> 16) & 0x3ff, n_carry = (sg.y >> 26) & 7;
     // Rows the previous segment of this chain left in the table: moved, not
@@ -445,7 +436,7 @@ __device__ __forceinline__ T* prog_setup_warp(unsigned char* smem_raw, int max_l
 }
 
 template <typename T, bool BATCH>
-size_t prog_smem_bytes(int max_locals, int warps_per_block) {
+__host__ __device__ size_t prog_smem_bytes(int max_locals, int warps_per_block) {
   return (size_t)warps_per_block * max_locals * (BATCH ? kGroup : 1) * sizeof(T) +
          (size_t)warps_per_block * sizeof(unsigned long long);
 }

@@ -99,9 +99,12 @@ struct pvglu_numeric {
   std::vector<int> prog_level_ml[5];  // table budget per phase and level
   pvglu::ProgSetDev progs{};
   std::vector<int> prog_level_chain[5];
+  std::vector<int> prog_level_wide_len[5];  // per program level: 0, or (WIDE level) its
+                                            // widest unit, for the launch's shared memory
   int prog_max_chains = 1;
   int prog_grid = 0;               // co-resident blocks of k_prog_persistent
-  int64_t prog_ops = 0, prog_loads = 0, prog_direct = 0;
+  size_t smem_optin = 48 * 1024;   // shared memory a block may opt in to
+  int64_t prog_ops = 0, prog_loads = 0, prog_wide_units = 0, prog_wide_levels = 0;
   unsigned int* barrier = nullptr;  // [2]: count, generation
   // A^T by rows (caller order): entries at_ptr[j]..at_ptr[j+1] of column j
   // of A, in row order, with their row and A-entry index.

@@ -17,6 +17,7 @@
 #include "chainprog.cuh"
 #include "kernels.cuh"
 #include "symbolic.hpp"
+#include "wide.cuh"
 
 namespace pvglu {
 
@@ -86,7 +87,8 @@ template <typename T, int KIND, bool BATCH>
 __device__ __forceinline__ bool prog_phase(const ProgDev& P, const DevStruct& d, T* v, T* x,
                                            int ld, int S, T* sm, WarpTma& tma,
                                            T pivot_tol, DevStatus* st, unsigned int* bar,
-                                           const int* done, bool* need_sync) {
+                                           const int* done, bool* need_sync,
+                                           unsigned char* smem_raw, int smem_bytes) {
   const int warp_id = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int n_warps = (gridDim.x * blockDim.x) >> 5;
   for (int lv = 0; lv < P.n_levels; lv++) {
@@ -97,6 +99,13 @@ __device__ __forceinline__ bool prog_phase(const ProgDev& P, const DevStruct& d,
       if (BATCH) fence_proxy_async();
     }
     *need_sync = true;
+    if (__ldg(P.level_wide + lv)) {
+      // Whole blocks on the wide units; the warps' tables are their scratch.
+      wide_run_level<T, KIND, BATCH>(P, d, P.level_chain[lv], P.level_chain[lv + 1], v, x, ld,
+                                     S, pivot_tol, st, done, smem_raw, smem_bytes, blockIdx.x,
+                                     gridDim.x);
+      continue;
+    }
     prog_run_level<T, KIND, BATCH>(P, d, P.level_chain[lv], P.level_chain[lv + 1], v, x, ld,
                                    S, sm, tma, pivot_tol, st, done, warp_id, n_warps);
     // A warp whose table wait ran out raises the abort word: every block
@@ -115,25 +124,28 @@ k_prog_persistent(ProgSetDev PS, DevStruct d, T* __restrict__ v, T* __restrict__
   extern __shared__ __align__(128) unsigned char smem_raw[];
   WarpTma tma;
   T* sm = prog_setup_warp<T, BATCH>(smem_raw, PS.p[0].max_locals, tma);
+  // The tables (not the mbarriers behind them) are scratch for wide levels.
+  const int tables = (int)(prog_smem_bytes<T, BATCH>(PS.p[0].max_locals, kProgWarps) -
+                           kProgWarps * sizeof(unsigned long long));
   bool need_sync = false;
   if (phases & PHASE_REFACTOR)
     if (!prog_phase<T, -1, BATCH>(PS.p[0], d, v, x, ld, S, sm, tma, pivot_tol, st, bar,
-                                  nullptr, &need_sync))
+                                  nullptr, &need_sync, smem_raw, tables))
       return;
   if (phases & PHASE_SOLVE) {
     if (!prog_phase<T, 0, BATCH>(PS.p[1], d, v, x, ld, S, sm, tma, pivot_tol, st, bar,
-                                 skip.done, &need_sync))
+                                 skip.done, &need_sync, smem_raw, tables))
       return;
     if (!prog_phase<T, 1, BATCH>(PS.p[2], d, v, x, ld, S, sm, tma, pivot_tol, st, bar,
-                                 skip.done, &need_sync))
+                                 skip.done, &need_sync, smem_raw, tables))
       return;
   }
   if (phases & PHASE_SOLVE_T) {
     if (!prog_phase<T, 2, BATCH>(PS.p[3], d, v, x, ld, S, sm, tma, pivot_tol, st, bar,
-                                 skip.done, &need_sync))
+                                 skip.done, &need_sync, smem_raw, tables))
       return;
     if (!prog_phase<T, 3, BATCH>(PS.p[4], d, v, x, ld, S, sm, tma, pivot_tol, st, bar,
-                                 skip.done, &need_sync))
+                                 skip.done, &need_sync, smem_raw, tables))
       return;
   }
 }

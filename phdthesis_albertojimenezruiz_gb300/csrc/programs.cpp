@@ -175,20 +175,98 @@ void build_chain_program(const Symbolic& s, int kind, int max_locals, ChainProgr
                       out);
 }
 
+namespace {
+
+// Column-scheduled gather plan of wide refactor unit k (WidePlan).
+void plan_wide_column(const Symbolic& s, int k, WidePlan& w) {
+  const int c0 = s.csc_colptr[k], dk = s.diag_slot[k], c1 = s.csc_colptr[k + 1];
+  const int len = c1 - c0;
+  std::vector<std::vector<std::pair<int, int>>> pairs(len);  // target -> (q, p)
+  for (int p = c0; p < dk; p++) {  // ascending j
+    const int j = s.csc_row[p];
+    const int q0 = s.diag_slot[j] + 1, q1 = s.csc_colptr[j + 1];
+    for (int q = q0; q < q1; q++) {
+      const int t = s.upd_tgt[s.upd_ptr[p] + (q - q0)];
+      pairs[t - c0].push_back({q, p});
+    }
+  }
+  // Level of each target: its U sources come first in slot order.
+  std::vector<int> lvl(len, 0);
+  int depth = 0;
+  for (int t = 0; t < len; t++) {
+    if (pairs[t].empty()) continue;
+    int m = 0;
+    for (const auto& qp : pairs[t]) m = std::max(m, lvl[qp.second - c0]);
+    lvl[t] = m + 1;
+    depth = std::max(depth, m + 1);
+  }
+  w.lvl.push_back((int)w.lv_tgt.size());
+  for (int l = 1; l <= depth; l++) {
+    w.lv_tgt.push_back((int)w.tg_slot.size());
+    for (int t = 0; t < len; t++) {
+      if (lvl[t] != l) continue;
+      w.tg_slot.push_back(c0 + t);
+      for (const auto& qp : pairs[t]) {
+        w.pr_q.push_back(qp.first);
+        w.pr_p.push_back(qp.second);
+      }
+      w.tg_pair.push_back((int)w.pr_q.size());
+    }
+  }
+}
+
+}  // namespace
+
 void build_chain_program(const Symbolic& s, int kind, const std::vector<int>& level_max_locals,
                          ChainProgram& out) {
   out = ChainProgram();
   out.kind = kind;
+  out.wide.tg_pair.push_back(0);
   const LevelSet& ls = level_set(s, kind);
-  out.level_chain = ls.start_levels;
-  out.level_max_locals.resize(ls.num_levels());
-  for (int lv = 0; lv < ls.num_levels(); lv++) {
-    out.level_max_locals[lv] = std::min(level_max_locals[lv], kMaxLocals);
-    out.max_locals = std::max(out.max_locals, out.level_max_locals[lv]);
-  }
-  int level = 0, max_locals = ls.num_levels() ? out.level_max_locals[0] : kMaxLocals;
   Table t;
   t.init(s.n, s.nnz_lu);
+
+  // 1. Program levels: each level of the level set cut around its wide units.
+  struct PLevel {
+    int src;
+    bool wide;
+    int budget;
+    std::vector<std::vector<int>> chains;
+  };
+  std::vector<PLevel> plv;
+  for (int lv = 0; lv < ls.num_levels(); lv++) {
+    const int budget = std::min(level_max_locals[lv], kMaxLocals);
+    std::vector<std::vector<std::vector<int>>> phase;  // phase -> chains -> units
+    auto put = [&](int ph, std::vector<int>&& chain) {
+      if ((int)phase.size() <= ph) phase.resize(ph + 1);
+      phase[ph].push_back(std::move(chain));
+    };
+    for (int c = ls.start_levels[lv]; c < ls.start_levels[lv + 1]; c++) {
+      int ph = 0;
+      std::vector<int> cur;
+      for (int k = ls.start_chains[c]; k < ls.start_chains[c + 1]; k++) {
+        const int u = ls.columns[k];
+        if (new_locals(s, kind, u, t) > budget) {
+          if (ph % 2 == 0) {
+            if (!cur.empty()) put(ph, std::move(cur));
+            cur.clear();
+            ph += 1;
+          } else {
+            ph += 2;  // a wide unit after a wide unit of the same chain
+          }
+          put(ph, std::vector<int>{u});
+        } else {
+          if (ph % 2 == 1) ph += 1;
+          cur.push_back(u);
+        }
+      }
+      if (!cur.empty()) put(ph, std::move(cur));
+    }
+    for (int ph = 0; ph < (int)phase.size(); ph++)
+      if (!phase[ph].empty()) plv.push_back(PLevel{lv, ph % 2 == 1, budget, std::move(phase[ph])});
+  }
+
+  // 2. Emit the program levels.
   std::vector<int> remap;
   // Entries written by the segments of the current chain so far (by ref).
   std::vector<char> written_x(s.n, 0), written_v(s.nnz_lu, 0);
@@ -197,7 +275,7 @@ void build_chain_program(const Symbolic& s, int kind, const std::vector<int>& le
     return (kind >= 0 && ref >= 0) ? written_x[ref] : written_v[kind < 0 ? ref : -ref - 1];
   };
   // Final table layout of the previous segment of the current chain
-  // (ref -> local), for carries.  Empty at a chain start and after DIRECT.
+  // (ref -> local), for carries.  Empty at a chain start.
   std::vector<std::pair<int, int>> prev_layout;
   auto close = [&]() {
     if (t.units.empty()) return;
@@ -254,59 +332,55 @@ void build_chain_program(const Symbolic& s, int kind, const std::vector<int>& le
     out.seg.push_back(g);
     t.reset();
   };
-  for (int c = 0; c < ls.num_chains(); c++) {
-    while (level + 1 < ls.num_levels() && c >= ls.start_levels[level + 1]) level++;
-    max_locals = out.level_max_locals.empty() ? kMaxLocals : out.level_max_locals[level];
-    for (int r : written_list) written(r) = 0;
-    written_list.clear();
-    prev_layout.clear();
-    out.chain_seg.push_back((int)out.seg.size());
-    const int first_seg = (int)out.seg.size();
-    for (int k = ls.start_chains[c]; k < ls.start_chains[c + 1]; k++) {
-      const int u = ls.columns[k];
-      int need = new_locals(s, kind, u, t);
-      if (t.size() + need > max_locals && !t.units.empty()) {
-        close();
-        need = new_locals(s, kind, u, t);
-      }
-      if (need > max_locals) {
-        // Too wide for the local table: executed from global memory, after
-        // the segment collected so far (chain order is execution order).
-        close();
-        out.seg.push_back(Segment{0, -1, 0, u, 0, 1});
-        prev_layout.clear();  // the DIRECT unit updates rows in global memory
-        // A DIRECT unit writes its own entries through global memory.
-        const int own_ref = kind < 0 ? -1 : u;
-        if (own_ref >= 0 && !written(own_ref)) {
-          written(own_ref) = 1;
-          written_list.push_back(own_ref);
-        }
-        if (kind < 0)
-          for (int q = s.csc_colptr[u]; q < s.csc_colptr[u + 1]; q++)
-            if (!written(q)) {
-              written(q) = 1;
-              written_list.push_back(q);
-            }
-        out.direct_segments++;
+  for (const PLevel& L : plv) {
+    out.level_chain.push_back((int)out.chain_seg.size());
+    out.level_src.push_back(L.src);
+    out.level_wide.push_back(L.wide ? 1 : 0);
+    out.level_max_locals.push_back(L.wide ? 1 : std::min(L.budget, kMaxLocals));
+    if (L.wide) out.wide_levels++;
+    for (const auto& chain : L.chains) {
+      out.chain_seg.push_back((int)out.seg.size());
+      out.chain_unit.push_back((int)out.units.size());
+      out.units.insert(out.units.end(), chain.begin(), chain.end());
+      if (L.wide) {
+        const int u = chain[0];
+        Segment g{0, -1, 0, (int)out.wide.unit.size(), 0};
+        out.seg.push_back(g);
+        out.wide.unit.push_back(u);
+        if (kind < 0) plan_wide_column(s, u, out.wide);
+        out.wide_units++;
         continue;
       }
-      emit_unit(s, kind, u, t);
+      for (int r : written_list) written(r) = 0;
+      written_list.clear();
+      prev_layout.clear();
+      const int first_seg = (int)out.seg.size();
+      for (const int u : chain) {
+        int need = new_locals(s, kind, u, t);
+        if (t.size() + need > L.budget && !t.units.empty()) close();
+        emit_unit(s, kind, u, t);
+      }
+      close();
+      out.longest_chain_segments =
+          std::max(out.longest_chain_segments, (int)out.seg.size() - first_seg);
     }
-    close();
-    out.longest_chain_segments =
-        std::max(out.longest_chain_segments, (int)out.seg.size() - first_seg);
   }
+  out.level_chain.push_back((int)out.chain_seg.size());
   out.chain_seg.push_back((int)out.seg.size());
+  out.chain_unit.push_back((int)out.units.size());
+  if (kind < 0) out.wide.lvl.push_back((int)out.wide.lv_tgt.size());
+  out.wide.lv_tgt.push_back((int)out.wide.tg_slot.size());
   // A level's table is as wide as its widest segment (the budget is only an
   // upper bound): shared memory per block, and so the blocks an SM holds,
   // follow what the level uses.  The narrow levels of a plant (one segment
   // per inverter chain) need a small part of the wide budget they are given.
   out.max_locals = 1;
-  for (int lv = 0; lv < ls.num_levels(); lv++) {
+  for (size_t lv = 0; lv + 1 < out.level_chain.size(); lv++) {
     int used = 1;
-    for (int c = ls.start_levels[lv]; c < ls.start_levels[lv + 1]; c++)
-      for (int g = out.chain_seg[c]; g < out.chain_seg[c + 1]; g++)
-        used = std::max(used, out.seg[g].n_load);
+    if (!out.level_wide[lv])
+      for (int c = out.level_chain[lv]; c < out.level_chain[lv + 1]; c++)
+        for (int g = out.chain_seg[c]; g < out.chain_seg[c + 1]; g++)
+          used = std::max(used, out.seg[g].n_load);
     out.level_max_locals[lv] = used;
     out.max_locals = std::max(out.max_locals, used);
   }

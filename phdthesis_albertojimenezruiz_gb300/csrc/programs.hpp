@@ -39,8 +39,9 @@ inline uint32_t pack_op(int code, int a, int b, int c) {
 // slot); solve programs reference solution entries (ref = i >= 0) or
 // read-only LU slots (ref = -(slot + 1)).  The first n_own loads are the
 // segment's own entries, written back after the operations.
-// A segment with n_load < 0 is DIRECT: unit `op_begin` (a column or row
-// too wide for the table) is executed straight from global memory.
+// A segment with n_load < 0 is WIDE: it is the whole chain of a wide
+// program level, and op_begin indexes the program's wide units (a column or
+// row too wide for any table, executed by a whole block: see WidePlan).
 // Up to kMaxCarry entries a segment needs that the previous segment of the
 // same chain already holds in its table are moved inside shared memory
 // instead of being loaded (carry[k] = from << 16 | to, -1 unused).
@@ -53,25 +54,60 @@ struct Segment {
   int carry[kMaxCarry] = {-1, -1, -1, -1};
 };
 
+// Program levels.  Every level of the reference's level set is executed as
+// one or more program levels: a chain is cut around each unit too wide for
+// the level's table budget, the pieces before the first wide unit form the
+// first program level, the wide units of that position the next one (a
+// WIDE level, one chain per wide unit), the pieces between the first and
+// second wide unit the next, and so on.  Chains of one level are
+// independent and each keeps its order, so the program levels in sequence
+// compute what the level computes.
+//
+// A wide refactor unit (column k) is executed in gather form, scheduled
+// inside the column: target slot t of column k receives
+//     M(t) -= L(i, j) * U(j, k)   for its pairs (q = slot of L(i, j), p = slot of U(j, k))
+// in ascending j (the order of the reference's right-looking loop, so FP64
+// stays bit-exact), and the targets are grouped into column levels: a
+// target's level is one more than the highest level of the U entries it
+// reads (targets without pairs have level 0 and need no work).  After the
+// last level the L part is divided by the pivot.
+struct WidePlan {
+  std::vector<int> unit;      // [W] column (refactor) or unknown (solves)
+  // refactor only:
+  std::vector<int> lvl;       // [W + 1] -> index into lv_tgt (the unit's column levels)
+  std::vector<int> lv_tgt;    // [column levels + 1] -> index into tg_slot
+  std::vector<int> tg_slot;   // [T] target slot
+  std::vector<int> tg_pair;   // [T + 1] -> index into pr_q / pr_p
+  std::vector<int> pr_q, pr_p;  // [P] L slot and U slot of every update
+};
+
 struct ChainProgram {
   int kind = -1;                 // -1 refactor, 0 L, 1 U, 2 U^T, 3 L^T
   int max_locals = 0;            // widest table of any level
-  std::vector<int> level_max_locals;  // [levels] table size of each level: its widest
-                                      // segment, at most the level's budget
+  std::vector<int> level_max_locals;  // [levels] table size of each program level: its
+                                      // widest segment, at most the level's budget
   std::vector<int> level_chain;  // [levels + 1] -> chain index
+  std::vector<int> level_src;    // [levels] level of the level set it belongs to
+  std::vector<char> level_wide;  // [levels] 1: a WIDE level
   std::vector<int> chain_seg;    // [chains + 1] -> segment index
+  std::vector<int> chain_unit;   // [chains + 1] -> index into units
+  std::vector<int> units;        // units of each chain, in execution order
   std::vector<Segment> seg;
   std::vector<int> loads;
   std::vector<uint32_t> ops;     // packed, each segment's run padded to 4
   std::vector<int> op_col;       // column of each SCALE operation (error reports)
+  WidePlan wide;
   int longest_chain_segments = 0;
-  int direct_segments = 0;
+  int wide_units = 0;
+  int wide_levels = 0;
 };
 
 // kind -1 uses s.lu; 0 s.l; 1 s.u; 2 s.lu; 3 s.lt.
 void build_chain_program(const Symbolic& s, int kind, int max_locals, ChainProgram& out);
-// As above with a table budget per level (levels with few chains can afford a
-// wide table: fewer segments, and the warps they leave idle cost nothing).
+// As above with a table budget per level of the level set (levels with few
+// chains can afford a wide table: fewer segments, and the warps they leave
+// idle cost nothing).  A unit whose own table would exceed its level's
+// budget is a wide unit.
 void build_chain_program(const Symbolic& s, int kind, const std::vector<int>& level_max_locals,
                          ChainProgram& out);
 // The level set a program kind walks.

@@ -1,0 +1,380 @@
+// Wide units: the columns (refactorization) and rows (solves) too wide for
+// any chain-program table, each executed by a whole block (programs.hpp,
+// WidePlan).  They are the dense trailing columns and rows of plants whose
+// strings share bus nodes: eliminating a string from its bus end fills the
+// bus row and column with one entry per string node.  The reference runs
+// such levels with 32 threads per column once a level's longest row passes 64
+// entries (factorize_electrical_system_CUDA.cu:75-77, triangular_substitution.cu:
+// 153-159), walking the column's updates with atomics.
+//
+// FP64 stays bit-exact with the reference's sequential order: every entry
+// receives its updates one at a time, in ascending j, each product and each
+// subtraction rounded on its own.  The parallelism comes from elsewhere:
+//   * refactorization of column k in gather form, scheduled inside the
+//     column: target slots whose U sources are final are computed together
+//     (a thread or, batched, a warp per target), one block barrier per column
+//     level;
+//   * a target or solve row with many updates: the block computes the
+//     products in parallel (each rounded as the sequential code rounds it)
+//     into shared memory and one thread (batched: one warp, a lane per two
+//     scenarios) subtracts them in order.
+// Single scenario: the column is staged in shared memory when it fits.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "chainprog.cuh"
+#include "kernels.cuh"
+
+namespace pvglu {
+
+// Separately rounded product and difference (the reference's rounding).
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+
+// Updates per target above which the block computes a target's products
+// together instead of one thread (warp) walking them.
+constexpr int kWideLong = 96;
+
+template <typename T>
+struct WideScalar {
+  using V = T;
+};
+
+// acc - sum_e a_e * b_e in the order e = 0 .. count-1, each product and each
+// difference rounded on its own: the block's threads (batched: warps, two
+// scenarios per lane) form the products of a chunk in shared memory, then
+// thread 0 (batched: warp 0) subtracts them in order.  `ab(e, a, b)` gives
+// the operands of entry e (T, or Vec2<T> for the lane's two scenarios).
+// Returns the result in thread 0 (batched: in warp 0's lanes).  All threads
+// of the block must call it; scratch: at least blockDim.x * sizeof(T)
+// (batched: kWideChunkRows * 32 * sizeof(Vec2<T>)) bytes.
+constexpr int kWideChunkRows = 16;
+
+template <typename T, bool BATCH, typename AB>
+__device__ __forceinline__ typename std::conditional<BATCH, typename Vec2<T>::type, T>::type
+ordered_sub_block(typename std::conditional<BATCH, typename Vec2<T>::type, T>::type acc,
+                  int count, AB ab, unsigned char* scratch) {
+  const int tid = threadIdx.x;
+  if constexpr (!BATCH) {
+    T* prod = reinterpret_cast<T*>(scratch);
+    for (int base = 0; base < count; base += blockDim.x) {
+      const int e = base + tid;
+      if (e < count) {
+        T a, b;
+        ab(e, a, b);
+        prod[tid] = mul_rn(a, b);
+      }
+      __syncthreads();
+      if (tid == 0) {
+        const int m = min((int)blockDim.x, count - base);
+        for (int i = 0; i < m; i++) acc = sub_rn(acc, prod[i]);
+      }
+      __syncthreads();
+    }
+    return acc;
+  } else {
+    using V2 = typename Vec2<T>::type;
+    V2* prod = reinterpret_cast<V2*>(scratch);  // [kWideChunkRows][32]
+    const int lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+    for (int base = 0; base < count; base += kWideChunkRows) {
+      for (int r = warp; r < kWideChunkRows && base + r < count; r += nw) {
+        V2 a, b;
+        ab(base + r, a, b);
+        V2 p;
+        p.x = mul_rn(a.x, b.x);
+        p.y = mul_rn(a.y, b.y);
+        prod[r * 32 + lane] = p;
+      }
+      __syncthreads();
+      if (warp == 0) {
+        const int m = min(kWideChunkRows, count - base);
+        for (int i = 0; i < m; i++) {
+          const V2 p = prod[i * 32 + lane];
+          acc.x = sub_rn(acc.x, p.x);
+          acc.y = sub_rn(acc.y, p.y);
+        }
+      }
+      __syncthreads();
+    }
+    return acc;
+  }
+}
+
+template <typename T, bool BATCH>
+__host__ __device__ constexpr int wide_scratch_bytes(int threads) {
+  return BATCH ? kWideChunkRows * 32 * 2 * (int)sizeof(T) : threads * (int)sizeof(T);
+}
+
+__device__ __forceinline__ double2 ldv2(const double* p) {
+  return __ldcg(reinterpret_cast<const double2*>(p));
+}
+__device__ __forceinline__ float2 ldv2(const float* p) {
+  return __ldcg(reinterpret_cast<const float2*>(p));
+}
+
+// ---------------------------------------------------------------------------
+// Refactorization of wide column k = P.w_unit[w] for the scenario group at
+// s0 (batched) or the single scenario.  smem: the block's shared memory
+// (smem_bytes of it); the column is staged there in single mode when
+// len * sizeof(T) + scratch fits.
+template <typename T, bool BATCH>
+__device__ void wide_refactor(const ProgDev& P, const DevStruct& d, int w, int s0,
+                              T* __restrict__ v, int ld, int S, T pivot_tol, DevStatus* st,
+                              unsigned char* smem, int smem_bytes) {
+  const int k = __ldg(P.w_unit + w);
+  const int c0 = __ldg(d.colptr + k), dk = __ldg(d.diag + k), c1 = __ldg(d.colptr + k + 1);
+  const int len = c1 - c0;
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const int l_begin = __ldg(P.w_lvl + w), l_end = __ldg(P.w_lvl + w + 1);
+  if constexpr (!BATCH) {
+    const int scratch = wide_scratch_bytes<T, false>(nthr);
+    const bool staged = (int64_t)len * (int)sizeof(T) + scratch <= smem_bytes;
+    T* col = reinterpret_cast<T*>(smem + scratch);
+    unsigned char* scr = smem;
+    if (staged)
+      for (int i = tid; i < len; i += nthr) col[i] = ldv(v + c0 + i);
+    __syncthreads();
+    auto get = [&](int slot) -> T { return staged ? col[slot - c0] : ldv(v + slot); };
+    auto put = [&](int slot, T val) {
+      if (staged) col[slot - c0] = val;
+      else v[slot] = val;
+    };
+    for (int l = l_begin; l < l_end; l++) {
+      const int t0 = __ldg(P.lv_tgt + l), t1 = __ldg(P.lv_tgt + l + 1);
+      for (int t = t0 + tid; t < t1; t += nthr) {
+        const int e0 = __ldg(P.tg_pair + t), e1 = __ldg(P.tg_pair + t + 1);
+        if (e1 - e0 > kWideLong) continue;
+        const int slot = __ldg(P.tg_slot + t);
+        T acc = get(slot);
+        for (int e = e0; e < e1; e++)
+          acc = fnms(acc, ldv(v + __ldg(P.pr_q + e)), get(__ldg(P.pr_p + e)));
+        put(slot, acc);
+      }
+      __syncthreads();
+      for (int t = t0; t < t1; t++) {  // long targets, one at a time by the block
+        const int e0 = __ldg(P.tg_pair + t), e1 = __ldg(P.tg_pair + t + 1);
+        if (e1 - e0 <= kWideLong) continue;
+        const int slot = __ldg(P.tg_slot + t);
+        T acc = get(slot);
+        acc = ordered_sub_block<T, false>(
+            acc, e1 - e0,
+            [&](int e, T& a, T& b) {
+              a = ldv(v + __ldg(P.pr_q + e0 + e));
+              b = get(__ldg(P.pr_p + e0 + e));
+            },
+            scr);
+        if (tid == 0) put(slot, acc);
+        __syncthreads();
+      }
+    }
+    const T piv = get(dk);
+    if (tid == 0 && !(fabs(piv) >= pivot_tol) && S > 0) report_error(st, 3, k, 0);
+    if constexpr (std::is_same<T, float>::value) {
+      const float r = __frcp_rn(piv);
+      for (int q = dk + 1 + tid; q < c1; q += nthr) put(q, get(q) * r);
+    } else {
+      for (int q = dk + 1 + tid; q < c1; q += nthr) put(q, get(q) / piv);
+    }
+    __syncthreads();
+    if (staged)
+      for (int i = tid; i < len; i += nthr) v[c0 + i] = col[i];
+    __syncthreads();
+  } else {
+    using V2 = typename Vec2<T>::type;
+    const int lane = tid & 31, warp = tid >> 5, nw = nthr >> 5;
+    const int s = s0 + 2 * lane;
+    auto row = [&](int slot) { return v + (int64_t)slot * ld + s; };
+    for (int l = l_begin; l < l_end; l++) {
+      const int t0 = __ldg(P.lv_tgt + l), t1 = __ldg(P.lv_tgt + l + 1);
+      for (int t = t0 + warp; t < t1; t += nw) {
+        const int e0 = __ldg(P.tg_pair + t), e1 = __ldg(P.tg_pair + t + 1);
+        if (e1 - e0 > kWideLong) continue;
+        T* tp = row(__ldg(P.tg_slot + t));
+        V2 acc = ldv2(tp);
+        int e = e0;
+        // Four updates' operands in flight at a time; the subtractions stay
+        // in order.
+        for (; e + 4 <= e1; e += 4) {
+          V2 a[4], b[4];
+#pragma unroll
+          for (int u = 0; u < 4; u++) {
+            a[u] = ldv2(row(__ldg(P.pr_q + e + u)));
+            b[u] = ldv2(row(__ldg(P.pr_p + e + u)));
+          }
+#pragma unroll
+          for (int u = 0; u < 4; u++) {
+            acc.x = fnms(acc.x, a[u].x, b[u].x);
+            acc.y = fnms(acc.y, a[u].y, b[u].y);
+          }
+        }
+        for (; e < e1; e++) {
+          const V2 a = ldv2(row(__ldg(P.pr_q + e))), b = ldv2(row(__ldg(P.pr_p + e)));
+          acc.x = fnms(acc.x, a.x, b.x);
+          acc.y = fnms(acc.y, a.y, b.y);
+        }
+        *reinterpret_cast<V2*>(tp) = acc;
+      }
+      __syncthreads();
+      for (int t = t0; t < t1; t++) {
+        const int e0 = __ldg(P.tg_pair + t), e1 = __ldg(P.tg_pair + t + 1);
+        if (e1 - e0 <= kWideLong) continue;
+        T* tp = row(__ldg(P.tg_slot + t));
+        V2 acc = ldv2(tp);
+        acc = ordered_sub_block<T, true>(
+            acc, e1 - e0,
+            [&](int e, V2& a, V2& b) {
+              a = ldv2(row(__ldg(P.pr_q + e0 + e)));
+              b = ldv2(row(__ldg(P.pr_p + e0 + e)));
+            },
+            smem);
+        if (warp == 0) *reinterpret_cast<V2*>(tp) = acc;
+        __syncthreads();
+      }
+    }
+    const V2 piv = ldv2(row(dk));
+    if (warp == 0) {
+      if (!(fabs(piv.x) >= pivot_tol) && s < S) report_error(st, 3, k, s);
+      if (!(fabs(piv.y) >= pivot_tol) && s + 1 < S) report_error(st, 3, k, s + 1);
+    }
+    for (int q = dk + 1 + warp; q < c1; q += nw) {
+      V2 val = ldv2(row(q));
+      if constexpr (std::is_same<T, float>::value) {
+        val.x *= __frcp_rn(piv.x);
+        val.y *= __frcp_rn(piv.y);
+      } else {
+        val.x = val.x / piv.x;
+        val.y = val.y / piv.y;
+      }
+      *reinterpret_cast<V2*>(row(q)) = val;
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// One wide unknown of a solve (KIND 0: L row, 1: U row, 2: U^T column, 3:
+// L^T column), the same arithmetic and order as solve_unknown.
+template <typename T, int KIND, bool BATCH>
+__device__ void wide_solve(const ProgDev& P, const DevStruct& d, int w, int s0,
+                           const T* __restrict__ v, T* __restrict__ x, int ld,
+                           unsigned char* smem) {
+  const int i = __ldg(P.w_unit + w);
+  int b0, cnt, dg = -1;
+  if (KIND == 0) {
+    b0 = __ldg(d.lrow_ptr + i);
+    cnt = __ldg(d.lrow_ptr + i + 1) - b0;
+  } else if (KIND == 1) {
+    b0 = __ldg(d.urow_ptr + i);
+    cnt = __ldg(d.urow_ptr + i + 1) - b0;
+    dg = __ldg(d.diag + i);
+  } else if (KIND == 2) {
+    b0 = __ldg(d.colptr + i);
+    dg = __ldg(d.diag + i);
+    cnt = dg - b0;
+  } else {
+    b0 = __ldg(d.diag + i) + 1;
+    cnt = __ldg(d.colptr + i + 1) - b0;
+  }
+  // Entry e (in order): value slot and solution row.
+  auto entry = [&](int e, int& slot, int& col) {
+    if (KIND == 0) {
+      slot = __ldg(d.lrow_slot + b0 + e);
+      col = __ldg(d.lrow_col + b0 + e);
+    } else if (KIND == 1) {  // descending: the reference's backward sweep order
+      slot = __ldg(d.urow_slot + b0 + cnt - 1 - e);
+      col = __ldg(d.urow_col + b0 + cnt - 1 - e);
+    } else {
+      slot = b0 + e;
+      col = __ldg(d.csc_row + b0 + e);
+    }
+  };
+  if constexpr (!BATCH) {
+    T acc = ldv(x + i);
+    acc = ordered_sub_block<T, false>(
+        acc, cnt,
+        [&](int e, T& a, T& b) {
+          int slot, col;
+          entry(e, slot, col);
+          a = ldv(v + slot);
+          b = ldv(x + col);
+        },
+        smem);
+    if (threadIdx.x == 0) {
+      if (dg >= 0) acc = acc / ldv(v + dg);
+      x[i] = acc;
+    }
+    __syncthreads();
+  } else {
+    using V2 = typename Vec2<T>::type;
+    const int s = s0 + 2 * (threadIdx.x & 31);
+    V2 acc = ldv2(x + (int64_t)i * ld + s);
+    acc = ordered_sub_block<T, true>(
+        acc, cnt,
+        [&](int e, V2& a, V2& b) {
+          int slot, col;
+          entry(e, slot, col);
+          a = ldv2(v + (int64_t)slot * ld + s);
+          b = ldv2(x + (int64_t)col * ld + s);
+        },
+        smem);
+    if ((threadIdx.x >> 5) == 0) {
+      if (dg >= 0) {
+        const V2 p = ldv2(v + (int64_t)dg * ld + s);
+        acc.x = acc.x / p.x;
+        acc.y = acc.y / p.y;
+      }
+      *reinterpret_cast<V2*>(x + (int64_t)i * ld + s) = acc;
+    }
+    __syncthreads();
+  }
+}
+
+// The wide units [cb, ce) of one WIDE program level: item = (unit, scenario
+// group), a block per item, blocks striding over the items.  done (solves of
+// a refinement): a group whose scenarios have all converged is skipped.
+template <typename T, int KIND, bool BATCH>
+__device__ __forceinline__ void wide_run_level(const ProgDev& P, const DevStruct& d, int cb,
+                                               int ce, T* __restrict__ v, T* __restrict__ x,
+                                               int ld, int S, T pivot_tol, DevStatus* st,
+                                               const int* done, unsigned char* smem,
+                                               int smem_bytes, int block, int n_blocks) {
+  const int groups = BATCH ? ld / kGroup : 1;
+  const int items = (ce - cb) * groups;
+  for (int it = block; it < items; it += n_blocks) {
+    const int ci = BATCH ? it / groups : it;
+    const int s0 = BATCH ? (it - ci * groups) * kGroup : 0;
+    if (BATCH && done) {
+      __shared__ int idle;
+      if (threadIdx.x == 0) {
+        int all = 1;
+        for (int s = s0; s < s0 + kGroup && all; s++) all = (s >= S || done[s]);
+        idle = all;
+      }
+      __syncthreads();
+      const int skip = idle;
+      __syncthreads();
+      if (skip) continue;
+    }
+    // The chain's single WIDE segment names the wide unit.
+    const int w = __ldg(&P.seg[__ldg(P.chain_seg + cb + ci)].z);
+    if (KIND < 0) wide_refactor<T, BATCH>(P, d, w, s0, v, ld, S, pivot_tol, st, smem, smem_bytes);
+    else wide_solve<T, (KIND < 0 ? 0 : KIND), BATCH>(P, d, w, s0, v, x, ld, smem);
+  }
+}
+
+// Launch form of a WIDE program level (the per-level schedule).
+template <typename T, int KIND, bool BATCH>
+__global__ void __launch_bounds__(kProgBlock)
+k_wide_level(ProgDev P, DevStruct d, int cb, int ce, T* __restrict__ v, T* __restrict__ x,
+             int ld, int S, T pivot_tol, DevStatus* st, const int* done, const int* ndone,
+             int smem_bytes) {
+  if (ndone && __ldcg(ndone) >= S) return;
+  if (__ldcg(&st->code) == 6) return;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  wide_run_level<T, KIND, BATCH>(P, d, cb, ce, v, x, ld, S, pivot_tol, st, done, smem_raw,
+                                 smem_bytes, blockIdx.x, gridDim.x);
+}
+
+}  // namespace pvglu

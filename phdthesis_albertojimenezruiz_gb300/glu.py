@@ -116,6 +116,15 @@ class Numeric:
         self.precision = precision
         self.set_schedule(schedule)
 
+    @property
+    def info(self) -> dict:
+        """pvglu_numeric_get_info: program levels, WIDE levels and units, widest
+        table, chain-program operations and loads."""
+        inf = N.NumericInfo()
+        N.check(N.lib().pvglu_numeric_get_info(self.handle, C.byref(inf)),
+                "pvglu_numeric_get_info")
+        return {f: getattr(inf, f) for f, _ in N.NumericInfo._fields_}
+
     def set_schedule(self, schedule: int) -> None:
         N.check(N.lib().pvglu_numeric_set_schedule(self.handle, schedule),
                 "pvglu_numeric_set_schedule")

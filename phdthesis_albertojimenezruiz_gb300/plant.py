@@ -23,6 +23,125 @@ SHADOWS = {
 }
 
 
+def block_plant(blocks: int, strings: int, panels: int, seed: int = 0):
+    """A Jacobian with the reference simulator's own plant topology
+    (PVPP_Plant_Simulator/003_create_electric_system.cpp:89-126, 184-262,
+    264-342; interconnection "nothing"): per block, `strings` series strings
+    of `panels` panels in parallel between two bus nodes; every panel has an
+    internal diode node with its series and shunt resistors and its diode;
+    the buses reach the block's inverter (a DC voltage source with its own
+    current unknown) through wires, one bus is grounded through a wire; per
+    block two AC phasor nodes (real and imaginary unknowns) on a ring of AC
+    wires closed at the point of common coupling, an AC voltage source.  The
+    inverters' AC injections are right-hand-side terms only (002b:205-237),
+    so they add no entries.  Unknowns in the reference's order: nodes in
+    creation order, then the voltage-source currents.
+
+    Eliminating a string from its bus end fills the bus rows and columns
+    with an entry per string node, so the factors have a few dense columns
+    and rows (about strings x panels entries each) and long dependency
+    chains: the shape the reference's own plant gives its GLU.
+
+    Values are this function's own (the reference's Rs = 0.115 ohm, Rsh =
+    90.85 ohm and 1e-5 ohm wires; seeded diode conductances of a forward-
+    biased operating point).  Returns (rowptr, colidx, values, b) in CSR.
+    """
+    rng = np.random.default_rng(seed)
+    g_rs, g_rsh, g_wire = 1.0 / 0.115, 1.0 / 90.85, 1.0 / 1e-5
+    entries: dict[tuple[int, int], float] = {}
+    n_nodes = 0
+
+    def node() -> int:  # 1-based node number, 0 = ground
+        nonlocal n_nodes
+        n_nodes += 1
+        return n_nodes
+
+    def add(r: int, c: int, v: float) -> None:
+        entries[(r, c)] = entries.get((r, c), 0.0) + v
+
+    def adm(n1: int, n2: int, g: float) -> None:
+        if n1:
+            add(n1 - 1, n1 - 1, g)
+        if n1 and n2:
+            add(n1 - 1, n2 - 1, -g)
+            add(n2 - 1, n1 - 1, -g)
+        if n2:
+            add(n2 - 1, n2 - 1, g)
+
+    def adm_ac(n1: int, n2: int, g: float) -> None:
+        # 2x2 real blocks [Re -Im; Im Re] of a complex admittance g + 0j
+        # (002b:41-67): the imaginary entries are stamped with zero.
+        for a_, b_, s in ((n1, n1, 1.0), (n1, n2, -1.0), (n2, n1, -1.0), (n2, n2, 1.0)):
+            if not a_ or not b_:
+                continue
+            r, c = a_ - 1, b_ - 1
+            add(r, c, s * g)
+            add(r, c + 1, 0.0)
+            add(r + 1, c, 0.0)
+            add(r + 1, c + 1, s * g)
+
+    sources = []  # (n+, n-, value)
+    rhs_nodes = []  # (node, value) current sources into the node
+    mains = []
+    for _ in range(blocks):
+        bus_in, bus_out = node(), node()
+        for _ in range(strings):
+            hi_prev = None
+            for j in range(panels):
+                hi = bus_in if j == panels - 1 else node()
+                lo = bus_out if j == 0 else hi_prev
+                hi_prev = hi
+                internal = node()
+                adm(internal, hi, g_rs)
+                adm(internal, lo, g_rsh)
+                adm(internal, lo, float(rng.uniform(1e-4, 2.0)))  # diode companion G
+                adm(lo, hi, float(rng.uniform(1e-9, 1e-6)))  # reverse-biased bypass diode
+                rhs_nodes.append((internal, 8.5))
+                rhs_nodes.append((lo, -8.5))
+        after_in, after_out = node(), node()
+        adm(after_in, bus_in, g_wire)
+        adm(after_out, bus_out, g_wire)
+        m0 = node()
+        node()
+        m1 = node()
+        node()
+        mains.append((m0, m1))
+        adm(after_out, 0, g_wire)
+        sources.append((after_in, after_out, 0.8 * 46.0 * panels))
+        if len(mains) > 1:
+            adm_ac(mains[-1][0], mains[-2][0], g_wire)
+            adm_ac(mains[-1][1], mains[-2][1], g_wire)
+    pcc = node()
+    node()
+    sources.append((pcc, 0, 25000.0))
+    sources.append((pcc + 1, 0, 0.0))
+    adm_ac(pcc, mains[0][0], g_wire)
+    adm_ac(0, mains[0][1], g_wire)
+    adm_ac(pcc, mains[-1][0], g_wire)
+    adm_ac(0, mains[-1][1], g_wire)
+    n = n_nodes + len(sources)
+    b = np.zeros(n)
+    for k, (p_, m_, val) in enumerate(sources):
+        row = n_nodes + k
+        if p_:
+            add(p_ - 1, row, -1.0)
+            add(row, p_ - 1, 1.0)
+        if m_:
+            add(m_ - 1, row, 1.0)
+            add(row, m_ - 1, -1.0)
+        b[row] += val
+    for nd, val in rhs_nodes:
+        b[nd - 1] += val
+    keys = np.array(list(entries.keys()), dtype=np.int64)
+    vals = np.array(list(entries.values()), dtype=np.float64)
+    order = np.lexsort((keys[:, 1], keys[:, 0]))
+    keys, vals = keys[order], vals[order]
+    rowptr = np.zeros(n + 1, np.int32)
+    np.add.at(rowptr, keys[:, 0] + 1, 1)
+    rowptr = np.cumsum(rowptr).astype(np.int32)
+    return rowptr, keys[:, 1].astype(np.int32), vals, b
+
+
 class Plant:
     def __init__(self, n_inverters: int, n_strings: int, n_series: int):
         h = C.c_void_p()

@@ -14,6 +14,12 @@ Each fixture holds the input pattern/values/RHS of one seeded test matrix
   x_perm              Substitute_LU_Vector_b_CSC_CPU on the permuted RHS with
                       lu_seq (GLU_CSC_CPU_Triangular.cpp:27-43)
   x                   the same solution in the caller's unknown order (000:233)
+
+orderings/block_plant_amd.npz holds the reference's AMD ordering (and its
+fill and level counts) of the reference-topology plants (plant.block_plant)
+of 1 x 50 x 50 and 7 x 50 x 50 panels, too large for a full fixture: with the
+ordering, the symbolic analysis reproduces the reference's arrays and the
+oracle's restatement gives the reference's factors.
 """
 from __future__ import annotations
 
@@ -30,7 +36,9 @@ sys.path.insert(0, str(ROOT / "tests"))
 import matrices as M  # noqa: E402
 from oracle import oracle as O  # noqa: E402
 
-FIXTURES = ("plant_1x2x2", "plant_c1", "mesh_12x10", "mesh_20x20", "random_300")
+FIXTURES = ("plant_1x2x2", "plant_c1", "mesh_12x10", "mesh_20x20", "random_300",
+            "block_1x20x20")
+BLOCK_ORDERINGS = ((1, 50, 50), (7, 50, 50))
 
 
 def main() -> None:
@@ -55,6 +63,19 @@ def main() -> None:
         np.savez_compressed(HERE / f"{name}.npz", rowptr=rp, colidx=ci, a=a, b=b, csc_in=csc,
                             lu_seq=lu_seq, lu_levels=lu_lev, x_perm=x_perm, x=x, **arrs)
         print(f"{name}: n={n} nnz_lu={len(csc)}")
+    out = {}
+    for dims in BLOCK_ORDERINGS:
+        rp, ci, _, _ = M.block(dims)
+        ref = O.Ref(rp, ci)
+        tag = "x".join(map(str, dims))
+        out[f"perm_{tag}"] = ref.get("perm_amd")
+        out[f"nnz_lu_{tag}"] = np.array(len(ref.get("csc_row")))
+        out[f"u_levels_{tag}"] = np.array(len(ref.get("u_sl")) - 1)
+        out[f"lu_levels_{tag}"] = np.array(len(ref.get("lu_sl")) - 1)
+        print(f"block {tag}: n={len(rp) - 1} nnz_lu={int(out[f'nnz_lu_{tag}'])} "
+              f"u_levels={int(out[f'u_levels_{tag}'])}")
+    (HERE / "orderings").mkdir(exist_ok=True)
+    np.savez_compressed(HERE / "orderings" / "block_plant_amd.npz", **out)
 
 
 if __name__ == "__main__":

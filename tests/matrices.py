@@ -119,6 +119,14 @@ def plant_batch(p, n_scenarios: int, seed0: int = 1, preset: str = "c1", t: floa
     return a, b
 
 
+def block(dims, seed: int = 0):
+    """(rowptr, colidx, A values, b) of a plant with the reference's own
+    topology (plant.block_plant): dense bus rows and columns after fill."""
+    from phdthesis_albertojimenezruiz_gb300.plant import block_plant
+
+    return block_plant(*dims, seed=seed)
+
+
 CASES = {
     "plant_1x2x2": lambda: plant((1, 2, 2)),
     "plant_c1": lambda: plant((4, 8, 20)),
@@ -127,4 +135,5 @@ CASES = {
     "mesh_30x30": lambda: mesh(30, 30, 5, seed=4),
     "random_300": lambda: random_mna(300, 3.0, 6, seed=5),
     "random_1500": lambda: random_mna(1500, 2.5, 10, seed=6),
+    "block_1x20x20": lambda: block((1, 20, 20), seed=8),
 }

@@ -3,6 +3,7 @@
 // device executors rely on for memory safety and ordering.
 //   usage: program_invariants <n> <rowptr.bin> <colidx.bin>
 // Exit status 0 when every check passes; the first violation is printed.
+#include <algorithm>
 #include <cstdio>
 #include <fstream>
 #include <string>
@@ -36,28 +37,105 @@ int fails = 0;
     }                                    \
   } while (0)
 
+// Table rows a unit needs on its own (what the compiler measures).
+int unit_need(const Symbolic& s, int kind, int u) {
+  std::vector<int> xs, vs;
+  auto x = [&](int i) { xs.push_back(i); };
+  auto v = [&](int q) { vs.push_back(q); };
+  if (kind == -1) {
+    const int c0 = s.csc_colptr[u], dk = s.diag_slot[u], c1 = s.csc_colptr[u + 1];
+    for (int q = c0; q < c1; q++) v(q);
+    for (int p = c0; p < dk; p++) {
+      const int j = s.csc_row[p];
+      for (int q = s.diag_slot[j] + 1; q < s.csc_colptr[j + 1]; q++) v(q);
+    }
+  } else if (kind == 0 || kind == 1) {
+    x(u);
+    const auto& ptr = kind == 0 ? s.lrow_ptr : s.urow_ptr;
+    const auto& slot = kind == 0 ? s.lrow_slot : s.urow_slot;
+    const auto& col = kind == 0 ? s.lrow_col : s.urow_col;
+    for (int e = ptr[u]; e < ptr[u + 1]; e++) {
+      x(col[e]);
+      v(slot[e]);
+    }
+    if (kind == 1) v(s.diag_slot[u]);
+  } else {
+    x(u);
+    const int b = kind == 2 ? s.csc_colptr[u] : s.diag_slot[u] + 1;
+    const int e = kind == 2 ? s.diag_slot[u] : s.csc_colptr[u + 1];
+    for (int q = b; q < e; q++) {
+      x(s.csc_row[q]);
+      v(q);
+    }
+    if (kind == 2) v(s.diag_slot[u]);
+  }
+  std::sort(xs.begin(), xs.end());
+  std::sort(vs.begin(), vs.end());
+  return (int)(std::unique(xs.begin(), xs.end()) - xs.begin() +
+               (std::unique(vs.begin(), vs.end()) - vs.begin()));
+}
+
 void check_program(const Symbolic& s, int kind, const std::vector<int>& budget) {
   ChainProgram pr;
   build_chain_program(s, kind, budget, pr);
   const LevelSet& ls = program_levels(s, kind);
-  CHECK(pr.level_chain == ls.start_levels, "kind %d level_chain", kind);
-  CHECK((int)pr.chain_seg.size() == ls.num_chains() + 1, "kind %d chain_seg size", kind);
-  CHECK((int)pr.level_max_locals.size() == ls.num_levels(), "kind %d level tables", kind);
-  for (int lv = 0; lv < ls.num_levels(); lv++) {
+  const int nlev = (int)pr.level_chain.size() - 1;
+  CHECK((int)pr.level_src.size() == nlev && (int)pr.level_wide.size() == nlev &&
+            (int)pr.level_max_locals.size() == nlev,
+        "kind %d level arrays", kind);
+  CHECK((int)pr.chain_seg.size() == pr.level_chain.back() + 1 &&
+            (int)pr.chain_unit.size() == pr.level_chain.back() + 1,
+        "kind %d chain arrays", kind);
+  // Every unit of the level set once, each chain's units in order, in the
+  // program levels of its own level.
+  std::vector<int> where_lv(s.n, -1), where_pos(s.n, -1);
+  int pos = 0;
+  for (int lv = 0; lv < nlev; lv++) {
+    CHECK(lv == 0 || pr.level_src[lv] >= pr.level_src[lv - 1], "kind %d level order", kind);
+    for (int c = pr.level_chain[lv]; c < pr.level_chain[lv + 1]; c++)
+      for (int k = pr.chain_unit[c]; k < pr.chain_unit[c + 1]; k++) {
+        const int u = pr.units[k];
+        CHECK(u >= 0 && u < s.n && where_lv[u] < 0, "kind %d unit %d twice", kind, u);
+        where_lv[u] = pr.level_src[lv];
+        where_pos[u] = pos++;
+      }
+  }
+  CHECK(pos == s.n, "kind %d units %d of %d", kind, pos, s.n);
+  for (int lv = 0; lv < ls.num_levels(); lv++)
+    for (int c = ls.start_levels[lv]; c < ls.start_levels[lv + 1]; c++)
+      for (int k = ls.start_chains[c]; k < ls.start_chains[c + 1]; k++) {
+        const int u = ls.columns[k];
+        CHECK(where_lv[u] == lv, "kind %d unit %d in level %d", kind, u, where_lv[u]);
+        if (k > ls.start_chains[c])
+          CHECK(where_pos[ls.columns[k - 1]] < where_pos[u], "kind %d chain order at %d", kind,
+                u);
+      }
+  for (int lv = 0; lv < nlev; lv++) {
     const int table = pr.level_max_locals[lv];
-    CHECK(table >= 1 && table <= budget[lv] && table <= pr.max_locals,
-          "kind %d level %d table %d budget %d", kind, lv, table, budget[lv]);
-    for (int c = ls.start_levels[lv]; c < ls.start_levels[lv + 1]; c++) {
+    const int bud = std::min(budget[pr.level_src[lv]], kMaxLocals);
+    CHECK(table >= 1 && table <= bud && table <= pr.max_locals,
+          "kind %d level %d table %d budget %d", kind, lv, table, bud);
+    for (int c = pr.level_chain[lv]; c < pr.level_chain[lv + 1]; c++) {
       CHECK(pr.chain_seg[c] <= pr.chain_seg[c + 1], "kind %d chain %d segments", kind, c);
+      if (pr.level_wide[lv]) {
+        CHECK(pr.chain_seg[c + 1] == pr.chain_seg[c] + 1 &&
+                  pr.chain_unit[c + 1] == pr.chain_unit[c] + 1,
+              "kind %d wide chain %d", kind, c);
+        const Segment& sg = pr.seg[pr.chain_seg[c]];
+        const int u = pr.units[pr.chain_unit[c]];
+        CHECK(sg.n_load < 0 && sg.op_begin >= 0 && sg.op_begin < (int)pr.wide.unit.size() &&
+                  pr.wide.unit[sg.op_begin] == u,
+              "kind %d wide segment of unit %d", kind, u);
+        CHECK(unit_need(s, kind, u) > bud, "kind %d unit %d is not wide", kind, u);
+        continue;
+      }
+      for (int k = pr.chain_unit[c]; k < pr.chain_unit[c + 1]; k++)
+        CHECK(unit_need(s, kind, pr.units[k]) <= bud, "kind %d unit %d too wide", kind,
+              pr.units[k]);
       int prev_nl = -1;  // table rows of the previous segment of the chain (-1: none)
       for (int g = pr.chain_seg[c]; g < pr.chain_seg[c + 1]; g++) {
         const Segment& sg = pr.seg[g];
-        if (sg.n_load < 0) {  // DIRECT unit
-          CHECK(sg.op_begin >= 0 && sg.op_begin < s.n, "kind %d DIRECT unit %d", kind,
-                sg.op_begin);
-          prev_nl = -1;
-          continue;
-        }
+        CHECK(sg.n_load > 0, "kind %d segment %d of a program level is WIDE", kind, g);
         CHECK(sg.n_load <= table, "kind %d level %d segment %d loads %d > table %d", kind, lv,
               g, sg.n_load, table);
         CHECK(sg.n_own >= 0 && sg.n_own <= sg.n_load, "kind %d segment %d own", kind, g);
@@ -101,6 +179,42 @@ void check_program(const Symbolic& s, int kind, const std::vector<int>& budget) 
       }
     }
   }
+  // Wide refactor plans: targets inside their column, pairs in ascending j,
+  // every U source of a target computed at an earlier column level, every
+  // update of the column present once.
+  if (kind == -1) {
+    const WidePlan& w = pr.wide;
+    CHECK(w.lvl.size() == w.unit.size() + 1, "wide lvl size");
+    for (size_t i = 0; i < w.unit.size(); i++) {
+      const int k = w.unit[i];
+      const int c0 = s.csc_colptr[k], dk = s.diag_slot[k], c1 = s.csc_colptr[k + 1];
+      std::vector<int> level_of(c1 - c0, 0);
+      int64_t updates = 0, expect = 0;
+      for (int p = c0; p < dk; p++) {
+        const int j = s.csc_row[p];
+        expect += s.csc_colptr[j + 1] - s.diag_slot[j] - 1;
+      }
+      for (int l = w.lvl[i]; l < w.lvl[i + 1]; l++)
+        for (int t = w.lv_tgt[l]; t < w.lv_tgt[l + 1]; t++) {
+          const int slot = w.tg_slot[t];
+          CHECK(slot >= c0 && slot < c1 && level_of[slot - c0] == 0, "wide target %d", slot);
+          level_of[slot - c0] = l - w.lvl[i] + 1;
+          int prev_p = -1;
+          for (int e = w.tg_pair[t]; e < w.tg_pair[t + 1]; e++) {
+            const int q = w.pr_q[e], p = w.pr_p[e];
+            CHECK(p >= c0 && p < dk && p > prev_p, "wide pair order %d", p);
+            CHECK(level_of[p - c0] < level_of[slot - c0], "wide pair level %d", p);
+            const int j = s.csc_row[p];
+            CHECK(q > s.diag_slot[j] && q < s.csc_colptr[j + 1] && s.csc_row[q] == s.csc_row[slot],
+                  "wide pair slot %d", q);
+            prev_p = p;
+            updates++;
+          }
+        }
+      CHECK(updates == expect, "wide column %d updates %lld of %lld", k, (long long)updates,
+            (long long)expect);
+    }
+  }
 }
 
 }  // namespace
@@ -121,7 +235,7 @@ int main(int argc, char** argv) {
   }
   for (int kind = -1; kind <= 3; kind++) {
     const LevelSet& ls = program_levels(s, kind);
-    for (int base : {8, 16, 24, 64, 1023}) {
+    for (int base : {8, 16, 24, 40, 64, 1023}) {
       std::vector<int> budget(ls.num_levels(), base);
       check_program(s, kind, budget);
       // The handle's rule: narrow levels get a wide budget.

@@ -305,6 +305,161 @@ def test_large_plants_fp32_refinement_vs_oracle(cuda, dims, preset, schedule):
         assert norm_err(x[:, k], x_ref) <= 1e-10, (k, sw[k])
 
 
+def block_batch(dims, S: int, seed0: int):
+    """A values [nnz_a, S] and b [n, S] of the reference-topology plant, one
+    seed (diode operating point) per scenario, same pattern."""
+    from phdthesis_albertojimenezruiz_gb300.plant import block_plant
+
+    cols = [block_plant(*dims, seed=seed0 + k) for k in range(S)]
+    return np.stack([c[2] for c in cols], 1), np.stack([c[3] for c in cols], 1)
+
+
+def block_ordering(tag: str):
+    """The reference's AMD ordering of the reference-topology plant (fixture)."""
+    from conftest import GOLDEN
+
+    with np.load(GOLDEN / "orderings" / "block_plant_amd.npz") as z:
+        return z[f"perm_{tag}"], int(z[f"nnz_lu_{tag}"]), int(z[f"u_levels_{tag}"])
+
+
+@pytest.mark.parametrize("schedule", [SCHED_LEVELS, SCHED_PERSISTENT])
+@pytest.mark.parametrize("S,max_locals", [(1, 8), (1, 40), (1, 0), (64, 8), (130, 16)])
+@pytest.mark.parametrize("name", ["block_1x20x20", "mesh_20x20", "random_300"])
+def test_wide_units_bit_exact(cuda, name, S, max_locals, schedule):
+    """Columns and rows too wide for the table run as WIDE program levels
+    (a block per unit: column-scheduled gather for the refactorization,
+    ordered block sums for the solves).  Small tables make many units wide;
+    FP64 factors and solutions stay bit-identical to the reference's
+    sequential GLU and substitution for every scenario, and the transposed
+    solve matches the oracle."""
+    import torch
+
+    g = load_golden(name)
+    s = Symbolic(g["rowptr"], g["colidx"], g["perm_amd"])
+    o = O.Port(g["rowptr"], g["colidx"], g["perm_amd"])
+    num = Numeric(s, S, FP64, schedule, max_locals=max_locals)
+    a = np.repeat(g["a"][:, None], S, axis=1)
+    num.scatter(dev(pad_cols(a, num.ld)))
+    num.refactor()
+    assert num.check()[0] == 0
+    lu = values_of(num, int(s.nnz_lu))[:, :S]
+    assert np.array_equal(lu, np.repeat(g["lu_seq"][:, None], S, axis=1))
+    b = np.repeat(to_perm(g, g["b"])[:, None], S, axis=1)
+    x = dev(pad_cols(b, num.ld))
+    num.solve(x)
+    xs = x.cpu().numpy().reshape(s.n, num.ld)[:, :S]
+    assert np.array_equal(xs, np.repeat(g["x_perm"][:, None], S, axis=1))
+    rng = np.random.default_rng(9)
+    bt = rng.uniform(-1, 1, s.n)
+    xt = dev(pad_cols(np.repeat(bt[:, None], S, axis=1), num.ld))
+    num.solve(xt, transpose=True)
+    torch.cuda.synchronize()
+    want = o.solve_transposed(g["lu_seq"], bt)
+    got = xt.cpu().numpy().reshape(s.n, num.ld)
+    for k in sorted({0, S - 1}):
+        assert np.array_equal(got[:, k], want), k
+
+
+@pytest.mark.parametrize("schedule", [SCHED_LEVELS, SCHED_PERSISTENT])
+@pytest.mark.parametrize("S", [1, 64])
+def test_reference_topology_plant_fp64(cuda, S, schedule):
+    """The reference's own plant topology (1 x 50 x 50 panels, strings between
+    shared bus nodes, internal diode nodes) with the reference's AMD ordering:
+    the analysis reproduces the reference's fill and level counts, the bus
+    columns and rows (2,500 entries) run as wide units, and FP64 factors and
+    solutions equal the oracle's (the reference's sequential arithmetic) bit
+    for bit."""
+    from phdthesis_albertojimenezruiz_gb300.plant import block_plant
+
+    perm, nnz_lu, u_levels = block_ordering("1x50x50")
+    a, b = block_batch((1, 50, 50), S, seed0=210)
+    rp, ci, _, _ = block_plant(1, 50, 50)
+    s = Symbolic(rp, ci, perm)
+    assert int(s.nnz_lu) == nnz_lu and s.info["u_levels"] == u_levels
+    o = O.Port(rp, ci, perm)
+    num = Numeric(s, S, FP64, schedule)
+    num.scatter(dev(pad_cols(a, num.ld)))
+    num.refactor()
+    assert num.check()[0] == 0
+    x = dev(pad_cols(b, num.ld))
+    num.solve(x, original=True)
+    x = x.cpu().numpy().reshape(s.n, num.ld)
+    lu = values_of(num, int(s.nnz_lu))
+    for k in sorted({0, S // 2, S - 1}):
+        lu_ref, x_ref = o.scatter_refactor_solve(a[:, k], b[:, k])
+        assert np.array_equal(lu[:, k], lu_ref), k
+        assert np.array_equal(x[:, k], x_ref), k
+
+
+@pytest.mark.parametrize("schedule", [SCHED_LEVELS, SCHED_PERSISTENT])
+def test_reference_topology_plant_fp32_refinement(cuda, schedule):
+    """FP32 factors (wide units included) + FP64 refinement on the
+    reference-topology plant: within 1e-10 of the oracle's FP64 solution."""
+    import torch
+
+    from phdthesis_albertojimenezruiz_gb300.plant import block_plant
+
+    perm, _, _ = block_ordering("1x50x50")
+    rp, ci, _, _ = block_plant(1, 50, 50)
+    s = Symbolic(rp, ci, perm)
+    o = O.Port(rp, ci, perm)
+    S = 64
+    a, b = block_batch((1, 50, 50), S, seed0=230)
+    num = Numeric(s, S, FP32, schedule)
+    a_dev = dev(pad_cols(a, num.ld))
+    b_dev = dev(pad_cols(b, num.ld))
+    num.scatter(a_dev)
+    num.refactor()
+    assert num.check()[0] == 0
+    x = torch.zeros_like(b_dev)
+    sweeps = torch.zeros(num.ld, dtype=torch.int32, device="cuda")
+    num.solve_refined(a_dev, b_dev, x, tol=1e-12, max_sweeps=30, sweeps=sweeps)
+    torch.cuda.synchronize()
+    sw = sweeps.cpu().numpy()[:S]
+    assert (sw > 0).all(), sw
+    x = x.cpu().numpy()
+    for k in (0, 31, 63):
+        _, x_ref = o.scatter_refactor_solve(a[:, k], b[:, k])
+        assert norm_err(x[:, k], x_ref) <= 1e-10, (k, sw[k])
+
+
+def test_group_with_wide_members(cuda):
+    """A size-class group whose members have WIDE levels: each member's wide
+    levels run as their own launches, the rest grouped; bit-identical to the
+    members alone."""
+    import torch
+
+    from phdthesis_albertojimenezruiz_gb300.glu import Group
+
+    names = ["block_1x20x20", "mesh_20x20", "plant_c1"]
+    members, refs, xs = [], [], []
+    for name in names:
+        g = load_golden(name)
+        s = Symbolic(g["rowptr"], g["colidx"], g["perm_amd"])
+        S = 64
+        a = np.repeat(g["a"][:, None], S, axis=1)
+        b = np.repeat(g["b"][:, None], S, axis=1)
+        alone = Numeric(s, S, FP64, SCHED_LEVELS, max_locals=8)
+        alone.scatter(dev(pad_cols(a, alone.ld)))
+        xa = dev(pad_cols(b, alone.ld))
+        alone.refactor()
+        alone.solve(xa, original=True)
+        torch.cuda.synchronize()
+        refs.append((values_of(alone, int(s.nnz_lu)), xa.cpu().numpy(), int(s.nnz_lu)))
+        grouped = Numeric(s, S, FP64, SCHED_LEVELS, max_locals=8)
+        grouped.scatter(dev(pad_cols(a, grouped.ld)))
+        members.append(grouped)
+        xs.append(dev(pad_cols(b, grouped.ld)))
+    grp = Group(members)
+    grp.refactor_solve(xs, original=True)
+    torch.cuda.synchronize()
+    for h, x, (lu_ref, x_ref, nnz) in zip(members, xs, refs):
+        assert h.check()[0] == 0
+        assert np.array_equal(values_of(h, nnz)[:, :64], lu_ref[:, :64])
+        assert np.array_equal(x.cpu().numpy().reshape(-1, h.ld)[:, :64],
+                              x_ref.reshape(-1, h.ld)[:, :64])
+
+
 @pytest.mark.parametrize("S,precision", [(1, FP64), (96, FP32), (64, FP64)])
 def test_autotune_picks_a_working_configuration(cuda, S, precision):
     from phdthesis_albertojimenezruiz_gb300.glu import autotune
