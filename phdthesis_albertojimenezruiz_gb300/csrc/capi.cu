@@ -791,13 +791,13 @@ int pvglu_numeric_create_ex(const pvglu_symbolic* sym, int n_scenarios, int prec
     h->prog_wide_levels += prog.wide_levels;
   }
   // Wide levels of the persistent kernel use the warps' tables as scratch:
-  // at least the ordered-sum buffer (wide.cuh) must fit.
-  {
+  // at least the smallest ordered-sum buffers (wide.cuh) must fit.
+  if (h->prog_wide_levels > 0) {
     const size_t need = precision == PVGLU_FP64
-                            ? (h->batch ? pvglu::wide_scratch_bytes<double, true>(pvglu::kProgBlock)
-                                        : pvglu::wide_scratch_bytes<double, false>(pvglu::kProgBlock))
-                            : (h->batch ? pvglu::wide_scratch_bytes<float, true>(pvglu::kProgBlock)
-                                        : pvglu::wide_scratch_bytes<float, false>(pvglu::kProgBlock));
+                            ? (h->batch ? pvglu::wide_scratch_min<double, true>(pvglu::kProgBlock)
+                                        : pvglu::wide_scratch_min<double, false>(pvglu::kProgBlock))
+                            : (h->batch ? pvglu::wide_scratch_min<float, true>(pvglu::kProgBlock)
+                                        : pvglu::wide_scratch_min<float, false>(pvglu::kProgBlock));
     const size_t per_row = (size_t)pvglu::kProgWarps * group * elem;
     h->table_max = std::max<int>(h->table_max, (int)((need + per_row - 1) / per_row));
   }

@@ -14,10 +14,11 @@
 //     column: target slots whose U sources are final are computed together
 //     (a thread or, batched, a warp per target), one block barrier per column
 //     level;
-//   * a target or solve row with many updates: the block computes the
-//     products in parallel (each rounded as the sequential code rounds it)
-//     into shared memory and one thread (batched: one warp, a lane per two
-//     scenarios) subtracts them in order.
+//   * a target or solve row with many updates: warps of the block compute the
+//     products of a chunk in parallel (each rounded as the sequential code
+//     rounds it) into shared memory while one warp subtracts the previous
+//     chunk's products in order (batched: a lane per two scenarios; single:
+//     one lane).
 // Single scenario: the column is staged in shared memory when it fits.
 #pragma once
 #include <cuda_runtime.h>
@@ -37,74 +38,97 @@ __device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, 
 // together instead of one thread (warp) walking them.
 constexpr int kWideLong = 96;
 
-template <typename T>
-struct WideScalar {
-  using V = T;
-};
-
 // acc - sum_e a_e * b_e in the order e = 0 .. count-1, each product and each
-// difference rounded on its own: the block's threads (batched: warps, two
-// scenarios per lane) form the products of a chunk in shared memory, then
-// thread 0 (batched: warp 0) subtracts them in order.  `ab(e, a, b)` gives
+// difference rounded on its own.  Warps 1.. of the block form the products of
+// a chunk of entries in shared memory (batched: a warp per entry, two
+// scenarios per lane; single: a thread per entry) while warp 0 subtracts the
+// previous chunk's products in order (batched: every lane for its two
+// scenarios; single: lane 0), two chunk buffers in turn.  `ab(e, a, b)` gives
 // the operands of entry e (T, or Vec2<T> for the lane's two scenarios).
-// Returns the result in thread 0 (batched: in warp 0's lanes).  All threads
-// of the block must call it; scratch: at least blockDim.x * sizeof(T)
-// (batched: kWideChunkRows * 32 * sizeof(Vec2<T>)) bytes.
-constexpr int kWideChunkRows = 16;
+// Returns the result in warp 0 (single: in its lane 0).  All threads of the
+// block (at least two warps) must call it.  scratch: scratch_bytes of shared
+// memory, at least wide_scratch_min<T, BATCH>(blockDim.x).
+template <typename T, bool BATCH>
+__host__ __device__ constexpr int wide_row_bytes() {
+  return BATCH ? 32 * 2 * (int)sizeof(T) : (int)sizeof(T);
+}
+// Smallest scratch: one chunk row per producer thread (single) or warp
+// (batched), two buffers.
+template <typename T, bool BATCH>
+__host__ __device__ constexpr int wide_scratch_min(int threads) {
+  return 2 * (BATCH ? threads / 32 - 1 : threads - 32) * wide_row_bytes<T, BATCH>();
+}
+// Scratch the wide-level launches give the ordered sums: chunks of 64 rows
+// (batched) or 8 products per producer thread (single), two buffers.
+template <typename T, bool BATCH>
+__host__ __device__ constexpr int wide_scratch_bytes(int threads) {
+  return 2 * (BATCH ? 64 : 8 * (threads - 32)) * wide_row_bytes<T, BATCH>();
+}
 
 template <typename T, bool BATCH, typename AB>
 __device__ __forceinline__ typename std::conditional<BATCH, typename Vec2<T>::type, T>::type
 ordered_sub_block(typename std::conditional<BATCH, typename Vec2<T>::type, T>::type acc,
-                  int count, AB ab, unsigned char* scratch) {
-  const int tid = threadIdx.x;
-  if constexpr (!BATCH) {
-    T* prod = reinterpret_cast<T*>(scratch);
-    for (int base = 0; base < count; base += blockDim.x) {
-      const int e = base + tid;
-      if (e < count) {
-        T a, b;
-        ab(e, a, b);
-        prod[tid] = mul_rn(a, b);
+                  int count, AB ab, unsigned char* scratch, int scratch_bytes) {
+  using V = typename std::conditional<BATCH, typename Vec2<T>::type, T>::type;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int producers = BATCH ? (blockDim.x >> 5) - 1 : (int)blockDim.x - 32;
+  const int rb = wide_row_bytes<T, BATCH>();
+  int ch = scratch_bytes / (2 * rb);
+  ch = max(producers, ch - ch % producers);  // rows per chunk, a multiple of the producers
+  V* buf = reinterpret_cast<V*>(scratch);
+  const int stride = BATCH ? 32 : 1;          // buffer elements per row
+  const int nchunks = (count + ch - 1) / ch;
+  auto produce = [&](int c) {
+    V* out = buf + (size_t)(c & 1) * ch * stride;
+    const int base = c * ch;
+    const int me = BATCH ? warp - 1 : tid - 32;
+    // Up to four entries' operands in flight, then their products.
+    for (int r0 = me; r0 < ch; r0 += 4 * producers) {
+      V a[4], b[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const int e = base + r0 + u * producers;
+        if (r0 + u * producers < ch && e < count) ab(e, a[u], b[u]);
       }
-      __syncthreads();
-      if (tid == 0) {
-        const int m = min((int)blockDim.x, count - base);
-        for (int i = 0; i < m; i++) acc = sub_rn(acc, prod[i]);
-      }
-      __syncthreads();
-    }
-    return acc;
-  } else {
-    using V2 = typename Vec2<T>::type;
-    V2* prod = reinterpret_cast<V2*>(scratch);  // [kWideChunkRows][32]
-    const int lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
-    for (int base = 0; base < count; base += kWideChunkRows) {
-      for (int r = warp; r < kWideChunkRows && base + r < count; r += nw) {
-        V2 a, b;
-        ab(base + r, a, b);
-        V2 p;
-        p.x = mul_rn(a.x, b.x);
-        p.y = mul_rn(a.y, b.y);
-        prod[r * 32 + lane] = p;
-      }
-      __syncthreads();
-      if (warp == 0) {
-        const int m = min(kWideChunkRows, count - base);
-        for (int i = 0; i < m; i++) {
-          const V2 p = prod[i * 32 + lane];
-          acc.x = sub_rn(acc.x, p.x);
-          acc.y = sub_rn(acc.y, p.y);
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const int r = r0 + u * producers;
+        if (r < ch && base + r < count) {
+          V p;
+          if constexpr (BATCH) {
+            p.x = mul_rn(a[u].x, b[u].x);
+            p.y = mul_rn(a[u].y, b[u].y);
+          } else {
+            p = mul_rn(a[u], b[u]);
+          }
+          out[r * stride + (BATCH ? lane : 0)] = p;
         }
       }
-      __syncthreads();
     }
-    return acc;
+  };
+  if (warp > 0 && nchunks > 0) produce(0);
+  __syncthreads();
+  for (int c = 0; c < nchunks; c++) {
+    if (warp == 0) {
+      if (BATCH || lane == 0) {
+        const V* in = buf + (size_t)(c & 1) * ch * stride;
+        const int m = min(ch, count - c * ch);
+        for (int i = 0; i < m; i++) {
+          const V p = in[i * stride + (BATCH ? lane : 0)];
+          if constexpr (BATCH) {
+            acc.x = sub_rn(acc.x, p.x);
+            acc.y = sub_rn(acc.y, p.y);
+          } else {
+            acc = sub_rn(acc, p);
+          }
+        }
+      }
+    } else if (c + 1 < nchunks) {
+      produce(c + 1);
+    }
+    __syncthreads();
   }
-}
-
-template <typename T, bool BATCH>
-__host__ __device__ constexpr int wide_scratch_bytes(int threads) {
-  return BATCH ? kWideChunkRows * 32 * 2 * (int)sizeof(T) : threads * (int)sizeof(T);
+  return acc;
 }
 
 __device__ __forceinline__ double2 ldv2(const double* p) {
@@ -129,7 +153,7 @@ __device__ void wide_refactor(const ProgDev& P, const DevStruct& d, int w, int s
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int l_begin = __ldg(P.w_lvl + w), l_end = __ldg(P.w_lvl + w + 1);
   if constexpr (!BATCH) {
-    const int scratch = wide_scratch_bytes<T, false>(nthr);
+    const int scratch = min(wide_scratch_bytes<T, false>(nthr), smem_bytes);
     const bool staged = (int64_t)len * (int)sizeof(T) + scratch <= smem_bytes;
     T* col = reinterpret_cast<T*>(smem + scratch);
     unsigned char* scr = smem;
@@ -164,7 +188,7 @@ __device__ void wide_refactor(const ProgDev& P, const DevStruct& d, int w, int s
               a = ldv(v + __ldg(P.pr_q + e0 + e));
               b = get(__ldg(P.pr_p + e0 + e));
             },
-            scr);
+            scr, scratch);
         if (tid == 0) put(slot, acc);
         __syncthreads();
       }
@@ -228,7 +252,7 @@ __device__ void wide_refactor(const ProgDev& P, const DevStruct& d, int w, int s
               a = ldv2(row(__ldg(P.pr_q + e0 + e)));
               b = ldv2(row(__ldg(P.pr_p + e0 + e)));
             },
-            smem);
+            smem, smem_bytes);
         if (warp == 0) *reinterpret_cast<V2*>(tp) = acc;
         __syncthreads();
       }
@@ -259,7 +283,7 @@ __device__ void wide_refactor(const ProgDev& P, const DevStruct& d, int w, int s
 template <typename T, int KIND, bool BATCH>
 __device__ void wide_solve(const ProgDev& P, const DevStruct& d, int w, int s0,
                            const T* __restrict__ v, T* __restrict__ x, int ld,
-                           unsigned char* smem) {
+                           unsigned char* smem, int smem_bytes) {
   const int i = __ldg(P.w_unit + w);
   int b0, cnt, dg = -1;
   if (KIND == 0) {
@@ -300,7 +324,7 @@ __device__ void wide_solve(const ProgDev& P, const DevStruct& d, int w, int s0,
           a = ldv(v + slot);
           b = ldv(x + col);
         },
-        smem);
+        smem, smem_bytes);
     if (threadIdx.x == 0) {
       if (dg >= 0) acc = acc / ldv(v + dg);
       x[i] = acc;
@@ -318,7 +342,7 @@ __device__ void wide_solve(const ProgDev& P, const DevStruct& d, int w, int s0,
           a = ldv2(v + (int64_t)slot * ld + s);
           b = ldv2(x + (int64_t)col * ld + s);
         },
-        smem);
+        smem, smem_bytes);
     if ((threadIdx.x >> 5) == 0) {
       if (dg >= 0) {
         const V2 p = ldv2(v + (int64_t)dg * ld + s);
@@ -360,7 +384,7 @@ __device__ __forceinline__ void wide_run_level(const ProgDev& P, const DevStruct
     // The chain's single WIDE segment names the wide unit.
     const int w = __ldg(&P.seg[__ldg(P.chain_seg + cb + ci)].z);
     if (KIND < 0) wide_refactor<T, BATCH>(P, d, w, s0, v, ld, S, pivot_tol, st, smem, smem_bytes);
-    else wide_solve<T, (KIND < 0 ? 0 : KIND), BATCH>(P, d, w, s0, v, x, ld, smem);
+    else wide_solve<T, (KIND < 0 ? 0 : KIND), BATCH>(P, d, w, s0, v, x, ld, smem, smem_bytes);
   }
 }
 
