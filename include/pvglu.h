@@ -331,6 +331,39 @@ int pvglu_group_refactor_solve(pvglu_group* g, void* const* x, int flags, void* 
 int pvglu_autotune(const pvglu_symbolic* s, int n_scenarios, int precision,
                    int* best_max_locals, int* best_schedule, double* best_ms);
 
+/* Every execution choice of a numeric handle:
+ *   max_locals      chain-program table size (0: the default), as for
+ *                   pvglu_numeric_create_ex;
+ *   wide_threshold  units (columns of the refactorization, unknowns of a
+ *                   solve) needing more table rows than this run as wide
+ *                   units, a whole block each, even where they would fit the
+ *                   table (0: only those too wide for it).  The reference
+ *                   switches its launch shape to 32 threads per column once a
+ *                   level's longest row passes 64 entries
+ *                   (009_get_max_numbers_per_column.cpp:3-31,
+ *                   factorize_electrical_system_CUDA.cu:75-77);
+ *   merge_chains    1: units regrouped into execution levels one unit at a
+ *                   time (a unit joins the chain of its last dependency); 0:
+ *                   the level set's own levels and chains, merged a whole
+ *                   level at a time as the reference does
+ *                   (007_convert_dependencies_in_levels.cpp:89-210);
+ *   schedule        PVGLU_SCHED_*. */
+typedef struct {
+  int max_locals;
+  int wide_threshold;
+  int merge_chains;
+  int schedule;
+} pvglu_tuning;
+int pvglu_numeric_create_tuned(const pvglu_symbolic* s, int n_scenarios, int precision,
+                               const pvglu_tuning* t, pvglu_numeric** out);
+/* The autotuner over all of pvglu_tuning: table sizes x schedules, and, where
+ * they change the handle's programs, chain merging on and off and a wide
+ * threshold at half the table.  Synchronous; allocates and frees temporary
+ * handles.  best receives the fastest combination, best_ms its time per
+ * scatter + refactor + solve.  No counterpart in the reference. */
+int pvglu_autotune_ex(const pvglu_symbolic* s, int n_scenarios, int precision,
+                      pvglu_tuning* best, double* best_ms);
+
 /* ---------------- failure-path self-test --------------------------------- */
 
 /* Runs one bounded grid barrier that waits for one block more than it

@@ -38,6 +38,11 @@ class SymbolicInfo(C.Structure):
     ]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("max_locals", C.c_int), ("wide_threshold", C.c_int),
+                ("merge_chains", C.c_int), ("schedule", C.c_int)]
+
+
 class NumericInfo(C.Structure):
     _fields_ = [
         ("program_levels", C.c_int), ("wide_levels", C.c_int), ("wide_units", C.c_int),
@@ -97,6 +102,8 @@ _SIGS = {
     "pvglu_solve_refined": ([_P, _P, _P, _P, C.c_double, _I, _P, _P], _I),
     "pvglu_selftest_barrier_timeout": ([_I, C.c_longlong, _IP, _IP], _I),
     "pvglu_autotune": ([_P, _I, _I, _IP, _IP, _DP], _I),
+    "pvglu_autotune_ex": ([_P, _I, _I, _P, _DP], _I),
+    "pvglu_numeric_create_tuned": ([_P, _I, _I, _P, _P], _I),
     "pvglu_group_create": ([_P, _I, C.POINTER(_P)], _I),
     "pvglu_group_destroy": ([_P], _I),
     "pvglu_group_refactor_solve": ([_P, _P, _I, _P], _I),

@@ -564,10 +564,20 @@ int pvglu_numeric_create(const pvglu_symbolic* sym, int n_scenarios, int precisi
 
 int pvglu_numeric_create_ex(const pvglu_symbolic* sym, int n_scenarios, int precision,
                             int max_locals, pvglu_numeric** out) {
-  if (!sym || !out || n_scenarios <= 0 ||
-      (precision != PVGLU_FP64 && precision != PVGLU_FP32) || max_locals < 0 ||
-      max_locals > pvglu::kMaxLocals)
+  const pvglu_tuning t{max_locals, 0, 1, PVGLU_SCHED_LEVELS};
+  return pvglu_numeric_create_tuned(sym, n_scenarios, precision, &t, out);
+}
+
+int pvglu_numeric_create_tuned(const pvglu_symbolic* sym, int n_scenarios, int precision,
+                               const pvglu_tuning* tuning, pvglu_numeric** out) {
+  if (!sym || !out || !tuning || n_scenarios <= 0 ||
+      (precision != PVGLU_FP64 && precision != PVGLU_FP32) || tuning->max_locals < 0 ||
+      tuning->max_locals > pvglu::kMaxLocals || tuning->wide_threshold < 0 ||
+      (tuning->merge_chains != 0 && tuning->merge_chains != 1) ||
+      (tuning->schedule != PVGLU_SCHED_LEVELS && tuning->schedule != PVGLU_SCHED_PERSISTENT &&
+       tuning->schedule != PVGLU_SCHED_THREAD_CHAIN))
     return fail(PVGLU_ERR_BAD_ARG, "bad numeric_create arguments");
+  const int max_locals = tuning->max_locals;
   if (max_locals > 0 && max_locals < 8)
     return fail(PVGLU_ERR_BAD_ARG, "max_locals must be 0 (default) or >= 8");
   *out = nullptr;
@@ -730,14 +740,13 @@ int pvglu_numeric_create_ex(const pvglu_symbolic* sym, int n_scenarios, int prec
   h->table_max = 0;
   for (int ph = 0; ph < 5; ph++) {
     pvglu::ChainProgram prog;
-    const pvglu::LevelSet& ls = pvglu::program_levels(s, ph - 1);
-    std::vector<int> budget(ls.num_levels(), h->max_locals);
-    for (int lv = 0; lv < ls.num_levels(); lv++) {
-      const int64_t items = (int64_t)(ls.start_levels[lv + 1] - ls.start_levels[lv]) * groups;
-      if (items <= (int64_t)h->sm_count * pvglu::kProgWarps)
-        budget[lv] = std::max(h->max_locals, wide);
-    }
-    pvglu::build_chain_program(s, ph - 1, budget, prog);
+    pvglu::ProgramOptions opt;
+    opt.max_locals = h->max_locals;
+    opt.wide_locals = wide;
+    opt.narrow_chains = (int)((int64_t)h->sm_count * pvglu::kProgWarps / groups);
+    opt.merge = tuning->merge_chains != 0;
+    opt.wide_threshold = tuning->wide_threshold;
+    pvglu::build_chain_program(s, ph - 1, opt, prog);
     h->prog_level_ml[ph] = prog.level_max_locals;
     h->table_max = std::max(h->table_max, prog.max_locals);
     std::vector<int4> seg(prog.seg.size()), ops(prog.ops.size() / 4), carry(prog.seg.size());
@@ -823,6 +832,11 @@ int pvglu_numeric_create_ex(const pvglu_symbolic* sym, int n_scenarios, int prec
     delete h;
     return fail(PVGLU_ERR_CUDA, "cannot configure the chain-program kernels");
   }
+  if (tuning->schedule == PVGLU_SCHED_PERSISTENT && h->prog_grid <= 0) {
+    delete h;
+    return fail(PVGLU_ERR_CUDA, "cooperative launch unavailable on this device");
+  }
+  h->schedule = tuning->schedule;
   *out = h;
   return PVGLU_OK;
 }
@@ -1358,11 +1372,14 @@ int pvglu_group_refactor_solve(pvglu_group* g, void* const* x, int flags, void* 
                          : group_run<float, false>(g, x, flags, st));
 }
 
-int pvglu_autotune(const pvglu_symbolic* sym, int n_scenarios, int precision,
-                   int* best_max_locals, int* best_schedule, double* best_ms) {
-  if (!sym || n_scenarios <= 0 || !best_max_locals || !best_schedule ||
-      (precision != PVGLU_FP64 && precision != PVGLU_FP32))
-    return fail(PVGLU_ERR_BAD_ARG, "bad autotune arguments");
+}  // extern "C"
+
+namespace {
+
+// Times scatter + refactor + solve of every candidate tuning on stand-in
+// values and returns the fastest (autotuner core).
+int autotune_over(const pvglu_symbolic* sym, int n_scenarios, int precision,
+                  const std::vector<pvglu_tuning>& cands, pvglu_tuning* best_t, double* best_ms) {
   const auto& s = sym->s;
   const int ld = n_scenarios == 1 ? 1 : ((n_scenarios + 63) / 64) * 64;
   // Row-diagonally-dominant values (diagonal n + 1, every other entry -1):
@@ -1377,42 +1394,34 @@ int pvglu_autotune(const pvglu_symbolic* sym, int n_scenarios, int precision,
     for (int k = 0; k < ld; k++) ah[(size_t)p * ld + k] = a1[p];
   double* ad = nullptr;
   if (upload(ah, &ad)) return fail(PVGLU_ERR_NO_MEMORY, "autotune buffers");
-  std::vector<int> cands;
-  if (ld == 1) cands = {0, 256, 64};
-  else if (precision == PVGLU_FP32) cands = {16, 24, 32, 48, 64};
-  else cands = {16, 24, 32, 40, 56};
-  const int scheds[2] = {PVGLU_SCHED_LEVELS, PVGLU_SCHED_PERSISTENT};
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   double best = 1e300;
-  int bml = 0, bs = PVGLU_SCHED_LEVELS;
+  pvglu_tuning bt{};
   const size_t xbytes = (size_t)s.n * ld * (precision == PVGLU_FP64 ? 8 : 4);
   void* xw = nullptr;
-  int rc = cudaMalloc(&xw, xbytes) == cudaSuccess ? PVGLU_OK : PVGLU_ERR_NO_MEMORY;
+  const int rc = cudaMalloc(&xw, xbytes) == cudaSuccess ? PVGLU_OK : PVGLU_ERR_NO_MEMORY;
   for (size_t ci = 0; !rc && ci < cands.size(); ci++) {
     pvglu_numeric* h = nullptr;
-    if (pvglu_numeric_create_ex(sym, n_scenarios, precision, cands[ci], &h)) continue;
-    for (int sc : scheds) {
-      if (pvglu_numeric_set_schedule(h, sc)) continue;
-      float total = 0.f;
-      bool ok = true;
-      for (int rep = 0; rep < 4 && ok; rep++) {
-        cudaMemsetAsync(xw, 0, xbytes, nullptr);
-        cudaEventRecord(e0, nullptr);
-        ok = pvglu_scatter(h, ad, nullptr) == PVGLU_OK &&
-             pvglu_refactor_solve(h, xw, 0, nullptr) == PVGLU_OK;
-        cudaEventRecord(e1, nullptr);
-        if (cudaEventSynchronize(e1) != cudaSuccess) ok = false;
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, e0, e1);
-        if (rep > 0) total += ms;  // the first repetition warms up
-      }
-      if (ok && total / 3 < best) {
-        best = total / 3;
-        bml = h->max_locals;
-        bs = sc;
-      }
+    if (pvglu_numeric_create_tuned(sym, n_scenarios, precision, &cands[ci], &h)) continue;
+    float total = 0.f;
+    bool ok = true;
+    for (int rep = 0; rep < 4 && ok; rep++) {
+      cudaMemsetAsync(xw, 0, xbytes, nullptr);
+      cudaEventRecord(e0, nullptr);
+      ok = pvglu_scatter(h, ad, nullptr) == PVGLU_OK &&
+           pvglu_refactor_solve(h, xw, 0, nullptr) == PVGLU_OK;
+      cudaEventRecord(e1, nullptr);
+      if (cudaEventSynchronize(e1) != cudaSuccess) ok = false;
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (rep > 0) total += ms;  // the first repetition warms up
+    }
+    if (ok && total / 3 < best) {
+      best = total / 3;
+      bt = cands[ci];
+      bt.max_locals = h->max_locals;
     }
     int code = 0, col = 0, scn = 0;
     pvglu_numeric_check(h, nullptr, &code, &col, &scn);
@@ -1424,10 +1433,81 @@ int pvglu_autotune(const pvglu_symbolic* sym, int n_scenarios, int precision,
   cudaEventDestroy(e1);
   if (rc) return fail(rc, "autotune allocation failed");
   if (best >= 1e300) return fail(PVGLU_ERR_CUDA, "no autotune candidate ran");
-  *best_max_locals = bml;
-  *best_schedule = bs;
+  *best_t = bt;
   if (best_ms) *best_ms = best;
   return PVGLU_OK;
+}
+
+std::vector<int> table_candidates(int ld, int precision) {
+  if (ld == 1) return {0, 256, 64};
+  if (precision == PVGLU_FP32) return {16, 24, 32, 48, 64};
+  return {16, 24, 32, 40, 56};
+}
+
+// Programs of the refactorization and the two solves under `opt`: levels,
+// chains and wide units, to tell whether an option changes anything.
+std::vector<int> program_shape(const pvglu::Symbolic& s, const pvglu::ProgramOptions& opt) {
+  std::vector<int> shape;
+  for (int kind = -1; kind <= 1; kind++) {
+    pvglu::ChainProgram pr;
+    pvglu::build_chain_program(s, kind, opt, pr);
+    shape.insert(shape.end(), pr.level_chain.begin(), pr.level_chain.end());
+    shape.insert(shape.end(), pr.chain_unit.begin(), pr.chain_unit.end());
+    shape.push_back(pr.wide_units);
+  }
+  return shape;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pvglu_autotune(const pvglu_symbolic* sym, int n_scenarios, int precision,
+                   int* best_max_locals, int* best_schedule, double* best_ms) {
+  if (!sym || n_scenarios <= 0 || !best_max_locals || !best_schedule ||
+      (precision != PVGLU_FP64 && precision != PVGLU_FP32))
+    return fail(PVGLU_ERR_BAD_ARG, "bad autotune arguments");
+  const int ld = n_scenarios == 1 ? 1 : ((n_scenarios + 63) / 64) * 64;
+  std::vector<pvglu_tuning> cands;
+  for (const int ml : table_candidates(ld, precision))
+    for (const int sc : {PVGLU_SCHED_LEVELS, PVGLU_SCHED_PERSISTENT})
+      cands.push_back(pvglu_tuning{ml, 0, 1, sc});
+  pvglu_tuning bt{};
+  const int rc = autotune_over(sym, n_scenarios, precision, cands, &bt, best_ms);
+  if (rc) return rc;
+  *best_max_locals = bt.max_locals;
+  *best_schedule = bt.schedule;
+  return PVGLU_OK;
+}
+
+int pvglu_autotune_ex(const pvglu_symbolic* sym, int n_scenarios, int precision,
+                      pvglu_tuning* best, double* best_ms) {
+  if (!sym || n_scenarios <= 0 || !best || (precision != PVGLU_FP64 && precision != PVGLU_FP32))
+    return fail(PVGLU_ERR_BAD_ARG, "bad autotune arguments");
+  const auto& s = sym->s;
+  const int ld = n_scenarios == 1 ? 1 : ((n_scenarios + 63) / 64) * 64;
+  std::vector<pvglu_tuning> cands;
+  for (const int ml : table_candidates(ld, precision)) {
+    const int table = ml > 0 ? ml : (ld == 1 ? pvglu::kMaxLocals
+                                             : (precision == PVGLU_FP32 ? 64 : 40));
+    pvglu::ProgramOptions o;
+    o.max_locals = table;
+    const std::vector<int> base = program_shape(s, o);
+    o.merge = false;
+    const bool merge_matters = program_shape(s, o) != base;
+    o.merge = true;
+    o.wide_threshold = table / 2;
+    const bool wide_matters = program_shape(s, o) != base;
+    for (const int merge : {1, 0}) {
+      if (merge == 0 && !merge_matters) continue;
+      for (const int wt : {0, table / 2}) {
+        if (wt > 0 && !wide_matters) continue;
+        for (const int sc : {PVGLU_SCHED_LEVELS, PVGLU_SCHED_PERSISTENT})
+          cands.push_back(pvglu_tuning{ml, wt, merge, sc});
+      }
+    }
+  }
+  return autotune_over(sym, n_scenarios, precision, cands, best, best_ms);
 }
 
 int pvglu_selftest_barrier_timeout(int blocks, long long max_spins, int* status_code,

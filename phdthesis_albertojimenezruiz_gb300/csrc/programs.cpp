@@ -170,9 +170,23 @@ void emit_unit(const Symbolic& s, int kind, int u, Table& t) {
 
 const LevelSet& program_levels(const Symbolic& s, int kind) { return level_set(s, kind); }
 
+void unit_deps(const Symbolic& s, int kind, int u, std::vector<int>& deps) {
+  deps.clear();
+  if (kind == -1 || kind == 2) {  // rows of column u's U part
+    for (int p = s.csc_colptr[u]; p < s.diag_slot[u]; p++) deps.push_back(s.csc_row[p]);
+  } else if (kind == 0) {
+    for (int e = s.lrow_ptr[u]; e < s.lrow_ptr[u + 1]; e++) deps.push_back(s.lrow_col[e]);
+  } else if (kind == 1) {
+    for (int e = s.urow_ptr[u]; e < s.urow_ptr[u + 1]; e++) deps.push_back(s.urow_col[e]);
+  } else {  // rows of column u's L part
+    for (int q = s.diag_slot[u] + 1; q < s.csc_colptr[u + 1]; q++) deps.push_back(s.csc_row[q]);
+  }
+}
+
 void build_chain_program(const Symbolic& s, int kind, int max_locals, ChainProgram& out) {
-  build_chain_program(s, kind, std::vector<int>(level_set(s, kind).num_levels(), max_locals),
-                      out);
+  ProgramOptions opt;
+  opt.max_locals = max_locals;
+  build_chain_program(s, kind, opt, out);
 }
 
 namespace {
@@ -217,7 +231,50 @@ void plan_wide_column(const Symbolic& s, int k, WidePlan& w) {
 
 }  // namespace
 
-void build_chain_program(const Symbolic& s, int kind, const std::vector<int>& level_max_locals,
+namespace {
+
+// Execution levels (see programs.hpp): every unit extends the chain that
+// holds all of its dependencies of the highest level, when that chain's last
+// unit is one of them, and starts a new chain one level above them
+// otherwise.  Extending never delays a unit (it had to wait for that last
+// unit anyway) and never makes another chain wait.
+void execution_levels(const Symbolic& s, int kind, const LevelSet& ls,
+                      std::vector<std::vector<std::vector<int>>>& exec) {
+  std::vector<int> lvl(s.n, -1), chain_of(s.n, -1), deps;
+  std::vector<int> tail, chain_pos;  // per chain (global numbers)
+  for (int k = 0; k < (int)ls.columns.size(); k++) {
+    const int u = ls.columns[k];
+    unit_deps(s, kind, u, deps);
+    int m = -1;
+    for (const int d : deps) m = std::max(m, lvl[d]);
+    int c = -1;
+    bool one_chain = true, has_tail = false;
+    for (const int d : deps) {
+      if (lvl[d] != m) continue;
+      if (c < 0) c = chain_of[d];
+      else if (chain_of[d] != c) one_chain = false;
+      if (tail[chain_of[d]] == d) has_tail = true;
+    }
+    if (m >= 0 && one_chain && has_tail) {
+      exec[m][chain_pos[c]].push_back(u);
+      tail[c] = u;
+      chain_of[u] = c;
+      lvl[u] = m;
+      continue;
+    }
+    const int lv = m + 1;
+    if ((int)exec.size() <= lv) exec.resize(lv + 1);
+    chain_of[u] = (int)tail.size();
+    tail.push_back(u);
+    chain_pos.push_back((int)exec[lv].size());
+    exec[lv].push_back(std::vector<int>{u});
+    lvl[u] = lv;
+  }
+}
+
+}  // namespace
+
+void build_chain_program(const Symbolic& s, int kind, const ProgramOptions& opt,
                          ChainProgram& out) {
   out = ChainProgram();
   out.kind = kind;
@@ -226,27 +283,42 @@ void build_chain_program(const Symbolic& s, int kind, const std::vector<int>& le
   Table t;
   t.init(s.n, s.nnz_lu);
 
-  // 1. Program levels: each level of the level set cut around its wide units.
+  // 0. Execution levels (levels -> chains -> units).
+  std::vector<std::vector<std::vector<int>>> exec;
+  if (!opt.merge) {
+    for (int lv = 0; lv < ls.num_levels(); lv++) {
+      exec.emplace_back();
+      for (int c = ls.start_levels[lv]; c < ls.start_levels[lv + 1]; c++)
+        exec.back().emplace_back(ls.columns.begin() + ls.start_chains[c],
+                                 ls.columns.begin() + ls.start_chains[c + 1]);
+    }
+  } else {
+    execution_levels(s, kind, ls, exec);
+  }
+
+  // 1. Program levels: each execution level cut around its wide units.
   struct PLevel {
     int src;
     bool wide;
-    int budget;
+    int budget, wide_at;
     std::vector<std::vector<int>> chains;
   };
   std::vector<PLevel> plv;
-  for (int lv = 0; lv < ls.num_levels(); lv++) {
-    const int budget = std::min(level_max_locals[lv], kMaxLocals);
+  for (int lv = 0; lv < (int)exec.size(); lv++) {
+    const bool narrow = (int)exec[lv].size() <= opt.narrow_chains;
+    const int budget =
+        std::min(narrow ? std::max(opt.max_locals, opt.wide_locals) : opt.max_locals, kMaxLocals);
+    const int wide_at = opt.wide_threshold > 0 ? std::min(budget, opt.wide_threshold) : budget;
     std::vector<std::vector<std::vector<int>>> phase;  // phase -> chains -> units
     auto put = [&](int ph, std::vector<int>&& chain) {
       if ((int)phase.size() <= ph) phase.resize(ph + 1);
       phase[ph].push_back(std::move(chain));
     };
-    for (int c = ls.start_levels[lv]; c < ls.start_levels[lv + 1]; c++) {
+    for (const auto& chain : exec[lv]) {
       int ph = 0;
       std::vector<int> cur;
-      for (int k = ls.start_chains[c]; k < ls.start_chains[c + 1]; k++) {
-        const int u = ls.columns[k];
-        if (new_locals(s, kind, u, t) > budget) {
+      for (const int u : chain) {
+        if (new_locals(s, kind, u, t) > wide_at) {
           if (ph % 2 == 0) {
             if (!cur.empty()) put(ph, std::move(cur));
             cur.clear();
@@ -263,7 +335,8 @@ void build_chain_program(const Symbolic& s, int kind, const std::vector<int>& le
       if (!cur.empty()) put(ph, std::move(cur));
     }
     for (int ph = 0; ph < (int)phase.size(); ph++)
-      if (!phase[ph].empty()) plv.push_back(PLevel{lv, ph % 2 == 1, budget, std::move(phase[ph])});
+      if (!phase[ph].empty())
+        plv.push_back(PLevel{lv, ph % 2 == 1, budget, wide_at, std::move(phase[ph])});
   }
 
   // 2. Emit the program levels.
@@ -335,6 +408,8 @@ void build_chain_program(const Symbolic& s, int kind, const std::vector<int>& le
   for (const PLevel& L : plv) {
     out.level_chain.push_back((int)out.chain_seg.size());
     out.level_src.push_back(L.src);
+    out.level_budget.push_back(L.budget);
+    out.level_wide_at.push_back(L.wide_at);
     out.level_wide.push_back(L.wide ? 1 : 0);
     out.level_max_locals.push_back(L.wide ? 1 : std::min(L.budget, kMaxLocals));
     if (L.wide) out.wide_levels++;

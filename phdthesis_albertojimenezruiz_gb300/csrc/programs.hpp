@@ -54,14 +54,30 @@ struct Segment {
   int carry[kMaxCarry] = {-1, -1, -1, -1};
 };
 
-// Program levels.  Every level of the reference's level set is executed as
-// one or more program levels: a chain is cut around each unit too wide for
-// the level's table budget, the pieces before the first wide unit form the
-// first program level, the wide units of that position the next one (a
-// WIDE level, one chain per wide unit), the pieces between the first and
-// second wide unit the next, and so on.  Chains of one level are
-// independent and each keeps its order, so the program levels in sequence
-// compute what the level computes.
+// Execution levels.  The units (columns of the refactorization, unknowns
+// of a solve) are regrouped from the reference's level set into execution
+// levels of chains: walking the units in the level set's order (a
+// topological order), let m be the highest execution level of a unit's
+// dependencies; when all its dependencies at level m lie in one chain whose
+// last unit is one of them, the unit extends that chain; otherwise it starts
+// a new chain at level m + 1 (level 0 without dependencies).  Every
+// dependency of a unit is then in an earlier level or earlier in its own
+// chain, so any execution that runs the levels in order and each chain in
+// order computes, unit for unit, the same arithmetic.  Extending a chain
+// never delays a unit (it waits for that chain's last unit in any order) and
+// never makes another chain wait.  The reference merges chains a whole basic
+// level at a time (007_convert_dependencies_in_levels.cpp:62-143): one unit
+// that cannot join keeps its whole level from merging.  The level set itself
+// (the symbolic arrays) is unchanged.
+//
+// Program levels.  Every execution level is executed as one or more program
+// levels: a chain is cut around each unit too wide for the level's table
+// budget, the pieces before the first wide unit form the first program
+// level, the wide units of that position the next one (a WIDE level, one
+// chain per wide unit), the pieces between the first and second wide unit
+// the next, and so on.  Chains of one level are independent and each keeps
+// its order, so the program levels in sequence compute what the level
+// computes.
 //
 // A wide refactor unit (column k) is executed in gather form, scheduled
 // inside the column: target slot t of column k receives
@@ -87,7 +103,9 @@ struct ChainProgram {
   std::vector<int> level_max_locals;  // [levels] table size of each program level: its
                                       // widest segment, at most the level's budget
   std::vector<int> level_chain;  // [levels + 1] -> chain index
-  std::vector<int> level_src;    // [levels] level of the level set it belongs to
+  std::vector<int> level_src;    // [levels] execution level it belongs to
+  std::vector<int> level_budget; // [levels] table budget of that execution level
+  std::vector<int> level_wide_at;  // [levels] units needing more rows than this are wide
   std::vector<char> level_wide;  // [levels] 1: a WIDE level
   std::vector<int> chain_seg;    // [chains + 1] -> segment index
   std::vector<int> chain_unit;   // [chains + 1] -> index into units
@@ -102,15 +120,28 @@ struct ChainProgram {
   int wide_levels = 0;
 };
 
+// Table budgets: max_locals values per table; an execution level with at
+// most narrow_chains chains gets max(max_locals, wide_locals) (levels with
+// few chains can afford a wide table: fewer segments, and the warps they
+// leave idle cost nothing).  A unit whose own table would exceed its level's
+// budget is a wide unit.  merge = false keeps the level set's levels and
+// chains as execution levels.
+struct ProgramOptions {
+  int max_locals = 64;
+  int wide_locals = 0;
+  int narrow_chains = 0;
+  bool merge = true;
+  // > 0: units needing more than this many table rows run as wide units
+  // even where they would fit the level's table (at most the budget).
+  int wide_threshold = 0;
+};
+
 // kind -1 uses s.lu; 0 s.l; 1 s.u; 2 s.lu; 3 s.lt.
-void build_chain_program(const Symbolic& s, int kind, int max_locals, ChainProgram& out);
-// As above with a table budget per level of the level set (levels with few
-// chains can afford a wide table: fewer segments, and the warps they leave
-// idle cost nothing).  A unit whose own table would exceed its level's
-// budget is a wide unit.
-void build_chain_program(const Symbolic& s, int kind, const std::vector<int>& level_max_locals,
+void build_chain_program(const Symbolic& s, int kind, const ProgramOptions& opt,
                          ChainProgram& out);
-// The level set a program kind walks.
+void build_chain_program(const Symbolic& s, int kind, int max_locals, ChainProgram& out);
+// The level set a program kind walks, and the units a unit depends on.
 const LevelSet& program_levels(const Symbolic& s, int kind);
+void unit_deps(const Symbolic& s, int kind, int u, std::vector<int>& deps);
 
 }  // namespace pvglu

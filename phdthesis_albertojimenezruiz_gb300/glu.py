@@ -103,12 +103,21 @@ class Numeric:
     """Device LU state for `n_scenarios` Jacobians sharing one `Symbolic`."""
 
     def __init__(self, sym: Symbolic, n_scenarios: int = 1, precision: int = N.FP64,
-                 schedule: int = N.SCHED_LEVELS, max_locals: int = 0):
+                 schedule: int = N.SCHED_LEVELS, max_locals: int = 0, tuning: dict | None = None):
+        """tuning (the dict of autotune_ex, pvglu_tuning's fields) overrides
+        schedule and max_locals."""
         self.sym = sym
         h = C.c_void_p()
-        N.check(N.lib().pvglu_numeric_create_ex(sym.handle, n_scenarios, precision,
-                                                int(max_locals), C.byref(h)),
-                "pvglu_numeric_create_ex")
+        if tuning is not None:
+            t = N.Tuning(**{f: int(tuning[f]) for f, _ in N.Tuning._fields_})
+            N.check(N.lib().pvglu_numeric_create_tuned(sym.handle, n_scenarios, precision,
+                                                       C.byref(t), C.byref(h)),
+                    "pvglu_numeric_create_tuned")
+            schedule = t.schedule
+        else:
+            N.check(N.lib().pvglu_numeric_create_ex(sym.handle, n_scenarios, precision,
+                                                    int(max_locals), C.byref(h)),
+                    "pvglu_numeric_create_ex")
         self.max_locals = N.lib().pvglu_numeric_max_locals(h)
         self.handle = h
         self.S = n_scenarios
@@ -261,6 +270,16 @@ def autotune(sym: Symbolic, n_scenarios: int, precision: int) -> tuple[int, int,
     N.check(N.lib().pvglu_autotune(sym.handle, int(n_scenarios), int(precision), C.byref(ml),
                                    C.byref(sc), C.byref(ms)), "pvglu_autotune")
     return ml.value, sc.value, ms.value
+
+
+def autotune_ex(sym: Symbolic, n_scenarios: int, precision: int) -> tuple[dict, float]:
+    """pvglu_autotune_ex: (tuning dict for Numeric(tuning=...), ms per
+    scatter+refactor+solve)."""
+    t = N.Tuning()
+    ms = C.c_double()
+    N.check(N.lib().pvglu_autotune_ex(sym.handle, int(n_scenarios), int(precision), C.byref(t),
+                                      C.byref(ms)), "pvglu_autotune_ex")
+    return {f: getattr(t, f) for f, _ in N.Tuning._fields_}, ms.value
 
 
 # Names of the reference's entry points, for callers porting a driver.

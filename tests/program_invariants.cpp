@@ -75,20 +75,24 @@ int unit_need(const Symbolic& s, int kind, int u) {
                (std::unique(vs.begin(), vs.end()) - vs.begin()));
 }
 
-void check_program(const Symbolic& s, int kind, const std::vector<int>& budget) {
+void check_program(const Symbolic& s, int kind, const ProgramOptions& opt) {
   ChainProgram pr;
-  build_chain_program(s, kind, budget, pr);
-  const LevelSet& ls = program_levels(s, kind);
+  build_chain_program(s, kind, opt, pr);
   const int nlev = (int)pr.level_chain.size() - 1;
+  CHECK((int)pr.level_wide_at.size() == nlev, "kind %d wide thresholds", kind);
+  for (int lv = 0; lv < nlev && (int)pr.level_wide_at.size() == nlev; lv++)
+    CHECK(pr.level_wide_at[lv] >= 1 && pr.level_wide_at[lv] <= pr.level_budget[lv] &&
+              (opt.wide_threshold <= 0 || pr.level_wide_at[lv] <= opt.wide_threshold),
+          "kind %d level %d wide threshold", kind, lv);
   CHECK((int)pr.level_src.size() == nlev && (int)pr.level_wide.size() == nlev &&
-            (int)pr.level_max_locals.size() == nlev,
+            (int)pr.level_max_locals.size() == nlev && (int)pr.level_budget.size() == nlev,
         "kind %d level arrays", kind);
   CHECK((int)pr.chain_seg.size() == pr.level_chain.back() + 1 &&
             (int)pr.chain_unit.size() == pr.level_chain.back() + 1,
         "kind %d chain arrays", kind);
-  // Every unit of the level set once, each chain's units in order, in the
-  // program levels of its own level.
-  std::vector<int> where_lv(s.n, -1), where_pos(s.n, -1);
+  // Every unit once; every dependency of a unit in an earlier program level
+  // or earlier in the unit's own chain.
+  std::vector<int> where_lv(s.n, -1), where_chain(s.n, -1), where_pos(s.n, -1);
   int pos = 0;
   for (int lv = 0; lv < nlev; lv++) {
     CHECK(lv == 0 || pr.level_src[lv] >= pr.level_src[lv - 1], "kind %d level order", kind);
@@ -96,23 +100,30 @@ void check_program(const Symbolic& s, int kind, const std::vector<int>& budget) 
       for (int k = pr.chain_unit[c]; k < pr.chain_unit[c + 1]; k++) {
         const int u = pr.units[k];
         CHECK(u >= 0 && u < s.n && where_lv[u] < 0, "kind %d unit %d twice", kind, u);
-        where_lv[u] = pr.level_src[lv];
+        where_lv[u] = lv;
+        where_chain[u] = c;
         where_pos[u] = pos++;
       }
   }
   CHECK(pos == s.n, "kind %d units %d of %d", kind, pos, s.n);
-  for (int lv = 0; lv < ls.num_levels(); lv++)
-    for (int c = ls.start_levels[lv]; c < ls.start_levels[lv + 1]; c++)
-      for (int k = ls.start_chains[c]; k < ls.start_chains[c + 1]; k++) {
-        const int u = ls.columns[k];
-        CHECK(where_lv[u] == lv, "kind %d unit %d in level %d", kind, u, where_lv[u]);
-        if (k > ls.start_chains[c])
-          CHECK(where_pos[ls.columns[k - 1]] < where_pos[u], "kind %d chain order at %d", kind,
-                u);
-      }
+  std::vector<int> deps;
+  for (int u = 0; u < s.n && pos == s.n; u++) {
+    unit_deps(s, kind, u, deps);
+    for (const int dd : deps)
+      CHECK(where_lv[dd] < where_lv[u] ||
+                (where_chain[dd] == where_chain[u] && where_pos[dd] < where_pos[u]),
+            "kind %d unit %d runs before its dependency %d", kind, u, dd);
+  }
+  auto budget_of = [&](int lv) {
+    const int b = pr.level_budget[lv];
+    CHECK(b == std::min(opt.max_locals, kMaxLocals) ||
+              b == std::min(std::max(opt.max_locals, opt.wide_locals), kMaxLocals),
+          "kind %d level %d budget %d", kind, lv, b);
+    return b;
+  };
   for (int lv = 0; lv < nlev; lv++) {
     const int table = pr.level_max_locals[lv];
-    const int bud = std::min(budget[pr.level_src[lv]], kMaxLocals);
+    const int bud = budget_of(lv);
     CHECK(table >= 1 && table <= bud && table <= pr.max_locals,
           "kind %d level %d table %d budget %d", kind, lv, table, bud);
     for (int c = pr.level_chain[lv]; c < pr.level_chain[lv + 1]; c++) {
@@ -126,11 +137,11 @@ void check_program(const Symbolic& s, int kind, const std::vector<int>& budget) 
         CHECK(sg.n_load < 0 && sg.op_begin >= 0 && sg.op_begin < (int)pr.wide.unit.size() &&
                   pr.wide.unit[sg.op_begin] == u,
               "kind %d wide segment of unit %d", kind, u);
-        CHECK(unit_need(s, kind, u) > bud, "kind %d unit %d is not wide", kind, u);
+        CHECK(unit_need(s, kind, u) > pr.level_wide_at[lv], "kind %d unit %d is not wide", kind, u);
         continue;
       }
       for (int k = pr.chain_unit[c]; k < pr.chain_unit[c + 1]; k++)
-        CHECK(unit_need(s, kind, pr.units[k]) <= bud, "kind %d unit %d too wide", kind,
+        CHECK(unit_need(s, kind, pr.units[k]) <= pr.level_wide_at[lv], "kind %d unit %d too wide", kind,
               pr.units[k]);
       int prev_nl = -1;  // table rows of the previous segment of the chain (-1: none)
       for (int g = pr.chain_seg[c]; g < pr.chain_seg[c + 1]; g++) {
@@ -234,14 +245,20 @@ int main(int argc, char** argv) {
     return 2;
   }
   for (int kind = -1; kind <= 3; kind++) {
-    const LevelSet& ls = program_levels(s, kind);
     for (int base : {8, 16, 24, 40, 64, 1023}) {
-      std::vector<int> budget(ls.num_levels(), base);
-      check_program(s, kind, budget);
-      // The handle's rule: narrow levels get a wide budget.
-      for (int lv = 0; lv < ls.num_levels(); lv++)
-        if (ls.start_levels[lv + 1] - ls.start_levels[lv] <= 64) budget[lv] = 226;
-      check_program(s, kind, budget);
+      for (int merge = 0; merge < 2; merge++) {
+        ProgramOptions opt;
+        opt.max_locals = base;
+        opt.merge = merge != 0;
+        check_program(s, kind, opt);
+        // The handle's rule: narrow levels get a wide budget.
+        opt.wide_locals = 226;
+        opt.narrow_chains = 64;
+        check_program(s, kind, opt);
+        // Units over half the table run as wide units.
+        opt.wide_threshold = base / 2;
+        check_program(s, kind, opt);
+      }
     }
   }
   std::printf("%s n=%d nnz_lu=%lld\n", fails ? "FAILED" : "ok", s.n, (long long)s.nnz_lu);

@@ -460,6 +460,57 @@ def test_group_with_wide_members(cuda):
                               x_ref.reshape(-1, h.ld)[:, :64])
 
 
+@pytest.mark.parametrize("schedule", [SCHED_LEVELS, SCHED_PERSISTENT])
+@pytest.mark.parametrize("merge,wide", [(1, 0), (0, 0), (1, 12), (0, 12)])
+@pytest.mark.parametrize("S", [1, 64])
+@pytest.mark.parametrize("name", ["block_1x20x20", "mesh_20x20"])
+def test_every_tuning_bit_exact(cuda, name, S, merge, wide, schedule):
+    """Every execution choice of pvglu_tuning (execution levels merged per
+    unit or the level set's own, wide units at half the table or only where
+    needed, each schedule) gives the reference's sequential FP64 factors and
+    solution bit for bit."""
+    g = load_golden(name)
+    s = Symbolic(g["rowptr"], g["colidx"], g["perm_amd"])
+    t = {"max_locals": 24, "wide_threshold": wide, "merge_chains": merge, "schedule": schedule}
+    num = Numeric(s, S, FP64, tuning=t)
+    a = np.repeat(g["a"][:, None], S, axis=1)
+    num.scatter(dev(pad_cols(a, num.ld)))
+    x = dev(pad_cols(np.repeat(to_perm(g, g["b"])[:, None], S, axis=1), num.ld))
+    num.refactor_solve(x)
+    assert num.check()[0] == 0
+    lu = values_of(num, int(s.nnz_lu))[:, :S]
+    assert np.array_equal(lu, np.repeat(g["lu_seq"][:, None], S, axis=1))
+    xs = x.cpu().numpy().reshape(s.n, num.ld)[:, :S]
+    assert np.array_equal(xs, np.repeat(g["x_perm"][:, None], S, axis=1))
+
+
+@pytest.mark.parametrize("name,S,precision", [("block_1x20x20", 1, FP64),
+                                              ("block_1x20x20", 130, FP64),
+                                              ("plant_c1", 64, FP32)])
+def test_autotune_ex_picks_a_working_tuning(cuda, name, S, precision):
+    from phdthesis_albertojimenezruiz_gb300.glu import autotune_ex
+
+    g = load_golden(name)
+    s = Symbolic(g["rowptr"], g["colidx"], g["perm_amd"])
+    t, ms = autotune_ex(s, S, precision)
+    assert ms > 0 and t["schedule"] in (SCHED_LEVELS, SCHED_PERSISTENT)
+    assert t["merge_chains"] in (0, 1) and t["wide_threshold"] >= 0
+    num = Numeric(s, S, precision, tuning=t)
+    a = np.repeat(g["a"][:, None], S, axis=1)
+    num.scatter(dev(pad_cols(a, num.ld)))
+    x = dev(pad_cols(np.repeat(to_perm(g, g["b"])[:, None], S, axis=1), num.ld),
+            np.float64 if precision == FP64 else np.float32)
+    num.refactor_solve(x)
+    assert num.check()[0] == 0
+    x = x.cpu().numpy().reshape(s.n, num.ld).astype(np.float64)
+    want = g["x_perm"]
+    for k in sorted({0, S - 1}):
+        if precision == FP64:
+            assert np.array_equal(x[:, k], want)
+        else:
+            assert norm_err(x[:, k], want) <= 1e-4
+
+
 @pytest.mark.parametrize("S,precision", [(1, FP64), (96, FP32), (64, FP64)])
 def test_autotune_picks_a_working_configuration(cuda, S, precision):
     from phdthesis_albertojimenezruiz_gb300.glu import autotune
