@@ -260,16 +260,19 @@ def newton_section(p, sym, stream, S: int, seed0: int, fd_check: bool = True,
     g_to_iph = p.info["iph_stc"] / 1000.0
     prec = FP64 if precision == "fp64" else FP32
 
-    from phdthesis_albertojimenezruiz_gb300.glu import autotune
+    from phdthesis_albertojimenezruiz_gb300.glu import autotune_ex
 
     tuned = {}
 
     def setup(g_cols, tol_ir=1e-12):
         count = g_cols.shape[1]
         if count not in tuned:
-            tuned[count] = fixed_tuning or autotune(sym, count, prec)[:2]
-        ml, sc = tuned[count]
-        num = Numeric(sym, count, prec, sc, max_locals=ml)
+            if fixed_tuning:
+                tuned[count] = {"max_locals": fixed_tuning[0], "wide_threshold": 0,
+                                "merge_chains": 1, "schedule": fixed_tuning[1]}
+            else:
+                tuned[count] = autotune_ex(sym, count, prec)[0]
+        num = Numeric(sym, count, prec, tuning=tuned[count])
         nw = Newton.for_plant(num, p)
         ld = num.ld
         iph = np.zeros((p.n_panels, ld))
@@ -310,7 +313,7 @@ def newton_section(p, sym, stream, S: int, seed0: int, fd_check: bool = True,
     lu = "FP64 LU" if prec == FP64 else "FP32 LU + FP64 refinement"
     res = {"workload": f"plant_{DIMS[0]}x{DIMS[1]}x{DIMS[2]}, {S} scenarios, {lu}, "
                        "gmin stages 100..0.05,off, tol 1e-6*n",
-           "scenarios": S, "tuning": {"max_locals": tuned[S][0], "schedule": tuned[S][1]},
+           "scenarios": S, "tuning": tuned[S],
            "iterations_min": int(it.min()), "iterations_max": int(it.max()),
            "converged": int((out == 0).sum()), "bodies_launched": bodies, "cuda_graph": graph,
            "newton_ms": newton_ms,
@@ -453,15 +456,15 @@ def config3_newton(dims, counts) -> dict:
     import torch
 
     from phdthesis_albertojimenezruiz_gb300 import FP64, Newton, Numeric, Plant, Symbolic
-    from phdthesis_albertojimenezruiz_gb300.glu import autotune
+    from phdthesis_albertojimenezruiz_gb300.glu import autotune_ex
 
     dev = torch.device("cuda", torch.cuda.current_device())
     lanes = []
     for k, (d, S) in enumerate(zip(dims, counts)):
         p = Plant(*d)
         sym = Symbolic(p.rowptr, p.colidx)
-        ml, sc, _ = autotune(sym, S, FP64)
-        num = Numeric(sym, S, FP64, sc, max_locals=ml)
+        tt, _ = autotune_ex(sym, S, FP64)
+        num = Numeric(sym, S, FP64, tuning=tt)
         nw = Newton.for_plant(num, p)
         ld = num.ld
         g = np.stack([p.irradiance(seed=7000 + 1000 * k + s, preset="c3") for s in range(S)], 1)
@@ -470,7 +473,7 @@ def config3_newton(dims, counts) -> dict:
         v0 = torch.from_numpy(_pad(np.repeat(p.flat_start()[:, None], S, 1), ld)).to(dev)
         nw.set_iph(iph, stream=st)
         lanes.append({"plant": "x".join(map(str, d)), "p": p, "num": num, "nw": nw, "st": st,
-                      "v0": v0, "tuning": {"max_locals": ml, "schedule": sc}})
+                      "v0": v0, "tuning": tt})
 
     def run(lane):
         lane["nw"].set_voltages(lane["v0"], stream=lane["st"])
@@ -506,7 +509,7 @@ def config4_section(stream, steps: int) -> dict:
     import torch
 
     from phdthesis_albertojimenezruiz_gb300 import FP32, FP64, Numeric, Symbolic
-    from phdthesis_albertojimenezruiz_gb300.glu import autotune
+    from phdthesis_albertojimenezruiz_gb300.glu import autotune_ex
 
     S, ld = 64, 64
     p, a, b = _plant_batch((200, 24, 28), S, ld, 9000, "c4")
@@ -515,8 +518,8 @@ def config4_section(stream, steps: int) -> dict:
     a_d = torch.from_numpy(a).to(dev)
     b_d = torch.from_numpy(b).to(dev)
     x_d = torch.zeros_like(b_d)
-    ml, sc, _ = autotune(sym, S, FP32)
-    num = Numeric(sym, S, FP32, sc, max_locals=ml)
+    t4, _ = autotune_ex(sym, S, FP32)
+    num = Numeric(sym, S, FP32, tuning=t4)
     sweeps = torch.zeros(ld, dtype=torch.int32, device=dev)
 
     def step():
@@ -549,7 +552,7 @@ def config4_section(stream, steps: int) -> dict:
     return {"workload": f"plant_200x24x28 ({sym.n} unknowns, nnz_lu {int(sym.nnz_lu)}), 64 "
                         "scenarios, scatter + FP32 refactor + FP64-refined solve",
             "value": S / (ms / 1000.0), "unit": UNIT, "ms_per_step": ms,
-            "tuning": {"max_locals": ml, "schedule": sc}, "sweeps_max": int(sw.max()),
+            "tuning": t4, "sweeps_max": int(sw.max()),
             "not_converged": int((sw <= 0).sum()), "max_rel_err_vs_gpu_fp64": err,
             "per_scenario": {"sweeps": [int(v) for v in sw],
                              "rel_err_vs_oracle_fp64": [float(f"{e:.2e}") for e in errs]},
@@ -570,21 +573,21 @@ def newton_iterates_section(stream, S: int, steps: int) -> dict:
 
     from phdthesis_albertojimenezruiz_gb300 import (FP32, FP64, GMIN_STAGES, Newton, Numeric,
                                                     Plant, Symbolic)
-    from phdthesis_albertojimenezruiz_gb300.glu import autotune
+    from phdthesis_albertojimenezruiz_gb300.glu import autotune_ex
 
     p = Plant(*DIMS)
     sym = Symbolic(p.rowptr, p.colidx)
     ld = ((S + 63) // 64) * 64
     dev = torch.device("cuda", torch.cuda.current_device())
     g = np.stack([p.irradiance(seed=1000 + s, preset="c2") for s in range(S)], axis=1)
-    ml64, sc64, _ = autotune(sym, S, FP64)
-    ml32, sc32, _ = autotune(sym, S, FP32)
-    nt = Numeric(sym, S, FP64, sc64, max_locals=ml64)
+    t64, _ = autotune_ex(sym, S, FP64)
+    t32, _ = autotune_ex(sym, S, FP32)
+    nt = Numeric(sym, S, FP64, tuning=t64)
     nw = Newton.for_plant(nt, p)
     nw.set_iph(torch.from_numpy(_pad(p.iph(g), ld)).to(dev))
     v0 = torch.from_numpy(_pad(np.repeat(p.flat_start()[:, None], S, 1), ld)).to(dev)
-    n32 = Numeric(sym, S, FP32, sc32, max_locals=ml32)
-    n64 = Numeric(sym, S, FP64, sc64, max_locals=ml64)
+    n32 = Numeric(sym, S, FP32, tuning=t32)
+    n64 = Numeric(sym, S, FP64, tuning=t64)
     sweeps = torch.zeros(ld, dtype=torch.int32, device=dev)
     out = []
     for j in (0, 2, 5, 8, 10, 11):
@@ -647,7 +650,7 @@ def wide_section(stream, steps: int, S: int = 512) -> dict:
     from oracle import oracle as O
     from phdthesis_albertojimenezruiz_gb300 import (FP32, FP64, SCHED_LEVELS, SCHED_PERSISTENT,
                                                     SCHED_THREAD_CHAIN, Numeric, Symbolic)
-    from phdthesis_albertojimenezruiz_gb300.glu import autotune
+    from phdthesis_albertojimenezruiz_gb300.glu import autotune_ex
     from phdthesis_albertojimenezruiz_gb300.plant import block_plant
 
     dev = torch.device("cuda", torch.cuda.current_device())
@@ -698,8 +701,8 @@ def wide_section(stream, steps: int, S: int = 512) -> dict:
         b[:, :S] = np.tile(b_few, (1, reps))[:, :S]
         a_d = torch.from_numpy(a).to(dev)
         b_d = torch.from_numpy(b).to(dev)
-        ml64, sc64, _ = autotune(sym, S, FP64)
-        n64 = Numeric(sym, S, FP64, sc64, max_locals=ml64)
+        t64, _ = autotune_ex(sym, S, FP64)
+        n64 = Numeric(sym, S, FP64, tuning=t64)
         x64 = torch.empty_like(b_d)
 
         def step64():
@@ -714,11 +717,11 @@ def wide_section(stream, steps: int, S: int = 512) -> dict:
         byt = (bm["scatter"] + bm["refactor"] + bm["solve"]) * S
         res["batched_fp64"] = {
             "value": S / (ms64 / 1000.0), "unit": UNIT, "ms_per_step": ms64,
-            "tuning": {"max_locals": ml64, "schedule": sc64}, "program_info": n64.info,
+            "tuning": t64, "program_info": n64.info,
             "hbm": {"bytes_per_step": byt, "achieved_gbs": byt / (ms64 / 1000.0) / 1e9,
                     "frac": byt / (ms64 / 1000.0) / 1e9 / peak if peak else None}}
-        ml32, sc32, _ = autotune(sym, S, FP32)
-        n32 = Numeric(sym, S, FP32, sc32, max_locals=ml32)
+        t32, _ = autotune_ex(sym, S, FP32)
+        n32 = Numeric(sym, S, FP32, tuning=t32)
         x32 = torch.zeros_like(b_d)
         sweeps = torch.zeros(ld, dtype=torch.int32, device=dev)
 
@@ -735,7 +738,7 @@ def wide_section(stream, steps: int, S: int = 512) -> dict:
         xa, xb = x32.cpu().numpy()[:, :S], x64.cpu().numpy()[:, :S]
         res["batched_fp32ir"] = {
             "value": S / (ms32 / 1000.0), "unit": UNIT, "ms_per_step": ms32,
-            "tuning": {"max_locals": ml32, "schedule": sc32},
+            "tuning": t32,
             "sweeps_max": int(sw.max()), "not_converged": int((sw <= 0).sum()),
             "max_rel_err_vs_fp64": float(np.max(np.abs(xa - xb).max(axis=0) /
                                                 np.abs(xb).max(axis=0)))}
@@ -757,10 +760,10 @@ def wide_section(stream, steps: int, S: int = 512) -> dict:
 
 def _newton_handle(p, sym, S: int, precision, tol_ir: float = 1e-12):
     from phdthesis_albertojimenezruiz_gb300 import FP32, Newton, Numeric
-    from phdthesis_albertojimenezruiz_gb300.glu import autotune
+    from phdthesis_albertojimenezruiz_gb300.glu import autotune_ex
 
-    ml, sc, _ = autotune(sym, S, precision)
-    num = Numeric(sym, S, precision, sc, max_locals=ml)
+    t, _ = autotune_ex(sym, S, precision)
+    num = Numeric(sym, S, precision, tuning=t)
     nw = Newton.for_plant(num, p)
     if precision == FP32:
         nw.set_refinement(tol_ir, IR_MAX_SWEEPS)
@@ -1156,10 +1159,14 @@ def main() -> None:
                  "schedule": SCHED_LEVELS if args.schedule == "levels" else SCHED_PERSISTENT,
                  "source": "flags"}
     else:
-        ml, sc, tms = autotune(sym, S, FP32)
-        tuned = {"max_locals": ml, "schedule": sc, "ms_scatter_refactor_solve": tms,
-                 "source": "pvglu_autotune"}
-    num = Numeric(sym, S, FP32, tuned["schedule"], max_locals=tuned["max_locals"])
+        from phdthesis_albertojimenezruiz_gb300.glu import autotune_ex
+
+        tt, tms = autotune_ex(sym, S, FP32)
+        tuned = dict(tt, ms_scatter_refactor_solve=tms, source="pvglu_autotune_ex")
+    num = Numeric(sym, S, FP32, tuned["schedule"], max_locals=tuned["max_locals"],
+                  tuning={k: tuned.get(k, d) for k, d in (("max_locals", 0), ("wide_threshold", 0),
+                                                          ("merge_chains", 1),
+                                                          ("schedule", SCHED_LEVELS))})
     persistent = tuned["schedule"] == SCHED_PERSISTENT
     assert num.ld == ld
 
@@ -1282,8 +1289,10 @@ def main() -> None:
     # The same 512-scenario batch in FP64 (scatter + FP64 refactor + solve,
     # autotuned), which splits the headline's gain over the plain path into
     # the part that batching gives and the part that FP32 + refinement adds.
-    ml64, sc64, _ = autotune(sym, S, FP64)
-    num64b = Numeric(sym, S, FP64, sc64, max_locals=ml64)
+    from phdthesis_albertojimenezruiz_gb300.glu import autotune_ex
+
+    t64, _ = autotune_ex(sym, S, FP64)
+    num64b = Numeric(sym, S, FP64, tuning=t64)
     x64b = torch.empty_like(b_d)
 
     def fp64_step():
@@ -1295,7 +1304,7 @@ def main() -> None:
         fp64_step()
     ms64 = _time_ms(fp64_step, stream, args.steps)
     batched_fp64 = {"value": S / (ms64 / 1000.0), "unit": UNIT, "ms_per_step": ms64,
-                    "tuning": {"max_locals": ml64, "schedule": sc64},
+                    "tuning": t64,
                     "max_rel_err_vs_fp32ir": float(np.max(
                         np.abs(x64b.cpu().numpy()[:, :S] - xa).max(axis=0) /
                         np.abs(xa).max(axis=0)))}
