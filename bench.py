@@ -43,6 +43,20 @@ RESIDUAL_TRAFFIC_512 = 735.3e6  # bytes, the same for one k_residual_rows launch
 IR_MAX_SWEEPS = 6
 
 
+_TUNED: dict = {}
+
+
+def _autotune(sym, S: int, precision: int):
+    """pvglu_autotune_ex, once per pattern, scenario count and precision in
+    this process (several sections use the same handles)."""
+    from phdthesis_albertojimenezruiz_gb300.glu import autotune_ex
+
+    key = (sym.n, int(sym.nnz_a), int(sym.nnz_lu), sym.info["lu_levels"], S, precision)
+    if key not in _TUNED:
+        _TUNED[key] = autotune_ex(sym, S, precision)
+    return dict(_TUNED[key][0]), _TUNED[key][1]
+
+
 def _peaks() -> dict:
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -174,7 +188,7 @@ def make_inputs(S: int, ld: int, seed0: int = 1000):
     from phdthesis_albertojimenezruiz_gb300 import Plant
 
     p = Plant(*DIMS)
-    g = np.stack([p.irradiance(seed=seed0 + s, preset="c2") for s in range(S)], axis=1)
+    g = p.irradiance_batch([seed0 + s for s in range(S)], preset="c2")
     v = np.repeat(p.flat_start()[:, None], S, axis=1)
     a, b = p.companion_batch(g, v, ld=ld)
     return p, a, b
@@ -184,7 +198,7 @@ def make_conductances(p, S: int, ld: int, seed0: int = 1000) -> np.ndarray:
     """Companion conductance of every panel for the scenarios of make_inputs
     (same seeds, flat start): [n_panels, ld], columns past S zero.  With the
     plant's stamps they give the same Jacobians as make_inputs' A values."""
-    g = np.stack([p.irradiance(seed=seed0 + s, preset="c2") for s in range(S)], axis=1)
+    g = p.irradiance_batch([seed0 + s for s in range(S)], preset="c2")
     v = np.repeat(p.flat_start()[:, None], S, axis=1)
     _, didv = p.panel_iv(p.iph(g).ravel(), v.ravel())
     out = np.zeros((p.n_panels, ld))
@@ -269,9 +283,9 @@ def newton_section(p, sym, stream, S: int, seed0: int, fd_check: bool = True,
         if count not in tuned:
             if fixed_tuning:
                 tuned[count] = {"max_locals": fixed_tuning[0], "wide_threshold": 0,
-                                "merge_chains": 1, "schedule": fixed_tuning[1]}
+                                "merge_chains": 0, "schedule": fixed_tuning[1]}
             else:
-                tuned[count] = autotune_ex(sym, count, prec)[0]
+                tuned[count] = _autotune(sym,count, prec)[0]
         num = Numeric(sym, count, prec, tuning=tuned[count])
         nw = Newton.for_plant(num, p)
         ld = num.ld
@@ -286,7 +300,7 @@ def newton_section(p, sym, stream, S: int, seed0: int, fd_check: bool = True,
             nw.set_refinement(tol_ir, IR_MAX_SWEEPS)
         return num, nw, v0_d, iph_d
 
-    g = np.stack([p.irradiance(seed=seed0 + s, preset="c2") for s in range(S)], axis=1)
+    g = p.irradiance_batch([seed0 + s for s in range(S)], preset="c2")
     num, nw, v0_d, _ = setup(g)
     dpdx = np.zeros((p.n, num.ld))
     dpdx[p.inv_current, :S] = -p.v_mppt
@@ -354,7 +368,7 @@ def _plant_batch(dims, S: int, ld: int, seed0: int, preset: str):
     from phdthesis_albertojimenezruiz_gb300 import Plant
 
     p = Plant(*dims)
-    g = np.stack([p.irradiance(seed=seed0 + s, preset=preset) for s in range(S)], axis=1)
+    g = p.irradiance_batch([seed0 + s for s in range(S)], preset=preset)
     v = np.repeat(p.flat_start()[:, None], S, axis=1)
     a, b = p.companion_batch(g, v, ld=ld)
     return p, a, b
@@ -463,11 +477,11 @@ def config3_newton(dims, counts) -> dict:
     for k, (d, S) in enumerate(zip(dims, counts)):
         p = Plant(*d)
         sym = Symbolic(p.rowptr, p.colidx)
-        tt, _ = autotune_ex(sym, S, FP64)
+        tt, _ = _autotune(sym,S, FP64)
         num = Numeric(sym, S, FP64, tuning=tt)
         nw = Newton.for_plant(num, p)
         ld = num.ld
-        g = np.stack([p.irradiance(seed=7000 + 1000 * k + s, preset="c3") for s in range(S)], 1)
+        g = p.irradiance_batch([7000 + 1000 * k + s for s in range(S)], preset="c3")
         st = torch.cuda.Stream()
         iph = torch.from_numpy(_pad(p.iph(g), ld)).to(dev)
         v0 = torch.from_numpy(_pad(np.repeat(p.flat_start()[:, None], S, 1), ld)).to(dev)
@@ -518,7 +532,7 @@ def config4_section(stream, steps: int) -> dict:
     a_d = torch.from_numpy(a).to(dev)
     b_d = torch.from_numpy(b).to(dev)
     x_d = torch.zeros_like(b_d)
-    t4, _ = autotune_ex(sym, S, FP32)
+    t4, _ = _autotune(sym,S, FP32)
     num = Numeric(sym, S, FP32, tuning=t4)
     sweeps = torch.zeros(ld, dtype=torch.int32, device=dev)
 
@@ -579,9 +593,9 @@ def newton_iterates_section(stream, S: int, steps: int) -> dict:
     sym = Symbolic(p.rowptr, p.colidx)
     ld = ((S + 63) // 64) * 64
     dev = torch.device("cuda", torch.cuda.current_device())
-    g = np.stack([p.irradiance(seed=1000 + s, preset="c2") for s in range(S)], axis=1)
-    t64, _ = autotune_ex(sym, S, FP64)
-    t32, _ = autotune_ex(sym, S, FP32)
+    g = p.irradiance_batch([1000 + s for s in range(S)], preset="c2")
+    t64, _ = _autotune(sym,S, FP64)
+    t32, _ = _autotune(sym,S, FP32)
     nt = Numeric(sym, S, FP64, tuning=t64)
     nw = Newton.for_plant(nt, p)
     nw.set_iph(torch.from_numpy(_pad(p.iph(g), ld)).to(dev))
@@ -633,7 +647,7 @@ def newton_iterates_section(stream, S: int, steps: int) -> dict:
                         "refinement tolerance 1e-12, up to 40 sweeps", "stages": out}
 
 
-def wide_section(stream, steps: int, S: int = 512) -> dict:
+def wide_section(stream, steps: int, S: int = 512, patterns: str = "ref,mesh,random") -> dict:
     """Patterns whose factors have columns and rows too wide for a chain-
     program table (run as WIDE program levels, a block per unit): the
     reference's own plant topology with the reference's AMD ordering (7
@@ -658,12 +672,16 @@ def wide_section(stream, steps: int, S: int = 512) -> dict:
     with np.load(ROOT / "tests" / "golden" / "orderings" / "block_plant_amd.npz") as z:
         perm7 = z["perm_7x50x50"]
     cases = []
-    cols = [block_plant(7, 50, 50, seed=300 + k) for k in range(8)]
-    cases.append(("reference_topology_7x50x50 (reference AMD ordering)", cols[0][0], cols[0][1],
-                  perm7, np.stack([c[2] for c in cols], 1), np.stack([c[3] for c in cols], 1)))
-    for name in ("mesh_30x30", "random_1500"):
-        rp, ci, a, b = M.CASES[name]()
-        cases.append((name, rp, ci, None, a[:, None], b[:, None]))
+    wanted = {p.strip() for p in patterns.split(",")}
+    if "ref" in wanted:
+        cols = [block_plant(7, 50, 50, seed=300 + k) for k in range(8)]
+        cases.append(("reference_topology_7x50x50 (reference AMD ordering)", cols[0][0],
+                      cols[0][1], perm7, np.stack([c[2] for c in cols], 1),
+                      np.stack([c[3] for c in cols], 1)))
+    for key, name in (("mesh", "mesh_30x30"), ("random", "random_1500")):
+        if key in wanted:
+            rp, ci, a, b = M.CASES[name]()
+            cases.append((name, rp, ci, None, a[:, None], b[:, None]))
     out = []
     for name, rp, ci, perm, a_few, b_few in cases:
         sym = Symbolic(rp, ci, perm)
@@ -701,7 +719,7 @@ def wide_section(stream, steps: int, S: int = 512) -> dict:
         b[:, :S] = np.tile(b_few, (1, reps))[:, :S]
         a_d = torch.from_numpy(a).to(dev)
         b_d = torch.from_numpy(b).to(dev)
-        t64, _ = autotune_ex(sym, S, FP64)
+        t64, _ = _autotune(sym,S, FP64)
         n64 = Numeric(sym, S, FP64, tuning=t64)
         x64 = torch.empty_like(b_d)
 
@@ -720,7 +738,7 @@ def wide_section(stream, steps: int, S: int = 512) -> dict:
             "tuning": t64, "program_info": n64.info,
             "hbm": {"bytes_per_step": byt, "achieved_gbs": byt / (ms64 / 1000.0) / 1e9,
                     "frac": byt / (ms64 / 1000.0) / 1e9 / peak if peak else None}}
-        t32, _ = autotune_ex(sym, S, FP32)
+        t32, _ = _autotune(sym,S, FP32)
         n32 = Numeric(sym, S, FP32, tuning=t32)
         x32 = torch.zeros_like(b_d)
         sweeps = torch.zeros(ld, dtype=torch.int32, device=dev)
@@ -762,7 +780,7 @@ def _newton_handle(p, sym, S: int, precision, tol_ir: float = 1e-12):
     from phdthesis_albertojimenezruiz_gb300 import FP32, Newton, Numeric
     from phdthesis_albertojimenezruiz_gb300.glu import autotune_ex
 
-    t, _ = autotune_ex(sym, S, precision)
+    t, _ = _autotune(sym,S, precision)
     num = Numeric(sym, S, precision, tuning=t)
     nw = Newton.for_plant(num, p)
     if precision == FP32:
@@ -1009,21 +1027,25 @@ class _VoltView:
 def run_configs(args, stream) -> dict:
     wanted = {c.strip() for c in args.configs.split(",") if c.strip()}
     out = {}
-    if "1" in wanted:
-        out["config1"] = config1_section()
-    if "2" in wanted:
-        out["config2"] = config2_section()
-    if "3" in wanted:
-        out["config3"] = config3_section(stream, max(5, args.steps))
-    if "4" in wanted:
-        out["config4"] = config4_section(stream, max(5, args.steps))
-    if "5" in wanted:
-        out["config5_fd"] = {m: config5_fd_section(m) for m in ("fp64", "fp32")}
-    if "i" in wanted:
-        out["fp32ir_on_newton_iterates"] = newton_iterates_section(stream, args.scenarios,
-                                                                   max(5, args.steps))
-    if "w" in wanted:
-        out["wide_units"] = wide_section(stream, max(5, args.steps), args.scenarios)
+    seconds = {}
+    sections = [
+        ("1", "config1", lambda: config1_section()),
+        ("2", "config2", lambda: config2_section()),
+        ("3", "config3", lambda: config3_section(stream, max(5, args.steps))),
+        ("4", "config4", lambda: config4_section(stream, max(5, args.steps))),
+        ("5", "config5_fd", lambda: {m: config5_fd_section(m) for m in ("fp64", "fp32")}),
+        ("i", "fp32ir_on_newton_iterates",
+         lambda: newton_iterates_section(stream, args.scenarios, max(5, args.steps))),
+        ("w", "wide_units",
+         lambda: wide_section(stream, max(5, args.steps), args.scenarios, args.wide_patterns)),
+    ]
+    for tag, key, fn in sections:
+        if tag in wanted:
+            t0 = time.perf_counter()
+            out[key] = fn()
+            seconds[key] = round(time.perf_counter() - t0, 1)
+    if seconds:
+        out["section_seconds"] = seconds
     return out
 
 
@@ -1094,6 +1116,9 @@ def main() -> None:
                          "i: FP32 + refinement vs FP64 on Newton-iterate Jacobians, "
                          "w: wide units on the reference's plant topology and fill-heavy "
                          "patterns; empty: none)")
+    ap.add_argument("--wide-patterns", default="ref",
+                    help="patterns of the wide-unit section (ref: the reference's plant topology, "
+                         "mesh: mesh_30x30, random: random_1500)")
     ap.add_argument("--only-configs", action="store_true",
                     help="run the --configs workloads alone (profiling runs)")
     ap.add_argument("--newton-max-locals", type=int, default=0,
@@ -1161,11 +1186,11 @@ def main() -> None:
     else:
         from phdthesis_albertojimenezruiz_gb300.glu import autotune_ex
 
-        tt, tms = autotune_ex(sym, S, FP32)
+        tt, tms = _autotune(sym,S, FP32)
         tuned = dict(tt, ms_scatter_refactor_solve=tms, source="pvglu_autotune_ex")
     num = Numeric(sym, S, FP32, tuned["schedule"], max_locals=tuned["max_locals"],
                   tuning={k: tuned.get(k, d) for k, d in (("max_locals", 0), ("wide_threshold", 0),
-                                                          ("merge_chains", 1),
+                                                          ("merge_chains", 0),
                                                           ("schedule", SCHED_LEVELS))})
     persistent = tuned["schedule"] == SCHED_PERSISTENT
     assert num.ld == ld
@@ -1291,7 +1316,7 @@ def main() -> None:
     # the part that batching gives and the part that FP32 + refinement adds.
     from phdthesis_albertojimenezruiz_gb300.glu import autotune_ex
 
-    t64, _ = autotune_ex(sym, S, FP64)
+    t64, _ = _autotune(sym,S, FP64)
     num64b = Numeric(sym, S, FP64, tuning=t64)
     x64b = torch.empty_like(b_d)
 

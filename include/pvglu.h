@@ -346,7 +346,10 @@ int pvglu_autotune(const pvglu_symbolic* s, int n_scenarios, int precision,
  *                   time (a unit joins the chain of its last dependency); 0:
  *                   the level set's own levels and chains, merged a whole
  *                   level at a time as the reference does
- *                   (007_convert_dependencies_in_levels.cpp:89-210);
+ *                   (007_convert_dependencies_in_levels.cpp:89-210), the
+ *                   choice of pvglu_numeric_create(_ex).  Regrouping removes
+ *                   levels on deep patterns but can lengthen the chains of a
+ *                   narrow level where no level is saved;
  *   schedule        PVGLU_SCHED_*. */
 typedef struct {
   int max_locals;

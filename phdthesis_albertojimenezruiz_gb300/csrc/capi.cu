@@ -564,7 +564,9 @@ int pvglu_numeric_create(const pvglu_symbolic* sym, int n_scenarios, int precisi
 
 int pvglu_numeric_create_ex(const pvglu_symbolic* sym, int n_scenarios, int precision,
                             int max_locals, pvglu_numeric** out) {
-  const pvglu_tuning t{max_locals, 0, 1, PVGLU_SCHED_LEVELS};
+  // The level set's own chains: regrouping per unit can lengthen a narrow
+  // level's chains without removing a level; the autotuner tries it.
+  const pvglu_tuning t{max_locals, 0, 0, PVGLU_SCHED_LEVELS};
   return pvglu_numeric_create_tuned(sym, n_scenarios, precision, &t, out);
 }
 
@@ -1406,6 +1408,7 @@ int autotune_over(const pvglu_symbolic* sym, int n_scenarios, int precision,
     pvglu_numeric* h = nullptr;
     if (pvglu_numeric_create_tuned(sym, n_scenarios, precision, &cands[ci], &h)) continue;
     float total = 0.f;
+    int timed = 0;
     bool ok = true;
     for (int rep = 0; rep < 4 && ok; rep++) {
       cudaMemsetAsync(xw, 0, xbytes, nullptr);
@@ -1416,10 +1419,15 @@ int autotune_over(const pvglu_symbolic* sym, int n_scenarios, int precision,
       if (cudaEventSynchronize(e1) != cudaSuccess) ok = false;
       float ms = 0.f;
       cudaEventElapsedTime(&ms, e0, e1);
-      if (rep > 0) total += ms;  // the first repetition warms up
+      if (rep > 0) {  // the first repetition warms up
+        total += ms;
+        timed++;
+        // A candidate already twice the best so far is not timed further.
+        if (ms > 2.0 * best) break;
+      }
     }
-    if (ok && total / 3 < best) {
-      best = total / 3;
+    if (ok && timed > 0 && total / timed < best) {
+      best = total / timed;
       bt = cands[ci];
       bt.max_locals = h->max_locals;
     }

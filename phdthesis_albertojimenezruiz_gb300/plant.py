@@ -187,6 +187,19 @@ class Plant:
                                                float(t), _ptr(g)), "pvglu_plant_irradiance")
         return g
 
+    def irradiance_batch(self, seeds, t: float = 0.0, preset: str = "c1") -> np.ndarray:
+        """`irradiance` of every seed, [n_panels, len(seeds)], computed on the
+        host's threads (the calls drop the GIL)."""
+        import os
+        from concurrent.futures import ThreadPoolExecutor
+
+        seeds = list(seeds)
+        out = np.empty((self.n_panels, len(seeds)))
+        with ThreadPoolExecutor(max_workers=os.cpu_count() or 1) as ex:
+            for k, g in enumerate(ex.map(lambda sd: self.irradiance(sd, t, preset), seeds)):
+                out[:, k] = g
+        return out
+
     def shadows(self, seed: int, preset: str = "c1") -> np.ndarray:
         """The seeded shadows of `irradiance(seed, t, preset)`: [count, 6] rows of
         (centre x, centre y, velocity x, velocity y, depth, sigma)."""
@@ -203,8 +216,23 @@ class Plant:
         v = np.ascontiguousarray(v, dtype=np.float64)
         cur = np.empty_like(v)
         didv = np.empty_like(v)
-        N.check(N.lib().pvglu_plant_panel_iv(self.handle, len(v), _ptr(iph), _ptr(v), _ptr(cur),
-                                             _ptr(didv)), "pvglu_plant_panel_iv")
+
+        def run(lo: int, hi: int) -> int:  # element range [lo, hi): the call drops the GIL
+            return N.lib().pvglu_plant_panel_iv(self.handle, hi - lo, _ptr(iph[lo:hi]),
+                                                _ptr(v[lo:hi]), _ptr(cur[lo:hi]),
+                                                _ptr(didv[lo:hi]))
+
+        chunk = 1 << 18
+        if len(v) <= chunk:
+            N.check(run(0, len(v)), "pvglu_plant_panel_iv")
+        else:
+            import os
+            from concurrent.futures import ThreadPoolExecutor
+
+            bounds = [(lo, min(lo + chunk, len(v))) for lo in range(0, len(v), chunk)]
+            with ThreadPoolExecutor(max_workers=os.cpu_count() or 1) as ex:
+                for rc in ex.map(lambda b: run(*b), bounds):
+                    N.check(rc, "pvglu_plant_panel_iv")
         return cur, didv
 
     def iph(self, g: np.ndarray) -> np.ndarray:
@@ -256,21 +284,28 @@ class Plant:
         panel's stamp (002b_sistema_electrico_base_matriz.cpp:198-202).
 
         Returns A values [nnz_a, ld] and b [n, ld] (columns past S zero)."""
+        import scipy.sparse as sp
+
         npan, S = g_irr.shape
         ld = ld or S
         cur, didv = self.panel_iv(self.iph(g_irr).ravel(), v_panel.ravel())
         gpan = (-didv).reshape(npan, S)
         ieq = (-cur).reshape(npan, S) - gpan * v_panel
-        counts = np.diff(self.contrib_ptr)
-        entry = np.repeat(np.arange(len(self.a_lin)), counts)
-        a = np.zeros((len(self.a_lin), ld))
-        a[:, :S] = self.a_lin[:, None]
+        if getattr(self, "_stamp_mats", None) is None:
+            # entry <- panel conductances, node <- panel currents
+            entry = np.repeat(np.arange(len(self.a_lin)), np.diff(self.contrib_ptr))
+            node = np.repeat(np.arange(self.n), np.diff(self.inc_ptr))
+            self._stamp_mats = (
+                sp.csr_matrix((self.contrib_sign.astype(np.float64), (entry, self.contrib_panel)),
+                              shape=(len(self.a_lin), npan)),
+                sp.csr_matrix((-self.inc_sign.astype(np.float64), (node, self.inc_panel)),
+                              shape=(self.n, npan)))
+        ma, mb = self._stamp_mats
         gst = gpan + gmin if gmin > 0 else gpan
-        np.add.at(a[:, :S], entry, self.contrib_sign[:, None] * gst[self.contrib_panel])
+        a = np.zeros((len(self.a_lin), ld))
+        a[:, :S] = self.a_lin[:, None] + ma @ gst
         b = np.zeros((self.n, ld))
-        b[:, :S] = self.b_lin[:, None]
-        node = np.repeat(np.arange(self.n), np.diff(self.inc_ptr))
-        np.add.at(b[:, :S], node, -self.inc_sign[:, None] * ieq[self.inc_panel])
+        b[:, :S] = self.b_lin[:, None] + mb @ ieq
         return a, b
 
     def __del__(self):
