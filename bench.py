@@ -647,7 +647,8 @@ def newton_iterates_section(stream, S: int, steps: int) -> dict:
                         "refinement tolerance 1e-12, up to 40 sweeps", "stages": out}
 
 
-def wide_section(stream, steps: int, S: int = 512, patterns: str = "ref,mesh,random") -> dict:
+def wide_section(stream, steps: int, S: int = 512, patterns: str = "ref,mesh,random",
+                 profile: bool = False) -> dict:
     """Patterns whose factors have columns and rows too wide for a chain-
     program table (run as WIDE program levels, a block per unit): the
     reference's own plant topology with the reference's AMD ordering (7
@@ -688,14 +689,16 @@ def wide_section(stream, steps: int, S: int = 512, patterns: str = "ref,mesh,ran
         n, nnz_a, nnz_lu = sym.n, int(sym.nnz_a), int(sym.nnz_lu)
         res = {"pattern": name, "n": n, "nnz_a": nnz_a, "nnz_lu": nnz_lu,
                "lu_levels": sym.info["lu_levels"], "u_levels": sym.info["u_levels"]}
-        # Single instance, FP64, every schedule.
+        # Single instance, FP64, every schedule (not in profiling runs, which
+        # time the batched FP64 step alone with the autotuner's choice for
+        # the reference topology fixed).
         a1 = torch.from_numpy(np.ascontiguousarray(a_few[:, 0])).to(dev)
         b1 = torch.from_numpy(np.ascontiguousarray(b_few[:, 0])).to(dev)
         x1 = b1.clone()
         single = {}
-        for sname, sched in (("thread_chain_levels", SCHED_THREAD_CHAIN),
-                             ("programs_levels", SCHED_LEVELS),
-                             ("programs_persistent", SCHED_PERSISTENT)):
+        for sname, sched in (() if profile else (("thread_chain_levels", SCHED_THREAD_CHAIN),
+                                                  ("programs_levels", SCHED_LEVELS),
+                                                  ("programs_persistent", SCHED_PERSISTENT))):
             one = Numeric(sym, 1, FP64, sched)
 
             def plain_step():
@@ -719,7 +722,11 @@ def wide_section(stream, steps: int, S: int = 512, patterns: str = "ref,mesh,ran
         b[:, :S] = np.tile(b_few, (1, reps))[:, :S]
         a_d = torch.from_numpy(a).to(dev)
         b_d = torch.from_numpy(b).to(dev)
-        t64, _ = _autotune(sym,S, FP64)
+        if profile:
+            t64 = {"max_locals": 16, "wide_threshold": 0, "merge_chains": 1,
+                   "schedule": SCHED_LEVELS}
+        else:
+            t64, _ = _autotune(sym, S, FP64)
         n64 = Numeric(sym, S, FP64, tuning=t64)
         x64 = torch.empty_like(b_d)
 
@@ -738,7 +745,11 @@ def wide_section(stream, steps: int, S: int = 512, patterns: str = "ref,mesh,ran
             "tuning": t64, "program_info": n64.info,
             "hbm": {"bytes_per_step": byt, "achieved_gbs": byt / (ms64 / 1000.0) / 1e9,
                     "frac": byt / (ms64 / 1000.0) / 1e9 / peak if peak else None}}
-        t32, _ = _autotune(sym,S, FP32)
+        if profile:
+            out.append(res)
+            del n64, a_d, b_d, x64
+            continue
+        t32, _ = _autotune(sym, S, FP32)
         n32 = Numeric(sym, S, FP32, tuning=t32)
         x32 = torch.zeros_like(b_d)
         sweeps = torch.zeros(ld, dtype=torch.int32, device=dev)
@@ -1037,7 +1048,8 @@ def run_configs(args, stream) -> dict:
         ("i", "fp32ir_on_newton_iterates",
          lambda: newton_iterates_section(stream, args.scenarios, max(5, args.steps))),
         ("w", "wide_units",
-         lambda: wide_section(stream, max(5, args.steps), args.scenarios, args.wide_patterns)),
+         lambda: wide_section(stream, max(5, args.steps), args.scenarios, args.wide_patterns,
+                              args.wide_profile)),
     ]
     for tag, key, fn in sections:
         if tag in wanted:
@@ -1119,6 +1131,9 @@ def main() -> None:
     ap.add_argument("--wide-patterns", default="ref",
                     help="patterns of the wide-unit section (ref: the reference's plant topology, "
                          "mesh: mesh_30x30, random: random_1500)")
+    ap.add_argument("--wide-profile", action="store_true",
+                    help="wide-unit section: the batched FP64 step alone, fixed tuning "
+                         "(profiling runs)")
     ap.add_argument("--only-configs", action="store_true",
                     help="run the --configs workloads alone (profiling runs)")
     ap.add_argument("--newton-max-locals", type=int, default=0,

@@ -52,10 +52,16 @@ constexpr int kProgBlock = 128;                  // threads per block of the exe
 constexpr int kProgWarps = kProgBlock / 32;
 // Resident blocks per SM the level executors are compiled for: FP32 tables
 // allow 9 blocks at the usual table sizes (at most 56 registers); FP64
-// executors are given up to 80 registers (6 blocks).
+// executors are given up to 80 registers (6 blocks).  Build-time settings.
+#ifndef PVGLU_FP32_MIN_BLOCKS
+#define PVGLU_FP32_MIN_BLOCKS 9
+#endif
+#ifndef PVGLU_FP64_MIN_BLOCKS
+#define PVGLU_FP64_MIN_BLOCKS 6
+#endif
 template <typename T>
 constexpr int prog_min_blocks() {
-  return sizeof(T) == 4 ? 9 : 6;
+  return sizeof(T) == 4 ? PVGLU_FP32_MIN_BLOCKS : PVGLU_FP64_MIN_BLOCKS;
 }
 constexpr long long kMbarMaxPolls = 1LL << 20;   // bounded mbarrier waits
 
