@@ -698,8 +698,14 @@ def wide_section(stream, steps: int, S: int = 512, patterns: str = "ref,mesh,ran
         single = {}
         for sname, sched in (() if profile else (("thread_chain_levels", SCHED_THREAD_CHAIN),
                                                   ("programs_levels", SCHED_LEVELS),
-                                                  ("programs_persistent", SCHED_PERSISTENT))):
-            one = Numeric(sym, 1, FP64, sched)
+                                                  ("programs_persistent", SCHED_PERSISTENT),
+                                                  ("programs_autotuned", None))):
+            if sched is None:
+                t1, _ = _autotune(sym, 1, FP64)
+                one = Numeric(sym, 1, FP64, tuning=t1)
+                res["single_autotuned"] = {"tuning": t1, "program_info": one.info}
+            else:
+                one = Numeric(sym, 1, FP64, sched)
 
             def plain_step():
                 one.scatter(a1, stream=stream)
@@ -723,7 +729,7 @@ def wide_section(stream, steps: int, S: int = 512, patterns: str = "ref,mesh,ran
         a_d = torch.from_numpy(a).to(dev)
         b_d = torch.from_numpy(b).to(dev)
         if profile:
-            t64 = {"max_locals": 16, "wide_threshold": 0, "merge_chains": 1,
+            t64 = {"max_locals": 24, "wide_threshold": 0, "merge_chains": 2,
                    "schedule": SCHED_LEVELS}
         else:
             t64, _ = _autotune(sym, S, FP64)
@@ -1303,10 +1309,16 @@ def main() -> None:
     e1 = torch.cuda.Event(enable_timing=True)
     plain_iters = 200
     single = {}
+    plain_tuning = None
     for name, sched in (("thread_chain_levels", SCHED_THREAD_CHAIN),
                         ("programs_levels", SCHED_LEVELS),
-                        ("programs_persistent", SCHED_PERSISTENT)):
-        one = Numeric(sym, 1, FP64, sched)
+                        ("programs_persistent", SCHED_PERSISTENT),
+                        ("programs_autotuned", None)):
+        if sched is None:
+            plain_tuning, _ = _autotune(sym, 1, FP64)
+            one = Numeric(sym, 1, FP64, tuning=plain_tuning)
+        else:
+            one = Numeric(sym, 1, FP64, sched)
 
         def plain_step():
             one.scatter(a1, stream=stream)
@@ -1504,7 +1516,7 @@ def main() -> None:
         # the split of the headline into batching and precision.
         "batched_fp64": batched_fp64,
         "plain_fp64": {"value": plain, "unit": UNIT, "schedule": plain_name,
-                       "all_schedules": single},
+                       "all_schedules": single, "autotuned": plain_tuning},
         "ratios": {"batched_fp32ir_over_plain_fp64": value / world / plain,
                    "batched_fp64_over_plain_fp64": batched_fp64["value"] / plain,
                    "batched_fp32ir_over_batched_fp64": value / world / batched_fp64["value"]},

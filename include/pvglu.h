@@ -343,9 +343,13 @@ int pvglu_autotune(const pvglu_symbolic* s, int n_scenarios, int precision,
  *                   (009_get_max_numbers_per_column.cpp:3-31,
  *                   factorize_electrical_system_CUDA.cu:75-77);
  *   merge_chains    1: units regrouped into execution levels one unit at a
- *                   time (a unit joins the chain of its last dependency); 0:
- *                   the level set's own levels and chains, merged a whole
- *                   level at a time as the reference does
+ *                   time (a unit joins the chain of its last dependency); 2:
+ *                   the same, and a unit also joins a chain whose unit
+ *                   before the last is its dependency (ladders of two-unit
+ *                   rungs, as the string nodes of a plant ordered from the
+ *                   bus end give in the U solve, become one chain); 0: the
+ *                   level set's own levels and chains, merged a whole level
+ *                   at a time as the reference does
  *                   (007_convert_dependencies_in_levels.cpp:89-210), the
  *                   choice of pvglu_numeric_create(_ex).  Regrouping removes
  *                   levels on deep patterns but can lengthen the chains of a
@@ -360,8 +364,8 @@ typedef struct {
 int pvglu_numeric_create_tuned(const pvglu_symbolic* s, int n_scenarios, int precision,
                                const pvglu_tuning* t, pvglu_numeric** out);
 /* The autotuner over all of pvglu_tuning: table sizes x schedules, and, where
- * they change the handle's programs, chain merging on and off and a wide
- * threshold at half the table.  Synchronous; allocates and frees temporary
+ * they change the handle's programs, the three chain merging modes and a
+ * wide threshold at half the table.  Synchronous; allocates and frees temporary
  * handles.  best receives the fastest combination, best_ms its time per
  * scatter + refactor + solve.  No counterpart in the reference. */
 int pvglu_autotune_ex(const pvglu_symbolic* s, int n_scenarios, int precision,

@@ -80,11 +80,21 @@ int prog_prepare(pvglu_numeric* h) {
   return 0;
 }
 
+// Threads per block of a WIDE level launch: a block per item (unit and
+// scenario group); levels with fewer items than SMs get larger blocks (more
+// chains of a column, and more producers of an ordered sum, at a time).
+int wide_threads(const pvglu_numeric* h, int64_t items) {
+  int threads = pvglu::kProgBlock;
+  while (threads < pvglu::kWideBlockMax && items * (threads * 2 / pvglu::kProgBlock) <= h->sm_count)
+    threads *= 2;
+  return threads;
+}
+
 // Shared memory of a WIDE level launch: the ordered-sum scratch, and in
 // single mode the level's widest column staged beside it when it fits.
 template <typename T, bool B>
-size_t wide_smem(const pvglu_numeric* h, int ph, int lv) {
-  const size_t scratch = pvglu::wide_scratch_bytes<T, B>(pvglu::kProgBlock);
+size_t wide_smem(const pvglu_numeric* h, int ph, int lv, int threads) {
+  const size_t scratch = pvglu::wide_scratch_bytes<T, B>(threads);
   if (B || ph != 0) return scratch;
   const size_t want = scratch + (size_t)h->prog_level_wide_len[ph][lv] * sizeof(T);
   return std::min(want, h->smem_optin);
@@ -100,9 +110,10 @@ void prog_levels(pvglu_numeric* h, T* x, const int* done, const int* ndone, cuda
     const int cb = lc[lv], ce = lc[lv + 1];
     const int64_t items = (int64_t)(ce - cb) * groups;
     if (h->prog_level_wide_len[ph][lv] > 0) {  // a WIDE level: a block per unit and group
-      const size_t smem = wide_smem<T, B>(h, ph, (int)lv);
+      const int threads = wide_threads(h, items);
+      const size_t smem = wide_smem<T, B>(h, ph, (int)lv, threads);
       pvglu::k_wide_level<T, KIND, B>
-          <<<launch_blocks(items, 1), pvglu::kProgBlock, smem, st>>>(
+          <<<launch_blocks(items, 1), threads, smem, st>>>(
               h->progs.p[ph], h->d, cb, ce, static_cast<T*>(h->values), x, h->ld, h->S,
               h->pivot_tol, h->status, done, ndone, (int)smem);
       continue;
@@ -575,7 +586,7 @@ int pvglu_numeric_create_tuned(const pvglu_symbolic* sym, int n_scenarios, int p
   if (!sym || !out || !tuning || n_scenarios <= 0 ||
       (precision != PVGLU_FP64 && precision != PVGLU_FP32) || tuning->max_locals < 0 ||
       tuning->max_locals > pvglu::kMaxLocals || tuning->wide_threshold < 0 ||
-      (tuning->merge_chains != 0 && tuning->merge_chains != 1) ||
+      tuning->merge_chains < 0 || tuning->merge_chains > 2 ||
       (tuning->schedule != PVGLU_SCHED_LEVELS && tuning->schedule != PVGLU_SCHED_PERSISTENT &&
        tuning->schedule != PVGLU_SCHED_THREAD_CHAIN))
     return fail(PVGLU_ERR_BAD_ARG, "bad numeric_create arguments");
@@ -746,7 +757,7 @@ int pvglu_numeric_create_tuned(const pvglu_symbolic* sym, int n_scenarios, int p
     opt.max_locals = h->max_locals;
     opt.wide_locals = wide;
     opt.narrow_chains = (int)((int64_t)h->sm_count * pvglu::kProgWarps / groups);
-    opt.merge = tuning->merge_chains != 0;
+    opt.merge = tuning->merge_chains;
     opt.wide_threshold = tuning->wide_threshold;
     pvglu::build_chain_program(s, ph - 1, opt, prog);
     h->prog_level_ml[ph] = prog.level_max_locals;
@@ -774,7 +785,8 @@ int pvglu_numeric_create_tuned(const pvglu_symbolic* sym, int n_scenarios, int p
     rc |= h->put(lwide, &P.level_wide);
     rc |= h->put(prog.wide.unit, &P.w_unit);
     rc |= h->put(prog.wide.lvl, &P.w_lvl);
-    rc |= h->put(prog.wide.lv_tgt, &P.lv_tgt);
+    rc |= h->put(prog.wide.lv_chain, &P.lv_chain);
+    rc |= h->put(prog.wide.ch_tgt, &P.ch_tgt);
     rc |= h->put(prog.wide.tg_slot, &P.tg_slot);
     rc |= h->put(prog.wide.tg_pair, &P.tg_pair);
     rc |= h->put(prog.wide.pr_q, &P.pr_q);
@@ -1241,8 +1253,9 @@ int group_phase(pvglu_group* g, T* const* xs, cudaStream_t st) {
         // A member's WIDE level: its own launch, a block per unit and group.
         const auto& lc = h->prog_level_chain[ph];
         const int64_t items = (int64_t)(lc[lv + 1] - lc[lv]) * (B ? h->ld / pvglu::kGroup : 1);
-        const size_t smem = wide_smem<T, B>(h, ph, lv);
-        pvglu::k_wide_level<T, KIND, B><<<launch_blocks(items, 1), pvglu::kProgBlock, smem, st>>>(
+        const int threads = wide_threads(h, items);
+        const size_t smem = wide_smem<T, B>(h, ph, lv, threads);
+        pvglu::k_wide_level<T, KIND, B><<<launch_blocks(items, 1), threads, smem, st>>>(
             h->progs.p[ph], h->d, lc[lv], lc[lv + 1], static_cast<T*>(h->values),
             xs ? xs[i] : nullptr, h->ld, h->S, (T)h->pivot_tol, h->status, nullptr, nullptr,
             (int)smem);
@@ -1479,7 +1492,7 @@ int pvglu_autotune(const pvglu_symbolic* sym, int n_scenarios, int precision,
   std::vector<pvglu_tuning> cands;
   for (const int ml : table_candidates(ld, precision))
     for (const int sc : {PVGLU_SCHED_LEVELS, PVGLU_SCHED_PERSISTENT})
-      cands.push_back(pvglu_tuning{ml, 0, 1, sc});
+      cands.push_back(pvglu_tuning{ml, 0, 0, sc});
   pvglu_tuning bt{};
   const int rc = autotune_over(sym, n_scenarios, precision, cands, &bt, best_ms);
   if (rc) return rc;
@@ -1500,14 +1513,20 @@ int pvglu_autotune_ex(const pvglu_symbolic* sym, int n_scenarios, int precision,
                                              : (precision == PVGLU_FP32 ? 64 : 40));
     pvglu::ProgramOptions o;
     o.max_locals = table;
-    const std::vector<int> base = program_shape(s, o);
-    o.merge = false;
-    const bool merge_matters = program_shape(s, o) != base;
-    o.merge = true;
+    // Chain merging modes that give programs of their own shape.
+    std::vector<int> merges;
+    std::vector<std::vector<int>> shapes;
+    for (const int merge : {1, 2, 0}) {
+      o.merge = merge;
+      std::vector<int> sh = program_shape(s, o);
+      if (std::find(shapes.begin(), shapes.end(), sh) != shapes.end()) continue;
+      merges.push_back(merge);
+      shapes.push_back(std::move(sh));
+    }
+    o.merge = 1;
     o.wide_threshold = table / 2;
-    const bool wide_matters = program_shape(s, o) != base;
-    for (const int merge : {1, 0}) {
-      if (merge == 0 && !merge_matters) continue;
+    const bool wide_matters = program_shape(s, o) != shapes[0];
+    for (const int merge : merges) {
       for (const int wt : {0, table / 2}) {
         if (wt > 0 && !wide_matters) continue;
         for (const int sc : {PVGLU_SCHED_LEVELS, PVGLU_SCHED_PERSISTENT})

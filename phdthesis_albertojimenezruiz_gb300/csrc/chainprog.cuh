@@ -40,7 +40,8 @@ struct ProgDev {
   // Wide units (programs.hpp, WidePlan).
   const int* w_unit;
   const int* w_lvl;
-  const int* lv_tgt;
+  const int* lv_chain;
+  const int* ch_tgt;
   const int* tg_slot;
   const int* tg_pair;
   const int* pr_q;

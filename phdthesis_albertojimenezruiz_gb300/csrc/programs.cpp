@@ -204,27 +204,61 @@ void plan_wide_column(const Symbolic& s, int k, WidePlan& w) {
       pairs[t - c0].push_back({q, p});
     }
   }
-  // Level of each target: its U sources come first in slot order.
-  std::vector<int> lvl(len, 0);
-  int depth = 0;
+  // Chains and chain levels (programs.hpp); a target's U sources precede it
+  // in slot order, so slot order is a topological order.
+  std::vector<int> clev(len, -1), chain_of(len, -1);
+  std::vector<int> tail;                 // per chain: its last target
+  std::vector<char> whole;               // per chain: a long target's own chain
+  std::vector<std::vector<int>> members;  // per chain: its targets
+  std::vector<std::vector<int>> level_chains;
   for (int t = 0; t < len; t++) {
     if (pairs[t].empty()) continue;
-    int m = 0;
-    for (const auto& qp : pairs[t]) m = std::max(m, lvl[qp.second - c0]);
-    lvl[t] = m + 1;
-    depth = std::max(depth, m + 1);
+    const bool lng = (int)pairs[t].size() > kWideLong;
+    int m = -1;
+    for (const auto& qp : pairs[t]) m = std::max(m, clev[qp.second - c0]);
+    int c = -1;
+    bool one_chain = true, has_tail = false;
+    for (const auto& qp : pairs[t]) {
+      const int d = qp.second - c0;
+      if (clev[d] < 0 || clev[d] != m) continue;
+      if (c < 0) c = chain_of[d];
+      else if (chain_of[d] != c) one_chain = false;
+      if (tail[chain_of[d]] == d) has_tail = true;
+    }
+    if (!lng && m >= 0 && one_chain && has_tail && !whole[c]) {
+      members[c].push_back(t);
+      tail[c] = t;
+      chain_of[t] = c;
+      clev[t] = m;
+      continue;
+    }
+    const int lv = m + 1;
+    if ((int)level_chains.size() <= lv) level_chains.resize(lv + 1);
+    chain_of[t] = (int)members.size();
+    level_chains[lv].push_back((int)members.size());
+    members.push_back({t});
+    tail.push_back(t);
+    whole.push_back(lng ? 1 : 0);
+    clev[t] = lv;
   }
-  w.lvl.push_back((int)w.lv_tgt.size());
-  for (int l = 1; l <= depth; l++) {
-    w.lv_tgt.push_back((int)w.tg_slot.size());
-    for (int t = 0; t < len; t++) {
-      if (lvl[t] != l) continue;
-      w.tg_slot.push_back(c0 + t);
-      for (const auto& qp : pairs[t]) {
-        w.pr_q.push_back(qp.first);
-        w.pr_p.push_back(qp.second);
+  w.lvl.push_back((int)w.lv_chain.size());
+  for (auto& chains : level_chains) {
+    // Longest chains first: the warps that take them start first.
+    std::stable_sort(chains.begin(), chains.end(), [&](int a, int b) {
+      return members[a].size() > members[b].size();
+    });
+    w.lv_chain.push_back((int)w.ch_tgt.size());
+    for (const int c : chains) {
+      w.ch_tgt.push_back((int)w.tg_slot.size());
+      for (const int t : members[c]) {
+        w.tg_slot.push_back(c0 + t);
+        for (const auto& qp : pairs[t]) {
+          w.pr_q.push_back(qp.first);
+          const int d = qp.second - c0;
+          w.pr_p.push_back(clev[d] >= 0 && chain_of[d] == c ? ~qp.second : qp.second);
+        }
+        w.tg_pair.push_back((int)w.pr_q.size());
       }
-      w.tg_pair.push_back((int)w.pr_q.size());
     }
   }
 }
@@ -234,38 +268,42 @@ void plan_wide_column(const Symbolic& s, int k, WidePlan& w) {
 namespace {
 
 // Execution levels (see programs.hpp): every unit extends the chain that
-// holds all of its dependencies of the highest level, when that chain's last
-// unit is one of them, and starts a new chain one level above them
-// otherwise.  Extending never delays a unit (it had to wait for that last
-// unit anyway) and never makes another chain wait.
-void execution_levels(const Symbolic& s, int kind, const LevelSet& ls,
+// holds all of its dependencies of the highest level, when one of them is
+// among the chain's last `1 + slack` units, and starts a new chain one level
+// above them otherwise.  With slack 0 extending never delays a unit (it had
+// to wait for that last unit anyway) and never makes another chain wait;
+// slack 1 lets a unit also wait for one unit it does not depend on, which
+// keeps two-unit rungs of a ladder (each rung's first unit depending on the
+// previous rung's first unit) in one chain.
+void execution_levels(const Symbolic& s, int kind, const LevelSet& ls, int slack,
                       std::vector<std::vector<std::vector<int>>>& exec) {
-  std::vector<int> lvl(s.n, -1), chain_of(s.n, -1), deps;
-  std::vector<int> tail, chain_pos;  // per chain (global numbers)
+  std::vector<int> lvl(s.n, -1), chain_of(s.n, -1), pos(s.n, -1), deps;
+  std::vector<int> len, chain_pos;  // per chain (global numbers)
   for (int k = 0; k < (int)ls.columns.size(); k++) {
     const int u = ls.columns[k];
     unit_deps(s, kind, u, deps);
     int m = -1;
     for (const int d : deps) m = std::max(m, lvl[d]);
     int c = -1;
-    bool one_chain = true, has_tail = false;
+    bool one_chain = true, near_tail = false;
     for (const int d : deps) {
       if (lvl[d] != m) continue;
       if (c < 0) c = chain_of[d];
       else if (chain_of[d] != c) one_chain = false;
-      if (tail[chain_of[d]] == d) has_tail = true;
+      if (pos[d] >= len[chain_of[d]] - 1 - slack) near_tail = true;
     }
-    if (m >= 0 && one_chain && has_tail) {
+    if (m >= 0 && one_chain && near_tail) {
       exec[m][chain_pos[c]].push_back(u);
-      tail[c] = u;
       chain_of[u] = c;
+      pos[u] = len[c]++;
       lvl[u] = m;
       continue;
     }
     const int lv = m + 1;
     if ((int)exec.size() <= lv) exec.resize(lv + 1);
-    chain_of[u] = (int)tail.size();
-    tail.push_back(u);
+    chain_of[u] = (int)len.size();
+    pos[u] = 0;
+    len.push_back(1);
     chain_pos.push_back((int)exec[lv].size());
     exec[lv].push_back(std::vector<int>{u});
     lvl[u] = lv;
@@ -285,7 +323,7 @@ void build_chain_program(const Symbolic& s, int kind, const ProgramOptions& opt,
 
   // 0. Execution levels (levels -> chains -> units).
   std::vector<std::vector<std::vector<int>>> exec;
-  if (!opt.merge) {
+  if (opt.merge <= 0) {
     for (int lv = 0; lv < ls.num_levels(); lv++) {
       exec.emplace_back();
       for (int c = ls.start_levels[lv]; c < ls.start_levels[lv + 1]; c++)
@@ -293,7 +331,7 @@ void build_chain_program(const Symbolic& s, int kind, const ProgramOptions& opt,
                                  ls.columns.begin() + ls.start_chains[c + 1]);
     }
   } else {
-    execution_levels(s, kind, ls, exec);
+    execution_levels(s, kind, ls, opt.merge - 1, exec);
   }
 
   // 1. Program levels: each execution level cut around its wide units.
@@ -443,8 +481,9 @@ void build_chain_program(const Symbolic& s, int kind, const ProgramOptions& opt,
   out.level_chain.push_back((int)out.chain_seg.size());
   out.chain_seg.push_back((int)out.seg.size());
   out.chain_unit.push_back((int)out.units.size());
-  if (kind < 0) out.wide.lvl.push_back((int)out.wide.lv_tgt.size());
-  out.wide.lv_tgt.push_back((int)out.wide.tg_slot.size());
+  if (kind < 0) out.wide.lvl.push_back((int)out.wide.lv_chain.size());
+  out.wide.lv_chain.push_back((int)out.wide.ch_tgt.size());
+  out.wide.ch_tgt.push_back((int)out.wide.tg_slot.size());
   // A level's table is as wide as its widest segment (the budget is only an
   // upper bound): shared memory per block, and so the blocks an SM holds,
   // follow what the level uses.  The narrow levels of a plant (one segment

@@ -65,10 +65,15 @@ struct Segment {
 // chain, so any execution that runs the levels in order and each chain in
 // order computes, unit for unit, the same arithmetic.  Extending a chain
 // never delays a unit (it waits for that chain's last unit in any order) and
-// never makes another chain wait.  The reference merges chains a whole basic
-// level at a time (007_convert_dependencies_in_levels.cpp:62-143): one unit
-// that cannot join keeps its whole level from merging.  The level set itself
-// (the symbolic arrays) is unchanged.
+// never makes another chain wait.  Ladder merging also extends the chain
+// when the dependency is the unit before its last: a unit then waits for one
+// unit it does not depend on, and a ladder of two-unit rungs (each rung's
+// first unit depending on the previous rung's first unit, as the string
+// nodes of a plant ordered from the bus end give in the U solve) becomes one
+// chain instead of one level per rung.  The reference merges chains a whole
+// basic level at a time (007_convert_dependencies_in_levels.cpp:62-143): one
+// unit that cannot join keeps its whole level from merging.  The level set
+// itself (the symbolic arrays) is unchanged.
 //
 // Program levels.  Every execution level is executed as one or more program
 // levels: a chain is cut around each unit too wide for the level's table
@@ -83,18 +88,28 @@ struct Segment {
 // inside the column: target slot t of column k receives
 //     M(t) -= L(i, j) * U(j, k)   for its pairs (q = slot of L(i, j), p = slot of U(j, k))
 // in ascending j (the order of the reference's right-looking loop, so FP64
-// stays bit-exact), and the targets are grouped into column levels: a
-// target's level is one more than the highest level of the U entries it
-// reads (targets without pairs have level 0 and need no work).  After the
-// last level the L part is divided by the pivot.
+// stays bit-exact).  The targets (slots with at least one pair) are grouped
+// into chains and chain levels by the execution-level rule applied inside
+// the column, one target at a time in slot order: a target whose sources
+// that are targets lie, at their highest chain level, in one chain whose last
+// target is one of them extends that chain; otherwise it starts a new chain
+// one level above them.  A chain is computed in order by one thread (one warp
+// batched), so a target reads a source of its own chain right after that
+// thread wrote it; a block barrier separates the chain levels.  A target
+// with more than kWideLong pairs is computed by the whole block (ordered
+// block sum) and is a chain of its own that no target extends.  After the
+// last level the L part is divided by the pivot.  A pair whose U source is
+// a target of the same chain carries ~p (negative) instead of p.
+constexpr int kWideLong = 96;
 struct WidePlan {
   std::vector<int> unit;      // [W] column (refactor) or unknown (solves)
   // refactor only:
-  std::vector<int> lvl;       // [W + 1] -> index into lv_tgt (the unit's column levels)
-  std::vector<int> lv_tgt;    // [column levels + 1] -> index into tg_slot
+  std::vector<int> lvl;       // [W + 1] -> index into lv_chain (the unit's chain levels)
+  std::vector<int> lv_chain;  // [chain levels + 1] -> index into ch_tgt
+  std::vector<int> ch_tgt;    // [chains + 1] -> index into tg_slot (a chain's targets, in order)
   std::vector<int> tg_slot;   // [T] target slot
   std::vector<int> tg_pair;   // [T + 1] -> index into pr_q / pr_p
-  std::vector<int> pr_q, pr_p;  // [P] L slot and U slot of every update
+  std::vector<int> pr_q, pr_p;  // [P] L slot and U slot (~slot: same chain) of every update
 };
 
 struct ChainProgram {
@@ -124,13 +139,13 @@ struct ChainProgram {
 // most narrow_chains chains gets max(max_locals, wide_locals) (levels with
 // few chains can afford a wide table: fewer segments, and the warps they
 // leave idle cost nothing).  A unit whose own table would exceed its level's
-// budget is a wide unit.  merge = false keeps the level set's levels and
-// chains as execution levels.
+// budget is a wide unit.  merge: 0 keeps the level set's levels and chains
+// as execution levels, 1 regroups them per unit, 2 with ladder merging.
 struct ProgramOptions {
   int max_locals = 64;
   int wide_locals = 0;
   int narrow_chains = 0;
-  bool merge = true;
+  int merge = 1;
   // > 0: units needing more than this many table rows run as wide units
   // even where they would fit the level's table (at most the budget).
   int wide_threshold = 0;

@@ -11,9 +11,10 @@
 // receives its updates one at a time, in ascending j, each product and each
 // subtraction rounded on its own.  The parallelism comes from elsewhere:
 //   * refactorization of column k in gather form, scheduled inside the
-//     column: target slots whose U sources are final are computed together
-//     (a thread or, batched, a warp per target), one block barrier per column
-//     level;
+//     column: the column's targets form chains (a target that reads only the
+//     target before it, as the string nodes of a bus column do, joins that
+//     target's chain), the chains of a chain level run in parallel (a thread
+//     or, batched, a warp per chain), one block barrier per chain level;
 //   * a target or solve row with many updates: warps of the block compute the
 //     products of a chunk in parallel (each rounded as the sequential code
 //     rounds it) into shared memory while one warp subtracts the previous
@@ -33,10 +34,6 @@ __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(
 __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
 __device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
-
-// Updates per target above which the block computes a target's products
-// together instead of one thread (warp) walking them.
-constexpr int kWideLong = 96;
 
 // acc - sum_e a_e * b_e in the order e = 0 .. count-1, each product and each
 // difference rounded on its own.  Warps 1.. of the block form the products of
@@ -82,16 +79,19 @@ ordered_sub_block(typename std::conditional<BATCH, typename Vec2<T>::type, T>::t
     V* out = buf + (size_t)(c & 1) * ch * stride;
     const int base = c * ch;
     const int me = BATCH ? warp - 1 : tid - 32;
-    // Up to four entries' operands in flight, then their products.
-    for (int r0 = me; r0 < ch; r0 += 4 * producers) {
-      V a[4], b[4];
+    // Up to U entries' operands in flight, then their products (two for
+    // FP64 pairs, which keeps the kernels of up to 512 threads within 128
+    // registers).
+    constexpr int U = (BATCH && sizeof(T) == 8) ? 2 : 4;
+    for (int r0 = me; r0 < ch; r0 += U * producers) {
+      V a[U], b[U];
 #pragma unroll
-      for (int u = 0; u < 4; u++) {
+      for (int u = 0; u < U; u++) {
         const int e = base + r0 + u * producers;
         if (r0 + u * producers < ch && e < count) ab(e, a[u], b[u]);
       }
 #pragma unroll
-      for (int u = 0; u < 4; u++) {
+      for (int u = 0; u < U; u++) {
         const int r = r0 + u * producers;
         if (r < ch && base + r < count) {
           V p;
@@ -140,18 +140,31 @@ __device__ __forceinline__ float2 ldv2(const float* p) {
 
 // ---------------------------------------------------------------------------
 // Refactorization of wide column k = P.w_unit[w] for the scenario group at
-// s0 (batched) or the single scenario.  smem: the block's shared memory
-// (smem_bytes of it); the column is staged there in single mode when
-// len * sizeof(T) + scratch fits.
+// s0 (batched) or the single scenario, chain level by chain level
+// (programs.hpp, WidePlan): the chains of a level spread over the block's
+// threads (batched: warps), each computed in order, then the level's long
+// targets one at a time by the whole block.  Inside a chain the loads of the
+// next few targets (their own values, and the L operand of single-pair
+// targets) are issued together; a source written
+// earlier in the same chain comes from the register that holds the previous
+// target or, further back, from a plain load after the thread's own store.
+// smem: the block's shared memory (smem_bytes of it); the column is staged
+// there in single mode when len * sizeof(T) + scratch fits.
 template <typename T, bool BATCH>
 __device__ void wide_refactor(const ProgDev& P, const DevStruct& d, int w, int s0,
                               T* __restrict__ v, int ld, int S, T pivot_tol, DevStatus* st,
                               unsigned char* smem, int smem_bytes) {
+  constexpr int G = 4;  // targets whose loads are in flight together
   const int k = __ldg(P.w_unit + w);
   const int c0 = __ldg(d.colptr + k), dk = __ldg(d.diag + k), c1 = __ldg(d.colptr + k + 1);
   const int len = c1 - c0;
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int l_begin = __ldg(P.w_lvl + w), l_end = __ldg(P.w_lvl + w + 1);
+  auto is_long = [&](int c) {
+    const int t0 = __ldg(P.ch_tgt + c);
+    return __ldg(P.ch_tgt + c + 1) - t0 == 1 &&
+           __ldg(P.tg_pair + t0 + 1) - __ldg(P.tg_pair + t0) > kWideLong;
+  };
   if constexpr (!BATCH) {
     const int scratch = min(wide_scratch_bytes<T, false>(nthr), smem_bytes);
     const bool staged = (int64_t)len * (int)sizeof(T) + scratch <= smem_bytes;
@@ -160,26 +173,40 @@ __device__ void wide_refactor(const ProgDev& P, const DevStruct& d, int w, int s
     if (staged)
       for (int i = tid; i < len; i += nthr) col[i] = ldv(v + c0 + i);
     __syncthreads();
+    // Final values (earlier levels, earlier columns) and values this thread
+    // wrote itself (plain accesses, ordered after its own stores).
     auto get = [&](int slot) -> T { return staged ? col[slot - c0] : ldv(v + slot); };
+    auto get_own = [&](int slot) -> T { return staged ? col[slot - c0] : v[slot]; };
     auto put = [&](int slot, T val) {
       if (staged) col[slot - c0] = val;
       else v[slot] = val;
     };
     for (int l = l_begin; l < l_end; l++) {
-      const int t0 = __ldg(P.lv_tgt + l), t1 = __ldg(P.lv_tgt + l + 1);
-      for (int t = t0 + tid; t < t1; t += nthr) {
-        const int e0 = __ldg(P.tg_pair + t), e1 = __ldg(P.tg_pair + t + 1);
-        if (e1 - e0 > kWideLong) continue;
-        const int slot = __ldg(P.tg_slot + t);
-        T acc = get(slot);
-        for (int e = e0; e < e1; e++)
-          acc = fnms(acc, ldv(v + __ldg(P.pr_q + e)), get(__ldg(P.pr_p + e)));
-        put(slot, acc);
+      const int h0 = __ldg(P.lv_chain + l), h1 = __ldg(P.lv_chain + l + 1);
+      for (int c = h0 + tid; c < h1; c += nthr) {
+        if (is_long(c)) continue;
+        const int t1 = __ldg(P.ch_tgt + c + 1);
+        int prev = -1;
+        T prev_v = T(0);
+        for (int t = __ldg(P.ch_tgt + c); t < t1; t++) {
+          const int slot = __ldg(P.tg_slot + t);
+          const int e1 = __ldg(P.tg_pair + t + 1);
+          T acc = get(slot);
+          for (int e = __ldg(P.tg_pair + t); e < e1; e++) {
+            const int p = __ldg(P.pr_p + e);
+            const T u = p >= 0 ? get(p) : (~p == prev ? prev_v : get_own(~p));
+            acc = fnms(acc, ldv(v + __ldg(P.pr_q + e)), u);
+          }
+          put(slot, acc);
+          prev = slot;
+          prev_v = acc;
+        }
       }
       __syncthreads();
-      for (int t = t0; t < t1; t++) {  // long targets, one at a time by the block
+      for (int c = h0; c < h1; c++) {  // long targets, one at a time by the block
+        if (!is_long(c)) continue;
+        const int t = __ldg(P.ch_tgt + c);
         const int e0 = __ldg(P.tg_pair + t), e1 = __ldg(P.tg_pair + t + 1);
-        if (e1 - e0 <= kWideLong) continue;
         const int slot = __ldg(P.tg_slot + t);
         T acc = get(slot);
         acc = ordered_sub_block<T, false>(
@@ -210,40 +237,80 @@ __device__ void wide_refactor(const ProgDev& P, const DevStruct& d, int w, int s
     const int lane = tid & 31, warp = tid >> 5, nw = nthr >> 5;
     const int s = s0 + 2 * lane;
     auto row = [&](int slot) { return v + (int64_t)slot * ld + s; };
+    auto fnms2 = [](V2 acc, V2 a, V2 b) {
+      acc.x = fnms(acc.x, a.x, b.x);
+      acc.y = fnms(acc.y, a.y, b.y);
+      return acc;
+    };
     for (int l = l_begin; l < l_end; l++) {
-      const int t0 = __ldg(P.lv_tgt + l), t1 = __ldg(P.lv_tgt + l + 1);
-      for (int t = t0 + warp; t < t1; t += nw) {
-        const int e0 = __ldg(P.tg_pair + t), e1 = __ldg(P.tg_pair + t + 1);
-        if (e1 - e0 > kWideLong) continue;
-        T* tp = row(__ldg(P.tg_slot + t));
-        V2 acc = ldv2(tp);
-        int e = e0;
-        // Four updates' operands in flight at a time; the subtractions stay
-        // in order.
-        for (; e + 4 <= e1; e += 4) {
-          V2 a[4], b[4];
+      const int h0 = __ldg(P.lv_chain + l), h1 = __ldg(P.lv_chain + l + 1);
+      for (int c = h0 + warp; c < h1; c += nw) {
+        if (is_long(c)) continue;
+        const int t1 = __ldg(P.ch_tgt + c + 1);
+        int prev = -1;
+        V2 prev_v{};
+        // A source of this chain: the previous target's register, or a
+        // plain load of a row this lane stored earlier.
+        auto own = [&](int p) -> V2 {
+          return p == prev ? prev_v : *reinterpret_cast<const V2*>(row(p));
+        };
+        for (int t = __ldg(P.ch_tgt + c); t < t1; t += G) {
+          V2 cur[G], qa[G];
+          int slot[G], np[G], ps[G];
 #pragma unroll
-          for (int u = 0; u < 4; u++) {
-            a[u] = ldv2(row(__ldg(P.pr_q + e + u)));
-            b[u] = ldv2(row(__ldg(P.pr_p + e + u)));
+          for (int u = 0; u < G; u++) {
+            np[u] = -1;
+            if (t + u < t1) {
+              slot[u] = __ldg(P.tg_slot + t + u);
+              const int e0 = __ldg(P.tg_pair + t + u);
+              np[u] = __ldg(P.tg_pair + t + u + 1) - e0;
+              cur[u] = ldv2(row(slot[u]));
+              if (np[u] == 1) {
+                qa[u] = ldv2(row(__ldg(P.pr_q + e0)));
+                ps[u] = __ldg(P.pr_p + e0);
+              }
+            }
           }
 #pragma unroll
-          for (int u = 0; u < 4; u++) {
-            acc.x = fnms(acc.x, a[u].x, b[u].x);
-            acc.y = fnms(acc.y, a[u].y, b[u].y);
+          for (int u = 0; u < G; u++) {
+            if (np[u] < 0) continue;
+            V2 acc = cur[u];
+            if (np[u] == 1) {
+              acc = fnms2(acc, qa[u], ps[u] >= 0 ? ldv2(row(ps[u])) : own(~ps[u]));
+            } else {
+              const int e0 = __ldg(P.tg_pair + t + u), e1 = e0 + np[u];
+              int e = e0;
+              // Two updates' operands in flight at a time; the subtractions
+              // stay in order.
+              for (; e + 2 <= e1; e += 2) {
+                V2 a[2], b[2];
+                int pp[2];
+#pragma unroll
+                for (int i = 0; i < 2; i++) {
+                  a[i] = ldv2(row(__ldg(P.pr_q + e + i)));
+                  pp[i] = __ldg(P.pr_p + e + i);
+                  if (pp[i] >= 0) b[i] = ldv2(row(pp[i]));
+                }
+#pragma unroll
+                for (int i = 0; i < 2; i++) acc = fnms2(acc, a[i], pp[i] >= 0 ? b[i] : own(~pp[i]));
+              }
+              for (; e < e1; e++) {
+                const int p = __ldg(P.pr_p + e);
+                const V2 a = ldv2(row(__ldg(P.pr_q + e)));
+                acc = fnms2(acc, a, p >= 0 ? ldv2(row(p)) : own(~p));
+              }
+            }
+            *reinterpret_cast<V2*>(row(slot[u])) = acc;
+            prev = slot[u];
+            prev_v = acc;
           }
         }
-        for (; e < e1; e++) {
-          const V2 a = ldv2(row(__ldg(P.pr_q + e))), b = ldv2(row(__ldg(P.pr_p + e)));
-          acc.x = fnms(acc.x, a.x, b.x);
-          acc.y = fnms(acc.y, a.y, b.y);
-        }
-        *reinterpret_cast<V2*>(tp) = acc;
       }
       __syncthreads();
-      for (int t = t0; t < t1; t++) {
+      for (int c = h0; c < h1; c++) {
+        if (!is_long(c)) continue;
+        const int t = __ldg(P.ch_tgt + c);
         const int e0 = __ldg(P.tg_pair + t), e1 = __ldg(P.tg_pair + t + 1);
-        if (e1 - e0 <= kWideLong) continue;
         T* tp = row(__ldg(P.tg_slot + t));
         V2 acc = ldv2(tp);
         acc = ordered_sub_block<T, true>(
@@ -388,9 +455,11 @@ __device__ __forceinline__ void wide_run_level(const ProgDev& P, const DevStruct
   }
 }
 
-// Launch form of a WIDE program level (the per-level schedule).
+// Launch form of a WIDE program level (the per-level schedule): kProgBlock
+// threads per block, or up to kWideBlockMax when the level has few items.
+constexpr int kWideBlockMax = 512;
 template <typename T, int KIND, bool BATCH>
-__global__ void __launch_bounds__(kProgBlock)
+__global__ void __launch_bounds__(kWideBlockMax, 1)
 k_wide_level(ProgDev P, DevStruct d, int cb, int ce, T* __restrict__ v, T* __restrict__ x,
              int ld, int S, T pivot_tol, DevStatus* st, const int* done, const int* ndone,
              int smem_bytes) {

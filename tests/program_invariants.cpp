@@ -191,37 +191,52 @@ void check_program(const Symbolic& s, int kind, const ProgramOptions& opt) {
     }
   }
   // Wide refactor plans: targets inside their column, pairs in ascending j,
-  // every U source of a target computed at an earlier column level, every
-  // update of the column present once.
+  // every U source of a target computed at an earlier chain level or earlier
+  // in the target's own chain (and marked so), long targets alone in their
+  // chain, every update of the column present once.
   if (kind == -1) {
     const WidePlan& w = pr.wide;
     CHECK(w.lvl.size() == w.unit.size() + 1, "wide lvl size");
     for (size_t i = 0; i < w.unit.size(); i++) {
       const int k = w.unit[i];
       const int c0 = s.csc_colptr[k], dk = s.diag_slot[k], c1 = s.csc_colptr[k + 1];
-      std::vector<int> level_of(c1 - c0, 0);
+      std::vector<int> level_of(c1 - c0, 0), chain_of(c1 - c0, -1);
       int64_t updates = 0, expect = 0;
       for (int p = c0; p < dk; p++) {
         const int j = s.csc_row[p];
         expect += s.csc_colptr[j + 1] - s.diag_slot[j] - 1;
       }
       for (int l = w.lvl[i]; l < w.lvl[i + 1]; l++)
-        for (int t = w.lv_tgt[l]; t < w.lv_tgt[l + 1]; t++) {
-          const int slot = w.tg_slot[t];
-          CHECK(slot >= c0 && slot < c1 && level_of[slot - c0] == 0, "wide target %d", slot);
-          level_of[slot - c0] = l - w.lvl[i] + 1;
-          int prev_p = -1;
-          for (int e = w.tg_pair[t]; e < w.tg_pair[t + 1]; e++) {
-            const int q = w.pr_q[e], p = w.pr_p[e];
-            CHECK(p >= c0 && p < dk && p > prev_p, "wide pair order %d", p);
-            CHECK(level_of[p - c0] < level_of[slot - c0], "wide pair level %d", p);
-            const int j = s.csc_row[p];
-            CHECK(q > s.diag_slot[j] && q < s.csc_colptr[j + 1] && s.csc_row[q] == s.csc_row[slot],
-                  "wide pair slot %d", q);
-            prev_p = p;
-            updates++;
+        for (int c = w.lv_chain[l]; c < w.lv_chain[l + 1]; c++)
+          for (int t = w.ch_tgt[c]; t < w.ch_tgt[c + 1]; t++) {
+            const int slot = w.tg_slot[t];
+            CHECK(slot >= c0 && slot < c1 && level_of[slot - c0] == 0, "wide target %d", slot);
+            const int np = w.tg_pair[t + 1] - w.tg_pair[t];
+            CHECK(np > 0, "wide target %d without pairs", slot);
+            CHECK(np <= kWideLong || w.ch_tgt[c + 1] - w.ch_tgt[c] == 1,
+                  "long wide target %d shares its chain", slot);
+            int prev_p = -1;
+            for (int e = w.tg_pair[t]; e < w.tg_pair[t + 1]; e++) {
+              const int q = w.pr_q[e];
+              const bool same = w.pr_p[e] < 0;
+              const int p = same ? ~w.pr_p[e] : w.pr_p[e];
+              CHECK(p >= c0 && p < dk && p > prev_p, "wide pair order %d", p);
+              if (same)
+                CHECK(chain_of[p - c0] == c && level_of[p - c0] == l - w.lvl[i] + 1,
+                      "wide same-chain source %d", p);
+              else
+                CHECK(level_of[p - c0] <= l - w.lvl[i] && chain_of[p - c0] != c,
+                      "wide pair level %d", p);
+              const int j = s.csc_row[p];
+              CHECK(q > s.diag_slot[j] && q < s.csc_colptr[j + 1] &&
+                        s.csc_row[q] == s.csc_row[slot],
+                    "wide pair slot %d", q);
+              prev_p = p;
+              updates++;
+            }
+            level_of[slot - c0] = l - w.lvl[i] + 1;
+            chain_of[slot - c0] = c;
           }
-        }
       CHECK(updates == expect, "wide column %d updates %lld of %lld", k, (long long)updates,
             (long long)expect);
     }
@@ -246,10 +261,10 @@ int main(int argc, char** argv) {
   }
   for (int kind = -1; kind <= 3; kind++) {
     for (int base : {8, 16, 24, 40, 64, 1023}) {
-      for (int merge = 0; merge < 2; merge++) {
+      for (int merge = 0; merge <= 2; merge++) {
         ProgramOptions opt;
         opt.max_locals = base;
-        opt.merge = merge != 0;
+        opt.merge = merge;
         check_program(s, kind, opt);
         // The handle's rule: narrow levels get a wide budget.
         opt.wide_locals = 226;

@@ -461,14 +461,14 @@ def test_group_with_wide_members(cuda):
 
 
 @pytest.mark.parametrize("schedule", [SCHED_LEVELS, SCHED_PERSISTENT])
-@pytest.mark.parametrize("merge,wide", [(1, 0), (0, 0), (1, 12), (0, 12)])
+@pytest.mark.parametrize("merge,wide", [(1, 0), (0, 0), (2, 0), (1, 12), (0, 12), (2, 12)])
 @pytest.mark.parametrize("S", [1, 64])
 @pytest.mark.parametrize("name", ["block_1x20x20", "mesh_20x20"])
 def test_every_tuning_bit_exact(cuda, name, S, merge, wide, schedule):
     """Every execution choice of pvglu_tuning (execution levels merged per
-    unit or the level set's own, wide units at half the table or only where
-    needed, each schedule) gives the reference's sequential FP64 factors and
-    solution bit for bit."""
+    unit, with ladder merging, or the level set's own; wide units at half the
+    table or only where needed; each schedule) gives the reference's
+    sequential FP64 factors and solution bit for bit."""
     g = load_golden(name)
     s = Symbolic(g["rowptr"], g["colidx"], g["perm_amd"])
     t = {"max_locals": 24, "wide_threshold": wide, "merge_chains": merge, "schedule": schedule}
@@ -494,7 +494,7 @@ def test_autotune_ex_picks_a_working_tuning(cuda, name, S, precision):
     s = Symbolic(g["rowptr"], g["colidx"], g["perm_amd"])
     t, ms = autotune_ex(s, S, precision)
     assert ms > 0 and t["schedule"] in (SCHED_LEVELS, SCHED_PERSISTENT)
-    assert t["merge_chains"] in (0, 1) and t["wide_threshold"] >= 0
+    assert t["merge_chains"] in (0, 1, 2) and t["wide_threshold"] >= 0
     num = Numeric(s, S, precision, tuning=t)
     a = np.repeat(g["a"][:, None], S, axis=1)
     num.scatter(dev(pad_cols(a, num.ld)))
