@@ -648,7 +648,7 @@ def newton_iterates_section(stream, S: int, steps: int) -> dict:
 
 
 def wide_section(stream, steps: int, S: int = 512, patterns: str = "ref,mesh,random",
-                 profile: bool = False) -> dict:
+                 profile: bool = False, profile_max_locals: int = 24) -> dict:
     """Patterns whose factors have columns and rows too wide for a chain-
     program table (run as WIDE program levels, a block per unit): the
     reference's own plant topology with the reference's AMD ordering (7
@@ -729,7 +729,7 @@ def wide_section(stream, steps: int, S: int = 512, patterns: str = "ref,mesh,ran
         a_d = torch.from_numpy(a).to(dev)
         b_d = torch.from_numpy(b).to(dev)
         if profile:
-            t64 = {"max_locals": 24, "wide_threshold": 0, "merge_chains": 2,
+            t64 = {"max_locals": profile_max_locals, "wide_threshold": 0, "merge_chains": 2,
                    "schedule": SCHED_LEVELS}
         else:
             t64, _ = _autotune(sym, S, FP64)
@@ -1055,7 +1055,7 @@ def run_configs(args, stream) -> dict:
          lambda: newton_iterates_section(stream, args.scenarios, max(5, args.steps))),
         ("w", "wide_units",
          lambda: wide_section(stream, max(5, args.steps), args.scenarios, args.wide_patterns,
-                              args.wide_profile)),
+                              args.wide_profile, args.wide_max_locals)),
     ]
     for tag, key, fn in sections:
         if tag in wanted:
@@ -1140,6 +1140,8 @@ def main() -> None:
     ap.add_argument("--wide-profile", action="store_true",
                     help="wide-unit section: the batched FP64 step alone, fixed tuning "
                          "(profiling runs)")
+    ap.add_argument("--wide-max-locals", type=int, default=24,
+                    help="table size of the fixed tuning of --wide-profile")
     ap.add_argument("--only-configs", action="store_true",
                     help="run the --configs workloads alone (profiling runs)")
     ap.add_argument("--newton-max-locals", type=int, default=0,
@@ -1362,6 +1364,43 @@ def main() -> None:
                         np.abs(xa).max(axis=0)))}
     del num64b, x64b
 
+    # The same batched step with the reference's own AMD ordering of this
+    # plant (a fixture made by the reference's code): its fill, levels and
+    # rate beside the built-in ordering's.
+    reference_ordering = None
+    amd = ROOT / "tests" / "golden" / "orderings" / "plant_amd.npz"
+    tag = "x".join(map(str, p.dims))
+    if amd.exists():
+        with np.load(amd) as z:
+            perm = z[f"perm_{tag}"] if f"perm_{tag}" in z else None
+        if perm is not None:
+            sym_r = Symbolic(p.rowptr, p.colidx, perm)
+            t_r, _ = _autotune(sym_r, S, FP32)
+            num_r = Numeric(sym_r, S, FP32, tuning=t_r)
+            x_r = torch.zeros_like(b_d)
+
+            def ref_order_step():
+                num_r.scatter(a_d, stream=stream)
+                num_r.refactor(stream=stream)
+                num_r.solve_refined(a_d, b_d, x_r, tol=IR_TOL, max_sweeps=IR_MAX_SWEEPS,
+                                    sweeps=sweeps, stream=stream)
+
+            for _ in range(args.warmup):
+                ref_order_step()
+            ms_r = _time_ms(ref_order_step, stream, args.steps)
+            sw_r = sweeps.cpu().numpy()[:S]
+            xr = x_r.cpu().numpy()[:, :S]
+            reference_ordering = {
+                "value": S / (ms_r / 1000.0), "unit": UNIT, "ms_per_step": ms_r,
+                "ordering": "the reference's AMD ordering (004a), fixture "
+                            "tests/golden/orderings/plant_amd.npz",
+                "nnz_lu": int(sym_r.nnz_lu), "lu_levels": sym_r.info["lu_levels"],
+                "u_levels": sym_r.info["u_levels"], "tuning": t_r,
+                "sweeps_max": int(sw_r.max()), "not_converged": int((sw_r <= 0).sum()),
+                "max_rel_err_vs_fp64": float(np.max(np.abs(xr - xb).max(axis=0) /
+                                                    np.abs(xb).max(axis=0)))}
+            del num_r, x_r
+
     # End to end through the host-buffer C ABI call: every step copies its
     # inputs from pinned host memory and its solutions back.  Two handles on
     # two streams alternate, so one batch's copies overlap the other's
@@ -1514,6 +1553,7 @@ def main() -> None:
         # Last on the line, so that a tail of the output keeps them: the
         # target's denominator (the plain single-instance FP64 GPU path) and
         # the split of the headline into batching and precision.
+        "reference_ordering": reference_ordering,
         "batched_fp64": batched_fp64,
         "plain_fp64": {"value": plain, "unit": UNIT, "schedule": plain_name,
                        "all_schedules": single, "autotuned": plain_tuning},

@@ -787,8 +787,13 @@ int pvglu_numeric_create_tuned(const pvglu_symbolic* sym, int n_scenarios, int p
     rc |= h->put(prog.wide.lvl, &P.w_lvl);
     rc |= h->put(prog.wide.lv_chain, &P.lv_chain);
     rc |= h->put(prog.wide.ch_tgt, &P.ch_tgt);
-    rc |= h->put(prog.wide.tg_slot, &P.tg_slot);
-    rc |= h->put(prog.wide.tg_pair, &P.tg_pair);
+    {
+      std::vector<int4> rec(prog.wide.targets());
+      for (size_t t = 0; t < rec.size(); t++)
+        rec[t] = make_int4(prog.wide.tg_rec[4 * t], prog.wide.tg_rec[4 * t + 1],
+                           prog.wide.tg_rec[4 * t + 2], prog.wide.tg_rec[4 * t + 3]);
+      rc |= h->put(rec, &P.tg_rec);
+    }
     rc |= h->put(prog.wide.pr_q, &P.pr_q);
     rc |= h->put(prog.wide.pr_p, &P.pr_p);
     P.n_levels = (int)prog.level_chain.size() - 1;

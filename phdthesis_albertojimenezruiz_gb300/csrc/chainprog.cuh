@@ -42,8 +42,7 @@ struct ProgDev {
   const int* w_lvl;
   const int* lv_chain;
   const int* ch_tgt;
-  const int* tg_slot;
-  const int* tg_pair;
+  const int4* tg_rec;      // {slot, src, n_pairs, q} per target
   const int* pr_q;
   const int* pr_p;
 };

@@ -249,15 +249,17 @@ void plan_wide_column(const Symbolic& s, int k, WidePlan& w) {
     });
     w.lv_chain.push_back((int)w.ch_tgt.size());
     for (const int c : chains) {
-      w.ch_tgt.push_back((int)w.tg_slot.size());
+      w.ch_tgt.push_back(w.targets());
       for (const int t : members[c]) {
-        w.tg_slot.push_back(c0 + t);
+        const int e0 = (int)w.pr_q.size();
         for (const auto& qp : pairs[t]) {
           w.pr_q.push_back(qp.first);
           const int d = qp.second - c0;
           w.pr_p.push_back(clev[d] >= 0 && chain_of[d] == c ? ~qp.second : qp.second);
         }
-        w.tg_pair.push_back((int)w.pr_q.size());
+        const int np = (int)pairs[t].size();
+        w.tg_rec.insert(w.tg_rec.end(), {c0 + t, np == 1 ? w.pr_p[e0] : e0, np,
+                                         np == 1 ? w.pr_q[e0] : -1});
       }
     }
   }
@@ -316,7 +318,6 @@ void build_chain_program(const Symbolic& s, int kind, const ProgramOptions& opt,
                          ChainProgram& out) {
   out = ChainProgram();
   out.kind = kind;
-  out.wide.tg_pair.push_back(0);
   const LevelSet& ls = level_set(s, kind);
   Table t;
   t.init(s.n, s.nnz_lu);
@@ -483,7 +484,7 @@ void build_chain_program(const Symbolic& s, int kind, const ProgramOptions& opt,
   out.chain_unit.push_back((int)out.units.size());
   if (kind < 0) out.wide.lvl.push_back((int)out.wide.lv_chain.size());
   out.wide.lv_chain.push_back((int)out.wide.ch_tgt.size());
-  out.wide.ch_tgt.push_back((int)out.wide.tg_slot.size());
+  out.wide.ch_tgt.push_back(out.wide.targets());
   // A level's table is as wide as its widest segment (the budget is only an
   // upper bound): shared memory per block, and so the blocks an SM holds,
   // follow what the level uses.  The narrow levels of a plant (one segment

@@ -100,16 +100,21 @@ struct Segment {
 // block sum) and is a chain of its own that no target extends.  After the
 // last level the L part is divided by the pivot.  A pair whose U source is
 // a target of the same chain carries ~p (negative) instead of p.
+//
+// Each target has one record of four ints {slot, src, n_pairs, q} (one
+// 16-byte load on the device): with one pair, src is its U slot (or ~slot)
+// and q its L slot; otherwise src is the index of its first pair in pr_q /
+// pr_p (the pairs of consecutive targets are consecutive) and q is -1.
 constexpr int kWideLong = 96;
 struct WidePlan {
   std::vector<int> unit;      // [W] column (refactor) or unknown (solves)
   // refactor only:
   std::vector<int> lvl;       // [W + 1] -> index into lv_chain (the unit's chain levels)
   std::vector<int> lv_chain;  // [chain levels + 1] -> index into ch_tgt
-  std::vector<int> ch_tgt;    // [chains + 1] -> index into tg_slot (a chain's targets, in order)
-  std::vector<int> tg_slot;   // [T] target slot
-  std::vector<int> tg_pair;   // [T + 1] -> index into pr_q / pr_p
+  std::vector<int> ch_tgt;    // [chains + 1] -> target index (a chain's targets, in order)
+  std::vector<int> tg_rec;    // [4 T] target records
   std::vector<int> pr_q, pr_p;  // [P] L slot and U slot (~slot: same chain) of every update
+  int targets() const { return (int)tg_rec.size() / 4; }
 };
 
 struct ChainProgram {

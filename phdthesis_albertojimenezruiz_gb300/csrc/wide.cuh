@@ -40,8 +40,12 @@ __device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, 
 // a chunk of entries in shared memory (batched: a warp per entry, two
 // scenarios per lane; single: a thread per entry) while warp 0 subtracts the
 // previous chunk's products in order (batched: every lane for its two
-// scenarios; single: lane 0), two chunk buffers in turn.  `ab(e, a, b)` gives
-// the operands of entry e (T, or Vec2<T> for the lane's two scenarios).
+// scenarios; single: lane 0), two chunk buffers in turn.  `ix(e, ia, ib)`
+// gives the two operand indices of entry e and `ab(ia, ib, a, b)` the
+// operands (T, or Vec2<T> for the lane's two scenarios); a batched producer
+// warp loads the indices of its entries with one lane each and broadcasts
+// them, so every entry costs one round of index loads and one of operand
+// loads, the entries' loads in flight together.
 // Returns the result in warp 0 (single: in its lane 0).  All threads of the
 // block (at least two warps) must call it.  scratch: scratch_bytes of shared
 // memory, at least wide_scratch_min<T, BATCH>(blockDim.x).
@@ -62,10 +66,10 @@ __host__ __device__ constexpr int wide_scratch_bytes(int threads) {
   return 2 * (BATCH ? 64 : 8 * (threads - 32)) * wide_row_bytes<T, BATCH>();
 }
 
-template <typename T, bool BATCH, typename AB>
+template <typename T, bool BATCH, typename IX, typename AB>
 __device__ __forceinline__ typename std::conditional<BATCH, typename Vec2<T>::type, T>::type
 ordered_sub_block(typename std::conditional<BATCH, typename Vec2<T>::type, T>::type acc,
-                  int count, AB ab, unsigned char* scratch, int scratch_bytes) {
+                  int count, IX ix, AB ab, unsigned char* scratch, int scratch_bytes) {
   using V = typename std::conditional<BATCH, typename Vec2<T>::type, T>::type;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int producers = BATCH ? (blockDim.x >> 5) - 1 : (int)blockDim.x - 32;
@@ -85,10 +89,27 @@ ordered_sub_block(typename std::conditional<BATCH, typename Vec2<T>::type, T>::t
     constexpr int U = (BATCH && sizeof(T) == 8) ? 2 : 4;
     for (int r0 = me; r0 < ch; r0 += U * producers) {
       V a[U], b[U];
+      if constexpr (BATCH) {
+        int ia = 0, ib = 0;
+        if (lane < U && r0 + lane * producers < ch && base + r0 + lane * producers < count)
+          ix(base + r0 + lane * producers, ia, ib);
 #pragma unroll
-      for (int u = 0; u < U; u++) {
-        const int e = base + r0 + u * producers;
-        if (r0 + u * producers < ch && e < count) ab(e, a[u], b[u]);
+        for (int u = 0; u < U; u++) {
+          const int ja = __shfl_sync(0xffffffffu, ia, u), jb = __shfl_sync(0xffffffffu, ib, u);
+          if (r0 + u * producers < ch && base + r0 + u * producers < count) ab(ja, jb, a[u], b[u]);
+        }
+      } else {
+        int ia[U], ib[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+          const int e = base + r0 + u * producers;
+          if (r0 + u * producers < ch && e < count) ix(e, ia[u], ib[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+          const int e = base + r0 + u * producers;
+          if (r0 + u * producers < ch && e < count) ab(ia[u], ib[u], a[u], b[u]);
+        }
       }
 #pragma unroll
       for (int u = 0; u < U; u++) {
@@ -143,18 +164,20 @@ __device__ __forceinline__ float2 ldv2(const float* p) {
 // s0 (batched) or the single scenario, chain level by chain level
 // (programs.hpp, WidePlan): the chains of a level spread over the block's
 // threads (batched: warps), each computed in order, then the level's long
-// targets one at a time by the whole block.  Inside a chain the loads of the
-// next few targets (their own values, and the L operand of single-pair
-// targets) are issued together; a source written
-// earlier in the same chain comes from the register that holds the previous
-// target or, further back, from a plain load after the thread's own store.
-// smem: the block's shared memory (smem_bytes of it); the column is staged
-// there in single mode when len * sizeof(T) + scratch fits.
+// targets one at a time by the whole block.  A batched warp loads the
+// records of 32 targets of its chain at a time (one per lane; the next 32
+// already in flight) and broadcasts them by shuffles; the row loads of the
+// next G targets (their own values, the L operand of single-pair targets)
+// are then issued together.  A source written earlier in the same chain
+// comes from the register that holds the previous target or, further back,
+// from a plain load after the thread's own store.  smem: the block's shared
+// memory (smem_bytes of it); the column is staged there in single mode when
+// len * sizeof(T) + scratch fits.
 template <typename T, bool BATCH>
 __device__ void wide_refactor(const ProgDev& P, const DevStruct& d, int w, int s0,
                               T* __restrict__ v, int ld, int S, T pivot_tol, DevStatus* st,
                               unsigned char* smem, int smem_bytes) {
-  constexpr int G = 4;  // targets whose loads are in flight together
+  constexpr int G = sizeof(T) == 8 ? 3 : 4;  // targets whose loads are in flight together
   const int k = __ldg(P.w_unit + w);
   const int c0 = __ldg(d.colptr + k), dk = __ldg(d.diag + k), c1 = __ldg(d.colptr + k + 1);
   const int len = c1 - c0;
@@ -162,8 +185,7 @@ __device__ void wide_refactor(const ProgDev& P, const DevStruct& d, int w, int s
   const int l_begin = __ldg(P.w_lvl + w), l_end = __ldg(P.w_lvl + w + 1);
   auto is_long = [&](int c) {
     const int t0 = __ldg(P.ch_tgt + c);
-    return __ldg(P.ch_tgt + c + 1) - t0 == 1 &&
-           __ldg(P.tg_pair + t0 + 1) - __ldg(P.tg_pair + t0) > kWideLong;
+    return __ldg(P.ch_tgt + c + 1) - t0 == 1 && __ldg(&P.tg_rec[t0].z) > kWideLong;
   };
   if constexpr (!BATCH) {
     const int scratch = min(wide_scratch_bytes<T, false>(nthr), smem_bytes);
@@ -189,34 +211,40 @@ __device__ void wide_refactor(const ProgDev& P, const DevStruct& d, int w, int s
         int prev = -1;
         T prev_v = T(0);
         for (int t = __ldg(P.ch_tgt + c); t < t1; t++) {
-          const int slot = __ldg(P.tg_slot + t);
-          const int e1 = __ldg(P.tg_pair + t + 1);
-          T acc = get(slot);
-          for (int e = __ldg(P.tg_pair + t); e < e1; e++) {
-            const int p = __ldg(P.pr_p + e);
-            const T u = p >= 0 ? get(p) : (~p == prev ? prev_v : get_own(~p));
-            acc = fnms(acc, ldv(v + __ldg(P.pr_q + e)), u);
+          const int4 r = __ldg(P.tg_rec + t);
+          T acc = get(r.x);
+          if (r.z == 1) {
+            const T u = r.y >= 0 ? get(r.y) : (~r.y == prev ? prev_v : get_own(~r.y));
+            acc = fnms(acc, ldv(v + r.w), u);
+          } else {
+            for (int e = r.y; e < r.y + r.z; e++) {
+              const int p = __ldg(P.pr_p + e);
+              const T u = p >= 0 ? get(p) : (~p == prev ? prev_v : get_own(~p));
+              acc = fnms(acc, ldv(v + __ldg(P.pr_q + e)), u);
+            }
           }
-          put(slot, acc);
-          prev = slot;
+          put(r.x, acc);
+          prev = r.x;
           prev_v = acc;
         }
       }
       __syncthreads();
       for (int c = h0; c < h1; c++) {  // long targets, one at a time by the block
         if (!is_long(c)) continue;
-        const int t = __ldg(P.ch_tgt + c);
-        const int e0 = __ldg(P.tg_pair + t), e1 = __ldg(P.tg_pair + t + 1);
-        const int slot = __ldg(P.tg_slot + t);
-        T acc = get(slot);
+        const int4 r = __ldg(P.tg_rec + __ldg(P.ch_tgt + c));
+        T acc = get(r.x);
         acc = ordered_sub_block<T, false>(
-            acc, e1 - e0,
-            [&](int e, T& a, T& b) {
-              a = ldv(v + __ldg(P.pr_q + e0 + e));
-              b = get(__ldg(P.pr_p + e0 + e));
+            acc, r.z,
+            [&](int e, int& ia, int& ib) {
+              ia = __ldg(P.pr_q + r.y + e);
+              ib = __ldg(P.pr_p + r.y + e);
+            },
+            [&](int ia, int ib, T& a, T& b) {
+              a = ldv(v + ia);
+              b = get(ib);
             },
             scr, scratch);
-        if (tid == 0) put(slot, acc);
+        if (tid == 0) put(r.x, acc);
         __syncthreads();
       }
     }
@@ -242,11 +270,18 @@ __device__ void wide_refactor(const ProgDev& P, const DevStruct& d, int w, int s
       acc.y = fnms(acc.y, a.y, b.y);
       return acc;
     };
+    auto shfl4 = [](int4 r, int src) {
+      r.x = __shfl_sync(0xffffffffu, r.x, src);
+      r.y = __shfl_sync(0xffffffffu, r.y, src);
+      r.z = __shfl_sync(0xffffffffu, r.z, src);
+      r.w = __shfl_sync(0xffffffffu, r.w, src);
+      return r;
+    };
     for (int l = l_begin; l < l_end; l++) {
       const int h0 = __ldg(P.lv_chain + l), h1 = __ldg(P.lv_chain + l + 1);
       for (int c = h0 + warp; c < h1; c += nw) {
         if (is_long(c)) continue;
-        const int t1 = __ldg(P.ch_tgt + c + 1);
+        const int ct0 = __ldg(P.ch_tgt + c), ct1 = __ldg(P.ch_tgt + c + 1);
         int prev = -1;
         V2 prev_v{};
         // A source of this chain: the previous target's register, or a
@@ -254,70 +289,76 @@ __device__ void wide_refactor(const ProgDev& P, const DevStruct& d, int w, int s
         auto own = [&](int p) -> V2 {
           return p == prev ? prev_v : *reinterpret_cast<const V2*>(row(p));
         };
-        for (int t = __ldg(P.ch_tgt + c); t < t1; t += G) {
-          V2 cur[G], qa[G];
-          int slot[G], np[G], ps[G];
+        int4 win = make_int4(0, 0, 0, 0);
+        if (ct0 + lane < ct1) win = __ldg(P.tg_rec + ct0 + lane);
+        for (int w0 = ct0; w0 < ct1; w0 += 32) {
+          const int wn = min(32, ct1 - w0);
+          int4 nxt = make_int4(0, 0, 0, 0);
+          if (w0 + 32 + lane < ct1) nxt = __ldg(P.tg_rec + w0 + 32 + lane);
+          for (int i0 = 0; i0 < wn; i0 += G) {
+            int4 r[G];
+            V2 cur[G], qa[G];
 #pragma unroll
-          for (int u = 0; u < G; u++) {
-            np[u] = -1;
-            if (t + u < t1) {
-              slot[u] = __ldg(P.tg_slot + t + u);
-              const int e0 = __ldg(P.tg_pair + t + u);
-              np[u] = __ldg(P.tg_pair + t + u + 1) - e0;
-              cur[u] = ldv2(row(slot[u]));
-              if (np[u] == 1) {
-                qa[u] = ldv2(row(__ldg(P.pr_q + e0)));
-                ps[u] = __ldg(P.pr_p + e0);
+            for (int u = 0; u < G; u++) {
+              if (i0 + u < wn) {
+                r[u] = shfl4(win, i0 + u);
+                cur[u] = ldv2(row(r[u].x));
+                if (r[u].z == 1) qa[u] = ldv2(row(r[u].w));
               }
             }
-          }
 #pragma unroll
-          for (int u = 0; u < G; u++) {
-            if (np[u] < 0) continue;
-            V2 acc = cur[u];
-            if (np[u] == 1) {
-              acc = fnms2(acc, qa[u], ps[u] >= 0 ? ldv2(row(ps[u])) : own(~ps[u]));
-            } else {
-              const int e0 = __ldg(P.tg_pair + t + u), e1 = e0 + np[u];
-              int e = e0;
-              // Two updates' operands in flight at a time; the subtractions
-              // stay in order.
-              for (; e + 2 <= e1; e += 2) {
-                V2 a[2], b[2];
-                int pp[2];
+            for (int u = 0; u < G; u++) {
+              if (i0 + u >= wn) continue;
+              V2 acc = cur[u];
+              if (r[u].z == 1) {
+                acc = fnms2(acc, qa[u], r[u].y >= 0 ? ldv2(row(r[u].y)) : own(~r[u].y));
+              } else {
+                const int e1 = r[u].y + r[u].z;
+                int e = r[u].y;
+                // Two updates' operands in flight at a time; the
+                // subtractions stay in order.
+                for (; e + 2 <= e1; e += 2) {
+                  V2 a[2], b[2];
+                  int pp[2];
 #pragma unroll
-                for (int i = 0; i < 2; i++) {
-                  a[i] = ldv2(row(__ldg(P.pr_q + e + i)));
-                  pp[i] = __ldg(P.pr_p + e + i);
-                  if (pp[i] >= 0) b[i] = ldv2(row(pp[i]));
+                  for (int i = 0; i < 2; i++) {
+                    a[i] = ldv2(row(__ldg(P.pr_q + e + i)));
+                    pp[i] = __ldg(P.pr_p + e + i);
+                    if (pp[i] >= 0) b[i] = ldv2(row(pp[i]));
+                  }
+#pragma unroll
+                  for (int i = 0; i < 2; i++)
+                    acc = fnms2(acc, a[i], pp[i] >= 0 ? b[i] : own(~pp[i]));
                 }
-#pragma unroll
-                for (int i = 0; i < 2; i++) acc = fnms2(acc, a[i], pp[i] >= 0 ? b[i] : own(~pp[i]));
+                for (; e < e1; e++) {
+                  const int p = __ldg(P.pr_p + e);
+                  const V2 a = ldv2(row(__ldg(P.pr_q + e)));
+                  acc = fnms2(acc, a, p >= 0 ? ldv2(row(p)) : own(~p));
+                }
               }
-              for (; e < e1; e++) {
-                const int p = __ldg(P.pr_p + e);
-                const V2 a = ldv2(row(__ldg(P.pr_q + e)));
-                acc = fnms2(acc, a, p >= 0 ? ldv2(row(p)) : own(~p));
-              }
+              *reinterpret_cast<V2*>(row(r[u].x)) = acc;
+              prev = r[u].x;
+              prev_v = acc;
             }
-            *reinterpret_cast<V2*>(row(slot[u])) = acc;
-            prev = slot[u];
-            prev_v = acc;
           }
+          win = nxt;
         }
       }
       __syncthreads();
       for (int c = h0; c < h1; c++) {
         if (!is_long(c)) continue;
-        const int t = __ldg(P.ch_tgt + c);
-        const int e0 = __ldg(P.tg_pair + t), e1 = __ldg(P.tg_pair + t + 1);
-        T* tp = row(__ldg(P.tg_slot + t));
+        const int4 r = __ldg(P.tg_rec + __ldg(P.ch_tgt + c));
+        T* tp = row(r.x);
         V2 acc = ldv2(tp);
         acc = ordered_sub_block<T, true>(
-            acc, e1 - e0,
-            [&](int e, V2& a, V2& b) {
-              a = ldv2(row(__ldg(P.pr_q + e0 + e)));
-              b = ldv2(row(__ldg(P.pr_p + e0 + e)));
+            acc, r.z,
+            [&](int e, int& ia, int& ib) {
+              ia = __ldg(P.pr_q + r.y + e);
+              ib = __ldg(P.pr_p + r.y + e);
+            },
+            [&](int ia, int ib, V2& a, V2& b) {
+              a = ldv2(row(ia));
+              b = ldv2(row(ib));
             },
             smem, smem_bytes);
         if (warp == 0) *reinterpret_cast<V2*>(tp) = acc;
@@ -384,10 +425,8 @@ __device__ void wide_solve(const ProgDev& P, const DevStruct& d, int w, int s0,
   if constexpr (!BATCH) {
     T acc = ldv(x + i);
     acc = ordered_sub_block<T, false>(
-        acc, cnt,
-        [&](int e, T& a, T& b) {
-          int slot, col;
-          entry(e, slot, col);
+        acc, cnt, [&](int e, int& slot, int& col) { entry(e, slot, col); },
+        [&](int slot, int col, T& a, T& b) {
           a = ldv(v + slot);
           b = ldv(x + col);
         },
@@ -402,10 +441,8 @@ __device__ void wide_solve(const ProgDev& P, const DevStruct& d, int w, int s0,
     const int s = s0 + 2 * (threadIdx.x & 31);
     V2 acc = ldv2(x + (int64_t)i * ld + s);
     acc = ordered_sub_block<T, true>(
-        acc, cnt,
-        [&](int e, V2& a, V2& b) {
-          int slot, col;
-          entry(e, slot, col);
+        acc, cnt, [&](int e, int& slot, int& col) { entry(e, slot, col); },
+        [&](int slot, int col, V2& a, V2& b) {
           a = ldv2(v + (int64_t)slot * ld + s);
           b = ldv2(x + (int64_t)col * ld + s);
         },

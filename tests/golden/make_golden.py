@@ -19,7 +19,9 @@ orderings/block_plant_amd.npz holds the reference's AMD ordering (and its
 fill and level counts) of the reference-topology plants (plant.block_plant)
 of 1 x 50 x 50 and 7 x 50 x 50 panels, too large for a full fixture: with the
 ordering, the symbolic analysis reproduces the reference's arrays and the
-oracle's restatement gives the reference's factors.
+oracle's restatement gives the reference's factors.  orderings/plant_amd.npz
+holds the same for the benchmark's string/combiner plant (plant.Plant) of
+50 x 24 x 28 panels.
 """
 from __future__ import annotations
 
@@ -39,11 +41,10 @@ from oracle import oracle as O  # noqa: E402
 FIXTURES = ("plant_1x2x2", "plant_c1", "mesh_12x10", "mesh_20x20", "random_300",
             "block_1x20x20")
 BLOCK_ORDERINGS = ((1, 50, 50), (7, 50, 50))
+PLANT_ORDERINGS = ((50, 24, 28),)
 
 
-def main() -> None:
-    if O.build_ref() is None:
-        raise SystemExit("reference sources not found; fixtures cannot be regenerated here")
+def fixtures() -> None:
     for name in FIXTURES:
         rp, ci, a, b = M.CASES[name]()
         ref = O.Ref(rp, ci)
@@ -63,19 +64,43 @@ def main() -> None:
         np.savez_compressed(HERE / f"{name}.npz", rowptr=rp, colidx=ci, a=a, b=b, csc_in=csc,
                             lu_seq=lu_seq, lu_levels=lu_lev, x_perm=x_perm, x=x, **arrs)
         print(f"{name}: n={n} nnz_lu={len(csc)}")
+
+
+def orderings(kind: str) -> None:
+    """The reference's AMD ordering with its fill and level counts:
+    kind "block" for plant.block_plant, "plant" for plant.Plant."""
+    from phdthesis_albertojimenezruiz_gb300 import Plant
+
     out = {}
-    for dims in BLOCK_ORDERINGS:
-        rp, ci, _, _ = M.block(dims)
+    for dims in (BLOCK_ORDERINGS if kind == "block" else PLANT_ORDERINGS):
+        if kind == "block":
+            rp, ci, _, _ = M.block(dims)
+        else:
+            p = Plant(*dims)
+            rp, ci = p.rowptr, p.colidx
         ref = O.Ref(rp, ci)
         tag = "x".join(map(str, dims))
         out[f"perm_{tag}"] = ref.get("perm_amd")
         out[f"nnz_lu_{tag}"] = np.array(len(ref.get("csc_row")))
         out[f"u_levels_{tag}"] = np.array(len(ref.get("u_sl")) - 1)
         out[f"lu_levels_{tag}"] = np.array(len(ref.get("lu_sl")) - 1)
-        print(f"block {tag}: n={len(rp) - 1} nnz_lu={int(out[f'nnz_lu_{tag}'])} "
+        print(f"{kind} {tag}: n={len(rp) - 1} nnz_lu={int(out[f'nnz_lu_{tag}'])} "
               f"u_levels={int(out[f'u_levels_{tag}'])}")
     (HERE / "orderings").mkdir(exist_ok=True)
-    np.savez_compressed(HERE / "orderings" / "block_plant_amd.npz", **out)
+    name = "block_plant_amd.npz" if kind == "block" else "plant_amd.npz"
+    np.savez_compressed(HERE / "orderings" / name, **out)
+
+
+def main() -> None:
+    """Arguments select what to regenerate (fixtures, block, plant); none: all."""
+    if O.build_ref() is None:
+        raise SystemExit("reference sources not found; fixtures cannot be regenerated here")
+    what = sys.argv[1:] or ["fixtures", "block", "plant"]
+    if "fixtures" in what:
+        fixtures()
+    for kind in ("block", "plant"):
+        if kind in what:
+            orderings(kind)
 
 
 if __name__ == "__main__":

@@ -197,6 +197,8 @@ void check_program(const Symbolic& s, int kind, const ProgramOptions& opt) {
   if (kind == -1) {
     const WidePlan& w = pr.wide;
     CHECK(w.lvl.size() == w.unit.size() + 1, "wide lvl size");
+    CHECK(w.tg_rec.size() % 4 == 0 && w.pr_q.size() == w.pr_p.size(), "wide plan sizes");
+    int next_pair = 0;
     for (size_t i = 0; i < w.unit.size(); i++) {
       const int k = w.unit[i];
       const int c0 = s.csc_colptr[k], dk = s.diag_slot[k], c1 = s.csc_colptr[k + 1];
@@ -209,14 +211,22 @@ void check_program(const Symbolic& s, int kind, const ProgramOptions& opt) {
       for (int l = w.lvl[i]; l < w.lvl[i + 1]; l++)
         for (int c = w.lv_chain[l]; c < w.lv_chain[l + 1]; c++)
           for (int t = w.ch_tgt[c]; t < w.ch_tgt[c + 1]; t++) {
-            const int slot = w.tg_slot[t];
+            const int* rec = &w.tg_rec[4 * t];
+            const int slot = rec[0], np = rec[2];
             CHECK(slot >= c0 && slot < c1 && level_of[slot - c0] == 0, "wide target %d", slot);
-            const int np = w.tg_pair[t + 1] - w.tg_pair[t];
             CHECK(np > 0, "wide target %d without pairs", slot);
             CHECK(np <= kWideLong || w.ch_tgt[c + 1] - w.ch_tgt[c] == 1,
                   "long wide target %d shares its chain", slot);
+            // The pairs of consecutive targets are consecutive.
+            const int e0 = np == 1 ? next_pair : rec[1];
+            CHECK(e0 == next_pair, "wide target %d pair index", slot);
+            next_pair = e0 + np;
+            if (np == 1)
+              CHECK(rec[1] == w.pr_p[e0] && rec[3] == w.pr_q[e0], "wide record %d", slot);
+            else
+              CHECK(rec[3] == -1, "wide record %d", slot);
             int prev_p = -1;
-            for (int e = w.tg_pair[t]; e < w.tg_pair[t + 1]; e++) {
+            for (int e = e0; e < e0 + np; e++) {
               const int q = w.pr_q[e];
               const bool same = w.pr_p[e] < 0;
               const int p = same ? ~w.pr_p[e] : w.pr_p[e];

@@ -82,6 +82,30 @@ def test_product_vs_port_own_ordering(dims):
     assert s.info["right_looking_hazards"] == 0
 
 
+@pytest.mark.parametrize("fixture,tag,make", [
+    ("plant_amd.npz", "50x24x28", lambda: (lambda p: (p.rowptr, p.colidx))(Plant(50, 24, 28))),
+    ("block_plant_amd.npz", "7x50x50", lambda: M.block((7, 50, 50))[:2]),
+])
+def test_reference_ordering_reproduces_reference_counts(fixture, tag, make):
+    """With the reference's own AMD ordering (fixtures made by the reference's
+    code), the analysis gives the reference's fill and level counts, and the
+    oracle's restatement the same arrays."""
+    from conftest import GOLDEN
+
+    with np.load(GOLDEN / "orderings" / fixture) as z:
+        perm = z[f"perm_{tag}"]
+        want = {k: int(z[f"{k}_{tag}"]) for k in ("nnz_lu", "lu_levels", "u_levels")}
+    rp, ci = make()
+    s = Symbolic(rp, ci, perm)
+    assert int(s.nnz_lu) == want["nnz_lu"]
+    assert s.info["lu_levels"] == want["lu_levels"] and s.info["u_levels"] == want["u_levels"]
+    assert np.array_equal(s.array("perm_amd"), perm)
+    if fixture == "plant_amd.npz":
+        got, ref = s.arrays(), O.Port(rp, ci, perm).arrays()
+        for k in REF_ARRAYS:
+            assert np.array_equal(got[k], ref[k]), k
+
+
 @pytest.mark.parametrize("case", ["mesh_30x30", "random_1500"])
 def test_product_vs_port_fill_heavy(case):
     rp, ci, _, _ = M.CASES[case]()
