@@ -76,6 +76,15 @@ int prog_prepare(pvglu_numeric* h) {
                        (const void*)pvglu::k_wide_level<T, 3, B>};
   for (const void* f : fns)
     if (pvglu::allow_max_dynamic_smem(f) != cudaSuccess) return 1;
+  if constexpr (B) {
+    const void* half[] = {(const void*)pvglu::k_wide_level<T, -1, B, 1>,
+                          (const void*)pvglu::k_wide_level<T, 0, B, 1>,
+                          (const void*)pvglu::k_wide_level<T, 1, B, 1>,
+                          (const void*)pvglu::k_wide_level<T, 2, B, 1>,
+                          (const void*)pvglu::k_wide_level<T, 3, B, 1>};
+    for (const void* f : half)
+      if (pvglu::allow_max_dynamic_smem(f) != cudaSuccess) return 1;
+  }
   h->prog_grid = pvglu::prog_persistent_grid<T, B>(h->table_max);
   return 0;
 }
@@ -100,6 +109,35 @@ size_t wide_smem(const pvglu_numeric* h, int ph, int lv, int threads) {
   return std::min(want, h->smem_optin);
 }
 
+// One WIDE level launch: a block per item (a unit and a group of 32 * LW
+// scenarios).  Batched levels with at most a quarter as many 64-scenario
+// items as SMs run with LW = 1: twice the items, each with half the
+// scenarios, still in blocks of 512 threads.  (With more items the blocks
+// would shrink, and that measured slower: 7 bus columns at 512 scenarios,
+// 3.25 against 3.12 ms per step; at 64 scenarios LW = 1 gives 1.29 against
+// 1.54 ms.)
+template <typename T, int KIND, bool B>
+void launch_wide(pvglu_numeric* h, int ph, int lv, int cb, int ce, T* x, const int* done,
+                 const int* ndone, cudaStream_t st) {
+  int64_t items = (int64_t)(ce - cb) * (B ? h->ld / pvglu::kGroup : 1);
+  const bool half = B && items * 4 <= h->sm_count;
+  if (half) items *= 2;
+  const int threads = wide_threads(h, items);
+  const size_t smem = wide_smem<T, B>(h, ph, lv, threads);
+  T* v = static_cast<T*>(h->values);
+  if constexpr (B) {
+    if (half) {
+      pvglu::k_wide_level<T, KIND, B, 1><<<launch_blocks(items, 1), threads, smem, st>>>(
+          h->progs.p[ph], h->d, cb, ce, v, x, h->ld, h->S, (T)h->pivot_tol, h->status, done,
+          ndone, (int)smem);
+      return;
+    }
+  }
+  pvglu::k_wide_level<T, KIND, B, 2><<<launch_blocks(items, 1), threads, smem, st>>>(
+      h->progs.p[ph], h->d, cb, ce, v, x, h->ld, h->S, (T)h->pivot_tol, h->status, done, ndone,
+      (int)smem);
+}
+
 // One phase of chain programs with one launch per level.
 template <typename T, bool B, int KIND>
 void prog_levels(pvglu_numeric* h, T* x, const int* done, const int* ndone, cudaStream_t st) {
@@ -110,12 +148,7 @@ void prog_levels(pvglu_numeric* h, T* x, const int* done, const int* ndone, cuda
     const int cb = lc[lv], ce = lc[lv + 1];
     const int64_t items = (int64_t)(ce - cb) * groups;
     if (h->prog_level_wide_len[ph][lv] > 0) {  // a WIDE level: a block per unit and group
-      const int threads = wide_threads(h, items);
-      const size_t smem = wide_smem<T, B>(h, ph, (int)lv, threads);
-      pvglu::k_wide_level<T, KIND, B>
-          <<<launch_blocks(items, 1), threads, smem, st>>>(
-              h->progs.p[ph], h->d, cb, ce, static_cast<T*>(h->values), x, h->ld, h->S,
-              h->pivot_tol, h->status, done, ndone, (int)smem);
+      launch_wide<T, KIND, B>(h, ph, (int)lv, cb, ce, x, done, ndone, st);
       continue;
     }
     const int table = h->prog_level_ml[ph][lv];
@@ -1257,13 +1290,8 @@ int group_phase(pvglu_group* g, T* const* xs, cudaStream_t st) {
       if (h->prog_level_wide_len[ph][lv] > 0) {
         // A member's WIDE level: its own launch, a block per unit and group.
         const auto& lc = h->prog_level_chain[ph];
-        const int64_t items = (int64_t)(lc[lv + 1] - lc[lv]) * (B ? h->ld / pvglu::kGroup : 1);
-        const int threads = wide_threads(h, items);
-        const size_t smem = wide_smem<T, B>(h, ph, lv, threads);
-        pvglu::k_wide_level<T, KIND, B><<<launch_blocks(items, 1), threads, smem, st>>>(
-            h->progs.p[ph], h->d, lc[lv], lc[lv + 1], static_cast<T*>(h->values),
-            xs ? xs[i] : nullptr, h->ld, h->S, (T)h->pivot_tol, h->status, nullptr, nullptr,
-            (int)smem);
+        launch_wide<T, KIND, B>(h, ph, lv, lc[lv], lc[lv + 1], xs ? xs[i] : nullptr, nullptr,
+                                nullptr, st);
         continue;
       }
       if (std::find(tables.begin(), tables.end(), h->prog_level_ml[ph][lv]) == tables.end())

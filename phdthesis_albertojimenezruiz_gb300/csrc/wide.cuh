@@ -35,6 +35,37 @@ __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, 
 __device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
 __device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
 
+// Lane values of the batched forms: LW scenarios per lane.  LW = 2: a warp
+// covers 64 scenarios with 16-byte accesses; LW = 1: 32 scenarios, for WIDE
+// levels with fewer items than SMs, which then spread over twice the blocks
+// (each block with half the FP64 work).
+template <typename T, int LW>
+using LaneV = typename std::conditional<LW == 2, typename Vec2<T>::type, T>::type;
+template <typename V, typename T>
+__device__ __forceinline__ V ld_lane(const T* p) {
+  if constexpr (std::is_same<V, T>::value) return __ldcg(p);
+  else return __ldcg(reinterpret_cast<const V*>(p));
+}
+template <typename T>
+__device__ __forceinline__ T mul_lane(T a, T b) { return mul_rn(a, b); }
+template <typename T>
+__device__ __forceinline__ T sub_lane(T a, T b) { return sub_rn(a, b); }
+template <typename T>
+__device__ __forceinline__ T fnms_lane(T acc, T a, T b) { return fnms(acc, a, b); }
+#define PVGLU_LANE2(V)                                                        \
+  __device__ __forceinline__ V mul_lane(V a, V b) {                           \
+    return {mul_rn(a.x, b.x), mul_rn(a.y, b.y)};                              \
+  }                                                                           \
+  __device__ __forceinline__ V sub_lane(V a, V b) {                           \
+    return {sub_rn(a.x, b.x), sub_rn(a.y, b.y)};                              \
+  }                                                                           \
+  __device__ __forceinline__ V fnms_lane(V acc, V a, V b) {                   \
+    return {fnms(acc.x, a.x, b.x), fnms(acc.y, a.y, b.y)};                    \
+  }
+PVGLU_LANE2(double2)
+PVGLU_LANE2(float2)
+#undef PVGLU_LANE2
+
 // acc - sum_e a_e * b_e in the order e = 0 .. count-1, each product and each
 // difference rounded on its own.  Warps 1.. of the block form the products of
 // a chunk of entries in shared memory (batched: a warp per entry, two
@@ -42,7 +73,7 @@ __device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, 
 // previous chunk's products in order (batched: every lane for its two
 // scenarios; single: lane 0), two chunk buffers in turn.  `ix(e, ia, ib)`
 // gives the two operand indices of entry e and `ab(ia, ib, a, b)` the
-// operands (T, or Vec2<T> for the lane's two scenarios); a batched producer
+// operands (T, or the lane's LW scenarios); a batched producer
 // warp loads the indices of its entries with one lane each and broadcasts
 // them, so every entry costs one round of index loads and one of operand
 // loads, the entries' loads in flight together.
@@ -66,14 +97,14 @@ __host__ __device__ constexpr int wide_scratch_bytes(int threads) {
   return 2 * (BATCH ? 64 : 8 * (threads - 32)) * wide_row_bytes<T, BATCH>();
 }
 
-template <typename T, bool BATCH, typename IX, typename AB>
-__device__ __forceinline__ typename std::conditional<BATCH, typename Vec2<T>::type, T>::type
-ordered_sub_block(typename std::conditional<BATCH, typename Vec2<T>::type, T>::type acc,
-                  int count, IX ix, AB ab, unsigned char* scratch, int scratch_bytes) {
-  using V = typename std::conditional<BATCH, typename Vec2<T>::type, T>::type;
+template <typename T, bool BATCH, int LW, typename IX, typename AB>
+__device__ __forceinline__ typename std::conditional<BATCH, LaneV<T, LW>, T>::type
+ordered_sub_block(typename std::conditional<BATCH, LaneV<T, LW>, T>::type acc, int count,
+                  IX ix, AB ab, unsigned char* scratch, int scratch_bytes) {
+  using V = typename std::conditional<BATCH, LaneV<T, LW>, T>::type;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int producers = BATCH ? (blockDim.x >> 5) - 1 : (int)blockDim.x - 32;
-  const int rb = wide_row_bytes<T, BATCH>();
+  const int rb = BATCH ? 32 * LW * (int)sizeof(T) : (int)sizeof(T);
   int ch = scratch_bytes / (2 * rb);
   ch = max(producers, ch - ch % producers);  // rows per chunk, a multiple of the producers
   V* buf = reinterpret_cast<V*>(scratch);
@@ -86,7 +117,7 @@ ordered_sub_block(typename std::conditional<BATCH, typename Vec2<T>::type, T>::t
     // Up to U entries' operands in flight, then their products (two for
     // FP64 pairs, which keeps the kernels of up to 512 threads within 128
     // registers).
-    constexpr int U = (BATCH && sizeof(T) == 8) ? 2 : 4;
+    constexpr int U = (BATCH && LW * sizeof(T) == 16) ? 2 : 4;
     for (int r0 = me; r0 < ch; r0 += U * producers) {
       V a[U], b[U];
       if constexpr (BATCH) {
@@ -114,16 +145,7 @@ ordered_sub_block(typename std::conditional<BATCH, typename Vec2<T>::type, T>::t
 #pragma unroll
       for (int u = 0; u < U; u++) {
         const int r = r0 + u * producers;
-        if (r < ch && base + r < count) {
-          V p;
-          if constexpr (BATCH) {
-            p.x = mul_rn(a[u].x, b[u].x);
-            p.y = mul_rn(a[u].y, b[u].y);
-          } else {
-            p = mul_rn(a[u], b[u]);
-          }
-          out[r * stride + (BATCH ? lane : 0)] = p;
-        }
+        if (r < ch && base + r < count) out[r * stride + (BATCH ? lane : 0)] = mul_lane(a[u], b[u]);
       }
     }
   };
@@ -134,15 +156,7 @@ ordered_sub_block(typename std::conditional<BATCH, typename Vec2<T>::type, T>::t
       if (BATCH || lane == 0) {
         const V* in = buf + (size_t)(c & 1) * ch * stride;
         const int m = min(ch, count - c * ch);
-        for (int i = 0; i < m; i++) {
-          const V p = in[i * stride + (BATCH ? lane : 0)];
-          if constexpr (BATCH) {
-            acc.x = sub_rn(acc.x, p.x);
-            acc.y = sub_rn(acc.y, p.y);
-          } else {
-            acc = sub_rn(acc, p);
-          }
-        }
+        for (int i = 0; i < m; i++) acc = sub_lane(acc, in[i * stride + (BATCH ? lane : 0)]);
       }
     } else if (c + 1 < nchunks) {
       produce(c + 1);
@@ -150,13 +164,6 @@ ordered_sub_block(typename std::conditional<BATCH, typename Vec2<T>::type, T>::t
     __syncthreads();
   }
   return acc;
-}
-
-__device__ __forceinline__ double2 ldv2(const double* p) {
-  return __ldcg(reinterpret_cast<const double2*>(p));
-}
-__device__ __forceinline__ float2 ldv2(const float* p) {
-  return __ldcg(reinterpret_cast<const float2*>(p));
 }
 
 // ---------------------------------------------------------------------------
@@ -173,7 +180,7 @@ __device__ __forceinline__ float2 ldv2(const float* p) {
 // from a plain load after the thread's own store.  smem: the block's shared
 // memory (smem_bytes of it); the column is staged there in single mode when
 // len * sizeof(T) + scratch fits.
-template <typename T, bool BATCH>
+template <typename T, bool BATCH, int LW = 2>
 __device__ void wide_refactor(const ProgDev& P, const DevStruct& d, int w, int s0,
                               T* __restrict__ v, int ld, int S, T pivot_tol, DevStatus* st,
                               unsigned char* smem, int smem_bytes) {
@@ -233,7 +240,7 @@ __device__ void wide_refactor(const ProgDev& P, const DevStruct& d, int w, int s
         if (!is_long(c)) continue;
         const int4 r = __ldg(P.tg_rec + __ldg(P.ch_tgt + c));
         T acc = get(r.x);
-        acc = ordered_sub_block<T, false>(
+        acc = ordered_sub_block<T, false, LW>(
             acc, r.z,
             [&](int e, int& ia, int& ib) {
               ia = __ldg(P.pr_q + r.y + e);
@@ -261,15 +268,10 @@ __device__ void wide_refactor(const ProgDev& P, const DevStruct& d, int w, int s
       for (int i = tid; i < len; i += nthr) v[c0 + i] = col[i];
     __syncthreads();
   } else {
-    using V2 = typename Vec2<T>::type;
+    using V2 = LaneV<T, LW>;
     const int lane = tid & 31, warp = tid >> 5, nw = nthr >> 5;
-    const int s = s0 + 2 * lane;
+    const int s = s0 + LW * lane;
     auto row = [&](int slot) { return v + (int64_t)slot * ld + s; };
-    auto fnms2 = [](V2 acc, V2 a, V2 b) {
-      acc.x = fnms(acc.x, a.x, b.x);
-      acc.y = fnms(acc.y, a.y, b.y);
-      return acc;
-    };
     auto shfl4 = [](int4 r, int src) {
       r.x = __shfl_sync(0xffffffffu, r.x, src);
       r.y = __shfl_sync(0xffffffffu, r.y, src);
@@ -302,8 +304,8 @@ __device__ void wide_refactor(const ProgDev& P, const DevStruct& d, int w, int s
             for (int u = 0; u < G; u++) {
               if (i0 + u < wn) {
                 r[u] = shfl4(win, i0 + u);
-                cur[u] = ldv2(row(r[u].x));
-                if (r[u].z == 1) qa[u] = ldv2(row(r[u].w));
+                cur[u] = ld_lane<V2>(row(r[u].x));
+                if (r[u].z == 1) qa[u] = ld_lane<V2>(row(r[u].w));
               }
             }
 #pragma unroll
@@ -311,7 +313,7 @@ __device__ void wide_refactor(const ProgDev& P, const DevStruct& d, int w, int s
               if (i0 + u >= wn) continue;
               V2 acc = cur[u];
               if (r[u].z == 1) {
-                acc = fnms2(acc, qa[u], r[u].y >= 0 ? ldv2(row(r[u].y)) : own(~r[u].y));
+                acc = fnms_lane(acc, qa[u], r[u].y >= 0 ? ld_lane<V2>(row(r[u].y)) : own(~r[u].y));
               } else {
                 const int e1 = r[u].y + r[u].z;
                 int e = r[u].y;
@@ -322,18 +324,18 @@ __device__ void wide_refactor(const ProgDev& P, const DevStruct& d, int w, int s
                   int pp[2];
 #pragma unroll
                   for (int i = 0; i < 2; i++) {
-                    a[i] = ldv2(row(__ldg(P.pr_q + e + i)));
+                    a[i] = ld_lane<V2>(row(__ldg(P.pr_q + e + i)));
                     pp[i] = __ldg(P.pr_p + e + i);
-                    if (pp[i] >= 0) b[i] = ldv2(row(pp[i]));
+                    if (pp[i] >= 0) b[i] = ld_lane<V2>(row(pp[i]));
                   }
 #pragma unroll
                   for (int i = 0; i < 2; i++)
-                    acc = fnms2(acc, a[i], pp[i] >= 0 ? b[i] : own(~pp[i]));
+                    acc = fnms_lane(acc, a[i], pp[i] >= 0 ? b[i] : own(~pp[i]));
                 }
                 for (; e < e1; e++) {
                   const int p = __ldg(P.pr_p + e);
-                  const V2 a = ldv2(row(__ldg(P.pr_q + e)));
-                  acc = fnms2(acc, a, p >= 0 ? ldv2(row(p)) : own(~p));
+                  const V2 a = ld_lane<V2>(row(__ldg(P.pr_q + e)));
+                  acc = fnms_lane(acc, a, p >= 0 ? ld_lane<V2>(row(p)) : own(~p));
                 }
               }
               *reinterpret_cast<V2*>(row(r[u].x)) = acc;
@@ -349,37 +351,42 @@ __device__ void wide_refactor(const ProgDev& P, const DevStruct& d, int w, int s
         if (!is_long(c)) continue;
         const int4 r = __ldg(P.tg_rec + __ldg(P.ch_tgt + c));
         T* tp = row(r.x);
-        V2 acc = ldv2(tp);
-        acc = ordered_sub_block<T, true>(
+        V2 acc = ld_lane<V2>(tp);
+        acc = ordered_sub_block<T, true, LW>(
             acc, r.z,
             [&](int e, int& ia, int& ib) {
               ia = __ldg(P.pr_q + r.y + e);
               ib = __ldg(P.pr_p + r.y + e);
             },
             [&](int ia, int ib, V2& a, V2& b) {
-              a = ldv2(row(ia));
-              b = ldv2(row(ib));
+              a = ld_lane<V2>(row(ia));
+              b = ld_lane<V2>(row(ib));
             },
             smem, smem_bytes);
         if (warp == 0) *reinterpret_cast<V2*>(tp) = acc;
         __syncthreads();
       }
     }
-    const V2 piv = ldv2(row(dk));
-    if (warp == 0) {
-      if (!(fabs(piv.x) >= pivot_tol) && s < S) report_error(st, 3, k, s);
-      if (!(fabs(piv.y) >= pivot_tol) && s + 1 < S) report_error(st, 3, k, s + 1);
-    }
-    for (int q = dk + 1 + warp; q < c1; q += nw) {
-      V2 val = ldv2(row(q));
-      if constexpr (std::is_same<T, float>::value) {
-        val.x *= __frcp_rn(piv.x);
-        val.y *= __frcp_rn(piv.y);
-      } else {
-        val.x = val.x / piv.x;
-        val.y = val.y / piv.y;
+    const V2 piv = ld_lane<V2>(row(dk));
+    // The L part divided by the pivot (FP32: times one reciprocal).
+    auto scale = [&](T val, T pv) -> T {
+      if constexpr (std::is_same<T, float>::value) return val * __frcp_rn(pv);
+      else return val / pv;
+    };
+    if constexpr (LW == 2) {
+      if (warp == 0) {
+        if (!(fabs(piv.x) >= pivot_tol) && s < S) report_error(st, 3, k, s);
+        if (!(fabs(piv.y) >= pivot_tol) && s + 1 < S) report_error(st, 3, k, s + 1);
       }
-      *reinterpret_cast<V2*>(row(q)) = val;
+      for (int q = dk + 1 + warp; q < c1; q += nw) {
+        V2 val = ld_lane<V2>(row(q));
+        val.x = scale(val.x, piv.x);
+        val.y = scale(val.y, piv.y);
+        *reinterpret_cast<V2*>(row(q)) = val;
+      }
+    } else {
+      if (warp == 0 && !(fabs(piv) >= pivot_tol) && s < S) report_error(st, 3, k, s);
+      for (int q = dk + 1 + warp; q < c1; q += nw) *row(q) = scale(ld_lane<V2>(row(q)), piv);
     }
     __syncthreads();
   }
@@ -388,7 +395,7 @@ __device__ void wide_refactor(const ProgDev& P, const DevStruct& d, int w, int s
 // ---------------------------------------------------------------------------
 // One wide unknown of a solve (KIND 0: L row, 1: U row, 2: U^T column, 3:
 // L^T column), the same arithmetic and order as solve_unknown.
-template <typename T, int KIND, bool BATCH>
+template <typename T, int KIND, bool BATCH, int LW = 2>
 __device__ void wide_solve(const ProgDev& P, const DevStruct& d, int w, int s0,
                            const T* __restrict__ v, T* __restrict__ x, int ld,
                            unsigned char* smem, int smem_bytes) {
@@ -424,7 +431,7 @@ __device__ void wide_solve(const ProgDev& P, const DevStruct& d, int w, int s0,
   };
   if constexpr (!BATCH) {
     T acc = ldv(x + i);
-    acc = ordered_sub_block<T, false>(
+    acc = ordered_sub_block<T, false, LW>(
         acc, cnt, [&](int e, int& slot, int& col) { entry(e, slot, col); },
         [&](int slot, int col, T& a, T& b) {
           a = ldv(v + slot);
@@ -437,21 +444,25 @@ __device__ void wide_solve(const ProgDev& P, const DevStruct& d, int w, int s0,
     }
     __syncthreads();
   } else {
-    using V2 = typename Vec2<T>::type;
-    const int s = s0 + 2 * (threadIdx.x & 31);
-    V2 acc = ldv2(x + (int64_t)i * ld + s);
-    acc = ordered_sub_block<T, true>(
+    using V2 = LaneV<T, LW>;
+    const int s = s0 + LW * (threadIdx.x & 31);
+    V2 acc = ld_lane<V2>(x + (int64_t)i * ld + s);
+    acc = ordered_sub_block<T, true, LW>(
         acc, cnt, [&](int e, int& slot, int& col) { entry(e, slot, col); },
         [&](int slot, int col, V2& a, V2& b) {
-          a = ldv2(v + (int64_t)slot * ld + s);
-          b = ldv2(x + (int64_t)col * ld + s);
+          a = ld_lane<V2>(v + (int64_t)slot * ld + s);
+          b = ld_lane<V2>(x + (int64_t)col * ld + s);
         },
         smem, smem_bytes);
     if ((threadIdx.x >> 5) == 0) {
       if (dg >= 0) {
-        const V2 p = ldv2(v + (int64_t)dg * ld + s);
-        acc.x = acc.x / p.x;
-        acc.y = acc.y / p.y;
+        const V2 p = ld_lane<V2>(v + (int64_t)dg * ld + s);
+        if constexpr (LW == 2) {
+          acc.x = acc.x / p.x;
+          acc.y = acc.y / p.y;
+        } else {
+          acc = acc / p;
+        }
       }
       *reinterpret_cast<V2*>(x + (int64_t)i * ld + s) = acc;
     }
@@ -462,22 +473,23 @@ __device__ void wide_solve(const ProgDev& P, const DevStruct& d, int w, int s0,
 // The wide units [cb, ce) of one WIDE program level: item = (unit, scenario
 // group), a block per item, blocks striding over the items.  done (solves of
 // a refinement): a group whose scenarios have all converged is skipped.
-template <typename T, int KIND, bool BATCH>
+template <typename T, int KIND, bool BATCH, int LW = 2>
 __device__ __forceinline__ void wide_run_level(const ProgDev& P, const DevStruct& d, int cb,
                                                int ce, T* __restrict__ v, T* __restrict__ x,
                                                int ld, int S, T pivot_tol, DevStatus* st,
                                                const int* done, unsigned char* smem,
                                                int smem_bytes, int block, int n_blocks) {
-  const int groups = BATCH ? ld / kGroup : 1;
+  constexpr int group = 32 * LW;  // scenarios of a batched item
+  const int groups = BATCH ? ld / group : 1;
   const int items = (ce - cb) * groups;
   for (int it = block; it < items; it += n_blocks) {
     const int ci = BATCH ? it / groups : it;
-    const int s0 = BATCH ? (it - ci * groups) * kGroup : 0;
+    const int s0 = BATCH ? (it - ci * groups) * group : 0;
     if (BATCH && done) {
       __shared__ int idle;
       if (threadIdx.x == 0) {
         int all = 1;
-        for (int s = s0; s < s0 + kGroup && all; s++) all = (s >= S || done[s]);
+        for (int s = s0; s < s0 + group && all; s++) all = (s >= S || done[s]);
         idle = all;
       }
       __syncthreads();
@@ -487,15 +499,16 @@ __device__ __forceinline__ void wide_run_level(const ProgDev& P, const DevStruct
     }
     // The chain's single WIDE segment names the wide unit.
     const int w = __ldg(&P.seg[__ldg(P.chain_seg + cb + ci)].z);
-    if (KIND < 0) wide_refactor<T, BATCH>(P, d, w, s0, v, ld, S, pivot_tol, st, smem, smem_bytes);
-    else wide_solve<T, (KIND < 0 ? 0 : KIND), BATCH>(P, d, w, s0, v, x, ld, smem, smem_bytes);
+    if (KIND < 0) wide_refactor<T, BATCH, LW>(P, d, w, s0, v, ld, S, pivot_tol, st, smem, smem_bytes);
+    else wide_solve<T, (KIND < 0 ? 0 : KIND), BATCH, LW>(P, d, w, s0, v, x, ld, smem, smem_bytes);
   }
 }
 
 // Launch form of a WIDE program level (the per-level schedule): kProgBlock
-// threads per block, or up to kWideBlockMax when the level has few items.
+// threads per block, or up to kWideBlockMax when the level has few items;
+// batched levels with fewer items than SMs also run with LW = 1.
 constexpr int kWideBlockMax = 512;
-template <typename T, int KIND, bool BATCH>
+template <typename T, int KIND, bool BATCH, int LW = 2>
 __global__ void __launch_bounds__(kWideBlockMax, 1)
 k_wide_level(ProgDev P, DevStruct d, int cb, int ce, T* __restrict__ v, T* __restrict__ x,
              int ld, int S, T pivot_tol, DevStatus* st, const int* done, const int* ndone,
@@ -503,8 +516,8 @@ k_wide_level(ProgDev P, DevStruct d, int cb, int ce, T* __restrict__ v, T* __res
   if (ndone && __ldcg(ndone) >= S) return;
   if (__ldcg(&st->code) == 6) return;
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  wide_run_level<T, KIND, BATCH>(P, d, cb, ce, v, x, ld, S, pivot_tol, st, done, smem_raw,
-                                 smem_bytes, blockIdx.x, gridDim.x);
+  wide_run_level<T, KIND, BATCH, LW>(P, d, cb, ce, v, x, ld, S, pivot_tol, st, done, smem_raw,
+                                     smem_bytes, blockIdx.x, gridDim.x);
 }
 
 }  // namespace pvglu
