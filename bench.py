@@ -1302,6 +1302,35 @@ def main() -> None:
         _, x_ref = port.scatter_refactor_solve(a[:, k], b[:, k])
         oracle_err.append(float(np.abs(xa[:, k] - x_ref).max() / np.abs(x_ref).max()))
 
+    # The same step with the refinement stopped at the benchmark spec's accuracy
+    # bar (1e-10 relative to the FP64 oracle) instead of 1e-12: its rate,
+    # sweeps and errors, reported beside the headline (which keeps 1e-12).
+    x_s = torch.zeros_like(b_d)
+
+    def spec_step():
+        num.scatter(a_d, stream=stream)
+        num.refactor(stream=stream)
+        num.solve_refined(a_d, b_d, x_s, tol=1e-10, max_sweeps=IR_MAX_SWEEPS, sweeps=sweeps,
+                          stream=stream)
+
+    for _ in range(args.warmup):
+        spec_step()
+    ms_s = _time_ms(spec_step, stream, args.steps)
+    sw_s = sweeps.cpu().numpy()[:S]
+    xs_h = x_s.cpu().numpy()[:, :S]
+    spec_oracle = []
+    for k in sorted({0, 1, S // 3, S // 2, (2 * S) // 3, S - 1}):
+        _, x_ref = port.scatter_refactor_solve(a[:, k], b[:, k])
+        spec_oracle.append(float(np.abs(xs_h[:, k] - x_ref).max() / np.abs(x_ref).max()))
+    at_spec_tolerance = {
+        "value": S / (ms_s / 1000.0), "unit": UNIT, "ms_per_step": ms_s, "ir_tol": 1e-10,
+        "sweeps_min": int(sw_s.min()), "sweeps_max": int(sw_s.max()),
+        "not_converged": int((sw_s <= 0).sum()),
+        "max_rel_err_vs_fp64": float(np.max(np.abs(xs_h - xb).max(axis=0) /
+                                            np.abs(xb).max(axis=0))),
+        "max_rel_err_vs_oracle_fp64": max(spec_oracle)}
+    del x_s
+
     # Plain single-instance FP64 GPU path: one scenario, scatter + refactor +
     # solve, in each schedule; the fastest is the denominator of the ratio.
     a1 = a_d[:, 0].contiguous()
@@ -1553,6 +1582,7 @@ def main() -> None:
         # Last on the line, so that a tail of the output keeps them: the
         # target's denominator (the plain single-instance FP64 GPU path) and
         # the split of the headline into batching and precision.
+        "at_spec_tolerance": at_spec_tolerance,
         "reference_ordering": reference_ordering,
         "batched_fp64": batched_fp64,
         "plain_fp64": {"value": plain, "unit": UNIT, "schedule": plain_name,

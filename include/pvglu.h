@@ -123,7 +123,9 @@ int pvglu_symbolic_get_array(const pvglu_symbolic* s, const char* name,
  * sharing the symbolic analysis.  Values are stored slot-major with the
  * scenario index fastest: value(slot, s) at [slot * ld + s], ld =
  * pvglu_numeric_ld() (n_scenarios rounded up for aligned vector access).
- * Replaces struct_CPU_CUDA_arrays::create_CUDA (factorize_electrical_system.h:63-98). */
+ * Per-level schedule; chain merging as described under merge_chains of
+ * pvglu_tuning.  Replaces struct_CPU_CUDA_arrays::create_CUDA
+ * (factorize_electrical_system.h:63-98). */
 int pvglu_numeric_create(const pvglu_symbolic* s, int n_scenarios, int precision,
                          pvglu_numeric** out);
 /* As pvglu_numeric_create with the table size of the chain programs:
@@ -350,8 +352,10 @@ int pvglu_autotune(const pvglu_symbolic* s, int n_scenarios, int precision,
  *                   bus end give in the U solve, become one chain); 0: the
  *                   level set's own levels and chains, merged a whole level
  *                   at a time as the reference does
- *                   (007_convert_dependencies_in_levels.cpp:89-210), the
- *                   choice of pvglu_numeric_create(_ex).  Regrouping removes
+ *                   (007_convert_dependencies_in_levels.cpp:89-210).
+ *                   pvglu_numeric_create(_ex) chooses 2 where that halves
+ *                   the execution levels of the refactorization and the L
+ *                   and U solves together, 0 otherwise.  Regrouping removes
  *                   levels on deep patterns but can lengthen the chains of a
  *                   narrow level where no level is saved;
  *   schedule        PVGLU_SCHED_*. */

@@ -30,6 +30,20 @@ namespace {
 
 cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
+// Chain merging of pvglu_numeric_create(_ex) and pvglu_autotune: the level
+// set's own chains, or ladder merging where that removes at least half of
+// the execution levels (the U solve of the reference's own plant topology
+// goes from 100 levels to 2).  Where no level is removed, regrouping can
+// only lengthen a narrow level's chains.
+int default_merge(const pvglu::Symbolic& s) {
+  int own = 0, ladder = 0;
+  for (int kind = -1; kind <= 1; kind++) {
+    own += pvglu::execution_level_count(s, kind, 0);
+    ladder += pvglu::execution_level_count(s, kind, 2);
+  }
+  return 2 * ladder <= own ? 2 : 0;
+}
+
 int launch_blocks(int64_t threads, int block) {
   int64_t b = (threads + block - 1) / block;
   return (int)std::max<int64_t>(1, std::min<int64_t>(b, 1 << 30));
@@ -608,9 +622,8 @@ int pvglu_numeric_create(const pvglu_symbolic* sym, int n_scenarios, int precisi
 
 int pvglu_numeric_create_ex(const pvglu_symbolic* sym, int n_scenarios, int precision,
                             int max_locals, pvglu_numeric** out) {
-  // The level set's own chains: regrouping per unit can lengthen a narrow
-  // level's chains without removing a level; the autotuner tries it.
-  const pvglu_tuning t{max_locals, 0, 0, PVGLU_SCHED_LEVELS};
+  if (!sym) return fail(PVGLU_ERR_BAD_ARG, "symbolic handle is NULL");
+  const pvglu_tuning t{max_locals, 0, default_merge(sym->s), PVGLU_SCHED_LEVELS};
   return pvglu_numeric_create_tuned(sym, n_scenarios, precision, &t, out);
 }
 
@@ -1523,9 +1536,10 @@ int pvglu_autotune(const pvglu_symbolic* sym, int n_scenarios, int precision,
     return fail(PVGLU_ERR_BAD_ARG, "bad autotune arguments");
   const int ld = n_scenarios == 1 ? 1 : ((n_scenarios + 63) / 64) * 64;
   std::vector<pvglu_tuning> cands;
+  const int merge = default_merge(sym->s);
   for (const int ml : table_candidates(ld, precision))
     for (const int sc : {PVGLU_SCHED_LEVELS, PVGLU_SCHED_PERSISTENT})
-      cands.push_back(pvglu_tuning{ml, 0, 0, sc});
+      cands.push_back(pvglu_tuning{ml, 0, merge, sc});
   pvglu_tuning bt{};
   const int rc = autotune_over(sym, n_scenarios, precision, cands, &bt, best_ms);
   if (rc) return rc;

@@ -314,6 +314,14 @@ void execution_levels(const Symbolic& s, int kind, const LevelSet& ls, int slack
 
 }  // namespace
 
+int execution_level_count(const Symbolic& s, int kind, int merge) {
+  const LevelSet& ls = level_set(s, kind);
+  if (merge <= 0) return ls.num_levels();
+  std::vector<std::vector<std::vector<int>>> exec;
+  execution_levels(s, kind, ls, merge - 1, exec);
+  return (int)exec.size();
+}
+
 void build_chain_program(const Symbolic& s, int kind, const ProgramOptions& opt,
                          ChainProgram& out) {
   out = ChainProgram();

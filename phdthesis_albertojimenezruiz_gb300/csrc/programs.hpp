@@ -162,6 +162,9 @@ void build_chain_program(const Symbolic& s, int kind, const ProgramOptions& opt,
 void build_chain_program(const Symbolic& s, int kind, int max_locals, ChainProgram& out);
 // The level set a program kind walks, and the units a unit depends on.
 const LevelSet& program_levels(const Symbolic& s, int kind);
+// Execution levels of a program kind with chain merging `merge` (as
+// ProgramOptions::merge), before any wide unit is cut out.
+int execution_level_count(const Symbolic& s, int kind, int merge);
 void unit_deps(const Symbolic& s, int kind, int u, std::vector<int>& deps);
 
 }  // namespace pvglu

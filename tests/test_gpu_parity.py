@@ -484,6 +484,28 @@ def test_every_tuning_bit_exact(cuda, name, S, merge, wide, schedule):
     assert np.array_equal(xs, np.repeat(g["x_perm"][:, None], S, axis=1))
 
 
+@pytest.mark.parametrize("name,ladder", [("block_1x20x20", True), ("plant_c1", False)])
+def test_default_chain_merging(cuda, name, ladder):
+    """pvglu_numeric_create merges chains with the ladder rule where that
+    halves the execution levels (the reference's plant topology: a U-solve
+    level per string rung otherwise) and keeps the level set's own chains
+    elsewhere; either way the FP64 solution is the reference's, bit for bit."""
+    g = load_golden(name)
+    s = Symbolic(g["rowptr"], g["colidx"], g["perm_amd"])
+    base = {"max_locals": 0, "wide_threshold": 0, "schedule": SCHED_LEVELS}
+    levels = {m: Numeric(s, 1, FP64, tuning=dict(base, merge_chains=m)).info["program_levels"]
+              for m in (0, 2)}
+    num = Numeric(s, 1, FP64)
+    assert num.info["program_levels"] == levels[2 if ladder else 0]
+    if ladder:
+        assert 2 * levels[2] <= levels[0]
+    num.scatter(dev(pad_cols(g["a"][:, None], num.ld)))
+    x = dev(pad_cols(to_perm(g, g["b"])[:, None], num.ld))
+    num.refactor_solve(x)
+    assert num.check()[0] == 0
+    assert np.array_equal(x.cpu().numpy().reshape(s.n, num.ld)[:, 0], g["x_perm"])
+
+
 @pytest.mark.parametrize("name,S,precision", [("block_1x20x20", 1, FP64),
                                               ("block_1x20x20", 130, FP64),
                                               ("plant_c1", 64, FP32)])
