@@ -98,6 +98,15 @@ int prog_prepare(pvglu_numeric* h) {
                           (const void*)pvglu::k_wide_level<T, 3, B, 1>};
     for (const void* f : half)
       if (pvglu::allow_max_dynamic_smem(f) != cudaSuccess) return 1;
+    if constexpr (std::is_same<T, double>::value) {
+      const void* half_prog[] = {(const void*)pvglu::k_prog_level<T, -1, B, 1>,
+                                 (const void*)pvglu::k_prog_level<T, 0, B, 1>,
+                                 (const void*)pvglu::k_prog_level<T, 1, B, 1>,
+                                 (const void*)pvglu::k_prog_level<T, 2, B, 1>,
+                                 (const void*)pvglu::k_prog_level<T, 3, B, 1>};
+      for (const void* f : half_prog)
+        if (pvglu::allow_max_dynamic_smem(f) != cudaSuccess) return 1;
+    }
   }
   h->prog_grid = pvglu::prog_persistent_grid<T, B>(h->table_max);
   return 0;
@@ -166,6 +175,19 @@ void prog_levels(pvglu_numeric* h, T* x, const int* done, const int* ndone, cuda
       continue;
     }
     const int table = h->prog_level_ml[ph][lv];
+    if constexpr (B && std::is_same<T, double>::value) {
+      // FP64 levels with few items (at most a quarter of the resident warps)
+      // run with one scenario per lane: twice the warps, each with half the
+      // FP64 work.
+      if (items * 4 <= (int64_t)h->sm_count * pvglu::prog_min_blocks<T>() * pvglu::kProgWarps) {
+        const size_t smem = pvglu::prog_smem_bytes<T, B, 1>(table, pvglu::kProgWarps);
+        pvglu::k_prog_level<T, KIND, B, 1>
+            <<<launch_blocks(items * 2, pvglu::kProgWarps), pvglu::kProgBlock, smem, st>>>(
+                h->progs.p[ph], table, h->d, cb, ce, static_cast<T*>(h->values), x, h->ld,
+                h->S, h->pivot_tol, h->status, done, ndone);
+        continue;
+      }
+    }
     const size_t smem = pvglu::prog_smem_bytes<T, B>(table, pvglu::kProgWarps);
     pvglu::k_prog_level<T, KIND, B>
         <<<launch_blocks(items, pvglu::kProgWarps), pvglu::kProgBlock, smem, st>>>(

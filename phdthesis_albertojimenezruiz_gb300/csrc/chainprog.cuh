@@ -130,6 +130,31 @@ struct Vec2<double> {
   using type = double2;
 };
 
+// Lane values of the batched forms: LW scenarios per lane.  LW = 2: a warp
+// item covers 64 scenarios with 16-byte accesses (the default); LW = 1: 32
+// scenarios, for FP64 levels with few items, which then spread over twice
+// the warps, each with half the FP64 work.
+template <typename T, int LW>
+using LaneV = typename std::conditional<LW == 2, typename Vec2<T>::type, T>::type;
+template <typename V, typename T>
+__device__ __forceinline__ V ld_lane(const T* p) {
+  if constexpr (std::is_same<V, T>::value) return __ldcg(p);
+  else return __ldcg(reinterpret_cast<const V*>(p));
+}
+template <typename T>
+__device__ __forceinline__ T fnms_lane(T acc, T a, T b) { return fnms(acc, a, b); }
+__device__ __forceinline__ double2 fnms_lane(double2 acc, double2 a, double2 b) {
+  return {fnms(acc.x, a.x, b.x), fnms(acc.y, a.y, b.y)};
+}
+__device__ __forceinline__ float2 fnms_lane(float2 acc, float2 a, float2 b) {
+  return {fnms(acc.x, a.x, b.x), fnms(acc.y, a.y, b.y)};
+}
+// Component k (< LW) of a lane value.
+template <typename T>
+__device__ __forceinline__ T& lane_part(T& v, int) { return v; }
+__device__ __forceinline__ double& lane_part(double2& v, int k) { return k ? v.y : v.x; }
+__device__ __forceinline__ float& lane_part(float2& v, int k) { return k ? v.y : v.x; }
+
 // ---------------------------------------------------------------------------
 // Single-scenario table access (ld == 1).
 template <typename T, int KIND>
@@ -162,47 +187,46 @@ __device__ __forceinline__ void decode_op(uint32_t op, int& code, int& a, int& b
   c = (op >> 22) & 1023;
 }
 
-// One operation on the two scenarios (x, y components) of this lane.
-template <typename T>
-__device__ __forceinline__ void exec_op2(uint32_t op, int op_index, const int* op_col,
-                                         typename Vec2<T>::type* t, int s0, int S,
-                                         T pivot_tol, DevStatus* st) {
+// One operation on the LW scenarios of this lane (the first is s).
+template <typename T, int LW>
+__device__ __forceinline__ void exec_op_lane(uint32_t op, int op_index, const int* op_col,
+                                             LaneV<T, LW>* t, int s, int S, T pivot_tol,
+                                             DevStatus* st) {
+  using V = LaneV<T, LW>;
   int code, a, b, c;
   decode_op(op, code, a, b, c);
   if (code == OP_FNMA) {
-    const auto ta = t[a << 5], tb = t[b << 5], tc = t[c << 5];
-    typename Vec2<T>::type r;
-    r.x = fnms(ta.x, tb.x, tc.x);
-    r.y = fnms(ta.y, tb.y, tc.y);
-    t[a << 5] = r;
+    t[a << 5] = fnms_lane(t[a << 5], t[b << 5], t[c << 5]);
   } else if (code == OP_SCALE) {
-    const auto p = t[a << 5];
-    if (!(fabs(p.x) >= pivot_tol) && s0 < S) report_error(st, 3, op_col[op_index], s0);
-    if (!(fabs(p.y) >= pivot_tol) && s0 + 1 < S)
-      report_error(st, 3, op_col[op_index], s0 + 1);
+    V p = t[a << 5];
+#pragma unroll
+    for (int k = 0; k < LW; k++)
+      if (!(fabs(lane_part(p, k)) >= pivot_tol) && s + k < S)
+        report_error(st, 3, op_col[op_index], s + k);
     if constexpr (std::is_same<T, float>::value) {
       // FP32 factors are refined afterwards: one reciprocal per pivot.
-      const float ix = __frcp_rn(p.x), iy = __frcp_rn(p.y);
+      V r;
+#pragma unroll
+      for (int k = 0; k < LW; k++) lane_part(r, k) = __frcp_rn(lane_part(p, k));
       for (int i = 0; i < c; i++) {
-        auto q = t[(b + i) << 5];
-        q.x *= ix;
-        q.y *= iy;
+        V q = t[(b + i) << 5];
+#pragma unroll
+        for (int k = 0; k < LW; k++) lane_part(q, k) *= lane_part(r, k);
         t[(b + i) << 5] = q;
       }
     } else {
       // FP64 divides like the reference (GLU_CSC_CPU_levels_strings.cpp:34).
       for (int i = 0; i < c; i++) {
-        auto q = t[(b + i) << 5];
-        q.x = q.x / p.x;
-        q.y = q.y / p.y;
+        V q = t[(b + i) << 5];
+#pragma unroll
+        for (int k = 0; k < LW; k++) lane_part(q, k) = lane_part(q, k) / lane_part(p, k);
         t[(b + i) << 5] = q;
       }
     }
   } else if (code == OP_DIV) {
-    auto q = t[a << 5];
-    const auto p = t[b << 5];
-    q.x = q.x / p.x;
-    q.y = q.y / p.y;
+    V q = t[a << 5], p = t[b << 5];
+#pragma unroll
+    for (int k = 0; k < LW; k++) lane_part(q, k) = lane_part(q, k) / lane_part(p, k);
     t[a << 5] = q;
   }
 }
@@ -245,9 +269,9 @@ __device__ __forceinline__ void prog_drain(WarpTma& tma) {
   __syncwarp();
 }
 
-// Runs every segment of `chain`, batched over the 64 scenarios starting at
-// s0 (BATCH) or for the single scenario.  sm: this warp's table.
-template <typename T, int KIND, bool BATCH>
+// Runs every segment of `chain`, batched over the 32 * LW scenarios starting
+// at s0 (BATCH) or for the single scenario.  sm: this warp's table.
+template <typename T, int KIND, bool BATCH, int LW = 2>
 __device__ __forceinline__ void prog_run_chain(const ProgDev& P, const DevStruct& d, int chain,
                                                T* __restrict__ v, T* __restrict__ x, int ld,
                                                int s0, int S, T* sm, WarpTma& tma,
@@ -273,8 +297,9 @@ __device__ __forceinline__ void prog_run_chain(const ProgDev& P, const DevStruct
       return l == c_to[0] || l == c_to[1] || l == c_to[2] || l == c_to[3];
     };
     if (BATCH) {
-      using V2 = typename Vec2<T>::type;
-      constexpr unsigned kRow = kGroup * sizeof(T);
+      using V2 = LaneV<T, LW>;
+      constexpr int kLaneRow = 32 * LW;  // T values of a table row
+      constexpr unsigned kRow = kLaneRow * sizeof(T);
       // The segment's operation words, one int4 (four operations) per lane,
       // fetched before the waits below and broadcast by shuffles: the
       // operations then wait on no memory but the table.
@@ -300,7 +325,7 @@ __device__ __forceinline__ void prog_run_chain(const ProgDev& P, const DevStruct
       __syncwarp();
       for (int l = lane; l < nl; l += 32)
         if (!is_carried(l))
-          bulk_load(sm + l * kGroup, prog_row<T, KIND>(__ldg(lr + l), v, x, ld, s0), kRow,
+          bulk_load(sm + l * kLaneRow, prog_row<T, KIND>(__ldg(lr + l), v, x, ld, s0), kRow,
                     tma.mbar);
       long long polls = 0;
       bool late = false;
@@ -329,10 +354,10 @@ __device__ __forceinline__ void prog_run_chain(const ProgDev& P, const DevStruct
           const uint32_t wz = (uint32_t)__shfl_sync(0xffffffffu, ow.z, k);
           const uint32_t ww = (uint32_t)__shfl_sync(0xffffffffu, ow.w, k);
           const int base = sg.z + 4 * (k0 + k);
-          exec_op2<T>(wx, base, P.op_col, t, s0 + 2 * lane, S, pivot_tol, st);
-          exec_op2<T>(wy, base + 1, P.op_col, t, s0 + 2 * lane, S, pivot_tol, st);
-          exec_op2<T>(wz, base + 2, P.op_col, t, s0 + 2 * lane, S, pivot_tol, st);
-          exec_op2<T>(ww, base + 3, P.op_col, t, s0 + 2 * lane, S, pivot_tol, st);
+          exec_op_lane<T, LW>(wx, base, P.op_col, t, s0 + LW * lane, S, pivot_tol, st);
+          exec_op_lane<T, LW>(wy, base + 1, P.op_col, t, s0 + LW * lane, S, pivot_tol, st);
+          exec_op_lane<T, LW>(wz, base + 2, P.op_col, t, s0 + LW * lane, S, pivot_tol, st);
+          exec_op_lane<T, LW>(ww, base + 3, P.op_col, t, s0 + LW * lane, S, pivot_tol, st);
         }
       }
       // Make this lane's table writes visible to the async proxy, then let
@@ -340,7 +365,7 @@ __device__ __forceinline__ void prog_run_chain(const ProgDev& P, const DevStruct
       fence_proxy_async();
       __syncwarp();
       for (int l = lane; l < n_own; l += 32)
-        bulk_store(prog_row<T, KIND>(__ldg(lr + l), v, x, ld, s0), sm + l * kGroup, kRow);
+        bulk_store(prog_row<T, KIND>(__ldg(lr + l), v, x, ld, s0), sm + l * kLaneRow, kRow);
       bulk_commit();
     } else {
       if (n_carry) {
@@ -372,29 +397,34 @@ __device__ __forceinline__ void prog_run_chain(const ProgDev& P, const DevStruct
   }
 }
 
-// Chains [cb, ce) of one level: work item = (chain, 64-scenario group) in
-// batched mode, chain alone in single mode; one warp per item.  In batched
-// mode every bulk store of the warp is complete when this returns.
-template <typename T, int KIND, bool BATCH>
+// Chains [cb, ce) of one level: work item = (chain, group of 32 * LW
+// scenarios) in batched mode, chain alone in single mode; one warp per item.
+// In batched mode every bulk store of the warp is complete when this returns.
+template <typename T, int KIND, bool BATCH, int LW = 2>
 __device__ __forceinline__ void prog_run_level(const ProgDev& P, const DevStruct& d, int cb,
                                                int ce, T* __restrict__ v, T* __restrict__ x,
                                                int ld, int S, T* sm_warp, WarpTma& tma,
                                                T pivot_tol, DevStatus* st,
                                                const int* done, int warp_id, int n_warps) {
-  const int groups = BATCH ? ld / kGroup : 1;
+  constexpr int group = 32 * LW;
+  const int groups = BATCH ? ld / group : 1;
   const int items = (ce - cb) * groups;
   const int lane = threadIdx.x & 31;
   for (int it = warp_id; it < items; it += n_warps) {
     if (BATCH && tma.aborted) break;
     const int ci = BATCH ? it / groups : it;
     const int c = cb + ci;
-    const int s0 = BATCH ? (it - ci * groups) * kGroup : 0;
+    const int s0 = BATCH ? (it - ci * groups) * group : 0;
     if (BATCH && done) {
-      const int sa = s0 + 2 * lane;
-      const bool idle = (sa >= S || done[sa]) && (sa + 1 >= S || done[sa + 1]);
+      bool idle = true;
+#pragma unroll
+      for (int k = 0; k < LW; k++) {
+        const int sa = s0 + LW * lane + k;
+        idle = idle && (sa >= S || done[sa]);
+      }
       if (__all_sync(0xffffffffu, idle)) continue;
     }
-    prog_run_chain<T, KIND, BATCH>(P, d, c, v, x, ld, s0, S, sm_warp, tma, pivot_tol, st);
+    prog_run_chain<T, KIND, BATCH, LW>(P, d, c, v, x, ld, s0, S, sm_warp, tma, pivot_tol, st);
   }
   if (BATCH) {
     bulk_wait_all();
@@ -423,12 +453,12 @@ inline cudaError_t allow_max_dynamic_smem(const void* kernel) {
 
 // Table layout of a block: warps_per_block tables, then one mbarrier per
 // warp.  Returns this warp's table and initialises its mbarrier.
-template <typename T, bool BATCH>
+template <typename T, bool BATCH, int LW = 2>
 __device__ __forceinline__ T* prog_setup_warp(unsigned char* smem_raw, int max_locals,
                                               WarpTma& tma) {
   const int w = threadIdx.x >> 5;
   const int nw = blockDim.x >> 5;
-  const size_t table = (size_t)max_locals * (BATCH ? kGroup : 1) * sizeof(T);
+  const size_t table = (size_t)max_locals * (BATCH ? 32 * LW : 1) * sizeof(T);
   T* sm = reinterpret_cast<T*>(smem_raw + (size_t)w * table);
   tma.mbar = reinterpret_cast<unsigned long long*>(smem_raw + (size_t)nw * table) + w;
   tma.phase = 0;
@@ -441,16 +471,17 @@ __device__ __forceinline__ T* prog_setup_warp(unsigned char* smem_raw, int max_l
   return sm;
 }
 
-template <typename T, bool BATCH>
+template <typename T, bool BATCH, int LW = 2>
 __host__ __device__ size_t prog_smem_bytes(int max_locals, int warps_per_block) {
-  return (size_t)warps_per_block * max_locals * (BATCH ? kGroup : 1) * sizeof(T) +
+  return (size_t)warps_per_block * max_locals * (BATCH ? 32 * LW : 1) * sizeof(T) +
          (size_t)warps_per_block * sizeof(unsigned long long);
 }
 
 // done: per-scenario skip of the solves (NULL for the refactorization);
 // ndone (or NULL): the launch does nothing once every scenario is done.
 // `table`: the level's table budget (its programs were built for it).
-template <typename T, int KIND, bool BATCH>
+// LW: scenarios per lane of the batched form (programs do not depend on it).
+template <typename T, int KIND, bool BATCH, int LW = 2>
 __global__ void __launch_bounds__(kProgBlock, prog_min_blocks<T>())
 k_prog_level(ProgDev P, int table, DevStruct d, int cb, int ce,
                              T* __restrict__ v, T* __restrict__ x, int ld, int S, T pivot_tol,
@@ -460,11 +491,11 @@ k_prog_level(ProgDev P, int table, DevStruct d, int cb, int ce,
   if (BATCH && __ldcg(&st->code) == 6) return;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   WarpTma tma;
-  T* sm = prog_setup_warp<T, BATCH>(smem_raw, table, tma);
+  T* sm = prog_setup_warp<T, BATCH, LW>(smem_raw, table, tma);
   const int warp_id = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int n_warps = (gridDim.x * blockDim.x) >> 5;
-  prog_run_level<T, KIND, BATCH>(P, d, cb, ce, v, x, ld, S, sm, tma, pivot_tol, st, done,
-                                 warp_id, n_warps);
+  prog_run_level<T, KIND, BATCH, LW>(P, d, cb, ce, v, x, ld, S, sm, tma, pivot_tol, st, done,
+                                     warp_id, n_warps);
 }
 
 // ---------------------------------------------------------------------------

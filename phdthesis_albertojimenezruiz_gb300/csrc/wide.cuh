@@ -35,32 +35,19 @@ __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, 
 __device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
 __device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
 
-// Lane values of the batched forms: LW scenarios per lane.  LW = 2: a warp
-// covers 64 scenarios with 16-byte accesses; LW = 1: 32 scenarios, for WIDE
-// levels with fewer items than SMs, which then spread over twice the blocks
-// (each block with half the FP64 work).
-template <typename T, int LW>
-using LaneV = typename std::conditional<LW == 2, typename Vec2<T>::type, T>::type;
-template <typename V, typename T>
-__device__ __forceinline__ V ld_lane(const T* p) {
-  if constexpr (std::is_same<V, T>::value) return __ldcg(p);
-  else return __ldcg(reinterpret_cast<const V*>(p));
-}
+// Products and differences of the lane values (LaneV, chainprog.cuh): a
+// WIDE level with few items runs with one scenario per lane (LW = 1), on
+// twice the blocks, each with half the FP64 work.
 template <typename T>
 __device__ __forceinline__ T mul_lane(T a, T b) { return mul_rn(a, b); }
 template <typename T>
 __device__ __forceinline__ T sub_lane(T a, T b) { return sub_rn(a, b); }
-template <typename T>
-__device__ __forceinline__ T fnms_lane(T acc, T a, T b) { return fnms(acc, a, b); }
 #define PVGLU_LANE2(V)                                                        \
   __device__ __forceinline__ V mul_lane(V a, V b) {                           \
     return {mul_rn(a.x, b.x), mul_rn(a.y, b.y)};                              \
   }                                                                           \
   __device__ __forceinline__ V sub_lane(V a, V b) {                           \
     return {sub_rn(a.x, b.x), sub_rn(a.y, b.y)};                              \
-  }                                                                           \
-  __device__ __forceinline__ V fnms_lane(V acc, V a, V b) {                   \
-    return {fnms(acc.x, a.x, b.x), fnms(acc.y, a.y, b.y)};                    \
   }
 PVGLU_LANE2(double2)
 PVGLU_LANE2(float2)
