@@ -191,7 +191,7 @@ void build_chain_program(const Symbolic& s, int kind, int max_locals, ChainProgr
 
 namespace {
 
-// Column-scheduled gather plan of wide refactor unit k (WidePlan).
+// Chain-scheduled gather plan of wide refactor unit k (WidePlan).
 void plan_wide_column(const Symbolic& s, int k, WidePlan& w) {
   const int c0 = s.csc_colptr[k], dk = s.diag_slot[k], c1 = s.csc_colptr[k + 1];
   const int len = c1 - c0;

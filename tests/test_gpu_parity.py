@@ -327,7 +327,7 @@ def block_ordering(tag: str):
 @pytest.mark.parametrize("name", ["block_1x20x20", "mesh_20x20", "random_300"])
 def test_wide_units_bit_exact(cuda, name, S, max_locals, schedule):
     """Columns and rows too wide for the table run as WIDE program levels
-    (a block per unit: column-scheduled gather for the refactorization,
+    (a block per unit: chain-scheduled gather for the refactorization,
     ordered block sums for the solves).  Small tables make many units wide;
     FP64 factors and solutions stay bit-identical to the reference's
     sequential GLU and substitution for every scenario, and the transposed
