@@ -176,10 +176,16 @@ void prog_levels(pvglu_numeric* h, T* x, const int* done, const int* ndone, cuda
     }
     const int table = h->prog_level_ml[ph][lv];
     if constexpr (B && std::is_same<T, double>::value) {
-      // FP64 levels with few items (at most a quarter of the resident warps)
-      // run with one scenario per lane: twice the warps, each with half the
-      // FP64 work.
-      if (items * 4 <= (int64_t)h->sm_count * pvglu::prog_min_blocks<T>() * pvglu::kProgWarps) {
+      // FP64 levels with few items run with one scenario per lane: twice the
+      // warps, each with half the FP64 work.  Solves: up to a quarter of the
+      // resident warps.  Refactorization (FP64-heavier): only while the
+      // doubled items fit one block per SM; past that some SMs get two blocks
+      // and the level is no faster (347 string chains at 64 scenarios: 220
+      // against 166 us).
+      const int64_t limit = KIND < 0 ? (int64_t)h->sm_count * pvglu::kProgWarps / 2
+                                     : (int64_t)h->sm_count * pvglu::prog_min_blocks<T>() *
+                                           pvglu::kProgWarps / 4;
+      if (items <= limit) {
         const size_t smem = pvglu::prog_smem_bytes<T, B, 1>(table, pvglu::kProgWarps);
         pvglu::k_prog_level<T, KIND, B, 1>
             <<<launch_blocks(items * 2, pvglu::kProgWarps), pvglu::kProgBlock, smem, st>>>(
