@@ -18,8 +18,8 @@
 //   * a target or solve row with many updates: warps of the block compute the
 //     products of a chunk in parallel (each rounded as the sequential code
 //     rounds it) into shared memory while one warp subtracts the previous
-//     chunk's products in order (batched: a lane per two scenarios; single:
-//     one lane).
+//     chunk's products in order (batched: a lane per scenario pair, or per
+//     scenario on levels with few items; single: one lane).
 // Single scenario: the column is staged in shared memory when it fits.
 #pragma once
 #include <cuda_runtime.h>
@@ -53,20 +53,8 @@ PVGLU_LANE2(double2)
 PVGLU_LANE2(float2)
 #undef PVGLU_LANE2
 
-// acc - sum_e a_e * b_e in the order e = 0 .. count-1, each product and each
-// difference rounded on its own.  Warps 1.. of the block form the products of
-// a chunk of entries in shared memory (batched: a warp per entry, two
-// scenarios per lane; single: a thread per entry) while warp 0 subtracts the
-// previous chunk's products in order (batched: every lane for its two
-// scenarios; single: lane 0), two chunk buffers in turn.  `ix(e, ia, ib)`
-// gives the two operand indices of entry e and `ab(ia, ib, a, b)` the
-// operands (T, or the lane's LW scenarios); a batched producer
-// warp loads the indices of its entries with one lane each and broadcasts
-// them, so every entry costs one round of index loads and one of operand
-// loads, the entries' loads in flight together.
-// Returns the result in warp 0 (single: in its lane 0).  All threads of the
-// block (at least two warps) must call it.  scratch: scratch_bytes of shared
-// memory, at least wide_scratch_min<T, BATCH>(blockDim.x).
+// Bytes of one scratch row of the ordered sums (two scenarios per lane: the
+// larger of the batched forms).
 template <typename T, bool BATCH>
 __host__ __device__ constexpr int wide_row_bytes() {
   return BATCH ? 32 * 2 * (int)sizeof(T) : (int)sizeof(T);
@@ -84,6 +72,20 @@ __host__ __device__ constexpr int wide_scratch_bytes(int threads) {
   return 2 * (BATCH ? 64 : 8 * (threads - 32)) * wide_row_bytes<T, BATCH>();
 }
 
+// acc - sum_e a_e * b_e in the order e = 0 .. count-1, each product and each
+// difference rounded on its own.  Warps 1.. of the block form the products of
+// a chunk of entries in shared memory (batched: a warp per entry, LW
+// scenarios per lane; single: a thread per entry) while warp 0 subtracts the
+// previous chunk's products in order (batched: every lane for its LW
+// scenarios; single: lane 0), two chunk buffers in turn.  `ix(e, ia, ib)`
+// gives the two operand indices of entry e and `ab(ia, ib, a, b)` the
+// operands (T, or the lane's LW scenarios); a batched producer
+// warp loads the indices of its entries with one lane each and broadcasts
+// them, so every entry costs one round of index loads and one of operand
+// loads, the entries' loads in flight together.
+// Returns the result in warp 0 (single: in its lane 0).  All threads of the
+// block (at least two warps) must call it.  scratch: scratch_bytes of shared
+// memory, at least wide_scratch_min<T, BATCH>(blockDim.x).
 template <typename T, bool BATCH, int LW, typename IX, typename AB>
 __device__ __forceinline__ typename std::conditional<BATCH, LaneV<T, LW>, T>::type
 ordered_sub_block(typename std::conditional<BATCH, LaneV<T, LW>, T>::type acc, int count,
