@@ -118,6 +118,11 @@ __device__ __forceinline__ void bulk_wait_all() {
 __device__ __forceinline__ void fence_proxy_async() {
   asm volatile("fence.proxy.async;" ::: "memory");
 }
+// The same for this CTA's shared memory only: table writes by the lanes
+// before bulk stores read the table.
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
 
 template <typename T>
 struct Vec2;
@@ -362,7 +367,7 @@ __device__ __forceinline__ void prog_run_chain(const ProgDev& P, const DevStruct
       }
       // Make this lane's table writes visible to the async proxy, then let
       // lanes write back the own rows with bulk stores.
-      fence_proxy_async();
+      fence_proxy_async_smem();
       __syncwarp();
       for (int l = lane; l < n_own; l += 32)
         bulk_store(prog_row<T, KIND>(__ldg(lr + l), v, x, ld, s0), sm + l * kLaneRow, kRow);
