@@ -282,9 +282,22 @@ __device__ __forceinline__ void prog_run_chain(const ProgDev& P, const DevStruct
                                                int s0, int S, T* sm, WarpTma& tma,
                                                T pivot_tol, DevStatus* st) {
   const int lane = threadIdx.x & 31;
-  const int g_end = __ldg(P.chain_seg + chain + 1);
-  for (int g = __ldg(P.chain_seg + chain); g < g_end; g++) {
-    const int4 sg = __ldg(P.seg + g);
+  const int g_begin = __ldg(P.chain_seg + chain), g_end = __ldg(P.chain_seg + chain + 1);
+  // Each segment's descriptor and carry moves (read-only) are read one
+  // segment ahead: a segment's copies then start without a dependent round
+  // of metadata loads.
+  int4 sg_next = make_int4(0, 0, 0, 0), cv_next = make_int4(-1, -1, -1, -1);
+  if (g_begin < g_end) {
+    sg_next = __ldg(P.seg + g_begin);
+    cv_next = __ldg(P.carry + g_begin);
+  }
+  for (int g = g_begin; g < g_end; g++) {
+    const int4 sg = sg_next;
+    const int4 cv_g = cv_next;
+    if (g + 1 < g_end) {
+      sg_next = __ldg(P.seg + g + 1);
+      cv_next = __ldg(P.carry + g + 1);
+    }
     const int* lr = P.loads + sg.x;
     const int nl = sg.y & 0xffff, n_own = (sg.y >> 16) & 0x3ff, n_carry = (sg.y >> 26) & 7;
     // Rows the previous segment of this chain left in the table: moved, not
@@ -292,7 +305,7 @@ __device__ __forceinline__ void prog_run_chain(const ProgDev& P, const DevStruct
     int c_to[4] = {-1, -1, -1, -1};
     int4 cv = make_int4(-1, -1, -1, -1);
     if (n_carry) {
-      cv = __ldg(P.carry + g);
+      cv = cv_g;
       c_to[0] = cv.x & 0xffff;
       if (n_carry > 1) c_to[1] = cv.y & 0xffff;
       if (n_carry > 2) c_to[2] = cv.z & 0xffff;
