@@ -87,6 +87,16 @@ void check_program(const Symbolic& s, int kind, const ProgramOptions& opt) {
   CHECK((int)pr.level_src.size() == nlev && (int)pr.level_wide.size() == nlev &&
             (int)pr.level_max_locals.size() == nlev && (int)pr.level_budget.size() == nlev,
         "kind %d level arrays", kind);
+  // Program levels come from the execution levels in order, and their count
+  // is what execution_level_count reports (the default chain merging of a
+  // handle is chosen from it).
+  if (nlev > 0 && (int)pr.level_src.size() == nlev) {
+    for (int lv = 1; lv < nlev; lv++)
+      CHECK(pr.level_src[lv] >= pr.level_src[lv - 1], "kind %d level order", kind);
+    CHECK(pr.level_src.back() + 1 == execution_level_count(s, kind, opt.merge),
+          "kind %d execution levels %d vs %d", kind, pr.level_src.back() + 1,
+          execution_level_count(s, kind, opt.merge));
+  }
   CHECK((int)pr.chain_seg.size() == pr.level_chain.back() + 1 &&
             (int)pr.chain_unit.size() == pr.level_chain.back() + 1,
         "kind %d chain arrays", kind);
