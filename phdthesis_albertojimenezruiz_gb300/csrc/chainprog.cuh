@@ -47,7 +47,7 @@ struct ProgDev {
   const int* pr_p;
 };
 
-constexpr int kGroup = 64;                       // scenarios per warp item
+constexpr int kGroup = 64;                       // scenarios per warp item (two per lane)
 constexpr int kProgBlock = 128;                  // threads per block of the executors
 constexpr int kProgWarps = kProgBlock / 32;
 // Resident blocks per SM the level executors are compiled for: FP32 tables
