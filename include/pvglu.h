@@ -187,6 +187,14 @@ int pvglu_scatter_stamps(pvglu_numeric* h, const double* g, const double* gmin, 
  * Replaces factorize_electrical_system_CUDA (factorize_electrical_system_CUDA.cu:61-152). */
 int pvglu_refactor(pvglu_numeric* h, void* stream);
 
+/* (a) + (b) in one call, with the same factors as pvglu_scatter then
+ * pvglu_refactor.  Batched handles on PVGLU_SCHED_LEVELS whose
+ * refactorization has no WIDE level, given 16-byte aligned a_values, run it
+ * as one pass: each level reads its columns' entries straight from a_values,
+ * so no scatter is launched and the factor values are written once.  Other
+ * handles run pvglu_scatter, then pvglu_refactor. */
+int pvglu_scatter_refactor(pvglu_numeric* h, const double* a_values, void* stream);
+
 /* (c) Triangular solves with the stored factors, every scenario.
  * x: device, [n * ld], same precision as the factors; holds b on entry.
  * Replaces triangular_substitution_LU_CUDA (triangular_substitution.cu:232-271);

@@ -92,6 +92,7 @@ _SIGS = {
     "pvglu_numeric_set_schedule": ([_P, _I], _I),
     "pvglu_numeric_set_pivot_tol": ([_P, C.c_double], _I),
     "pvglu_scatter": ([_P, _P, _P], _I),
+    "pvglu_scatter_refactor": ([_P, _P, _P], _I),
     "pvglu_refactor": ([_P, _P], _I),
     "pvglu_solve": ([_P, _P, _I, _P], _I),
     "pvglu_refactor_solve": ([_P, _P, _I, _P], _I),

@@ -108,6 +108,12 @@ int prog_prepare(pvglu_numeric* h) {
         if (pvglu::allow_max_dynamic_smem(f) != cudaSuccess) return 1;
     }
   }
+  if constexpr (B) {
+    const void* from_a[] = {(const void*)pvglu::k_prog_refactor_from_a<T, 2>,
+                            (const void*)pvglu::k_prog_refactor_from_a<T, 1>};
+    for (const void* f : from_a)
+      if (pvglu::allow_max_dynamic_smem(f) != cudaSuccess) return 1;
+  }
   h->prog_grid = pvglu::prog_persistent_grid<T, B>(h->table_max);
   return 0;
 }
@@ -161,9 +167,12 @@ void launch_wide(pvglu_numeric* h, int ph, int lv, int cb, int ce, T* x, const i
       (int)smem);
 }
 
-// One phase of chain programs with one launch per level.
+// One phase of chain programs with one launch per level.  a (batched
+// refactorization without WIDE levels, or NULL): the caller's FP64 values,
+// read by the levels in place of a scatter (k_prog_refactor_from_a).
 template <typename T, bool B, int KIND>
-void prog_levels(pvglu_numeric* h, T* x, const int* done, const int* ndone, cudaStream_t st) {
+void prog_levels(pvglu_numeric* h, T* x, const int* done, const int* ndone, cudaStream_t st,
+                 const double* a = nullptr) {
   const int ph = KIND + 1;
   const auto& lc = h->prog_level_chain[ph];
   const int groups = B ? h->ld / pvglu::kGroup : 1;
@@ -187,6 +196,15 @@ void prog_levels(pvglu_numeric* h, T* x, const int* done, const int* ndone, cuda
                                            pvglu::kProgWarps / 4;
       if (items <= limit) {
         const size_t smem = pvglu::prog_smem_bytes<T, B, 1>(table, pvglu::kProgWarps);
+        if constexpr (KIND < 0) {
+          if (a) {
+            pvglu::k_prog_refactor_from_a<T, 1>
+                <<<launch_blocks(items * 2, pvglu::kProgWarps), pvglu::kProgBlock, smem, st>>>(
+                    h->progs.p[ph], table, h->d, cb, ce, static_cast<T*>(h->values), a, h->ld,
+                    h->S, h->pivot_tol, h->status);
+            continue;
+          }
+        }
         pvglu::k_prog_level<T, KIND, B, 1>
             <<<launch_blocks(items * 2, pvglu::kProgWarps), pvglu::kProgBlock, smem, st>>>(
                 h->progs.p[ph], table, h->d, cb, ce, static_cast<T*>(h->values), x, h->ld,
@@ -195,6 +213,15 @@ void prog_levels(pvglu_numeric* h, T* x, const int* done, const int* ndone, cuda
       }
     }
     const size_t smem = pvglu::prog_smem_bytes<T, B>(table, pvglu::kProgWarps);
+    if constexpr (KIND < 0 && B) {
+      if (a) {
+        pvglu::k_prog_refactor_from_a<T>
+            <<<launch_blocks(items, pvglu::kProgWarps), pvglu::kProgBlock, smem, st>>>(
+                h->progs.p[ph], table, h->d, cb, ce, static_cast<T*>(h->values), a, h->ld, h->S,
+                h->pivot_tol, h->status);
+        continue;
+      }
+    }
     pvglu::k_prog_level<T, KIND, B>
         <<<launch_blocks(items, pvglu::kProgWarps), pvglu::kProgBlock, smem, st>>>(
             h->progs.p[ph], table, h->d, cb, ce, static_cast<T*>(h->values), x, h->ld, h->S,
@@ -306,6 +333,26 @@ int run_scatter(pvglu_numeric* h, const AValues& A, const int* ndone, cudaStream
   else
     k_scatter<float><<<blocks, 256, 0, st>>>(h->d.slot_src, h->nnz, h->ld, h->S, A,
                                              (float*)h->values, ndone);
+  PVGLU_CUDA(cudaGetLastError());
+  return PVGLU_OK;
+}
+
+// Scatter and refactorization in one pass (k_prog_refactor_from_a): batched
+// handles on the per-level schedule whose refactorization has no WIDE level,
+// with 16-byte aligned values.  Otherwise the scatter, then the refactor.
+int run_scatter_refactor(pvglu_numeric* h, const double* a, cudaStream_t st) {
+  bool one_pass = h->batch && h->schedule == PVGLU_SCHED_LEVELS && h->ld % 64 == 0 &&
+                  !(reinterpret_cast<uintptr_t>(a) & 15);
+  for (const int w : h->prog_level_wide_len[0]) one_pass = one_pass && w == 0;
+  if (!one_pass) {
+    const AValues A{a, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    const int rc = run_scatter(h, A, nullptr, st);
+    return rc ? rc : run_refactor(h, st, SkipDone{nullptr, nullptr});
+  }
+  if (h->precision == PVGLU_FP64)
+    prog_levels<double, true, -1>(h, nullptr, nullptr, nullptr, st, a);
+  else
+    prog_levels<float, true, -1>(h, nullptr, nullptr, nullptr, st, a);
   PVGLU_CUDA(cudaGetLastError());
   return PVGLU_OK;
 }
@@ -1042,6 +1089,11 @@ int pvglu_refine(pvglu_numeric* h, const double* a_values, const double* g, cons
 int pvglu_refactor(pvglu_numeric* h, void* stream) {
   if (!h) return fail(PVGLU_ERR_BAD_ARG, "NULL handle");
   return pvglu::run_refactor(h, as_stream(stream), pvglu::SkipDone{nullptr, nullptr});
+}
+
+int pvglu_scatter_refactor(pvglu_numeric* h, const double* a_values, void* stream) {
+  if (!h || !a_values) return fail(PVGLU_ERR_BAD_ARG, "NULL argument");
+  return pvglu::run_scatter_refactor(h, a_values, as_stream(stream));
 }
 
 int pvglu_refactor_solve(pvglu_numeric* h, void* x, int flags, void* stream) {

@@ -103,6 +103,10 @@ __device__ __forceinline__ void bulk_store(void* gdst, const void* smem_src, uns
                "r"(smem_u32(smem_src)), "r"(bytes)
                : "memory");
 }
+// Starts moving `bytes` (a multiple of 16) at gsrc into L2; no completion.
+__device__ __forceinline__ void bulk_prefetch_l2(const void* gsrc, unsigned bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(gsrc), "r"(bytes) : "memory");
+}
 __device__ __forceinline__ void bulk_commit() {
   asm volatile("cp.async.bulk.commit_group;" ::: "memory");
 }
@@ -274,13 +278,89 @@ __device__ __forceinline__ void prog_drain(WarpTma& tma) {
   __syncwarp();
 }
 
+// Own rows of a refactorization segment taken straight from A's FP64 values
+// (FROM_A): row l of the table gets A(slot_src[ref], s) converted to T, zero
+// at fill slots and past S, which is what the scatter would have stored.
+// Every LU slot is an own row of exactly one segment (its column's) and no
+// segment reads it earlier, so these loads replace the scatter's write and
+// the refactorization's first read of the slot.  Plain 8 * LW-byte loads by
+// all lanes, kOwnInFlight rows at a time; the table's other rows keep their
+// bulk copies, which are already under way.
+#ifndef PVGLU_OWN_IN_FLIGHT_F32
+#define PVGLU_OWN_IN_FLIGHT_F32 4
+#endif
+#ifndef PVGLU_OWN_IN_FLIGHT_F64
+#define PVGLU_OWN_IN_FLIGHT_F64 2
+#endif
+template <typename T, int LW>
+__device__ __forceinline__ void load_own_from_a(const int* lr, int n_a, const int* c_to,
+                                                const int* __restrict__ slot_src,
+                                                const double* __restrict__ a, int ld, int s0,
+                                                int S, LaneV<T, LW>* t) {
+  using VA = LaneV<double, LW>;
+  using V = LaneV<T, LW>;
+  constexpr int kOwnInFlight = sizeof(T) == 4 ? PVGLU_OWN_IN_FLIGHT_F32 : PVGLU_OWN_IN_FLIGHT_F64;
+  const int lane = threadIdx.x & 31;
+  const int s = s0 + LW * lane;
+  for (int l0 = 0; l0 < n_a; l0 += 32) {
+    const int nb = min(32, n_a - l0);
+    const int m = lane < nb ? __ldg(slot_src + __ldg(lr + l0 + lane)) : -1;
+    for (int k = 0; k < nb; k += kOwnInFlight) {
+      VA av[kOwnInFlight];
+#pragma unroll
+      for (int j = 0; j < kOwnInFlight; j++) {
+        const int mj = __shfl_sync(0xffffffffu, m, (k + j) & 31);
+        av[j] = VA{};
+        if (k + j < nb && mj >= 0)
+          av[j] = ld_lane<VA>(a + (size_t)(unsigned)mj * (unsigned)ld + s);
+      }
+#pragma unroll
+      for (int j = 0; j < kOwnInFlight; j++) {
+        const int l = l0 + k + j;
+        if (k + j < nb && l != c_to[0] && l != c_to[1] && l != c_to[2] && l != c_to[3]) {
+          V o;
+#pragma unroll
+          for (int p = 0; p < LW; p++)
+            lane_part(o, p) = s + p < S ? convert<T>(lane_part(av[j], p)) : T(0);
+          t[l << 5] = o;
+        }
+      }
+    }
+  }
+}
+
+// L2 prefetch of the A rows that load_own_from_a will read for a segment's
+// own rows [0, n_a): issued a segment ahead, so that those plain loads find
+// their rows in L2 instead of waiting for DRAM.
+template <int LW>
+__device__ __forceinline__ void prefetch_own_from_a(const int* lr, int n_a,
+                                                    const int* __restrict__ slot_src,
+                                                    const double* __restrict__ a, int ld,
+                                                    int s0) {
+  for (int l = threadIdx.x & 31; l < n_a; l += 32) {
+    const int m = __ldg(slot_src + __ldg(lr + l));
+    if (m >= 0)
+      bulk_prefetch_l2(a + (size_t)(unsigned)m * (unsigned)ld + s0, 32 * LW * sizeof(double));
+  }
+}
+
+#ifndef PVGLU_PREFETCH_OWN_F32
+#define PVGLU_PREFETCH_OWN_F32 0
+#endif
+template <typename T>
+constexpr bool kPrefetchOwn = sizeof(T) == 8 || PVGLU_PREFETCH_OWN_F32;
+
 // Runs every segment of `chain`, batched over the 32 * LW scenarios starting
 // at s0 (BATCH) or for the single scenario.  sm: this warp's table.
-template <typename T, int KIND, bool BATCH, int LW = 2>
+// FROM_A (batched refactorization only): own rows come from `a` (the
+// caller's FP64 values, leading dimension ld) instead of the factor values.
+template <typename T, int KIND, bool BATCH, int LW = 2, bool FROM_A = false>
 __device__ __forceinline__ void prog_run_chain(const ProgDev& P, const DevStruct& d, int chain,
                                                T* __restrict__ v, T* __restrict__ x, int ld,
                                                int s0, int S, T* sm, WarpTma& tma,
-                                               T pivot_tol, DevStatus* st) {
+                                               T pivot_tol, DevStatus* st,
+                                               const double* __restrict__ a = nullptr) {
+  static_assert(!FROM_A || (KIND < 0 && BATCH), "own rows from A: batched refactor only");
   const int lane = threadIdx.x & 31;
   const int g_begin = __ldg(P.chain_seg + chain), g_end = __ldg(P.chain_seg + chain + 1);
   // Each segment's descriptor and carry moves (read-only) are read one
@@ -290,6 +370,9 @@ __device__ __forceinline__ void prog_run_chain(const ProgDev& P, const DevStruct
   if (g_begin < g_end) {
     sg_next = __ldg(P.seg + g_begin);
     cv_next = __ldg(P.carry + g_begin);
+    if constexpr (FROM_A && kPrefetchOwn<T>)
+      prefetch_own_from_a<LW>(P.loads + sg_next.x, (sg_next.y >> 16) & 0x3ff, d.slot_src, a, ld,
+                              s0);
   }
   for (int g = g_begin; g < g_end; g++) {
     const int4 sg = sg_next;
@@ -339,12 +422,24 @@ __device__ __forceinline__ void prog_run_chain(const ProgDev& P, const DevStruct
         for (int c = 0; c < n_carry; c++) t[c_to[c] << 5] = hold[c];
         __syncwarp();
       }
-      if (lane == 0) mbar_arrive_expect_tx(tma.mbar, (unsigned)(nl - n_carry) * kRow);
+      // Rows [0, n_a) are read from A below, the rest by bulk copies.
+      const int n_a = FROM_A ? n_own : 0;
+      int n_bulk = nl - n_a;
+      for (int c = 0; c < n_carry; c++)
+        if (c_to[c] >= n_a) n_bulk--;
+      if (lane == 0) mbar_arrive_expect_tx(tma.mbar, (unsigned)n_bulk * kRow);
       __syncwarp();
-      for (int l = lane; l < nl; l += 32)
+      for (int l = n_a + lane; l < nl; l += 32)
         if (!is_carried(l))
           bulk_load(sm + l * kLaneRow, prog_row<T, KIND>(__ldg(lr + l), v, x, ld, s0), kRow,
                     tma.mbar);
+      if constexpr (FROM_A) {
+        if (kPrefetchOwn<T> && g + 1 < g_end)
+          prefetch_own_from_a<LW>(P.loads + sg_next.x, (sg_next.y >> 16) & 0x3ff, d.slot_src, a,
+                                  ld, s0);
+        load_own_from_a<T, LW>(lr, n_a, c_to, d.slot_src, a, ld, s0, S,
+                               reinterpret_cast<V2*>(sm) + lane);
+      }
       long long polls = 0;
       bool late = false;
       while (!mbar_try_wait(tma.mbar, tma.phase)) {
@@ -418,12 +513,13 @@ __device__ __forceinline__ void prog_run_chain(const ProgDev& P, const DevStruct
 // Chains [cb, ce) of one level: work item = (chain, group of 32 * LW
 // scenarios) in batched mode, chain alone in single mode; one warp per item.
 // In batched mode every bulk store of the warp is complete when this returns.
-template <typename T, int KIND, bool BATCH, int LW = 2>
+template <typename T, int KIND, bool BATCH, int LW = 2, bool FROM_A = false>
 __device__ __forceinline__ void prog_run_level(const ProgDev& P, const DevStruct& d, int cb,
                                                int ce, T* __restrict__ v, T* __restrict__ x,
                                                int ld, int S, T* sm_warp, WarpTma& tma,
                                                T pivot_tol, DevStatus* st,
-                                               const int* done, int warp_id, int n_warps) {
+                                               const int* done, int warp_id, int n_warps,
+                                               const double* __restrict__ a = nullptr) {
   constexpr int group = 32 * LW;
   const int groups = BATCH ? ld / group : 1;
   const int items = (ce - cb) * groups;
@@ -442,7 +538,8 @@ __device__ __forceinline__ void prog_run_level(const ProgDev& P, const DevStruct
       }
       if (__all_sync(0xffffffffu, idle)) continue;
     }
-    prog_run_chain<T, KIND, BATCH, LW>(P, d, c, v, x, ld, s0, S, sm_warp, tma, pivot_tol, st);
+    prog_run_chain<T, KIND, BATCH, LW, FROM_A>(P, d, c, v, x, ld, s0, S, sm_warp, tma,
+                                               pivot_tol, st, a);
   }
   if (BATCH) {
     bulk_wait_all();
@@ -514,6 +611,25 @@ k_prog_level(ProgDev P, int table, DevStruct d, int cb, int ce,
   const int n_warps = (gridDim.x * blockDim.x) >> 5;
   prog_run_level<T, KIND, BATCH, LW>(P, d, cb, ce, v, x, ld, S, sm, tma, pivot_tol, st, done,
                                      warp_id, n_warps);
+}
+
+// One level of the batched refactorization whose own rows are read from the
+// caller's FP64 values `a` (leading dimension ld): scatter and refactor in
+// one pass.  Only for programs without WIDE levels, where every LU slot is an
+// own row of some level's segment.
+template <typename T, int LW = 2>
+__global__ void __launch_bounds__(kProgBlock, prog_min_blocks<T>())
+k_prog_refactor_from_a(ProgDev P, int table, DevStruct d, int cb, int ce, T* __restrict__ v,
+                       const double* __restrict__ a, int ld, int S, T pivot_tol,
+                       DevStatus* st) {
+  if (__ldcg(&st->code) == 6) return;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  WarpTma tma;
+  T* sm = prog_setup_warp<T, true, LW>(smem_raw, table, tma);
+  const int warp_id = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int n_warps = (gridDim.x * blockDim.x) >> 5;
+  prog_run_level<T, -1, true, LW, true>(P, d, cb, ce, v, nullptr, ld, S, sm, tma, pivot_tol, st,
+                                        nullptr, warp_id, n_warps, a);
 }
 
 // ---------------------------------------------------------------------------

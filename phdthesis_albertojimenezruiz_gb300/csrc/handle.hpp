@@ -154,6 +154,8 @@ int run_scatter(pvglu_numeric* h, const AValues& A, const int* ndone, cudaStream
 // skip.ndone (or NULL): nothing runs once every scenario is done; the
 // refactorization itself never skips single scenarios.
 int run_refactor(pvglu_numeric* h, cudaStream_t st, SkipDone skip = SkipDone{nullptr, nullptr});
+// Scatter + refactor from A's FP64 values (one pass where the programs allow).
+int run_scatter_refactor(pvglu_numeric* h, const double* a, cudaStream_t st);
 // Solve in pivot order in place (x: T = double or float per the handle).
 int run_solve_perm(pvglu_numeric* h, void* x, bool transpose, SkipDone skip, cudaStream_t st);
 // Refactor + pivot-order solve; one persistent launch where the schedule has it.

@@ -152,6 +152,11 @@ class Numeric:
     def refactor(self, stream=None) -> None:
         N.check(N.lib().pvglu_refactor(self.handle, _stream_ptr(stream)), "pvglu_refactor")
 
+    def scatter_refactor(self, a_values, stream=None) -> None:
+        """pvglu_scatter_refactor: the factors of scatter() then refactor()."""
+        N.check(N.lib().pvglu_scatter_refactor(self.handle, _ptr(a_values), _stream_ptr(stream)),
+                "pvglu_scatter_refactor")
+
     def solve(self, x, transpose: bool = False, original: bool = False, stream=None) -> None:
         flags = (N.SOLVE_TRANSPOSE if transpose else 0) | (N.SOLVE_ORIGINAL if original else 0)
         N.check(N.lib().pvglu_solve(self.handle, _ptr(x), flags, _stream_ptr(stream)),

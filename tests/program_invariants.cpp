@@ -131,6 +131,9 @@ void check_program(const Symbolic& s, int kind, const ProgramOptions& opt) {
           "kind %d level %d budget %d", kind, lv, b);
     return b;
   };
+  // Refactorization: own-row count of every LU slot (a WIDE column's slots
+  // count once for the column).
+  std::vector<int> owned(kind < 0 ? s.nnz_lu : 0, 0);
   for (int lv = 0; lv < nlev; lv++) {
     const int table = pr.level_max_locals[lv];
     const int bud = budget_of(lv);
@@ -148,6 +151,8 @@ void check_program(const Symbolic& s, int kind, const ProgramOptions& opt) {
                   pr.wide.unit[sg.op_begin] == u,
               "kind %d wide segment of unit %d", kind, u);
         CHECK(unit_need(s, kind, u) > pr.level_wide_at[lv], "kind %d unit %d is not wide", kind, u);
+        if (kind < 0)
+          for (int q = s.csc_colptr[u]; q < s.csc_colptr[u + 1]; q++) owned[q]++;
         continue;
       }
       for (int k = pr.chain_unit[c]; k < pr.chain_unit[c + 1]; k++)
@@ -167,6 +172,9 @@ void check_program(const Symbolic& s, int kind, const ProgramOptions& opt) {
           const int from = sg.carry[k] >> 16, to = sg.carry[k] & 0xffff;
           CHECK(from >= 0 && from < prev_nl, "kind %d segment %d carry from %d", kind, g, from);
           CHECK(to >= 0 && to < sg.n_load, "kind %d segment %d carry to %d", kind, g, to);
+          // A refactorization's own rows are the slots' first use: never
+          // carried (the one-pass scatter reads them from A).
+          CHECK(kind >= 0 || to >= sg.n_own, "kind %d segment %d carries an own row", kind, g);
           for (int j = 0; j < k; j++)
             CHECK((sg.carry[j] & 0xffff) != to, "kind %d segment %d duplicate carry", kind, g);
         }
@@ -174,6 +182,8 @@ void check_program(const Symbolic& s, int kind, const ProgramOptions& opt) {
           const int r = pr.loads[sg.load_begin + l];
           if (kind < 0) {
             CHECK(r >= 0 && r < s.nnz_lu, "kind %d load %d", kind, r);
+            if (l < sg.n_own) owned[r]++;
+            else CHECK(owned[r] == 1, "kind %d slot %d read before its own segment", kind, r);
           } else if (r >= 0) {
             CHECK(r < s.n, "kind %d solution row %d", kind, r);
           } else {
@@ -200,6 +210,8 @@ void check_program(const Symbolic& s, int kind, const ProgramOptions& opt) {
       }
     }
   }
+  for (int q = 0; q < (int)owned.size(); q++)
+    CHECK(owned[q] == 1, "kind %d slot %d is an own row %d times", kind, q, owned[q]);
   // Wide refactor plans: targets inside their column, pairs in ascending j,
   // every U source of a target computed at an earlier chain level or earlier
   // in the target's own chain (and marked so), long targets alone in their

@@ -847,3 +847,83 @@ def test_refine_stamps_host_matches_oracle(cuda):
     for k in (0, 17, S - 1):
         _, x_ref = o.scatter_refactor_solve(a[:, k], b[:, k])
         assert np.abs(x[:, k] - x_ref).max() / np.abs(x_ref).max() <= 1e-10
+
+
+def _values_bits(num: Numeric, count: int) -> np.ndarray:
+    """The factor values' bit patterns, padding scenarios included."""
+    import torch
+
+    ts, it = ("<f8", np.uint64) if num.precision == FP64 else ("<f4", np.uint32)
+    t = torch.as_tensor(_DevView(num.values_ptr(), (count * num.ld,), ts), device="cuda")
+    torch.cuda.synchronize()
+    return t.cpu().numpy().view(it).reshape(count, num.ld).copy()
+
+
+@pytest.mark.parametrize("precision", [FP64, FP32])
+@pytest.mark.parametrize("name,S,max_locals,merge,schedule", [
+    ("plant_10x16x20", 37, 24, 1, SCHED_LEVELS),
+    ("plant_10x16x20", 130, 8, 0, SCHED_LEVELS),
+    ("plant_4x8x20", 64, 16, 2, SCHED_PERSISTENT),
+    ("mesh_30x30", 64, 0, 2, SCHED_LEVELS),
+    ("mesh_12x10", 64, 16, 1, SCHED_LEVELS),
+    ("random_1500", 100, 0, 1, SCHED_LEVELS),
+    ("block_1x20x20", 64, 24, 2, SCHED_LEVELS),
+])
+def test_scatter_refactor_one_pass_bit_identical(cuda, precision, name, S, max_locals, merge,
+                                                 schedule):
+    """pvglu_scatter_refactor reads each column's entries straight from A
+    where the handle allows (batched, per-level schedule, no WIDE level) and
+    falls back to scatter + refactor elsewhere (the persistent schedule; the
+    reference-topology block plant, which has WIDE levels): the factors equal
+    pvglu_scatter then pvglu_refactor bit for bit, padding scenarios
+    included, after stale factors of other values were in the handle."""
+    if name.startswith("plant_"):
+        p = Plant(*map(int, name[6:].split("x")))
+        s = Symbolic(p.rowptr, p.colidx)
+        a, _ = M.plant_batch(p, S, seed0=70, preset="c3")
+    elif name in M.CASES:
+        rp, ci, a1, _ = M.CASES[name]()
+        s = Symbolic(rp, ci)
+        a = a1[:, None] * (1.0 + 1e-3 * np.arange(S))[None, :]
+    else:
+        g = load_golden(name)
+        s = Symbolic(g["rowptr"], g["colidx"], g["perm_amd"])
+        a = g["a"][:, None] * (1.0 + 1e-3 * np.arange(S))[None, :]
+    t = {"max_locals": max_locals, "wide_threshold": 0, "merge_chains": merge,
+         "schedule": schedule}
+    ref = Numeric(s, S, precision, tuning=t)
+    a_dev = dev(pad_cols(a, ref.ld))
+    ref.scatter(a_dev)
+    ref.refactor()
+    assert ref.check()[0] == 0
+    want = _values_bits(ref, int(s.nnz_lu))
+    one = Numeric(s, S, precision, tuning=t)
+    one.scatter(dev(pad_cols(a[:, ::-1] * 3.0, one.ld)))
+    one.refactor()
+    one.check()
+    one.scatter_refactor(a_dev)
+    assert one.check()[0] == 0
+    assert np.array_equal(_values_bits(one, int(s.nnz_lu)), want)
+
+
+@pytest.mark.parametrize("precision", [FP64, FP32])
+def test_scatter_refactor_reports_zero_pivot(cuda, precision):
+    """A zero pivot in one scenario: the one-pass scatter + refactor reports
+    the same column and scenario as pvglu_scatter + pvglu_refactor."""
+    p = Plant(4, 8, 20)
+    s = Symbolic(p.rowptr, p.colidx)
+    S = 33
+    a, _ = M.plant_batch(p, S, seed0=5)
+    row = int(s.array("row_orig")[0])
+    a[p.rowptr[row]:p.rowptr[row + 1], 17] = 0.0
+    got = []
+    for one_pass in (False, True):
+        num = Numeric(s, S, precision, SCHED_LEVELS)
+        a_dev = dev(pad_cols(a, num.ld))
+        if one_pass:
+            num.scatter_refactor(a_dev)
+        else:
+            num.scatter(a_dev)
+            num.refactor()
+        got.append(num.check())
+    assert got[0] == got[1] and got[0][0] == N.OK + 3 and got[0][2] == 17, got
