@@ -38,7 +38,7 @@ DIMS = (50, 24, 28)
 METRIC = "refactor+solve/s, 35k-unknown PV Jacobian: batched+FP32-IR vs plain FP64 GPU"
 UNIT = "refactor+solve/s"
 IR_TOL = 1e-12
-REFACTOR_TRAFFIC_512 = 362.0e6  # bytes, ncu dram__bytes_read.sum + dram__bytes_write.sum
+REFACTOR_TRAFFIC_512 = None  # bytes, ncu dram__bytes_read.sum + dram__bytes_write.sum
 RESIDUAL_TRAFFIC_512 = 735.3e6  # bytes, the same for one k_residual_rows launch
 IR_MAX_SWEEPS = 6
 
@@ -212,6 +212,8 @@ def bytes_model(nnz_a: int, nnz_lu: int, n: int, w: int) -> dict:
     return {
         "scatter": 8 * nnz_a + w * nnz_lu,
         "refactor": 2 * w * nnz_lu,
+        # one pass: A's values in, the factors out (pvglu_scatter_refactor)
+        "scatter_refactor": 8 * nnz_a + w * nnz_lu,
         "solve": w * nnz_lu + 4 * w * n,
         "residual": 8 * nnz_a + 8 * n + 8 * n + 4 * n,
         "update": 4 * n + 16 * n,
@@ -537,8 +539,7 @@ def config4_section(stream, steps: int) -> dict:
     sweeps = torch.zeros(ld, dtype=torch.int32, device=dev)
 
     def step():
-        num.scatter(a_d, stream=stream)
-        num.refactor(stream=stream)
+        num.scatter_refactor(a_d, stream=stream)
         num.solve_refined(a_d, b_d, x_d, tol=IR_TOL, max_sweeps=IR_MAX_SWEEPS, sweeps=sweeps,
                           stream=stream)
 
@@ -1219,8 +1220,7 @@ def main() -> None:
     assert num.ld == ld
 
     def step():
-        num.scatter(a_d, stream=stream)
-        num.refactor(stream=stream)
+        num.scatter_refactor(a_d, stream=stream)
         num.solve_refined(a_d, b_d, x_d, tol=IR_TOL, max_sweeps=IR_MAX_SWEEPS, sweeps=sweeps,
                           stream=stream)
 
@@ -1232,7 +1232,8 @@ def main() -> None:
         raise SystemExit(f"refactor failed: status {code} column {col} scenario {sc}")
 
     # Timed region: K steps, barrier + synchronize on both sides, CUDA events
-    # on the launching stream; per-step events around the refactor kernel.
+    # on the launching stream; per-step events around the one-pass scatter +
+    # refactorization.
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     rf = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
@@ -1243,9 +1244,8 @@ def main() -> None:
     with ClockSampler(local) as clk:
         ev0.record(stream)
         for k in range(args.steps):
-            num.scatter(a_d, stream=stream)
             rf[k][0].record(stream)
-            num.refactor(stream=stream)
+            num.scatter_refactor(a_d, stream=stream)
             rf[k][1].record(stream)
             num.solve_refined(a_d, b_d, x_d, tol=IR_TOL, max_sweeps=IR_MAX_SWEEPS,
                               sweeps=sweeps, stream=stream)
@@ -1308,8 +1308,7 @@ def main() -> None:
     x_s = torch.zeros_like(b_d)
 
     def spec_step():
-        num.scatter(a_d, stream=stream)
-        num.refactor(stream=stream)
+        num.scatter_refactor(a_d, stream=stream)
         num.solve_refined(a_d, b_d, x_s, tol=1e-10, max_sweeps=IR_MAX_SWEEPS, sweeps=sweeps,
                           stream=stream)
 
@@ -1379,9 +1378,14 @@ def main() -> None:
     x64b = torch.empty_like(b_d)
 
     def fp64_step():
-        num64b.scatter(a_d, stream=stream)
-        x64b.copy_(b_d)
-        num64b.refactor_solve(x64b, original=True, stream=stream)
+        if t64["schedule"] == SCHED_LEVELS:  # scatter + refactor in one pass
+            num64b.scatter_refactor(a_d, stream=stream)
+            x64b.copy_(b_d)
+            num64b.solve(x64b, original=True, stream=stream)
+        else:  # refactor + solve in one persistent launch
+            num64b.scatter(a_d, stream=stream)
+            x64b.copy_(b_d)
+            num64b.refactor_solve(x64b, original=True, stream=stream)
 
     for _ in range(args.warmup):
         fp64_step()
@@ -1409,8 +1413,7 @@ def main() -> None:
             x_r = torch.zeros_like(b_d)
 
             def ref_order_step():
-                num_r.scatter(a_d, stream=stream)
-                num_r.refactor(stream=stream)
+                num_r.scatter_refactor(a_d, stream=stream)
                 num_r.solve_refined(a_d, b_d, x_r, tol=IR_TOL, max_sweeps=IR_MAX_SWEEPS,
                                     sweeps=sweeps, stream=stream)
 
@@ -1504,18 +1507,22 @@ def main() -> None:
     bm = bytes_model(nnz_a, nnz_lu, n, 4)
     peaks = _peaks()
     peak = peaks.get("hbm_gbs")
-    achieved = bm["refactor"] * S / (refactor_ms / 1000.0) / 1e9
+    # The per-level schedule scatters and refactors in one pass (without
+    # WIDE levels, as on this plant); the persistent one scatters first.
+    one_pass = not persistent and num.info["wide_levels"] == 0
+    rf_bytes = bm["scatter_refactor"] if one_pass else bm["refactor"]
+    achieved = rf_bytes * S / (refactor_ms / 1000.0) / 1e9
     roofline_refactor = {
-        "kernel": ("k_prog_persistent<float,batched>" if persistent else
-                   "k_prog_level<float,refactor,batched>") + " (refactor phase)",
+        "kernel": ("k_prog_refactor_from_a<float> (scatter + refactor in one pass, both levels)"
+                   if one_pass else "k_prog_persistent<float,batched> (refactor phase)"),
         "bound": "hbm",
         "achieved": achieved, "peak": peak, "unit": "GB/s",
         "frac": achieved / peak if peak else None,
-        # DRAM read + write bytes of one refactorization (its two level
-        # launches) from an ncu capture of this workload (512 scenarios).
-        "traffic": REFACTOR_TRAFFIC_512 if S == 512 else None,
+        # DRAM read + write bytes of one scatter + refactorization (its two
+        # level launches) from an ncu capture of this workload (512 scenarios).
+        "traffic": REFACTOR_TRAFFIC_512 if S == 512 and one_pass else None,
         "peak_source": "measured" if peak else "fallback",
-        "bytes_per_launch": bm["refactor"] * S, "avg_launch_ms": refactor_ms}
+        "bytes_per_launch": rf_bytes * S, "avg_launch_ms": refactor_ms}
     achieved_r = bm["residual"] * S / (resid_ms / 1000.0) / 1e9
     roofline = {
         "kernel": "k_residual_rows (FP64 residual of the refinement, the largest share of a "
@@ -1539,8 +1546,9 @@ def main() -> None:
               if args.newton_scenarios > 0 else None)
     cpu = cpu_baseline(a[:, :S], b[:, :S], p, sym.array("perm_amd"), args.cpu_budget,
                        os.cpu_count() or 1, prefer_ref=True)
-    # per step: scatter, permute b, refactor, then per sweep (all launched;
-    # converged work exits at once) solve, update, check and residual.
+    # per step: scatter + refactor (one launch per level in one pass, else a
+    # scatter first), permute b, then per sweep (all launched; converged work
+    # exits at once) solve, update, check and residual.
     refactor_launches = 1 if persistent else sym.info["lu_levels"]
     solve_launches = 1 if persistent else sym.info["l_levels"] + sym.info["u_levels"]
     sweeps_run = int(sw.max())
@@ -1548,7 +1556,7 @@ def main() -> None:
         refine_launches = IR_MAX_SWEEPS * (solve_launches + 2) + IR_MAX_SWEEPS - 1
     else:  # graph: permute, first sweep, then residual + solve + update + check per sweep
         refine_launches = 1 + (solve_launches + 2) + (sweeps_run - 1) * (solve_launches + 3)
-    launches = args.steps * (1 + refactor_launches + refine_launches)
+    launches = args.steps * ((0 if one_pass else 1) + refactor_launches + refine_launches)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,

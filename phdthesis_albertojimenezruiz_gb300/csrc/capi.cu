@@ -900,6 +900,15 @@ int pvglu_numeric_create_tuned(const pvglu_symbolic* sym, int n_scenarios, int p
     rc |= h->put(seg, &P.seg);
     rc |= h->put(carry, &P.carry);
     rc |= h->put(prog.loads, &P.loads);
+    P.load_src = nullptr;
+    if (ph == 0) {
+      // One pass from A: the A entry of every own row's slot (-1 at fill).
+      std::vector<int> src(prog.loads.size(), -1);
+      for (const auto& sg : prog.seg)
+        for (int l = 0; l < std::max(sg.n_own, 0); l++)
+          src[sg.load_begin + l] = s.slot_src[prog.loads[sg.load_begin + l]];
+      rc |= h->put(src, &P.load_src);
+    }
     rc |= h->put(ops, &P.ops);
     rc |= h->put(prog.op_col, &P.op_col);
     std::vector<int> lwide(prog.level_wide.begin(), prog.level_wide.end());
@@ -1172,8 +1181,7 @@ int pvglu_scatter_refactor_solve_host(pvglu_numeric* h, const double* a_values_h
                              cudaMemcpyHostToDevice, st));
   PVGLU_CUDA(cudaMemcpyAsync(x, b_host, (size_t)h->n * h->ld * sizeof(double),
                              cudaMemcpyHostToDevice, st));
-  int rc = pvglu_scatter(h, a, stream);
-  if (!rc) rc = pvglu_refactor(h, stream);
+  int rc = pvglu_scatter_refactor(h, a, stream);
   if (!rc) rc = pvglu_solve(h, x, PVGLU_SOLVE_ORIGINAL, stream);
   if (rc) return rc;
   PVGLU_CUDA(cudaMemcpyAsync(x_host, x, (size_t)h->n * h->ld * sizeof(double),
@@ -1205,8 +1213,7 @@ int pvglu_refine_system_host(pvglu_numeric* h, const double* a_values_host,
                              cudaMemcpyHostToDevice, st));
   PVGLU_CUDA(cudaMemcpyAsync(h->b64, b_host, (size_t)h->n * h->ld * sizeof(double),
                              cudaMemcpyHostToDevice, st));
-  int rc = pvglu_scatter(h, a, stream);
-  if (!rc) rc = pvglu_refactor(h, stream);
+  int rc = pvglu_scatter_refactor(h, a, stream);
   if (!rc) rc = pvglu_solve_refined(h, a, h->b64, h->x64, tol, max_sweeps, sweeps_out, stream);
   if (rc) return rc;
   PVGLU_CUDA(cudaMemcpyAsync(x_host, h->x64, (size_t)h->n * h->ld * sizeof(double),
@@ -1236,8 +1243,7 @@ int pvglu_refine_stamps_host(pvglu_numeric* h, const double* g_host, const doubl
   pvglu::k_assemble<<<pvglu::rows_grid(h->nnz_a, h->ld, 256), 256, 0, st>>>(
       h->nnz_a, h->ld, h->S, h->stamps(h->g64, nullptr), a);
   PVGLU_CUDA(cudaGetLastError());
-  int rc = pvglu_scatter(h, a, stream);
-  if (!rc) rc = pvglu_refactor(h, stream);
+  int rc = pvglu_scatter_refactor(h, a, stream);
   if (!rc) rc = pvglu_solve_refined(h, a, h->b64, h->x64, tol, max_sweeps, sweeps_out, stream);
   if (rc) return rc;
   PVGLU_CUDA(cudaMemcpyAsync(x_host, h->x64, (size_t)h->n * h->ld * sizeof(double),
@@ -1552,8 +1558,13 @@ int autotune_over(const pvglu_symbolic* sym, int n_scenarios, int precision,
     for (int rep = 0; rep < 4 && ok; rep++) {
       cudaMemsetAsync(xw, 0, xbytes, nullptr);
       cudaEventRecord(e0, nullptr);
-      ok = pvglu_scatter(h, ad, nullptr) == PVGLU_OK &&
-           pvglu_refactor_solve(h, xw, 0, nullptr) == PVGLU_OK;
+      // The per-level schedule scatters and refactors in one pass; the
+      // persistent schedule refactors and solves in one launch.
+      ok = h->schedule == PVGLU_SCHED_LEVELS
+               ? pvglu_scatter_refactor(h, ad, nullptr) == PVGLU_OK &&
+                     pvglu_solve(h, xw, 0, nullptr) == PVGLU_OK
+               : pvglu_scatter(h, ad, nullptr) == PVGLU_OK &&
+                     pvglu_refactor_solve(h, xw, 0, nullptr) == PVGLU_OK;
       cudaEventRecord(e1, nullptr);
       if (cudaEventSynchronize(e1) != cudaSuccess) ok = false;
       float ms = 0.f;

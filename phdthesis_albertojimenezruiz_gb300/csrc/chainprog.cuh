@@ -34,6 +34,8 @@ struct ProgDev {
                            //  reads_own_chain << 30 (or -1: WIDE), op_begin, n_op}
   const int4* carry;       // [segments] up to 4 moves (from << 16 | to) of table rows
   const int* loads;
+  const int* load_src;     // refactorization, per load: A entry of an own row's slot
+                           // (-1 at fill slots and for read-only rows); else NULL
   const int4* ops;         // packed operations, 4 per int4
   const int* op_col;       // column of each SCALE operation
   int max_locals;
@@ -278,23 +280,26 @@ __device__ __forceinline__ void prog_drain(WarpTma& tma) {
   __syncwarp();
 }
 
-// Own rows of a refactorization segment taken straight from A's FP64 values
-// (FROM_A): row l of the table gets A(slot_src[ref], s) converted to T, zero
-// at fill slots and past S, which is what the scatter would have stored.
-// Every LU slot is an own row of exactly one segment (its column's) and no
-// segment reads it earlier, so these loads replace the scatter's write and
-// the refactorization's first read of the slot.  Plain 8 * LW-byte loads by
-// all lanes, kOwnInFlight rows at a time; the table's other rows keep their
-// bulk copies, which are already under way.
+// One pass from A (prog_run_chain's FROM_A): the own rows of a
+// refactorization segment take A(src, s) converted to T, zero at fill slots
+// (src < 0) and past S, which is what the scatter would have stored; src is
+// ProgDev::load_src of the row.  Every LU slot is an own row of exactly one
+// segment (its column's) and no segment reads it earlier, so these rows
+// replace the scatter's write and the refactorization's first read of the
+// slot.  Plain 8 * LW-byte loads by all lanes, kOwnInFlight rows at a time,
+// while the table's other rows arrive by bulk copies.  Four rows measured
+// best for both precisions (35k plant, 512 scenarios: FP32 2 / 4 / 6 rows
+// 212 / 179 / 195 us, FP64 2 / 4 rows 464 / 432 us).
 #ifndef PVGLU_OWN_IN_FLIGHT_F32
 #define PVGLU_OWN_IN_FLIGHT_F32 4
 #endif
 #ifndef PVGLU_OWN_IN_FLIGHT_F64
-#define PVGLU_OWN_IN_FLIGHT_F64 2
+#define PVGLU_OWN_IN_FLIGHT_F64 4
 #endif
+// Own rows [l_begin, l_end) of the segment whose sources start at src
+// (ProgDev::load_src + load_begin).
 template <typename T, int LW>
-__device__ __forceinline__ void load_own_from_a(const int* lr, int n_a, const int* c_to,
-                                                const int* __restrict__ slot_src,
+__device__ __forceinline__ void load_own_from_a(const int* src, int l_begin, int l_end,
                                                 const double* __restrict__ a, int ld, int s0,
                                                 int S, LaneV<T, LW>* t) {
   using VA = LaneV<double, LW>;
@@ -302,9 +307,9 @@ __device__ __forceinline__ void load_own_from_a(const int* lr, int n_a, const in
   constexpr int kOwnInFlight = sizeof(T) == 4 ? PVGLU_OWN_IN_FLIGHT_F32 : PVGLU_OWN_IN_FLIGHT_F64;
   const int lane = threadIdx.x & 31;
   const int s = s0 + LW * lane;
-  for (int l0 = 0; l0 < n_a; l0 += 32) {
-    const int nb = min(32, n_a - l0);
-    const int m = lane < nb ? __ldg(slot_src + __ldg(lr + l0 + lane)) : -1;
+  for (int l0 = l_begin; l0 < l_end; l0 += 32) {
+    const int nb = min(32, l_end - l0);
+    const int m = lane < nb ? __ldg(src + l0 + lane) : -1;
     for (int k = 0; k < nb; k += kOwnInFlight) {
       VA av[kOwnInFlight];
 #pragma unroll
@@ -316,29 +321,29 @@ __device__ __forceinline__ void load_own_from_a(const int* lr, int n_a, const in
       }
 #pragma unroll
       for (int j = 0; j < kOwnInFlight; j++) {
-        const int l = l0 + k + j;
-        if (k + j < nb && l != c_to[0] && l != c_to[1] && l != c_to[2] && l != c_to[3]) {
+        if (k + j < nb) {
           V o;
 #pragma unroll
           for (int p = 0; p < LW; p++)
             lane_part(o, p) = s + p < S ? convert<T>(lane_part(av[j], p)) : T(0);
-          t[l << 5] = o;
+          t[(l0 + k + j) << 5] = o;
         }
       }
     }
   }
 }
 
-// L2 prefetch of the A rows that load_own_from_a will read for a segment's
-// own rows [0, n_a): issued a segment ahead, so that those plain loads find
-// their rows in L2 instead of waiting for DRAM.
+// L2 prefetch of the A rows that load_own_from_a will read for own rows
+// [0, n_a): issued a segment ahead, so that those plain loads find their rows
+// in L2 instead of waiting for DRAM.  FP64 only: the FP64 levels are bound by
+// the FP64 pipe and hide the prefetch's index load (486 -> 466 us at two rows
+// in flight); the FP32 levels wait on it (179 -> 210 us).
 template <int LW>
-__device__ __forceinline__ void prefetch_own_from_a(const int* lr, int n_a,
-                                                    const int* __restrict__ slot_src,
+__device__ __forceinline__ void prefetch_own_from_a(const int* src, int n_a,
                                                     const double* __restrict__ a, int ld,
                                                     int s0) {
   for (int l = threadIdx.x & 31; l < n_a; l += 32) {
-    const int m = __ldg(slot_src + __ldg(lr + l));
+    const int m = __ldg(src + l);
     if (m >= 0)
       bulk_prefetch_l2(a + (size_t)(unsigned)m * (unsigned)ld + s0, 32 * LW * sizeof(double));
   }
@@ -371,8 +376,7 @@ __device__ __forceinline__ void prog_run_chain(const ProgDev& P, const DevStruct
     sg_next = __ldg(P.seg + g_begin);
     cv_next = __ldg(P.carry + g_begin);
     if constexpr (FROM_A && kPrefetchOwn<T>)
-      prefetch_own_from_a<LW>(P.loads + sg_next.x, (sg_next.y >> 16) & 0x3ff, d.slot_src, a, ld,
-                              s0);
+      prefetch_own_from_a<LW>(P.load_src + sg_next.x, (sg_next.y >> 16) & 0x3ff, a, ld, s0);
   }
   for (int g = g_begin; g < g_end; g++) {
     const int4 sg = sg_next;
@@ -422,7 +426,8 @@ __device__ __forceinline__ void prog_run_chain(const ProgDev& P, const DevStruct
         for (int c = 0; c < n_carry; c++) t[c_to[c] << 5] = hold[c];
         __syncwarp();
       }
-      // Rows [0, n_a) are read from A below, the rest by bulk copies.
+      // One pass from A: own rows [0, n_a) are read from A below, the rest
+      // by bulk copies.
       const int n_a = FROM_A ? n_own : 0;
       int n_bulk = nl - n_a;
       for (int c = 0; c < n_carry; c++)
@@ -435,9 +440,8 @@ __device__ __forceinline__ void prog_run_chain(const ProgDev& P, const DevStruct
                     tma.mbar);
       if constexpr (FROM_A) {
         if (kPrefetchOwn<T> && g + 1 < g_end)
-          prefetch_own_from_a<LW>(P.loads + sg_next.x, (sg_next.y >> 16) & 0x3ff, d.slot_src, a,
-                                  ld, s0);
-        load_own_from_a<T, LW>(lr, n_a, c_to, d.slot_src, a, ld, s0, S,
+          prefetch_own_from_a<LW>(P.load_src + sg_next.x, (sg_next.y >> 16) & 0x3ff, a, ld, s0);
+        load_own_from_a<T, LW>(P.load_src + sg.x, 0, n_a, a, ld, s0, S,
                                reinterpret_cast<V2*>(sm) + lane);
       }
       long long polls = 0;
