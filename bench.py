@@ -38,7 +38,7 @@ DIMS = (50, 24, 28)
 METRIC = "refactor+solve/s, 35k-unknown PV Jacobian: batched+FP32-IR vs plain FP64 GPU"
 UNIT = "refactor+solve/s"
 IR_TOL = 1e-12
-REFACTOR_TRAFFIC_512 = None  # bytes, ncu dram__bytes_read.sum + dram__bytes_write.sum
+REFACTOR_TRAFFIC_512 = 610.6e6  # bytes, ncu dram__bytes_read.sum + dram__bytes_write.sum
 RESIDUAL_TRAFFIC_512 = 735.3e6  # bytes, the same for one k_residual_rows launch
 IR_MAX_SWEEPS = 6
 
