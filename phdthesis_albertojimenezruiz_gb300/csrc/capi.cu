@@ -110,7 +110,9 @@ int prog_prepare(pvglu_numeric* h) {
   }
   if constexpr (B) {
     const void* from_a[] = {(const void*)pvglu::k_prog_refactor_from_a<T, 2>,
-                            (const void*)pvglu::k_prog_refactor_from_a<T, 1>};
+                            (const void*)pvglu::k_prog_refactor_from_a<T, 1>,
+                            (const void*)pvglu::k_prog_refactor_from_a<T, 2, true>,
+                            (const void*)pvglu::k_prog_refactor_from_a<T, 1, true>};
     for (const void* f : from_a)
       if (pvglu::allow_max_dynamic_smem(f) != cudaSuccess) return 1;
   }
@@ -198,10 +200,12 @@ void prog_levels(pvglu_numeric* h, T* x, const int* done, const int* ndone, cuda
         const size_t smem = pvglu::prog_smem_bytes<T, B, 1>(table, pvglu::kProgWarps);
         if constexpr (KIND < 0) {
           if (a) {
-            pvglu::k_prog_refactor_from_a<T, 1>
-                <<<launch_blocks(items * 2, pvglu::kProgWarps), pvglu::kProgBlock, smem, st>>>(
-                    h->progs.p[ph], table, h->d, cb, ce, static_cast<T*>(h->values), a, h->ld,
-                    h->S, h->pivot_tol, h->status);
+            const auto k = items * 2 <= (int64_t)h->sm_count * pvglu::kProgWarps
+                               ? pvglu::k_prog_refactor_from_a<T, 1, true>
+                               : pvglu::k_prog_refactor_from_a<T, 1>;
+            k<<<launch_blocks(items * 2, pvglu::kProgWarps), pvglu::kProgBlock, smem, st>>>(
+                h->progs.p[ph], table, h->d, cb, ce, static_cast<T*>(h->values), a, h->ld, h->S,
+                h->pivot_tol, h->status);
             continue;
           }
         }
@@ -215,10 +219,14 @@ void prog_levels(pvglu_numeric* h, T* x, const int* done, const int* ndone, cuda
     const size_t smem = pvglu::prog_smem_bytes<T, B>(table, pvglu::kProgWarps);
     if constexpr (KIND < 0 && B) {
       if (a) {
-        pvglu::k_prog_refactor_from_a<T>
-            <<<launch_blocks(items, pvglu::kProgWarps), pvglu::kProgBlock, smem, st>>>(
-                h->progs.p[ph], table, h->d, cb, ce, static_cast<T*>(h->values), a, h->ld, h->S,
-                h->pivot_tol, h->status);
+        // Narrow levels (at most one block of items per SM) keep more own
+        // rows in flight.
+        const auto k = items <= (int64_t)h->sm_count * pvglu::kProgWarps
+                           ? pvglu::k_prog_refactor_from_a<T, 2, true>
+                           : pvglu::k_prog_refactor_from_a<T, 2>;
+        k<<<launch_blocks(items, pvglu::kProgWarps), pvglu::kProgBlock, smem, st>>>(
+            h->progs.p[ph], table, h->d, cb, ce, static_cast<T*>(h->values), a, h->ld, h->S,
+            h->pivot_tol, h->status);
         continue;
       }
     }

@@ -296,15 +296,21 @@ __device__ __forceinline__ void prog_drain(WarpTma& tma) {
 #ifndef PVGLU_OWN_IN_FLIGHT_F64
 #define PVGLU_OWN_IN_FLIGHT_F64 4
 #endif
+// Levels with at most one block of items per SM (the narrow levels: a few
+// warps per SM, registers to spare) keep this many own rows in flight.
+constexpr int kOwnInFlightNarrow = 16;
+
 // Own rows [l_begin, l_end) of the segment whose sources start at src
-// (ProgDev::load_src + load_begin).
-template <typename T, int LW>
+// (ProgDev::load_src + load_begin).  NARROW: kOwnInFlightNarrow rows at a time.
+template <typename T, int LW, bool NARROW = false>
 __device__ __forceinline__ void load_own_from_a(const int* src, int l_begin, int l_end,
                                                 const double* __restrict__ a, int ld, int s0,
                                                 int S, LaneV<T, LW>* t) {
   using VA = LaneV<double, LW>;
   using V = LaneV<T, LW>;
-  constexpr int kOwnInFlight = sizeof(T) == 4 ? PVGLU_OWN_IN_FLIGHT_F32 : PVGLU_OWN_IN_FLIGHT_F64;
+  constexpr int kOwnInFlight =
+      NARROW ? kOwnInFlightNarrow
+             : (sizeof(T) == 4 ? PVGLU_OWN_IN_FLIGHT_F32 : PVGLU_OWN_IN_FLIGHT_F64);
   const int lane = threadIdx.x & 31;
   const int s = s0 + LW * lane;
   for (int l0 = l_begin; l0 < l_end; l0 += 32) {
@@ -358,8 +364,9 @@ constexpr bool kPrefetchOwn = sizeof(T) == 8 || PVGLU_PREFETCH_OWN_F32;
 // Runs every segment of `chain`, batched over the 32 * LW scenarios starting
 // at s0 (BATCH) or for the single scenario.  sm: this warp's table.
 // FROM_A (batched refactorization only): own rows come from `a` (the
-// caller's FP64 values, leading dimension ld) instead of the factor values.
-template <typename T, int KIND, bool BATCH, int LW = 2, bool FROM_A = false>
+// caller's FP64 values, leading dimension ld) instead of the factor values;
+// 2: a narrow level's form (load_own_from_a's NARROW).
+template <typename T, int KIND, bool BATCH, int LW = 2, int FROM_A = 0>
 __device__ __forceinline__ void prog_run_chain(const ProgDev& P, const DevStruct& d, int chain,
                                                T* __restrict__ v, T* __restrict__ x, int ld,
                                                int s0, int S, T* sm, WarpTma& tma,
@@ -441,8 +448,8 @@ __device__ __forceinline__ void prog_run_chain(const ProgDev& P, const DevStruct
       if constexpr (FROM_A) {
         if (kPrefetchOwn<T> && g + 1 < g_end)
           prefetch_own_from_a<LW>(P.load_src + sg_next.x, (sg_next.y >> 16) & 0x3ff, a, ld, s0);
-        load_own_from_a<T, LW>(P.load_src + sg.x, 0, n_a, a, ld, s0, S,
-                               reinterpret_cast<V2*>(sm) + lane);
+        load_own_from_a<T, LW, FROM_A == 2>(P.load_src + sg.x, 0, n_a, a, ld, s0, S,
+                                            reinterpret_cast<V2*>(sm) + lane);
       }
       long long polls = 0;
       bool late = false;
@@ -517,7 +524,7 @@ __device__ __forceinline__ void prog_run_chain(const ProgDev& P, const DevStruct
 // Chains [cb, ce) of one level: work item = (chain, group of 32 * LW
 // scenarios) in batched mode, chain alone in single mode; one warp per item.
 // In batched mode every bulk store of the warp is complete when this returns.
-template <typename T, int KIND, bool BATCH, int LW = 2, bool FROM_A = false>
+template <typename T, int KIND, bool BATCH, int LW = 2, int FROM_A = 0>
 __device__ __forceinline__ void prog_run_level(const ProgDev& P, const DevStruct& d, int cb,
                                                int ce, T* __restrict__ v, T* __restrict__ x,
                                                int ld, int S, T* sm_warp, WarpTma& tma,
@@ -620,9 +627,10 @@ k_prog_level(ProgDev P, int table, DevStruct d, int cb, int ce,
 // One level of the batched refactorization whose own rows are read from the
 // caller's FP64 values `a` (leading dimension ld): scatter and refactor in
 // one pass.  Only for programs without WIDE levels, where every LU slot is an
-// own row of some level's segment.
-template <typename T, int LW = 2>
-__global__ void __launch_bounds__(kProgBlock, prog_min_blocks<T>())
+// own row of some level's segment.  NARROW: for levels with at most one block
+// of items per SM, compiled for one block per SM (more own rows in flight).
+template <typename T, int LW = 2, bool NARROW = false>
+__global__ void __launch_bounds__(kProgBlock, NARROW ? 1 : prog_min_blocks<T>())
 k_prog_refactor_from_a(ProgDev P, int table, DevStruct d, int cb, int ce, T* __restrict__ v,
                        const double* __restrict__ a, int ld, int S, T pivot_tol,
                        DevStatus* st) {
@@ -632,8 +640,8 @@ k_prog_refactor_from_a(ProgDev P, int table, DevStruct d, int cb, int ce, T* __r
   T* sm = prog_setup_warp<T, true, LW>(smem_raw, table, tma);
   const int warp_id = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int n_warps = (gridDim.x * blockDim.x) >> 5;
-  prog_run_level<T, -1, true, LW, true>(P, d, cb, ce, v, nullptr, ld, S, sm, tma, pivot_tol, st,
-                                        nullptr, warp_id, n_warps, a);
+  prog_run_level<T, -1, true, LW, NARROW ? 2 : 1>(P, d, cb, ce, v, nullptr, ld, S, sm, tma,
+                                                  pivot_tol, st, nullptr, warp_id, n_warps, a);
 }
 
 // ---------------------------------------------------------------------------
