@@ -6,7 +6,10 @@ S scenarios with seeded Gaussian-shadow irradiance fields (5 shadows),
 companion Jacobians at the flat start.  Each step scatters the FP64 Jacobian
 values into the filled pattern, refactorizes in FP32 and solves with FP64
 iterative refinement until every scenario reaches max|dx| <= 1e-12 max|x|
-(which puts the solution within 1e-10 of the FP64 solution).  `value` counts
+(which puts the solution within 1e-10 of the FP64 solution).  The S
+scenarios run as --blocks scenario blocks side by side, each on a stream of
+its own (pvglu_blocks_step; one handle of all S is timed beside it as
+`single_handle`).  `value` counts
 refactor+solves (scenarios) per second with inputs resident in HBM; `e2e` is
 the same through the host-buffer C-ABI call (H2D of A and b, D2H of x every
 step).  The plain single-instance FP64 GPU path (scatter + refactor + solve,
@@ -41,6 +44,9 @@ IR_TOL = 1e-12
 REFACTOR_TRAFFIC_512 = 610.6e6  # bytes, ncu dram__bytes_read.sum + dram__bytes_write.sum
 RESIDUAL_TRAFFIC_512 = 735.3e6  # bytes, the same for one k_residual_rows launch
 IR_MAX_SWEEPS = 6
+# The headline's 512 scenarios as 4 blocks of 128 on 4 streams (pvglu_blocks):
+# measured per step 1 / 2 / 4 / 8 blocks 1.010 / 1.006 / 0.960 / 0.989 ms.
+HEADLINE_BLOCKS = 4
 
 
 _TUNED: dict = {}
@@ -1118,6 +1124,9 @@ def main() -> None:
     ap.add_argument("--ir-sweeps", type=int, default=IR_MAX_SWEEPS)
     ap.add_argument("--only-batched", action="store_true",
                     help="time the batched FP32+IR path only (profiling runs)")
+    ap.add_argument("--blocks", type=int, default=HEADLINE_BLOCKS,
+                    help="scenario blocks of the headline step, each on its own stream "
+                         "(pvglu_blocks; 1: one handle)")
     ap.add_argument("--newton-scenarios", type=int, default=128,
                     help="scenarios of the device Newton + adjoint section (0: skip)")
     ap.add_argument("--only-newton", action="store_true",
@@ -1167,7 +1176,8 @@ def main() -> None:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
 
     from phdthesis_albertojimenezruiz_gb300 import (FP32, FP64, SCHED_LEVELS, SCHED_PERSISTENT,
-                                                    SCHED_THREAD_CHAIN, Numeric, Symbolic)
+                                                    SCHED_THREAD_CHAIN, Blocks, Numeric,
+                                                    Symbolic)
     from phdthesis_albertojimenezruiz_gb300.replicas import max_over_ranks
 
     if args.only_configs:
@@ -1212,12 +1222,34 @@ def main() -> None:
 
         tt, tms = _autotune(sym,S, FP32)
         tuned = dict(tt, ms_scatter_refactor_solve=tms, source="pvglu_autotune_ex")
+    tuning = {k: tuned.get(k, d) for k, d in (("max_locals", 0), ("wide_threshold", 0),
+                                              ("merge_chains", 0), ("schedule", SCHED_LEVELS))}
     num = Numeric(sym, S, FP32, tuned["schedule"], max_locals=tuned["max_locals"],
-                  tuning={k: tuned.get(k, d) for k, d in (("max_locals", 0), ("wide_threshold", 0),
-                                                          ("merge_chains", 0),
-                                                          ("schedule", SCHED_LEVELS))})
+                  tuning=tuning)
     persistent = tuned["schedule"] == SCHED_PERSISTENT
     assert num.ld == ld
+    # The headline's scenario blocks: block k holds scenarios [k H, (k+1) H)
+    # in buffers of its own layout (inputs resident before the timed region).
+    n_blk = args.blocks if args.blocks > 1 and S % args.blocks == 0 else 1
+    blk = blk_a = blk_b = blk_x = blk_sw = None
+    if n_blk > 1:
+        H = S // n_blk
+        blk = Blocks(sym, S, n_blk, FP32, tuning=tuning)
+
+        def block_cols(t, k, ld_k):
+            out = torch.zeros((t.shape[0], ld_k), dtype=t.dtype, device=dev)
+            out[:, :H] = t[:, k * H:(k + 1) * H]
+            return out
+
+        blk_a = [block_cols(a_d, k, blk.parts[k].ld) for k in range(n_blk)]
+        blk_b = [block_cols(b_d, k, blk.parts[k].ld) for k in range(n_blk)]
+        blk_x = [torch.zeros_like(t) for t in blk_b]
+        blk_sw = [torch.zeros(blk.parts[k].ld, dtype=torch.int32, device=dev)
+                  for k in range(n_blk)]
+
+    def block_step():
+        blk.step(blk_a, blk_b, blk_x, tol=IR_TOL, max_sweeps=IR_MAX_SWEEPS, sweeps=blk_sw,
+                 stream=stream)
 
     def step():
         num.scatter_refactor(a_d, stream=stream)
@@ -1226,14 +1258,18 @@ def main() -> None:
 
     for _ in range(args.warmup):
         step()
+        if blk is not None:
+            block_step()
     torch.cuda.synchronize()
-    code, col, sc = num.check()
-    if code:
-        raise SystemExit(f"refactor failed: status {code} column {col} scenario {sc}")
+    for h_ in [num] + (blk.parts if blk is not None else []):
+        code, col, sc = h_.check()
+        if code:
+            raise SystemExit(f"refactor failed: status {code} column {col} scenario {sc}")
 
-    # Timed region: K steps, barrier + synchronize on both sides, CUDA events
-    # on the launching stream; per-step events around the one-pass scatter +
-    # refactorization.
+    # Timed regions: K steps each, barrier + synchronize on both sides, CUDA
+    # events on the launching stream.  The one handle first, with per-step
+    # events around the one-pass scatter + refactorization (the roofline);
+    # then the headline, the scenario blocks (the same 512 scenarios).
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     rf = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
@@ -1251,10 +1287,35 @@ def main() -> None:
                               sweeps=sweeps, stream=stream)
         ev1.record(stream)
         torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
-    ms = max_over_ranks(ev0.elapsed_time(ev1), dist, dev)
+        if dist:
+            dist.barrier()
+        ms_one = max_over_ranks(ev0.elapsed_time(ev1), dist, dev)
+        ms = ms_one
+        if blk is not None:
+            eb0 = torch.cuda.Event(enable_timing=True)
+            eb1 = torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            eb0.record(stream)
+            for k in range(args.steps):
+                block_step()
+            eb1.record(stream)
+            torch.cuda.synchronize()
+            if dist:
+                dist.barrier()
+            ms = max_over_ranks(eb0.elapsed_time(eb1), dist, dev)
     refactor_ms = float(np.mean([s.elapsed_time(e) for s, e in rf]))
+    single_handle = {"value": S * world * args.steps / (ms_one / 1000.0), "unit": UNIT,
+                     "ms_per_step": ms_one / args.steps,
+                     "call": "one handle of all scenarios: pvglu_scatter_refactor + "
+                             "pvglu_solve_refined"}
+    if blk is not None:
+        # The blocks' solutions and sweeps against the one handle's.
+        same = all(
+            torch.equal(blk_x[k][:, :S // n_blk], x_d[:, k * (S // n_blk):(k + 1) * (S // n_blk)])
+            and torch.equal(blk_sw[k][:S // n_blk],
+                            sweeps[k * (S // n_blk):(k + 1) * (S // n_blk)])
+            for k in range(n_blk))
+        single_handle["blocks_bit_identical"] = bool(same)
     # The residual kernel alone (the largest share of a step: two launches per
     # step), timed with CUDA events on the launching stream over 20 calls.
     r_buf = torch.empty(n * ld, dtype=torch.float32, device=dev)
@@ -1275,8 +1336,8 @@ def main() -> None:
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT,
                               "ms_per_step": ms / args.steps, "refactor_ms": refactor_ms,
-                              "scenarios": S, "sweeps_max": int(sw.max()),
-                              "tuning": tuned}))
+                              "scenarios": S, "blocks": n_blk, "sweeps_max": int(sw.max()),
+                              "single_handle": single_handle, "tuning": tuned}))
         if dist:
             dist.destroy_process_group()
         return
@@ -1305,18 +1366,28 @@ def main() -> None:
     # The same step with the refinement stopped at the benchmark spec's accuracy
     # bar (1e-10 relative to the FP64 oracle) instead of 1e-12: its rate,
     # sweeps and errors, reported beside the headline (which keeps 1e-12).
+    # The same scenario blocks as the headline.
     x_s = torch.zeros_like(b_d)
 
     def spec_step():
-        num.scatter_refactor(a_d, stream=stream)
-        num.solve_refined(a_d, b_d, x_s, tol=1e-10, max_sweeps=IR_MAX_SWEEPS, sweeps=sweeps,
-                          stream=stream)
+        if blk is not None:
+            blk.step(blk_a, blk_b, blk_x, tol=1e-10, max_sweeps=IR_MAX_SWEEPS, sweeps=blk_sw,
+                     stream=stream)
+        else:
+            num.scatter_refactor(a_d, stream=stream)
+            num.solve_refined(a_d, b_d, x_s, tol=1e-10, max_sweeps=IR_MAX_SWEEPS,
+                              sweeps=sweeps, stream=stream)
 
     for _ in range(args.warmup):
         spec_step()
     ms_s = _time_ms(spec_step, stream, args.steps)
-    sw_s = sweeps.cpu().numpy()[:S]
-    xs_h = x_s.cpu().numpy()[:, :S]
+    if blk is not None:
+        Hb = S // n_blk
+        sw_s = np.concatenate([t.cpu().numpy()[:Hb] for t in blk_sw])
+        xs_h = np.concatenate([t.cpu().numpy()[:, :Hb] for t in blk_x], axis=1)
+    else:
+        sw_s = sweeps.cpu().numpy()[:S]
+        xs_h = x_s.cpu().numpy()[:, :S]
     spec_oracle = []
     for k in sorted({0, 1, S // 3, S // 2, (2 * S) // 3, S - 1}):
         _, x_ref = port.scatter_refactor_solve(a[:, k], b[:, k])
@@ -1551,12 +1622,18 @@ def main() -> None:
     # exits at once) solve, update, check and residual.
     refactor_launches = 1 if persistent else sym.info["lu_levels"]
     solve_launches = 1 if persistent else sym.info["l_levels"] + sym.info["u_levels"]
-    sweeps_run = int(sw.max())
-    if persistent:  # sweep by sweep: every sweep up to the cap is launched
-        refine_launches = IR_MAX_SWEEPS * (solve_launches + 2) + IR_MAX_SWEEPS - 1
-    else:  # graph: permute, first sweep, then residual + solve + update + check per sweep
-        refine_launches = 1 + (solve_launches + 2) + (sweeps_run - 1) * (solve_launches + 3)
-    launches = args.steps * ((0 if one_pass else 1) + refactor_launches + refine_launches)
+    def handle_launches(sweeps_run: int) -> int:
+        if persistent:  # sweep by sweep: every sweep up to the cap is launched
+            refine = IR_MAX_SWEEPS * (solve_launches + 2) + IR_MAX_SWEEPS - 1
+        else:  # graph: permute, first sweep, then residual + solve + update + check per sweep
+            refine = 1 + (solve_launches + 2) + (sweeps_run - 1) * (solve_launches + 3)
+        return (0 if one_pass else 1) + refactor_launches + refine
+
+    if blk is not None:  # every block launches its own sequence
+        launches = args.steps * sum(handle_launches(int(t[:S // n_blk].max().item()))
+                                    for t in blk_sw)
+    else:
+        launches = args.steps * handle_launches(int(sw.max()))
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
@@ -1566,6 +1643,11 @@ def main() -> None:
                                f"{nnz_a}, nnz_lu {nnz_lu}): scatter + FP32 GLU refactor + "
                                f"FP64-refined solve, {S} scenarios per step",
                    "scenarios_per_step": S, "parallelism": f"replicas x{world}",
+                   "blocks": n_blk,
+                   "call": (f"pvglu_blocks_step: {n_blk} blocks of {S // n_blk} scenarios, each "
+                            "pvglu_scatter_refactor + pvglu_solve_refined on a stream of its own"
+                            if n_blk > 1 else
+                            "pvglu_scatter_refactor + pvglu_solve_refined"),
                    "l2": "inputs larger than L2 (FP64 Jacobian values "
                          f"{8 * nnz_a * ld / 1e6:.0f} MB per batch)",
                    "ir_tol": IR_TOL, "ir_max_sweeps": IR_MAX_SWEEPS, "tuning": tuned,
@@ -1580,6 +1662,7 @@ def main() -> None:
                 "sweeps_max": int(e2e_sw.max()), "not_converged": int((e2e_sw <= 0).sum()),
                 "max_rel_err_vs_fp64": e2e_err},
         "e2e_structured": e2e_structured,
+        "single_handle": single_handle,
         "roofline": roofline,
         "roofline_refactor": roofline_refactor,
         "cpu_baseline": cpu,

@@ -8,12 +8,12 @@ Python view; importing it loads the library and fails if it is missing.
 from . import _native
 from ._native import (FP32, FP64, SCHED_LEVELS, SCHED_PERSISTENT, SCHED_THREAD_CHAIN,
                       PvgluError)
-from .glu import Numeric, Symbolic
+from .glu import Blocks, Numeric, Symbolic
 from .newton import GMIN_STAGES, Newton, plant_power
 from .plant import Plant
 
 _native.lib()  # fail loudly at import when the native library is absent
 
-__all__ = ["FP32", "FP64", "GMIN_STAGES", "SCHED_LEVELS", "SCHED_PERSISTENT",
+__all__ = ["Blocks", "FP32", "FP64", "GMIN_STAGES", "SCHED_LEVELS", "SCHED_PERSISTENT",
            "SCHED_THREAD_CHAIN", "Newton", "Numeric", "PvgluError", "Plant", "Symbolic",
            "plant_power"]

@@ -106,6 +106,10 @@ _SIGS = {
     "pvglu_autotune_ex": ([_P, _I, _I, _P, _DP], _I),
     "pvglu_numeric_create_tuned": ([_P, _I, _I, _P, _P], _I),
     "pvglu_group_create": ([_P, _I, C.POINTER(_P)], _I),
+    "pvglu_blocks_create": ([_P, _I, _I, _I, _P, _P], _I),
+    "pvglu_blocks_destroy": ([_P], _I),
+    "pvglu_blocks_part": ([_P, _I, _P], _I),
+    "pvglu_blocks_step": ([_P, _P, _P, _P, C.c_double, _I, _P, _P], _I),
     "pvglu_group_destroy": ([_P], _I),
     "pvglu_group_refactor_solve": ([_P, _P, _I, _P], _I),
     "pvglu_refine_system_host": ([_P, _P, _P, _P, C.c_double, _I, _P, _P], _I),

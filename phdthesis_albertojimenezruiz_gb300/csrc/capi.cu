@@ -1723,3 +1723,110 @@ int pvglu_solve_refined(pvglu_numeric* h, const double* a_values, const double* 
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Scenario blocks: handles of one batch run side by side on their own streams.
+struct pvglu_blocks {
+  std::vector<pvglu_numeric*> parts;
+  std::vector<cudaStream_t> streams;
+  std::vector<cudaEvent_t> joins;
+  cudaEvent_t fork = nullptr;
+  ~pvglu_blocks() {
+    for (pvglu_numeric* h : parts)
+      if (h) pvglu_numeric_destroy(h);
+    for (cudaStream_t st : streams)
+      if (st) cudaStreamDestroy(st);
+    for (cudaEvent_t e : joins)
+      if (e) cudaEventDestroy(e);
+    if (fork) cudaEventDestroy(fork);
+  }
+};
+
+extern "C" {
+
+int pvglu_blocks_create(const pvglu_symbolic* s, int n_scenarios, int parts, int precision,
+                        const pvglu_tuning* tuning, pvglu_blocks** out) {
+  if (!s || !out || parts < 1 || n_scenarios < parts || n_scenarios % parts)
+    return fail(PVGLU_ERR_BAD_ARG, "blocks need n_scenarios a positive multiple of parts");
+  *out = nullptr;
+  auto* b = new pvglu_blocks();
+  const int per = n_scenarios / parts;
+  b->parts.assign(parts, nullptr);
+  b->streams.assign(parts, nullptr);
+  b->joins.assign(parts, nullptr);
+  int rc = PVGLU_OK;
+  for (int k = 0; k < parts && !rc; k++)
+    rc = tuning ? pvglu_numeric_create_tuned(s, per, precision, tuning, &b->parts[k])
+                : pvglu_numeric_create(s, per, precision, &b->parts[k]);
+  for (int k = 0; k < parts && !rc; k++)
+    if (cudaStreamCreateWithFlags(&b->streams[k], cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->joins[k], cudaEventDisableTiming) != cudaSuccess)
+      rc = fail(PVGLU_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
+  if (!rc && cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess)
+    rc = fail(PVGLU_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
+  if (rc) {
+    delete b;
+    return rc;
+  }
+  *out = b;
+  return PVGLU_OK;
+}
+
+int pvglu_blocks_destroy(pvglu_blocks* b) {
+  if (!b) return fail(PVGLU_ERR_BAD_ARG, "NULL blocks");
+  for (cudaStream_t st : b->streams)
+    if (st) cudaStreamSynchronize(st);
+  delete b;
+  return PVGLU_OK;
+}
+
+int pvglu_blocks_part(pvglu_blocks* b, int k, pvglu_numeric** out) {
+  if (!b || !out || k < 0 || k >= (int)b->parts.size())
+    return fail(PVGLU_ERR_BAD_ARG, "bad block index");
+  *out = b->parts[k];
+  return PVGLU_OK;
+}
+
+int pvglu_blocks_step(pvglu_blocks* b, const double* const* a_values, const double* const* rhs,
+                      double* const* x, double tol, int max_sweeps, int* const* sweeps_out,
+                      void* stream) {
+  if (!b || !a_values || !rhs || !x) return fail(PVGLU_ERR_BAD_ARG, "NULL argument");
+  const int parts = (int)b->parts.size();
+  for (int k = 0; k < parts; k++)
+    if (!a_values[k] || !rhs[k] || !x[k]) return fail(PVGLU_ERR_BAD_ARG, "NULL block buffer");
+  if (b->parts[0]->precision == PVGLU_FP32 && (max_sweeps <= 0 || !(tol > 0.0)))
+    return fail(PVGLU_ERR_BAD_ARG, "bad refinement arguments");
+  cudaStream_t caller = as_stream(stream);
+  PVGLU_CUDA(cudaEventRecord(b->fork, caller));
+  int rc = PVGLU_OK;
+  for (int k = 0; k < parts; k++) {
+    pvglu_numeric* h = b->parts[k];
+    cudaStream_t st = b->streams[k];
+    // Every block joins back, also after an error, so no stream is left
+    // ahead of the caller's.
+    int rk = cudaStreamWaitEvent(st, b->fork, 0) == cudaSuccess
+                 ? PVGLU_OK
+                 : fail(PVGLU_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
+    if (!rk && !rc) rk = pvglu_scatter_refactor(h, a_values[k], st);
+    if (!rk && !rc) {
+      if (h->precision == PVGLU_FP32) {
+        rk = pvglu_solve_refined(h, a_values[k], rhs[k], x[k], tol, max_sweeps,
+                                 sweeps_out ? sweeps_out[k] : nullptr, st);
+      } else {
+        rk = cudaMemcpyAsync(x[k], rhs[k], (size_t)h->n * h->ld * sizeof(double),
+                             cudaMemcpyDeviceToDevice, st) == cudaSuccess
+                 ? PVGLU_OK
+                 : fail(PVGLU_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
+        if (!rk) rk = pvglu_solve(h, x[k], PVGLU_SOLVE_ORIGINAL, st);
+      }
+    }
+    if (cudaEventRecord(b->joins[k], st) != cudaSuccess ||
+        cudaStreamWaitEvent(caller, b->joins[k], 0) != cudaSuccess)
+      rk = rk ? rk : fail(PVGLU_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
+    rc = rc ? rc : rk;
+  }
+  return rc;
+}
+
+}  // extern "C"
+

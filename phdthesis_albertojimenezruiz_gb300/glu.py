@@ -238,8 +238,69 @@ class Numeric:
 
     def __del__(self):
         h = getattr(self, "handle", None)
-        if h and N._lib is not None:
+        if h and N._lib is not None and getattr(self, "_owned", True):
             N.lib().pvglu_numeric_destroy(h)
+            self.handle = None
+
+    @classmethod
+    def _borrow(cls, sym: Symbolic, handle: C.c_void_p, n_scenarios: int,
+                precision: int) -> "Numeric":
+        """A view of a handle owned elsewhere (a block of Blocks)."""
+        self = cls.__new__(cls)
+        self._owned = False
+        self.sym = sym
+        self.handle = handle
+        self.S = n_scenarios
+        self.ld = N.lib().pvglu_numeric_ld(handle)
+        self.max_locals = N.lib().pvglu_numeric_max_locals(handle)
+        self.precision = precision
+        self.schedule = None
+        return self
+
+
+class Blocks:
+    """One batch of scenarios as `parts` numeric handles of n_scenarios /
+    parts scenarios, run side by side on streams of their own
+    (pvglu_blocks_*).  Block k's buffers have the layout of parts[k]."""
+
+    def __init__(self, sym: Symbolic, n_scenarios: int, parts: int, precision: int = N.FP32,
+                 tuning: dict | None = None):
+        h = C.c_void_p()
+        t = None
+        if tuning is not None:
+            t = N.Tuning(**{f: int(tuning[f]) for f, _ in N.Tuning._fields_})
+        N.check(N.lib().pvglu_blocks_create(sym.handle, int(n_scenarios), int(parts),
+                                            int(precision), C.byref(t) if t else None,
+                                            C.byref(h)), "pvglu_blocks_create")
+        self.handle = h
+        self.sym = sym
+        self.S = n_scenarios
+        self.precision = precision
+        self.parts = []
+        for k in range(parts):
+            hk = C.c_void_p()
+            N.check(N.lib().pvglu_blocks_part(h, k, C.byref(hk)), "pvglu_blocks_part")
+            self.parts.append(Numeric._borrow(sym, hk, n_scenarios // parts, precision))
+
+    def step(self, a_values, b, x, tol=1e-12, max_sweeps=10, sweeps=None, stream=None) -> None:
+        """pvglu_blocks_step: per block k, factors from a_values[k] and
+        x[k] = J^-1 b[k] (refined to tol for FP32 blocks)."""
+        n = len(self.parts)
+
+        def arr(bufs):
+            return (C.c_void_p * n)(*[_ptr(t).value for t in bufs])
+
+        sw = None if sweeps is None else arr(sweeps)
+        N.check(N.lib().pvglu_blocks_step(self.handle, arr(a_values), arr(b), arr(x), float(tol),
+                                          int(max_sweeps), sw, _stream_ptr(stream)),
+                "pvglu_blocks_step")
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h and N._lib is not None:
+            for p in getattr(self, "parts", []):
+                p.handle = None
+            N.lib().pvglu_blocks_destroy(h)
             self.handle = None
 
 

@@ -79,3 +79,23 @@ int main(void) {
                     f"-Wl,-rpath,{lib.parent}"], check=True, timeout=120)
     out = subprocess.run([str(exe)], check=True, capture_output=True, text=True, timeout=120)
     assert "n=3 nnz_lu=7" in out.stdout
+
+
+def test_blocks_reject_bad_splits():
+    """pvglu_blocks_create checks its split before touching the device: a
+    batch that does not divide into the blocks, and zero blocks, are
+    PVGLU_ERR_BAD_ARG (1); so are NULL handles to the other blocks calls."""
+    import numpy as np
+
+    from phdthesis_albertojimenezruiz_gb300 import FP32, Symbolic
+
+    s = Symbolic(np.array([0, 2, 5, 7]), np.array([0, 1, 0, 1, 2, 1, 2]))
+    out = C.c_void_p()
+    lib = N.lib()
+    for n_scen, parts in ((10, 4), (3, 4), (8, 0), (0, 1)):
+        assert lib.pvglu_blocks_create(s.handle, n_scen, parts, FP32, None,
+                                       C.byref(out)) == 1, (n_scen, parts)
+        assert not out.value
+    assert lib.pvglu_blocks_destroy(None) == 1
+    assert lib.pvglu_blocks_part(None, 0, C.byref(out)) == 1
+    assert lib.pvglu_blocks_step(None, None, None, None, 1e-12, 4, None, None) == 1

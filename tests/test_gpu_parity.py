@@ -927,3 +927,46 @@ def test_scatter_refactor_reports_zero_pivot(cuda, precision):
             num.refactor()
         got.append(num.check())
     assert got[0] == got[1] and got[0][0] == N.OK + 3 and got[0][2] == 17, got
+
+
+@pytest.mark.parametrize("precision,parts", [(FP32, 4), (FP64, 2)])
+def test_blocks_match_one_handle(cuda, precision, parts):
+    """pvglu_blocks: the scenarios split into blocks on streams of their own
+    give, block by block, the same solutions (and refinement sweeps) as one
+    handle over all of them, bit for bit."""
+    import torch
+
+    from phdthesis_albertojimenezruiz_gb300 import Blocks
+
+    p = Plant(10, 16, 20)
+    s = Symbolic(p.rowptr, p.colidx)
+    S = 256
+    a, b = M.plant_batch(p, S, seed0=1200, preset="c3")
+    one = Numeric(s, S, precision, SCHED_LEVELS)
+    a_dev, b_dev = dev(pad_cols(a, one.ld)), dev(pad_cols(b, one.ld))
+    x_one = torch.zeros_like(b_dev)
+    sw_one = torch.zeros(one.ld, dtype=torch.int32, device="cuda")
+    one.scatter_refactor(a_dev)
+    if precision == FP32:
+        one.solve_refined(a_dev, b_dev, x_one, tol=1e-12, max_sweeps=8, sweeps=sw_one)
+    else:
+        x_one.copy_(b_dev)
+        one.solve(x_one, original=True)
+    torch.cuda.synchronize()
+    blk = Blocks(s, S, parts, precision)
+    H = S // parts
+    a_k = [dev(pad_cols(a[:, k * H:(k + 1) * H], blk.parts[k].ld)) for k in range(parts)]
+    b_k = [dev(pad_cols(b[:, k * H:(k + 1) * H], blk.parts[k].ld)) for k in range(parts)]
+    x_k = [torch.full_like(t, float("nan")) for t in b_k]
+    sw_k = [torch.zeros(blk.parts[k].ld, dtype=torch.int32, device="cuda") for k in range(parts)]
+    stream = torch.cuda.Stream()
+    blk.step(a_k, b_k, x_k, tol=1e-12, max_sweeps=8, sweeps=sw_k, stream=stream)
+    stream.synchronize()
+    for k in range(parts):
+        assert blk.parts[k].check()[0] == 0
+        got = x_k[k].cpu().numpy()[:, :H]
+        want = x_one.cpu().numpy()[:, k * H:(k + 1) * H]
+        assert np.array_equal(got, want), k
+        if precision == FP32:
+            assert np.array_equal(sw_k[k].cpu().numpy()[:H],
+                                  sw_one.cpu().numpy()[k * H:(k + 1) * H]), k
