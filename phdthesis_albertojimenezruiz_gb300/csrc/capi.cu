@@ -1798,32 +1798,39 @@ int pvglu_blocks_step(pvglu_blocks* b, const double* const* a_values, const doub
     return fail(PVGLU_ERR_BAD_ARG, "bad refinement arguments");
   cudaStream_t caller = as_stream(stream);
   PVGLU_CUDA(cudaEventRecord(b->fork, caller));
+  // Every block's factorization is issued before any block's solve, so that
+  // all blocks start within a few launches of each other.
+  std::vector<int> rk(parts, PVGLU_OK);
+  for (int k = 0; k < parts; k++) {
+    pvglu_numeric* h = b->parts[k];
+    cudaStream_t st = b->streams[k];
+    rk[k] = cudaStreamWaitEvent(st, b->fork, 0) == cudaSuccess
+                ? PVGLU_OK
+                : fail(PVGLU_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
+    if (!rk[k]) rk[k] = pvglu_scatter_refactor(h, a_values[k], st);
+  }
   int rc = PVGLU_OK;
   for (int k = 0; k < parts; k++) {
     pvglu_numeric* h = b->parts[k];
     cudaStream_t st = b->streams[k];
-    // Every block joins back, also after an error, so no stream is left
-    // ahead of the caller's.
-    int rk = cudaStreamWaitEvent(st, b->fork, 0) == cudaSuccess
-                 ? PVGLU_OK
-                 : fail(PVGLU_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
-    if (!rk && !rc) rk = pvglu_scatter_refactor(h, a_values[k], st);
-    if (!rk && !rc) {
+    if (!rk[k]) {
       if (h->precision == PVGLU_FP32) {
-        rk = pvglu_solve_refined(h, a_values[k], rhs[k], x[k], tol, max_sweeps,
-                                 sweeps_out ? sweeps_out[k] : nullptr, st);
+        rk[k] = pvglu_solve_refined(h, a_values[k], rhs[k], x[k], tol, max_sweeps,
+                                    sweeps_out ? sweeps_out[k] : nullptr, st);
       } else {
-        rk = cudaMemcpyAsync(x[k], rhs[k], (size_t)h->n * h->ld * sizeof(double),
-                             cudaMemcpyDeviceToDevice, st) == cudaSuccess
-                 ? PVGLU_OK
-                 : fail(PVGLU_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
-        if (!rk) rk = pvglu_solve(h, x[k], PVGLU_SOLVE_ORIGINAL, st);
+        rk[k] = cudaMemcpyAsync(x[k], rhs[k], (size_t)h->n * h->ld * sizeof(double),
+                                cudaMemcpyDeviceToDevice, st) == cudaSuccess
+                    ? PVGLU_OK
+                    : fail(PVGLU_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
+        if (!rk[k]) rk[k] = pvglu_solve(h, x[k], PVGLU_SOLVE_ORIGINAL, st);
       }
     }
+    // Every block joins back, also after an error, so no stream is left
+    // ahead of the caller's.
     if (cudaEventRecord(b->joins[k], st) != cudaSuccess ||
         cudaStreamWaitEvent(caller, b->joins[k], 0) != cudaSuccess)
-      rk = rk ? rk : fail(PVGLU_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
-    rc = rc ? rc : rk;
+      rk[k] = rk[k] ? rk[k] : fail(PVGLU_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
+    rc = rc ? rc : rk[k];
   }
   return rc;
 }
