@@ -592,8 +592,8 @@ def newton_iterates_section(stream, S: int, steps: int) -> dict:
     counts and its error against the FP64 solution."""
     import torch
 
-    from phdthesis_albertojimenezruiz_gb300 import (FP32, FP64, GMIN_STAGES, Newton, Numeric,
-                                                    Plant, Symbolic)
+    from phdthesis_albertojimenezruiz_gb300 import (FP32, FP64, GMIN_STAGES, SCHED_LEVELS,
+                                                    Newton, Numeric, Plant, Symbolic)
     from phdthesis_albertojimenezruiz_gb300.glu import autotune_ex
 
     p = Plant(*DIMS)
@@ -624,15 +624,19 @@ def newton_iterates_section(stream, S: int, steps: int) -> dict:
         x64 = torch.empty_like(b_d)
 
         def step32():
-            n32.scatter(a_d, stream=stream)
-            n32.refactor(stream=stream)
+            n32.scatter_refactor(a_d, stream=stream)
             n32.solve_refined(a_d, b_d, x32, tol=IR_TOL, max_sweeps=40, sweeps=sweeps,
                               stream=stream)
 
         def step64():
-            n64.scatter(a_d, stream=stream)
-            x64.copy_(b_d)
-            n64.refactor_solve(x64, original=True, stream=stream)
+            if t64["schedule"] == SCHED_LEVELS:  # scatter + refactor in one pass
+                n64.scatter_refactor(a_d, stream=stream)
+                x64.copy_(b_d)
+                n64.solve(x64, original=True, stream=stream)
+            else:  # refactor + solve in one persistent launch
+                n64.scatter(a_d, stream=stream)
+                x64.copy_(b_d)
+                n64.refactor_solve(x64, original=True, stream=stream)
 
         for _ in range(3):
             step32()
@@ -1466,6 +1470,24 @@ def main() -> None:
                     "max_rel_err_vs_fp32ir": float(np.max(
                         np.abs(x64b.cpu().numpy()[:, :S] - xa).max(axis=0) /
                         np.abs(xa).max(axis=0)))}
+    if blk is not None and t64["schedule"] == SCHED_LEVELS:
+        # The FP64 step as the headline's scenario blocks too.
+        blk64 = Blocks(sym, S, n_blk, FP64, tuning={k: t64[k] for k in tuning})
+        x64k = [torch.empty_like(t) for t in blk_b]
+
+        def fp64_block_step():
+            blk64.step(blk_a, blk_b, x64k, stream=stream)
+
+        for _ in range(args.warmup):
+            fp64_block_step()
+        ms64k = _time_ms(fp64_block_step, stream, args.steps)
+        Hb = S // n_blk
+        same64 = all(torch.equal(x64k[k][:, :Hb], x64b[:, k * Hb:(k + 1) * Hb])
+                     for k in range(n_blk))
+        batched_fp64["blocks"] = {"value": S / (ms64k / 1000.0), "unit": UNIT,
+                                  "ms_per_step": ms64k, "blocks": n_blk,
+                                  "bit_identical_to_one_handle": bool(same64)}
+        del blk64, x64k
     del num64b, x64b
 
     # The same batched step with the reference's own AMD ordering of this
