@@ -675,7 +675,8 @@ def wide_section(stream, steps: int, S: int = 512, patterns: str = "ref,mesh,ran
     import matrices as M
     from oracle import oracle as O
     from phdthesis_albertojimenezruiz_gb300 import (FP32, FP64, SCHED_LEVELS, SCHED_PERSISTENT,
-                                                    SCHED_THREAD_CHAIN, Numeric, Symbolic)
+                                                    SCHED_THREAD_CHAIN, Blocks, Numeric,
+                                                    Symbolic)
     from phdthesis_albertojimenezruiz_gb300.glu import autotune_ex
     from phdthesis_albertojimenezruiz_gb300.plant import block_plant
 
@@ -762,6 +763,33 @@ def wide_section(stream, steps: int, S: int = 512, patterns: str = "ref,mesh,ran
             "tuning": t64, "program_info": n64.info,
             "hbm": {"bytes_per_step": byt, "achieved_gbs": byt / (ms64 / 1000.0) / 1e9,
                     "frac": byt / (ms64 / 1000.0) / 1e9 / peak if peak else None}}
+        if not profile and S % 4 == 0 and S // 4 >= 128 and t64["schedule"] == SCHED_LEVELS:
+            # The same step as 4 scenario blocks of at least 128 scenarios
+            # (smaller blocks leave the long chains' lanes half empty: 2
+            # blocks of 32 took 1.79 ms against 1.14 ms for one handle of 64).
+            Hb = S // 4
+            blk = Blocks(sym, S, 4, FP64, tuning=t64)
+
+            def block_cols(t, k, ld_k):
+                out_ = torch.zeros((t.shape[0], ld_k), dtype=t.dtype, device=dev)
+                out_[:, :Hb] = t[:, k * Hb:(k + 1) * Hb]
+                return out_
+
+            ak = [block_cols(a_d, k, blk.parts[k].ld) for k in range(4)]
+            bk = [block_cols(b_d, k, blk.parts[k].ld) for k in range(4)]
+            xk = [torch.empty_like(t) for t in bk]
+
+            def step_blocks():
+                blk.step(ak, bk, xk, stream=stream)
+
+            for _ in range(3):
+                step_blocks()
+            msb = _time_ms(step_blocks, stream, steps)
+            res["batched_fp64"]["blocks"] = {
+                "value": S / (msb / 1000.0), "unit": UNIT, "ms_per_step": msb, "blocks": 4,
+                "bit_identical_to_one_handle": bool(all(
+                    torch.equal(xk[k][:, :Hb], x64[:, k * Hb:(k + 1) * Hb]) for k in range(4)))}
+            del blk, ak, bk, xk
         if profile:
             out.append(res)
             del n64, a_d, b_d, x64
