@@ -408,11 +408,16 @@ int pvglu_blocks_part(pvglu_blocks* b, int k, pvglu_numeric** out);
  * sweeps_out[k] or NULL per block; FP64 blocks: a copy of b[k] solved with
  * PVGLU_SOLVE_ORIGINAL).  a_values[k] [nnz_a * ld_k], b[k] and x[k]
  * [n * ld_k] are FP64 device buffers.  The blocks start after the work
- * already on `stream` and `stream` waits for all of them; also under stream
- * capture. */
+ * already on `stream`, and `stream` waits for all of them, also under
+ * stream capture; with PVGLU_BLOCKS_NO_JOIN in flags it does not, and each
+ * block's stream runs on into its next step as soon as its own step ends
+ * (blocks are independent): pvglu_blocks_join then makes `stream` wait for
+ * every block. */
+enum { PVGLU_BLOCKS_NO_JOIN = 1 };
 int pvglu_blocks_step(pvglu_blocks* b, const double* const* a_values, const double* const* rhs,
                       double* const* x, double tol, int max_sweeps, int* const* sweeps_out,
-                      void* stream);
+                      int flags, void* stream);
+int pvglu_blocks_join(pvglu_blocks* b, void* stream);
 
 /* ---------------- failure-path self-test --------------------------------- */
 

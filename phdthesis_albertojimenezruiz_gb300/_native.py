@@ -18,6 +18,7 @@ ERR_NAMES = {
 }
 FP64, FP32 = 0, 1
 SOLVE_TRANSPOSE, SOLVE_ORIGINAL = 1, 2
+BLOCKS_NO_JOIN = 1
 SCHED_LEVELS, SCHED_PERSISTENT, SCHED_THREAD_CHAIN = 0, 1, 2
 NEWTON_CONVERGED, NEWTON_RUNNING, NEWTON_MAX_ITERATIONS, NEWTON_DAMPING = 0, 1, 2, 3
 
@@ -109,7 +110,8 @@ _SIGS = {
     "pvglu_blocks_create": ([_P, _I, _I, _I, _P, _P], _I),
     "pvglu_blocks_destroy": ([_P], _I),
     "pvglu_blocks_part": ([_P, _I, _P], _I),
-    "pvglu_blocks_step": ([_P, _P, _P, _P, C.c_double, _I, _P, _P], _I),
+    "pvglu_blocks_step": ([_P, _P, _P, _P, C.c_double, _I, _P, _I, _P], _I),
+    "pvglu_blocks_join": ([_P, _P], _I),
     "pvglu_group_destroy": ([_P], _I),
     "pvglu_group_refactor_solve": ([_P, _P, _I, _P], _I),
     "pvglu_refine_system_host": ([_P, _P, _P, _P, C.c_double, _I, _P, _P], _I),

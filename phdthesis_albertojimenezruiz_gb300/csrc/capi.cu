@@ -1789,7 +1789,7 @@ int pvglu_blocks_part(pvglu_blocks* b, int k, pvglu_numeric** out) {
 
 int pvglu_blocks_step(pvglu_blocks* b, const double* const* a_values, const double* const* rhs,
                       double* const* x, double tol, int max_sweeps, int* const* sweeps_out,
-                      void* stream) {
+                      int flags, void* stream) {
   if (!b || !a_values || !rhs || !x) return fail(PVGLU_ERR_BAD_ARG, "NULL argument");
   const int parts = (int)b->parts.size();
   for (int k = 0; k < parts; k++)
@@ -1826,13 +1826,24 @@ int pvglu_blocks_step(pvglu_blocks* b, const double* const* a_values, const doub
       }
     }
     // Every block joins back, also after an error, so no stream is left
-    // ahead of the caller's.
-    if (cudaEventRecord(b->joins[k], st) != cudaSuccess ||
-        cudaStreamWaitEvent(caller, b->joins[k], 0) != cudaSuccess)
+    // ahead of the caller's (unless the caller joins later).
+    if (!(flags & PVGLU_BLOCKS_NO_JOIN) &&
+        (cudaEventRecord(b->joins[k], st) != cudaSuccess ||
+         cudaStreamWaitEvent(caller, b->joins[k], 0) != cudaSuccess))
       rk[k] = rk[k] ? rk[k] : fail(PVGLU_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
     rc = rc ? rc : rk[k];
   }
   return rc;
+}
+
+int pvglu_blocks_join(pvglu_blocks* b, void* stream) {
+  if (!b) return fail(PVGLU_ERR_BAD_ARG, "NULL blocks");
+  cudaStream_t caller = as_stream(stream);
+  for (size_t k = 0; k < b->parts.size(); k++)
+    if (cudaEventRecord(b->joins[k], b->streams[k]) != cudaSuccess ||
+        cudaStreamWaitEvent(caller, b->joins[k], 0) != cudaSuccess)
+      return fail(PVGLU_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
+  return PVGLU_OK;
 }
 
 }  // extern "C"

@@ -282,18 +282,25 @@ class Blocks:
             N.check(N.lib().pvglu_blocks_part(h, k, C.byref(hk)), "pvglu_blocks_part")
             self.parts.append(Numeric._borrow(sym, hk, n_scenarios // parts, precision))
 
-    def step(self, a_values, b, x, tol=1e-12, max_sweeps=10, sweeps=None, stream=None) -> None:
+    def step(self, a_values, b, x, tol=1e-12, max_sweeps=10, sweeps=None, stream=None,
+             join: bool = True) -> None:
         """pvglu_blocks_step: per block k, factors from a_values[k] and
-        x[k] = J^-1 b[k] (refined to tol for FP32 blocks)."""
+        x[k] = J^-1 b[k] (refined to tol for FP32 blocks).  join=False: the
+        stream does not wait for the blocks (see join())."""
         n = len(self.parts)
 
         def arr(bufs):
             return (C.c_void_p * n)(*[_ptr(t).value for t in bufs])
 
         sw = None if sweeps is None else arr(sweeps)
+        flags = 0 if join else N.BLOCKS_NO_JOIN
         N.check(N.lib().pvglu_blocks_step(self.handle, arr(a_values), arr(b), arr(x), float(tol),
-                                          int(max_sweeps), sw, _stream_ptr(stream)),
+                                          int(max_sweeps), sw, flags, _stream_ptr(stream)),
                 "pvglu_blocks_step")
+
+    def join(self, stream=None) -> None:
+        """pvglu_blocks_join: the stream waits for every block's work so far."""
+        N.check(N.lib().pvglu_blocks_join(self.handle, _stream_ptr(stream)), "pvglu_blocks_join")
 
     def __del__(self):
         h = getattr(self, "handle", None)

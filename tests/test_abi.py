@@ -98,4 +98,5 @@ def test_blocks_reject_bad_splits():
         assert not out.value
     assert lib.pvglu_blocks_destroy(None) == 1
     assert lib.pvglu_blocks_part(None, 0, C.byref(out)) == 1
-    assert lib.pvglu_blocks_step(None, None, None, None, 1e-12, 4, None, None) == 1
+    assert lib.pvglu_blocks_step(None, None, None, None, 1e-12, 4, None, 0, None) == 1
+    assert lib.pvglu_blocks_join(None, None) == 1

@@ -962,6 +962,11 @@ def test_blocks_match_one_handle(cuda, precision, parts):
     stream = torch.cuda.Stream()
     blk.step(a_k, b_k, x_k, tol=1e-12, max_sweeps=8, sweeps=sw_k, stream=stream)
     stream.synchronize()
+    # Unjoined steps, each block running on: the same after a join.
+    for _ in range(2):
+        blk.step(a_k, b_k, x_k, tol=1e-12, max_sweeps=8, sweeps=sw_k, stream=stream, join=False)
+    blk.join(stream)
+    stream.synchronize()
     for k in range(parts):
         assert blk.parts[k].check()[0] == 0
         got = x_k[k].cpu().numpy()[:, :H]
