@@ -88,19 +88,21 @@ __device__ __forceinline__ float fnms(float a, float b, float c) { return a - b 
 // even); magnitudes below the smallest normal float become signed zero,
 // overflow gives infinity, NaN stays NaN.
 __device__ __forceinline__ float d2f_bits(double x) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  const unsigned int sign = (unsigned int)(b >> 32) & 0x80000000u;
-  const int e = (int)((b >> 52) & 0x7ff);
-  const unsigned long long m = b & 0x000fffffffffffffull;
-  if (e == 0x7ff) return __uint_as_float(sign | 0x7f800000u | (m ? 0x400000u : 0u));
-  const int fe = e - 1023 + 127;
-  if (fe <= 0) return __uint_as_float(sign);
-  if (fe >= 255) return __uint_as_float(sign | 0x7f800000u);
-  // exponent and mantissa as one field: a rounding carry moves into the
-  // exponent (and to infinity past the largest float), as IEEE requires.
-  const unsigned long long em = ((unsigned long long)fe << 52) | m;
-  const unsigned long long r = em + 0x0fffffffull + ((em >> 29) & 1ull);
-  return __uint_as_float(sign | (unsigned int)(r >> 29));
+  const unsigned lo = (unsigned)__double2loint(x), hi = (unsigned)__double2hiint(x);
+  const unsigned sign = hi & 0x80000000u;
+  const unsigned ahi = hi & 0x7fffffffu;
+  const unsigned e = ahi >> 20;  // biased double exponent
+  if (e - 897u < 254u) {         // a normal float: exponent 1..254 after rebiasing
+    // The 32 bits of |x| >> 29 hold exponent and 23 mantissa bits; the
+    // exponent's lost top bits cancel in the 32-bit rebias (896 << 23).
+    const unsigned q = __funnelshift_l(lo, ahi, 3) - 0xC0000000u;
+    // Round to nearest even on the 29 bits shifted out; a carry moves into
+    // the exponent (and to infinity past the largest float), as IEEE requires.
+    const unsigned up = ((lo & 0x1fffffffu) + (q & 1u) + 0x0fffffffu) >> 29;
+    return __uint_as_float(sign | (q + up));
+  }
+  if (e == 0x7ffu) return __uint_as_float(sign | 0x7f800000u | (((ahi & 0xfffffu) | lo) ? 0x400000u : 0u));
+  return __uint_as_float(e < 897u ? sign : (sign | 0x7f800000u));
 }
 
 __device__ __forceinline__ double f2d_bits(float f) {
