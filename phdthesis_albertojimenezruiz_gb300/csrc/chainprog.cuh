@@ -287,11 +287,11 @@ __device__ __forceinline__ void prog_drain(WarpTma& tma) {
 // segment (its column's) and no segment reads it earlier, so these rows
 // replace the scatter's write and the refactorization's first read of the
 // slot.  Plain 8 * LW-byte loads by all lanes, kOwnInFlight rows at a time,
-// while the table's other rows arrive by bulk copies.  Four rows measured
-// best for both precisions (35k plant, 512 scenarios: FP32 2 / 4 / 6 rows
-// 212 / 179 / 195 us, FP64 2 / 4 rows 464 / 432 us).
+// while the table's other rows arrive by bulk copies.  FP64: four rows (35k
+// plant, 512 scenarios: 2 / 4 rows 464 / 432 us); FP32: five, with the
+// kernel's register budget below (from_a_min_blocks).
 #ifndef PVGLU_OWN_IN_FLIGHT_F32
-#define PVGLU_OWN_IN_FLIGHT_F32 4
+#define PVGLU_OWN_IN_FLIGHT_F32 5
 #endif
 #ifndef PVGLU_OWN_IN_FLIGHT_F64
 #define PVGLU_OWN_IN_FLIGHT_F64 4
@@ -629,8 +629,20 @@ k_prog_level(ProgDev P, int table, DevStruct d, int cb, int ce,
 // one pass.  Only for programs without WIDE levels, where every LU slot is an
 // own row of some level's segment.  NARROW: for levels with at most one block
 // of items per SM, compiled for one block per SM (more own rows in flight).
+// The FP32 one pass is compiled for 8 resident blocks per SM (64 registers)
+// where the other FP32 executors take 9: the own rows' loads then keep five
+// rows in flight without spilling (35k plant, 512 scenarios: 9 blocks with 4
+// rows 171-173 us, 8 with 5 / 6 / 7 rows 159 / 160-161 / 162 us, 7 or 6
+// blocks with 8 rows 195 / 191 us).
+#ifndef PVGLU_FROM_A_MIN_BLOCKS_F32
+#define PVGLU_FROM_A_MIN_BLOCKS_F32 8
+#endif
+template <typename T>
+constexpr int from_a_min_blocks() {
+  return sizeof(T) == 4 ? PVGLU_FROM_A_MIN_BLOCKS_F32 : prog_min_blocks<T>();
+}
 template <typename T, int LW = 2, bool NARROW = false>
-__global__ void __launch_bounds__(kProgBlock, NARROW ? 1 : prog_min_blocks<T>())
+__global__ void __launch_bounds__(kProgBlock, NARROW ? 1 : from_a_min_blocks<T>())
 k_prog_refactor_from_a(ProgDev P, int table, DevStruct d, int cb, int ce, T* __restrict__ v,
                        const double* __restrict__ a, int ld, int S, T pivot_tol,
                        DevStatus* st) {
