@@ -391,8 +391,8 @@ int pvglu_autotune_ex(const pvglu_symbolic* s, int n_scenarios, int precision,
  * its own.  A step runs the blocks side by side, so one block's narrow,
  * latency-bound levels and launch tails overlap the other blocks' work (512
  * scenarios of the 35k plant, FP32 + refinement, each block running its steps
- * back to back: 4 blocks of 128 take 0.960-0.972 ms per step, one handle of
- * 512 1.010-1.030 ms; 8 of 64: 0.989 ms).  Every value
+ * back to back: 4 blocks of 128 take 0.948-0.972 ms per step, one handle of
+ * 512 1.003-1.030 ms; 8 of 64: 0.989 ms).  Every value
  * is the same as one handle's for the same scenarios.  Buffers are per
  * block, in that block's layout (ld_k = pvglu_numeric_ld of the block).  No
  * counterpart in the reference (one circuit per run).  n_scenarios must be
