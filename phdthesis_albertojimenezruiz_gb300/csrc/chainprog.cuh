@@ -52,11 +52,14 @@ struct ProgDev {
 constexpr int kGroup = 64;                       // scenarios per warp item (two per lane)
 constexpr int kProgBlock = 128;                  // threads per block of the executors
 constexpr int kProgWarps = kProgBlock / 32;
-// Resident blocks per SM the level executors are compiled for: FP32 tables
-// allow 9 blocks at the usual table sizes (at most 56 registers); FP64
-// executors are given up to 80 registers (6 blocks).  Build-time settings.
+// Resident blocks per SM the level executors are compiled for: FP32
+// executors 8 (up to 64 registers; the usual tables would allow 9 blocks,
+// but 64 registers measured faster with scenario blocks side by side: 512
+// scenarios of the 35k plant as 4 blocks, 0.949 -> 0.935 ms per step, one
+// handle unchanged at 0.996 ms); FP64 executors up to 80 registers (6
+// blocks).  Build-time settings.
 #ifndef PVGLU_FP32_MIN_BLOCKS
-#define PVGLU_FP32_MIN_BLOCKS 9
+#define PVGLU_FP32_MIN_BLOCKS 8
 #endif
 #ifndef PVGLU_FP64_MIN_BLOCKS
 #define PVGLU_FP64_MIN_BLOCKS 6
@@ -629,11 +632,10 @@ k_prog_level(ProgDev P, int table, DevStruct d, int cb, int ce,
 // one pass.  Only for programs without WIDE levels, where every LU slot is an
 // own row of some level's segment.  NARROW: for levels with at most one block
 // of items per SM, compiled for one block per SM (more own rows in flight).
-// The FP32 one pass is compiled for 8 resident blocks per SM (64 registers)
-// where the other FP32 executors take 9: the own rows' loads then keep five
-// rows in flight without spilling (35k plant, 512 scenarios: 9 blocks with 4
-// rows 171-173 us, 8 with 5 / 6 / 7 rows 159 / 160-161 / 162 us, 7 or 6
-// blocks with 8 rows 195 / 191 us).
+// The FP32 one pass at 8 resident blocks per SM (64 registers) keeps five
+// own rows in flight without spilling (35k plant, 512 scenarios: 9 blocks
+// with 4 rows 171-173 us, 8 with 5 / 6 / 7 rows 159 / 160-161 / 162 us, 7 or
+// 6 blocks with 8 rows 195 / 191 us).
 #ifndef PVGLU_FROM_A_MIN_BLOCKS_F32
 #define PVGLU_FROM_A_MIN_BLOCKS_F32 8
 #endif
