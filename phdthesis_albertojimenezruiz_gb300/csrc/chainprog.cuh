@@ -53,10 +53,10 @@ constexpr int kGroup = 64;                       // scenarios per warp item (two
 constexpr int kProgBlock = 128;                  // threads per block of the executors
 constexpr int kProgWarps = kProgBlock / 32;
 // Resident blocks per SM the level executors are compiled for: FP32
-// executors 8 (up to 64 registers; the usual tables would allow 9 blocks,
-// but 64 registers measured faster with scenario blocks side by side: 512
-// scenarios of the 35k plant as 4 blocks, 0.949 -> 0.935 ms per step, one
-// handle unchanged at 0.996 ms); FP64 executors up to 80 registers (6
+// executors 8 (up to 64 registers; the usual tables would allow 9 blocks.
+// With scenario blocks side by side, 512 scenarios of the 35k plant as 4
+// blocks, 64 registers measured 0.935 against 0.949 ms per step in one A/B,
+// one handle unchanged at 0.996 ms); FP64 executors up to 80 registers (6
 // blocks).  Build-time settings.
 #ifndef PVGLU_FP32_MIN_BLOCKS
 #define PVGLU_FP32_MIN_BLOCKS 8
